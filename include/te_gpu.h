@@ -1,0 +1,214 @@
+/*
+ * te_gpu.h -- C ABI of the GB300 geometric-multigrid hot path.
+ *
+ * Every entry point is plain C: opaque handles, device pointers, sizes and an
+ * int status (TE_OK == 0).  No CUDA, torch or C++ types cross this boundary,
+ * so a C++ adapter (see include/thunderegg_gb300/adapters.hpp), ctypes or any
+ * other FFI can bind it.  Each function names the ThunderEgg interface it
+ * replaces (paths are inside the ThunderEgg source tree, src/ThunderEgg/...).
+ *
+ * Data layout (identical to ThunderEgg's Vector<D>, Vector.h:133-153):
+ *   one level vector = num_patches patches, contiguous;
+ *   one patch        = [component][z][y][x], x fastest, every spatial axis
+ *                      padded by num_ghost cells on both sides.
+ * So a device level buffer can be wrapped by ThunderEgg's unmanaged Vector
+ * constructor (Vector.h:199) with patch_starts[i] = base + i * patch_stride.
+ *
+ * Mesh tables (te_level_desc) are the flattened Domain<D>/PatchInfo<D>/NbrInfo
+ * data (PatchInfo.h:66-126): local index == position in the arrays.  Face
+ * slots follow PatchInfo's nbr_infos indexing, Face<D,M>::sum_of_faces +
+ * face index (Face.h:75-78): 2D corners 0..3, sides 4..7; 3D corners 0..7,
+ * edges 8..19, sides 20..25.  Side index = 2*axis + is_upper (Face.h:558-584).
+ *
+ * Threading: a handle is bound to the stream that was current (te_set_stream)
+ * when it was created; calls on one handle are not thread safe.
+ */
+#ifndef TE_GPU_H
+#define TE_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+enum {
+  TE_OK = 0,
+  TE_ERR_INVALID = 1,     /* bad argument (null handle, size mismatch, ...) */
+  TE_ERR_CUDA = 2,        /* a CUDA runtime call failed                     */
+  TE_ERR_BREAKDOWN = 3,   /* Krylov breakdown: rho == 0 (BreakdownError.h)  */
+  TE_ERR_UNSUPPORTED = 4, /* combination not supported (e.g. odd n trilinear) */
+  TE_ERR_BUDGET = 5,      /* serving admission: request over memory budget  */
+  TE_ERR_TIMEOUT = 6,     /* bounded device-side wait ran out               */
+  TE_ERR_NOT_CONVERGED = 7
+};
+
+/* arithmetic type of a level vector */
+enum { TE_F64 = 0, TE_F32 = 1 };
+
+/* neighbour types (NbrType.h); -1 = no neighbour on that face */
+enum { TE_NBR_NONE = -1, TE_NBR_NORMAL = 0, TE_NBR_COARSE = 1, TE_NBR_FINE = 2 };
+
+/* ghost schemes and GhostFillingType (GhostFillingType.h:33-47) */
+enum { TE_GHOST_BILINEAR = 0, TE_GHOST_BIQUADRATIC = 1, TE_GHOST_TRILINEAR = 2 };
+enum { TE_FILL_FACES = 0, TE_FILL_EDGES = 1, TE_FILL_CORNERS = 2 };
+
+/* One level of the mesh: the flattened PatchInfo<D> vector of a Domain<D>.
+ * All pointers are HOST pointers; the arrays are copied at te_domain_create. */
+typedef struct te_level_desc {
+  int dim;            /* D = 2 or 3                                        */
+  int ns[3];          /* cells per patch along each axis                   */
+  int num_ghost;      /* ghost layers per side (>= 1)                      */
+  int num_patches;    /* P                                                 */
+  const int* id;             /* [P]                                        */
+  const int* refine_level;   /* [P]                                        */
+  const int* parent_id;      /* [P]      -1 = none                         */
+  const int* orth_on_parent; /* [P]      -1 = Orthant::null()              */
+  const int* child_ids;      /* [P*2^D]  -1 = none                         */
+  const double* starts;      /* [P*D]                                      */
+  const double* spacings;    /* [P*D]                                      */
+  const int* nbr_type;       /* [P*F]    TE_NBR_*, F = 8 (2D) / 26 (3D)    */
+  const int* nbr_ids;        /* [P*F*4]  neighbour ids (fine: by orthant)  */
+  const int* nbr_orth;       /* [P*F]    orth_on_coarse for coarse nbrs    */
+} te_level_desc;
+
+typedef struct te_domain te_domain;
+typedef struct te_ghost_filler te_ghost_filler;
+typedef struct te_operator te_operator;
+typedef struct te_patch_solver te_patch_solver;
+typedef struct te_restrictor te_restrictor;
+typedef struct te_interpolator te_interpolator;
+typedef struct te_cycle te_cycle;
+
+/* ---- library ------------------------------------------------------------ */
+const char* te_last_error_message(void);
+/* Stream used by handles created after this call (a cudaStream_t, or NULL
+ * for the legacy default stream). */
+int te_set_stream(void* cuda_stream);
+int te_synchronize(void);
+/* Number of kernels this library has launched since load (for accounting). */
+long long te_kernel_launch_count(void);
+
+/* ---- Domain<D> (Domain.h:94-248) ---------------------------------------- */
+/* Uploads the level's flattened metadata; resolves neighbour ids to local
+ * indexes exactly as Domain::indexPatchesLocal (Domain.h:94-110). */
+int te_domain_create(const te_level_desc* desc, te_domain** out);
+int te_domain_destroy(te_domain* d);
+/* doubles (or floats) of one patch with ncomp components, ghosts included */
+long long te_domain_patch_stride(const te_domain* d, int ncomp);
+int te_domain_num_patches(const te_domain* d);
+
+/* ---- Vector<D> algebra (Vector.h:391-611); interior cells only unless
+ *      with_ghost.  x, a, b, c are device level buffers of the domain. ---- */
+int te_vec_set(const te_domain* d, int ncomp, int dtype, void* x, double alpha, int with_ghost);
+int te_vec_scale(const te_domain* d, int ncomp, int dtype, void* x, double alpha);
+int te_vec_shift(const te_domain* d, int ncomp, int dtype, void* x, double delta);
+int te_vec_copy(const te_domain* d, int ncomp, int dtype, void* x, const void* b, int with_ghost);
+int te_vec_add(const te_domain* d, int ncomp, int dtype, void* x, const void* b);
+/* x += alpha*a */
+int te_vec_add_scaled(const te_domain* d, int ncomp, int dtype, void* x, double alpha, const void* a);
+/* x += alpha*a + beta*b */
+int te_vec_add_scaled2(const te_domain* d, int ncomp, int dtype, void* x, double alpha,
+                       const void* a, double beta, const void* b);
+/* x = alpha*x + b */
+int te_vec_scale_then_add(const te_domain* d, int ncomp, int dtype, void* x, double alpha,
+                          const void* b);
+/* x = alpha*x + beta*b */
+int te_vec_scale_then_add_scaled(const te_domain* d, int ncomp, int dtype, void* x,
+                                 double alpha, double beta, const void* b);
+/* x = alpha*x + beta*b + gamma*c */
+int te_vec_scale_then_add_scaled2(const te_domain* d, int ncomp, int dtype, void* x,
+                                  double alpha, double beta, const void* b, double gamma,
+                                  const void* c);
+/* reductions return a host double; accumulation is FP64, fixed order */
+int te_vec_two_norm(const te_domain* d, int ncomp, int dtype, const void* x, double* out);
+int te_vec_inf_norm(const te_domain* d, int ncomp, int dtype, const void* x, double* out);
+int te_vec_dot(const te_domain* d, int ncomp, int dtype, const void* x, const void* b,
+               double* out);
+/* precision conversion between level buffers of the same domain (all cells) */
+int te_vec_convert(const te_domain* d, int ncomp, int dst_dtype, void* dst, int src_dtype,
+                   const void* src);
+
+/* ---- GhostFiller<D> (GhostFiller.h:46, MPIGhostFiller.h:956-1092) -------- */
+int te_ghost_filler_create(const te_domain* d, int scheme, int fill_type, te_ghost_filler** out);
+int te_ghost_filler_destroy(te_ghost_filler* g);
+int te_ghost_fill(const te_ghost_filler* g, int ncomp, int dtype, void* u);
+/* Length of the call list (number of fillGhostCellsFor*NbrPatch calls per
+ * fill) and the list itself, in the reference's enumeration order
+ * (MPIGhostFiller.h:821-895): rows of
+ * {caller local index, nbr local index, face dimensionality M, face index,
+ *  nbr type, orthant}. */
+int te_ghost_filler_num_calls(const te_ghost_filler* g);
+int te_ghost_filler_calls(const te_ghost_filler* g, int* rows6);
+
+/* ---- PatchOperator<D> (PatchOperator.h:126-143) ------------------------- */
+/* Poisson::StarPatchOperator (Poisson/StarPatchOperator.h:52-63) */
+int te_poisson_operator_create(const te_domain* d, const te_ghost_filler* g, int neumann,
+                               te_operator** out);
+/* VarPoisson::StarPatchOperator (VarPoisson/StarPatchOperator.h:61-71):
+ * coeffs is a device FP64 level buffer with 1 component, ghosts included;
+ * it is copied and its ghosts filled with g. */
+int te_varpoisson_operator_create(const te_domain* d, const te_ghost_filler* g,
+                                  const void* coeffs, te_operator** out);
+int te_operator_destroy(te_operator* op);
+/* f = A u  (f.setWithGhost(0); fillGhost(u); applySinglePatch per patch) */
+int te_operator_apply(const te_operator* op, int ncomp, int dtype, void* u, void* f);
+/* modifyRHSForInternalBoundaryConditions on every patch: f_in -= ... using
+ * u's ghosts (which the caller has filled) */
+int te_operator_modify_rhs(const te_operator* op, int ncomp, int dtype, const void* u, void* f);
+
+/* ---- PatchSolver<D> / GMG::Smoother<D> (PatchSolver.h:107-170) ---------- */
+/* Poisson::DFTPatchSolver (Poisson/DFTPatchSolver.h:385-450); neumann_mask
+ * bit i = Side index i is Neumann (when it has no neighbour). */
+int te_dft_patch_solver_create(const te_operator* op, int neumann_mask, te_patch_solver** out);
+/* Iterative::PatchSolver with an inner BiCGStab (Iterative/PatchSolver.h:121-175) */
+int te_bicgstab_patch_solver_create(const te_operator* op, double tol, int max_iterations,
+                                    int continue_on_breakdown, te_patch_solver** out);
+int te_patch_solver_destroy(te_patch_solver* s);
+/* smooth: fillGhost(u), then solveSinglePatch on every patch (block Jacobi) */
+int te_patch_solver_smooth(const te_patch_solver* s, int ncomp, int dtype, const void* f, void* u);
+/* apply: u.setWithGhost(0), then solveSinglePatch on every patch */
+int te_patch_solver_apply(const te_patch_solver* s, int ncomp, int dtype, const void* f, void* u);
+
+/* ---- GMG transfers -------------------------------------------------------- */
+/* GMG::LinearRestrictor (GMG/LinearRestrictor.h:166-191, MPIRestrictor.h:55-83)
+ * coarse_out is overwritten (ghosts included). */
+int te_linear_restrictor_create(const te_domain* fine, const te_domain* coarse,
+                                int extrapolate_boundary_ghosts, te_restrictor** out);
+int te_restrictor_destroy(te_restrictor* r);
+int te_restrict(const te_restrictor* r, int ncomp, int dtype, const void* fine, void* coarse_out);
+/* GMG::DirectInterpolator (GMG/DirectInterpolator.h:60-91): fine += P coarse */
+int te_direct_interpolator_create(const te_domain* coarse, const te_domain* fine,
+                                  te_interpolator** out);
+int te_interpolator_destroy(te_interpolator* i);
+int te_interpolate(const te_interpolator* i, int ncomp, int dtype, const void* coarse, void* fine);
+
+/* ---- GMG::Cycle (GMG/Cycle.h:94-98, VCycle.h:46-70, CycleBuilder.h:97-192) */
+typedef struct te_cycle_level {
+  const te_operator* op;           /* level operator                        */
+  const te_patch_solver* smoother; /* level smoother                        */
+  const te_restrictor* restrictor; /* to the next coarser level (NULL at coarsest) */
+  const te_interpolator* interpolator; /* from this level to the next finer (NULL at finest) */
+} te_cycle_level;
+typedef struct te_cycle_opts {
+  int pre_sweeps, post_sweeps, mid_sweeps, coarse_sweeps; /* CycleOpts.h:33-55 */
+} te_cycle_opts;
+/* levels[0] is the finest.  All level objects must be FP64-capable; the
+ * cycle runs in `dtype` internally (TE_F32 = mixed-precision V-cycle: the
+ * cycle converts f to FP32, cycles in FP32 and writes FP64 u). */
+int te_vcycle_create(const te_cycle_level* levels, int num_levels, te_cycle_opts opts, int dtype,
+                     te_cycle** out);
+int te_cycle_destroy(te_cycle* c);
+/* u = M f  (u.setWithGhost(0); visit(finest, f, u)); f and u are FP64 */
+int te_cycle_apply(const te_cycle* c, int ncomp, const void* f, void* u);
+
+/* ---- Iterative::BiCGStab (Iterative/BiCGStab.h:111-203) ------------------- */
+/* Right-preconditioned BiCGStab in FP64 on device vectors of A's domain.
+ * M may be NULL.  Stops when ||r||/||b|| <= tol.  Returns TE_ERR_BREAKDOWN
+ * when rho == 0 (the reference throws BreakdownError). */
+int te_bicgstab_solve(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M,
+                      double tol, int max_iterations, int* iterations, double* final_residual);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TE_GPU_H */

@@ -1,0 +1,28 @@
+/* te_oracle.h -- TEST INFRASTRUCTURE ONLY: C API shared by the oracle
+ * restatement (te_oracle.cpp, prefix teo_) and by the reference driver
+ * (ref/teref.cpp, prefix teref_).  Host pointers throughout; vectors use the
+ * level layout of include/te_gpu.h. */
+#ifndef TE_ORACLE_H
+#define TE_ORACLE_H
+#include "te_gpu.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+typedef struct teo_gmg_config {
+  int scheme, fill_type;  /* ghost filler of every level                   */
+  int op_kind;            /* 0 Poisson::StarPatchOperator, 1 VarPoisson     */
+  int neumann;            /* Poisson operator neumann flag                  */
+  int smoother;           /* 0 DFTPatchSolver, 1 Iterative::PatchSolver     */
+  int dft_neumann_mask;
+  double inner_tol;       /* inner BiCGStab of the patch solver             */
+  int inner_max_it, inner_continue_on_breakdown;
+  int pre_sweeps, post_sweeps, coarse_sweeps;
+  int extrapolate_boundary_ghosts;
+  double tol;             /* outer BiCGStab                                 */
+  int max_it;
+  int use_precond;        /* 0: BiCGStab without the V-cycle                */
+} teo_gmg_config;
+#ifdef __cplusplus
+}
+#endif
+#endif

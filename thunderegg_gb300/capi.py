@@ -1,0 +1,138 @@
+"""ctypes binding of the C ABI declared in include/te_gpu.h.
+
+The shared library ``thunderegg_gb300/_build/libte_gpu.so`` is built in-tree
+by :func:`thunderegg_gb300.build.build`.  Loading fails loudly when it is
+missing: there is no fallback path.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libte_gpu.so")
+
+TE_OK, TE_ERR_INVALID, TE_ERR_CUDA, TE_ERR_BREAKDOWN = 0, 1, 2, 3
+TE_ERR_UNSUPPORTED, TE_ERR_BUDGET, TE_ERR_TIMEOUT, TE_ERR_NOT_CONVERGED = 4, 5, 6, 7
+TE_F64, TE_F32 = 0, 1
+TE_GHOST_BILINEAR, TE_GHOST_BIQUADRATIC, TE_GHOST_TRILINEAR = 0, 1, 2
+TE_FILL_FACES, TE_FILL_EDGES, TE_FILL_CORNERS = 0, 1, 2
+
+_ip = ctypes.POINTER(ctypes.c_int)
+_dp = ctypes.POINTER(ctypes.c_double)
+
+
+class TeLevelDesc(ctypes.Structure):
+    _fields_ = [
+        ("dim", ctypes.c_int), ("ns", ctypes.c_int * 3), ("num_ghost", ctypes.c_int),
+        ("num_patches", ctypes.c_int),
+        ("id", _ip), ("refine_level", _ip), ("parent_id", _ip), ("orth_on_parent", _ip),
+        ("child_ids", _ip), ("starts", _dp), ("spacings", _dp),
+        ("nbr_type", _ip), ("nbr_ids", _ip), ("nbr_orth", _ip),
+    ]
+
+
+class TeCycleLevel(ctypes.Structure):
+    _fields_ = [("op", ctypes.c_void_p), ("smoother", ctypes.c_void_p),
+                ("restrictor", ctypes.c_void_p), ("interpolator", ctypes.c_void_p)]
+
+
+class TeCycleOpts(ctypes.Structure):
+    _fields_ = [("pre_sweeps", ctypes.c_int), ("post_sweeps", ctypes.c_int),
+                ("mid_sweeps", ctypes.c_int), ("coarse_sweeps", ctypes.c_int)]
+
+
+class TeError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"te_gpu error {code}: {msg}")
+        self.code = code
+
+
+class BreakdownError(TeError):
+    """Mirror of ThunderEgg::Iterative::BreakdownError (BreakdownError.h:35-44)."""
+
+
+_V = ctypes.c_void_p
+_I = ctypes.c_int
+_D = ctypes.c_double
+_SIGS = {
+    "te_last_error_message": (ctypes.c_char_p, []),
+    "te_set_stream": (_I, [_V]),
+    "te_synchronize": (_I, []),
+    "te_kernel_launch_count": (ctypes.c_longlong, []),
+    "te_domain_create": (_I, [ctypes.POINTER(TeLevelDesc), ctypes.POINTER(_V)]),
+    "te_domain_destroy": (_I, [_V]),
+    "te_domain_patch_stride": (ctypes.c_longlong, [_V, _I]),
+    "te_domain_num_patches": (_I, [_V]),
+    "te_vec_set": (_I, [_V, _I, _I, _V, _D, _I]),
+    "te_vec_scale": (_I, [_V, _I, _I, _V, _D]),
+    "te_vec_shift": (_I, [_V, _I, _I, _V, _D]),
+    "te_vec_copy": (_I, [_V, _I, _I, _V, _V, _I]),
+    "te_vec_add": (_I, [_V, _I, _I, _V, _V]),
+    "te_vec_add_scaled": (_I, [_V, _I, _I, _V, _D, _V]),
+    "te_vec_add_scaled2": (_I, [_V, _I, _I, _V, _D, _V, _D, _V]),
+    "te_vec_scale_then_add": (_I, [_V, _I, _I, _V, _D, _V]),
+    "te_vec_scale_then_add_scaled": (_I, [_V, _I, _I, _V, _D, _D, _V]),
+    "te_vec_scale_then_add_scaled2": (_I, [_V, _I, _I, _V, _D, _D, _V, _D, _V]),
+    "te_vec_two_norm": (_I, [_V, _I, _I, _V, _dp]),
+    "te_vec_inf_norm": (_I, [_V, _I, _I, _V, _dp]),
+    "te_vec_dot": (_I, [_V, _I, _I, _V, _V, _dp]),
+    "te_vec_convert": (_I, [_V, _I, _I, _V, _I, _V]),
+    "te_ghost_filler_create": (_I, [_V, _I, _I, ctypes.POINTER(_V)]),
+    "te_ghost_filler_destroy": (_I, [_V]),
+    "te_ghost_fill": (_I, [_V, _I, _I, _V]),
+    "te_ghost_filler_num_calls": (_I, [_V]),
+    "te_ghost_filler_calls": (_I, [_V, _ip]),
+    "te_poisson_operator_create": (_I, [_V, _V, _I, ctypes.POINTER(_V)]),
+    "te_varpoisson_operator_create": (_I, [_V, _V, _V, ctypes.POINTER(_V)]),
+    "te_operator_destroy": (_I, [_V]),
+    "te_operator_apply": (_I, [_V, _I, _I, _V, _V]),
+    "te_operator_modify_rhs": (_I, [_V, _I, _I, _V, _V]),
+    "te_dft_patch_solver_create": (_I, [_V, _I, ctypes.POINTER(_V)]),
+    "te_bicgstab_patch_solver_create": (_I, [_V, _D, _I, _I, ctypes.POINTER(_V)]),
+    "te_patch_solver_destroy": (_I, [_V]),
+    "te_patch_solver_smooth": (_I, [_V, _I, _I, _V, _V]),
+    "te_patch_solver_apply": (_I, [_V, _I, _I, _V, _V]),
+    "te_linear_restrictor_create": (_I, [_V, _V, _I, ctypes.POINTER(_V)]),
+    "te_restrictor_destroy": (_I, [_V]),
+    "te_restrict": (_I, [_V, _I, _I, _V, _V]),
+    "te_direct_interpolator_create": (_I, [_V, _V, ctypes.POINTER(_V)]),
+    "te_interpolator_destroy": (_I, [_V]),
+    "te_interpolate": (_I, [_V, _I, _I, _V, _V]),
+    "te_vcycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, ctypes.POINTER(_V)]),
+    "te_cycle_destroy": (_I, [_V]),
+    "te_cycle_apply": (_I, [_V, _I, _V, _V]),
+    "te_bicgstab_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, _ip, _dp]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded te_gpu library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(rc):
+    if rc != TE_OK:
+        msg = lib().te_last_error_message()
+        msg = msg.decode() if msg else ""
+        if rc == TE_ERR_BREAKDOWN:
+            raise BreakdownError(rc, msg)
+        raise TeError(rc, msg)
+    return rc
+
+
+def exported_symbols():
+    return list(_SIGS)
