@@ -204,9 +204,15 @@ int te_cycle_apply(const te_cycle* c, int ncomp, const void* f, void* u);
 /* ---- Iterative::BiCGStab (Iterative/BiCGStab.h:111-203) ------------------- */
 /* Right-preconditioned BiCGStab in FP64 on device vectors of A's domain.
  * M may be NULL.  Stops when ||r||/||b|| <= tol.  Returns TE_ERR_BREAKDOWN
- * when rho == 0 (the reference throws BreakdownError). */
+ * when rho == 0 (the reference throws BreakdownError).
+ * flags: 0 = the reference's update rule exactly; TE_BICGSTAB_PRECONDITIONED_EXIT
+ * = on the early exit (||s|| small) add alpha * M p instead of alpha * p
+ * (the reference adds alpha * p, BiCGStab.h:160-168, which leaves the true
+ * residual of a preconditioned solve well above tol). */
+enum { TE_BICGSTAB_PRECONDITIONED_EXIT = 1 };
 int te_bicgstab_solve(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M,
-                      double tol, int max_iterations, int* iterations, double* final_residual);
+                      double tol, int max_iterations, int flags, int* iterations,
+                      double* final_residual);
 
 #ifdef __cplusplus
 }

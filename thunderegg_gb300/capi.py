@@ -102,7 +102,7 @@ _SIGS = {
     "te_vcycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, ctypes.POINTER(_V)]),
     "te_cycle_destroy": (_I, [_V]),
     "te_cycle_apply": (_I, [_V, _I, _V, _V]),
-    "te_bicgstab_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, _ip, _dp]),
+    "te_bicgstab_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, _I, _ip, _dp]),
 }
 
 _lib = None

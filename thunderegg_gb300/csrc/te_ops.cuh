@@ -1,0 +1,45 @@
+// te_ops.cuh -- operator and patch-solver handles (internal).
+#pragma once
+#include "te_ghost.cuh"
+
+struct te_operator {
+  const te_domain* dom = nullptr;
+  const te_ghost_filler* gf = nullptr;
+  int kind = 0;  // 0 Poisson::StarPatchOperator, 1 VarPoisson::StarPatchOperator
+  int neumann = 0;
+  te::DevBuf<double> coeffs;    // VarPoisson: ghost-filled coefficient level buffer (1 component)
+  te::DevBuf<float> coeffs_f;   // FP32 copy for the mixed-precision cycle
+  te::FaceTable faces;
+  const void* coeff_ptr(int dtype) const {
+    return kind == 0 ? nullptr : (dtype == TE_F64 ? (const void*)coeffs.p : (const void*)coeffs_f.p);
+  }
+};
+
+struct te_patch_solver {
+  const te_operator* op = nullptr;
+  int kind = 0;  // 0 DFT, 1 BiCGStab patch solver
+  // DFT plans (Poisson/DFTPatchSolver.h:385-413)
+  int neumann_mask = 0;
+  int nplans = 0;
+  te::DevBuf<int> plan_of_patch;       // [P]
+  te::DevBuf<int> plan_mats;           // [nplans * 6]: fwd matrix id per axis, inv matrix id per axis
+  te::DevBuf<double> mats;             // transposed matrices, n*n each, concatenated
+  te::DevBuf<float> mats_f;
+  te::DevBuf<int> mat_off;             // offset of each matrix
+  te::DevBuf<double> inv_eig;          // [nplans * n0*n1*n2]  1 / eigenvalue
+  te::DevBuf<float> inv_eig_f;
+  te::DevBuf<int> zero_mode;           // [P] pure-Neumann patch without neighbours
+  // BiCGStab patch solver (Iterative/PatchSolver.h:121-175)
+  double tol = 1e-12;
+  int max_it = 1000;
+  int cont = 1;
+  te::DevBuf<unsigned long long> its;  // total inner iterations (statistics)
+  te::DevBuf<int> status;              // breakdown flag
+  mutable te::DevBuf<char> scratch;    // global-memory fallback for large patches
+};
+
+namespace te {
+void operator_apply(const te_operator* op, int nc, int dtype, void* u, void* f, cudaStream_t s);
+void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, void* u, bool zero_first,
+                  cudaStream_t s);
+}  // namespace te

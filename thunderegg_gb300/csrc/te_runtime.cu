@@ -1,0 +1,455 @@
+// te_runtime.cu -- library state, Domain upload and Vector<D> algebra.
+//
+// Vector algebra follows ThunderEgg's Vector<D> (Vector.h:391-611): every
+// operation touches interior cells only (ghosts preserved) unless it is one
+// of the *WithGhost variants.  Reductions accumulate in FP64 in a fixed order
+// (per-block tree, then the block partials in index order), so repeated runs
+// are bit-identical.
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "te_internal.cuh"
+
+namespace te {
+
+static thread_local std::string t_err;
+static cudaStream_t g_stream = nullptr;
+std::atomic<long long> g_launches{0};
+
+void set_error(const std::string& msg) { t_err = msg; }
+
+int guard_impl(void (*fn)(void*), void* ctx) {
+  try {
+    fn(ctx);
+    return TE_OK;
+  } catch (const Error& e) {
+    t_err = e.what();
+    return e.code;
+  } catch (const std::exception& e) {
+    t_err = e.what();
+    return TE_ERR_INVALID;
+  }
+}
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) throw Error(TE_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+cudaStream_t current_stream() { return g_stream; }
+
+// ---------------------------------------------------------------------------
+// element access in either precision
+// ---------------------------------------------------------------------------
+template <class T>
+struct Elem;
+
+// one thread per interior cell of (P x nc) padded patches
+__device__ __forceinline__ long long interior_index(const Layout& L, int nc, long long i) {
+  int x = (int)(i % L.n0);
+  long long r = i / L.n0;
+  int y = (int)(r % L.n1);
+  r /= L.n1;
+  int z = (int)(r % L.n2);
+  r /= L.n2;  // r = p * nc + c
+  return r * L.cs + L.at(x, y, z);
+}
+
+template <class T, int OP>
+__global__ void vec_kernel(Layout L, int nc, long long n, T* x, const T* a, const T* b, double alpha,
+                           double beta, double gamma) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long k = interior_index(L, nc, i);
+    T xv = x[k];
+    if (OP == OP_SET) xv = (T)alpha;
+    if (OP == OP_SCALE) xv *= (T)alpha;
+    if (OP == OP_SHIFT) xv += (T)alpha;
+    if (OP == OP_COPY) xv = a[k];
+    if (OP == OP_ADD) xv += a[k];
+    // reference: view += b_view * alpha  (Vector.h:495)
+    if (OP == OP_ADD_SCALED) xv += a[k] * (T)alpha;
+    // view += a * alpha + b * beta  (Vector.h:507-511)
+    if (OP == OP_ADD_SCALED2) xv += a[k] * (T)alpha + b[k] * (T)beta;
+    // view = view * alpha + b  (Vector.h:523)
+    if (OP == OP_SCALE_THEN_ADD) xv = xv * (T)alpha + a[k];
+    if (OP == OP_SCALE_THEN_ADD_SCALED) xv = xv * (T)alpha + a[k] * (T)beta;
+    if (OP == OP_SCALE_THEN_ADD_SCALED2) xv = xv * (T)alpha + a[k] * (T)beta + b[k] * (T)gamma;
+    x[k] = xv;
+  }
+}
+
+template <class T>
+__global__ void fill_all_kernel(T* x, long long n, T v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = v;
+}
+
+template <class TD, class TS>
+__global__ void convert_kernel(TD* dst, const TS* src, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (TD)src[i];
+}
+
+static int grid_for(long long n, int block = 256) {
+  long long g = (n + block - 1) / block;
+  int cap = 152 * 16;
+  return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+template <class T>
+static void launch_vec(const te_domain* d, int nc, int op, T* x, const T* a, const T* b, double al,
+                       double be, double ga, cudaStream_t s) {
+  long long n = (long long)d->lay.P * nc * d->lay.interior();
+  if (n == 0) return;
+  int grid = grid_for(n);
+#define TE_VEC_CASE(OPV)                                                                   \
+  case OPV:                                                                                \
+    vec_kernel<T, OPV><<<grid, 256, 0, s>>>(d->lay, nc, n, x, a, b, al, be, ga);          \
+    break;
+  switch (op) {
+    TE_VEC_CASE(OP_SET)
+    TE_VEC_CASE(OP_SCALE)
+    TE_VEC_CASE(OP_SHIFT)
+    TE_VEC_CASE(OP_COPY)
+    TE_VEC_CASE(OP_ADD)
+    TE_VEC_CASE(OP_ADD_SCALED)
+    TE_VEC_CASE(OP_ADD_SCALED2)
+    TE_VEC_CASE(OP_SCALE_THEN_ADD)
+    TE_VEC_CASE(OP_SCALE_THEN_ADD_SCALED)
+    TE_VEC_CASE(OP_SCALE_THEN_ADD_SCALED2)
+  }
+#undef TE_VEC_CASE
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
+void vec_dispatch(const te_domain* d, int nc, int dtype, int op, void* x, const void* a,
+                         const void* b, double al, double be, double ga) {
+  require(d != nullptr && x != nullptr, "null domain or vector");
+  require(nc >= 1, "ncomp must be >= 1");
+  cudaStream_t s = d->stream;
+  if (dtype == TE_F64)
+    launch_vec<double>(d, nc, op, (double*)x, (const double*)a, (const double*)b, al, be, ga, s);
+  else if (dtype == TE_F32)
+    launch_vec<float>(d, nc, op, (float*)x, (const float*)a, (const float*)b, al, be, ga, s);
+  else
+    throw Error(TE_ERR_INVALID, "bad dtype");
+}
+
+// ---------------------------------------------------------------------------
+// deterministic reductions: block tree + last-block-done final pass
+// ---------------------------------------------------------------------------
+constexpr int RED_THREADS = 256;
+
+__device__ __forceinline__ double warp_sum(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  return v;
+}
+
+template <bool MAX>
+__device__ double block_reduce(double v) {
+  __shared__ double sm[RED_THREADS / 32];
+  v = MAX ? warp_max(v) : warp_sum(v);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    v = l < RED_THREADS / 32 ? sm[l] : (MAX ? 0.0 : 0.0);
+    v = MAX ? warp_max(v) : warp_sum(v);
+  }
+  return v;
+}
+
+// MODE 0: dot(x, y); MODE 1: max(x) with 0 floor (Vector::infNorm, Vector.h:568-578)
+template <class T, int MODE>
+__global__ void reduce_kernel(Layout L, int nc, long long n, const T* x, const T* y, double* partials,
+                              unsigned int* counter, double* out) {
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long k = interior_index(L, nc, i);
+    if (MODE == 0)
+      acc += (double)x[k] * (double)y[k];
+    else
+      acc = fmax((double)x[k], acc);
+  }
+  double b = block_reduce<MODE == 1>(acc);
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = b;
+    __threadfence();
+    unsigned int done = atomicAdd(counter, 1u);
+    last = (done == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    double v = 0.0;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+      double pv = ((volatile double*)partials)[i];
+      v = MODE == 0 ? v + pv : fmax(v, pv);
+    }
+    v = block_reduce<MODE == 1>(v);
+    if (threadIdx.x == 0) {
+      *out = v;
+      *counter = 0u;
+    }
+  }
+}
+
+static void reduce_launch(const te_domain* d, int nc, int dtype, const void* x, const void* y, int mode,
+                          double* d_out, cudaStream_t s) {
+  long long n = (long long)d->lay.P * nc * d->lay.interior();
+  int grid = d->red_blocks;
+  if (dtype == TE_F64) {
+    if (mode == 0)
+      reduce_kernel<double, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, nc, n, (const double*)x, (const double*)y,
+                                                            d->d_partials.p, d->d_counter.p, d_out);
+    else
+      reduce_kernel<double, 1><<<grid, RED_THREADS, 0, s>>>(d->lay, nc, n, (const double*)x, nullptr,
+                                                            d->d_partials.p, d->d_counter.p, d_out);
+  } else {
+    if (mode == 0)
+      reduce_kernel<float, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, nc, n, (const float*)x, (const float*)y,
+                                                           d->d_partials.p, d->d_counter.p, d_out);
+    else
+      reduce_kernel<float, 1><<<grid, RED_THREADS, 0, s>>>(d->lay, nc, n, (const float*)x, nullptr,
+                                                           d->d_partials.p, d->d_counter.p, d_out);
+  }
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
+void reduce_dot(const te_domain* d, int nc, int dtype, const void* x, const void* y, double* d_out,
+                cudaStream_t s) {
+  reduce_launch(d, nc, dtype, x, y, 0, d_out, s);
+}
+void reduce_max(const te_domain* d, int nc, int dtype, const void* x, double* d_out, cudaStream_t s) {
+  reduce_launch(d, nc, dtype, x, nullptr, 1, d_out, s);
+}
+
+static double reduce_host(const te_domain* d, int nc, int dtype, const void* x, const void* y, int mode) {
+  require(d && x, "null domain or vector");
+  reduce_launch(d, nc, dtype, x, y, mode, d->d_result.p, d->stream);
+  TE_CUDA(cudaMemcpyAsync(d->h_result, d->d_result.p, sizeof(double), cudaMemcpyDeviceToHost, d->stream));
+  TE_CUDA(cudaStreamSynchronize(d->stream));
+  return *d->h_result;
+}
+
+void convert_level(const te_domain* d, int nc, int dst_dtype, void* dst, int src_dtype, const void* src,
+                   cudaStream_t s) {
+  long long n = (long long)d->lay.P * d->lay.pstride(nc);
+  int grid = grid_for(n);
+  if (dst_dtype == TE_F32 && src_dtype == TE_F64)
+    convert_kernel<float, double><<<grid, 256, 0, s>>>((float*)dst, (const double*)src, n);
+  else if (dst_dtype == TE_F64 && src_dtype == TE_F32)
+    convert_kernel<double, float><<<grid, 256, 0, s>>>((double*)dst, (const float*)src, n);
+  else if (dst_dtype == src_dtype) {
+    TE_CUDA(cudaMemcpyAsync(dst, src, n * (dst_dtype == TE_F64 ? 8 : 4), cudaMemcpyDeviceToDevice, s));
+    return;
+  } else
+    throw Error(TE_ERR_INVALID, "bad dtype");
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
+}  // namespace te
+
+te_domain::~te_domain() {
+  if (h_result) cudaFreeHost(h_result);
+}
+
+using namespace te;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* te_last_error_message(void) { return t_err.c_str(); }
+
+int te_set_stream(void* s) {
+  g_stream = (cudaStream_t)s;
+  return TE_OK;
+}
+
+int te_synchronize(void) {
+  return guard([&] { TE_CUDA(cudaStreamSynchronize(g_stream)); });
+}
+
+long long te_kernel_launch_count(void) { return g_launches.load(); }
+
+int te_domain_create(const te_level_desc* desc, te_domain** out) {
+  return guard([&] {
+    require(desc && out, "null argument");
+    require(desc->dim == 2 || desc->dim == 3, "dim must be 2 or 3");
+    require(desc->num_ghost >= 1, "num_ghost must be >= 1");
+    require(desc->num_patches >= 1, "num_patches must be >= 1");
+    auto d = std::make_unique<te_domain>();
+    int D = desc->dim, P = desc->num_patches;
+    d->stream = g_stream;
+    Layout& L = d->lay;
+    L.D = D;
+    L.n0 = desc->ns[0];
+    L.n1 = D > 1 ? desc->ns[1] : 1;
+    L.n2 = D > 2 ? desc->ns[2] : 1;
+    for (int a = 0; a < D; a++) require(desc->ns[a] >= 1, "ns must be >= 1");
+    L.g = desc->num_ghost;
+    L.P = P;
+    int g = L.g;
+    L.sy = L.n0 + 2 * g;
+    L.sz = D > 2 ? L.sy * (L.n1 + 2 * g) : 0;
+    L.cs = D > 2 ? L.sz * (L.n2 + 2 * g) : L.sy * (L.n1 + 2 * g);
+    if (D == 2) L.sz = 0;
+    int F = num_slots(D), C = 1 << D;
+    d->F = F;
+    d->id.assign(desc->id, desc->id + P);
+    d->refine_level.assign(desc->refine_level, desc->refine_level + P);
+    d->parent_id.assign(desc->parent_id, desc->parent_id + P);
+    d->orth_on_parent.assign(desc->orth_on_parent, desc->orth_on_parent + P);
+    d->child_ids.assign(desc->child_ids, desc->child_ids + (size_t)P * C);
+    d->starts.assign(desc->starts, desc->starts + (size_t)P * D);
+    d->spacings.assign(desc->spacings, desc->spacings + (size_t)P * D);
+    d->nbr_type.assign(desc->nbr_type, desc->nbr_type + (size_t)P * F);
+    d->nbr_ids.assign(desc->nbr_ids, desc->nbr_ids + (size_t)P * F * 4);
+    d->nbr_orth.assign(desc->nbr_orth, desc->nbr_orth + (size_t)P * F);
+    // Domain::indexPatchesLocal (Domain.h:94-110): local index = position
+    for (int p = 0; p < P; p++) {
+      require(d->id2l.count(d->id[p]) == 0, "duplicate patch id");
+      d->id2l[d->id[p]] = p;
+    }
+    d->nbr_local.assign((size_t)P * F * 4, -1);
+    for (int p = 0; p < P; p++)
+      for (int s = 0; s < F; s++) {
+        int t = d->nbr_type[(size_t)p * F + s];
+        if (t < 0) continue;
+        require(t <= 2, "bad neighbour type");
+        int nn = 1;
+        if (t == TE_NBR_FINE) {
+          int M = (D == 2) ? (s < 4 ? 0 : 1) : (s < 8 ? 0 : (s < 20 ? 1 : 2));
+          nn = 1 << M;
+        }
+        for (int i = 0; i < nn; i++) {
+          auto it = d->id2l.find(d->nbr_ids[((size_t)p * F + s) * 4 + i]);
+          require(it != d->id2l.end(), "neighbour id not on this level (multi-rank meshes are not supported)");
+          d->nbr_local[((size_t)p * F + s) * 4 + i] = it->second;
+        }
+      }
+    cudaStream_t st = d->stream;
+    std::vector<int8_t> t8(d->nbr_type.begin(), d->nbr_type.end()), o8(d->nbr_orth.begin(), d->nbr_orth.end());
+    d->d_nbr_type.upload(t8, st);
+    d->d_nbr_orth.upload(o8, st);
+    d->d_nbr_local.upload(d->nbr_local, st);
+    d->d_spacings.upload(d->spacings, st);
+    std::vector<float> spf(d->spacings.begin(), d->spacings.end());
+    d->d_spacings_f.upload(spf, st);
+    d->red_blocks = 152 * 2;
+    d->d_partials.alloc(d->red_blocks);
+    d->d_counter.alloc(1);
+    TE_CUDA(cudaMemsetAsync(d->d_counter.p, 0, sizeof(unsigned int), st));
+    d->d_result.alloc(1);
+    TE_CUDA(cudaMallocHost(&d->h_result, sizeof(double)));
+    TE_CUDA(cudaStreamSynchronize(st));
+    *out = d.release();
+  });
+}
+
+int te_domain_destroy(te_domain* d) {
+  delete d;
+  return TE_OK;
+}
+
+long long te_domain_patch_stride(const te_domain* d, int ncomp) { return d ? d->lay.pstride(ncomp) : -1; }
+int te_domain_num_patches(const te_domain* d) { return d ? d->lay.P : -1; }
+
+int te_vec_set(const te_domain* d, int nc, int dt, void* x, double alpha, int with_ghost) {
+  return guard([&] {
+    require(d && x, "null argument");
+    if (with_ghost) {  // Vector::setWithGhost (Vector.h:404-412)
+      long long n = (long long)d->lay.P * d->lay.pstride(nc);
+      if (dt == TE_F64)
+        fill_all_kernel<double><<<grid_for(n), 256, 0, d->stream>>>((double*)x, n, alpha);
+      else
+        fill_all_kernel<float><<<grid_for(n), 256, 0, d->stream>>>((float*)x, n, (float)alpha);
+      count_launch();
+      TE_LAUNCH_CHECK();
+    } else {
+      vec_dispatch(d, nc, dt, OP_SET, x, nullptr, nullptr, alpha, 0, 0);
+    }
+  });
+}
+int te_vec_scale(const te_domain* d, int nc, int dt, void* x, double alpha) {
+  return guard([&] { vec_dispatch(d, nc, dt, OP_SCALE, x, nullptr, nullptr, alpha, 0, 0); });
+}
+int te_vec_shift(const te_domain* d, int nc, int dt, void* x, double delta) {
+  return guard([&] { vec_dispatch(d, nc, dt, OP_SHIFT, x, nullptr, nullptr, delta, 0, 0); });
+}
+int te_vec_copy(const te_domain* d, int nc, int dt, void* x, const void* b, int with_ghost) {
+  return guard([&] {
+    require(d && x && b, "null argument");
+    if (with_ghost) {  // Vector::copyWithGhost (Vector.h:455-463)
+      long long n = (long long)d->lay.P * d->lay.pstride(nc);
+      TE_CUDA(cudaMemcpyAsync(x, b, n * (dt == TE_F64 ? 8 : 4), cudaMemcpyDeviceToDevice, d->stream));
+    } else {
+      vec_dispatch(d, nc, dt, OP_COPY, x, b, nullptr, 0, 0, 0);
+    }
+  });
+}
+int te_vec_add(const te_domain* d, int nc, int dt, void* x, const void* b) {
+  return guard([&] { vec_dispatch(d, nc, dt, OP_ADD, x, b, nullptr, 0, 0, 0); });
+}
+int te_vec_add_scaled(const te_domain* d, int nc, int dt, void* x, double alpha, const void* a) {
+  return guard([&] { vec_dispatch(d, nc, dt, OP_ADD_SCALED, x, a, nullptr, alpha, 0, 0); });
+}
+int te_vec_add_scaled2(const te_domain* d, int nc, int dt, void* x, double alpha, const void* a, double beta,
+                       const void* b) {
+  return guard([&] { vec_dispatch(d, nc, dt, OP_ADD_SCALED2, x, a, b, alpha, beta, 0); });
+}
+int te_vec_scale_then_add(const te_domain* d, int nc, int dt, void* x, double alpha, const void* b) {
+  return guard([&] { vec_dispatch(d, nc, dt, OP_SCALE_THEN_ADD, x, b, nullptr, alpha, 0, 0); });
+}
+int te_vec_scale_then_add_scaled(const te_domain* d, int nc, int dt, void* x, double alpha, double beta,
+                                 const void* b) {
+  return guard([&] { vec_dispatch(d, nc, dt, OP_SCALE_THEN_ADD_SCALED, x, b, nullptr, alpha, beta, 0); });
+}
+int te_vec_scale_then_add_scaled2(const te_domain* d, int nc, int dt, void* x, double alpha, double beta,
+                                  const void* b, double gamma, const void* c) {
+  return guard([&] { vec_dispatch(d, nc, dt, OP_SCALE_THEN_ADD_SCALED2, x, b, c, alpha, beta, gamma); });
+}
+int te_vec_two_norm(const te_domain* d, int nc, int dt, const void* x, double* out) {
+  return guard([&] {
+    require(out != nullptr, "null output");
+    *out = std::sqrt(reduce_host(d, nc, dt, x, x, 0));
+  });
+}
+int te_vec_inf_norm(const te_domain* d, int nc, int dt, const void* x, double* out) {
+  return guard([&] {
+    require(out != nullptr, "null output");
+    *out = reduce_host(d, nc, dt, x, nullptr, 1);
+  });
+}
+int te_vec_dot(const te_domain* d, int nc, int dt, const void* x, const void* b, double* out) {
+  return guard([&] {
+    require(out != nullptr && b != nullptr, "null argument");
+    *out = reduce_host(d, nc, dt, x, b, 0);
+  });
+}
+int te_vec_convert(const te_domain* d, int nc, int dst_dtype, void* dst, int src_dtype, const void* src) {
+  return guard([&] {
+    require(d && dst && src, "null argument");
+    convert_level(d, nc, dst_dtype, dst, src_dtype, src, d->stream);
+  });
+}
+
+}  // extern "C"

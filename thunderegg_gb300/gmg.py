@@ -1,0 +1,89 @@
+"""Assemble a full GMG-preconditioned BiCGStab solve on the GPU.
+
+This is the setup a ThunderEgg user writes by hand (see the reference's
+CycleBuilder doc example, GMG/CycleBuilder.h:36-53): one Domain, ghost
+filler, operator and smoother per level, LinearRestrictor/DirectInterpolator
+between levels, a V-cycle, and Iterative::BiCGStab on the finest level.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import (BiCGStab, BiCGStabPatchSolver, BiLinearGhostFiller, BiQuadraticGhostFiller, CycleBuilder,
+               CycleOpts, DFTPatchSolver, DirectInterpolator, Domain, LinearRestrictor,
+               PoissonStarPatchOperator, TriLinearGhostFiller, VarPoissonStarPatchOperator, Vector)
+from .capi import TE_F32, TE_F64
+
+SMOOTHER_DFT, SMOOTHER_BICGSTAB = 0, 1
+
+
+@dataclass
+class GmgOptions:
+    scheme: int = 0                 # 0 BiLinear, 1 BiQuadratic, 2 TriLinear
+    fill_type: int = 0
+    smoother: int = SMOOTHER_DFT
+    inner_tol: float = 1e-12        # BiCGStab patch smoother (pinned as in the oracle)
+    inner_max_it: int = 1000
+    inner_continue_on_breakdown: bool = True
+    pre_sweeps: int = 1
+    post_sweeps: int = 1
+    coarse_sweeps: int = 1
+    extrapolate_boundary_ghosts: bool = False
+    tol: float = 1e-10
+    max_it: int = 1000
+    cycle_dtype: int = TE_F64       # TE_F32: mixed-precision V-cycle
+    bicgstab_flags: int = 0         # 1: preconditioned early-exit update
+
+
+class GmgSolver:
+    """All device objects of one multigrid hierarchy."""
+
+    def __init__(self, levels, opts: GmgOptions = GmgOptions(), coeffs=None):
+        self.levels = levels
+        self.opts = opts
+        fill_cls = [BiLinearGhostFiller, BiQuadraticGhostFiller, TriLinearGhostFiller][opts.scheme]
+        self.domains = [Domain(lv) for lv in levels]
+        self.fillers = [fill_cls(d, opts.fill_type) for d in self.domains]
+        self.coeff_vecs = None
+        if coeffs is not None:
+            self.coeff_vecs = [Vector.from_numpy(d, c) for d, c in zip(self.domains, coeffs)]
+            self.ops = [VarPoissonStarPatchOperator(c, d, g)
+                        for c, d, g in zip(self.coeff_vecs, self.domains, self.fillers)]
+        else:
+            self.ops = [PoissonStarPatchOperator(d, g) for d, g in zip(self.domains, self.fillers)]
+        if opts.smoother == SMOOTHER_DFT:
+            self.smoothers = [DFTPatchSolver(op) for op in self.ops]
+        else:
+            self.smoothers = [BiCGStabPatchSolver(op, opts.inner_tol, opts.inner_max_it,
+                                                  opts.inner_continue_on_breakdown) for op in self.ops]
+        n = len(levels)
+        self.restrictors = [LinearRestrictor(self.domains[k], self.domains[k + 1], opts.extrapolate_boundary_ghosts)
+                            for k in range(n - 1)]
+        self.interpolators = [None] + [DirectInterpolator(self.domains[k], self.domains[k - 1])
+                                       for k in range(1, n)]
+        b = CycleBuilder(CycleOpts(opts.pre_sweeps, opts.post_sweeps, 1, opts.coarse_sweeps))
+        for k in range(n):
+            if k == 0 and n > 1:
+                b.addFinestLevel(self.ops[0], self.smoothers[0], self.restrictors[0])
+            elif k + 1 < n:
+                b.addIntermediateLevel(self.ops[k], self.smoothers[k], self.restrictors[k], self.interpolators[k])
+            else:
+                b.addCoarsestLevel(self.ops[k], self.smoothers[k], self.interpolators[k])
+        self.cycle = b.getCycle(opts.cycle_dtype)
+        self.krylov = BiCGStab(opts.tol, opts.max_it, opts.bicgstab_flags)
+
+    @property
+    def finest(self):
+        return self.domains[0]
+
+    def solve(self, f: Vector, u: Vector, precondition=True):
+        return self.krylov.solve(self.ops[0], u, f, self.cycle if precondition else None)
+
+    def residual(self, f: Vector, u: Vector):
+        """||f - A u|| / ||f|| in FP64 on the device."""
+        r = f.getZeroClone()
+        self.ops[0].apply(u, r)
+        r.scaleThenAdd(-1.0, f)
+        return r.twoNorm() / f.twoNorm()
