@@ -1,0 +1,317 @@
+"""Benchmark: solves/s and latency of the adaptive 2D Poisson GMG solve on GB300.
+
+Workload (one "step" = one complete solve to a 1e-10 relative FP64 residual):
+  2D Poisson -Lap(u) = f on the unit square, quadtree refined from level 3 to
+  level 7 where a leaf box meets the circle r = 0.3 about (0.5, 0.5), 2:1
+  balanced (1444 leaves, 8 GMG levels), 32x32-cell patches, u = exp(xy),
+  Dirichlet data from u; BiQuadratic ghost filling, DFT patch smoother,
+  V(1,1) cycle, BiCGStab outer solver.
+  value: mixed precision (FP32 V-cycle, FP64 BiCGStab/residuals), inputs
+         resident in HBM.  The plain FP64 drop-in is reported beside it.
+  e2e:   the same solve through the C ABI from pinned host buffers: f copied
+         host->device and u device->host inside the timed region.
+  L2: flushed (256 MiB write) between timed steps, outside the step timing.
+
+--impl reference times the CPU restatement of the reference's algorithm
+(oracle/, FP64, same workload) on the host cores, one solve per process.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "solves/s and p99 latency: mixed-prec served vs plain FP64 GMG, 1e-10 resid"
+WORKLOAD = ("2D adaptive Poisson, circle r=0.3 quadtree L3-7 2:1 balanced, 1444 patches 32x32, "
+            "u=exp(xy) Dirichlet, BiQuadratic, DFT smoother, V(1,1), BiCGStab to 1e-10")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--only-mixed", action="store_true",
+                    help="time the mixed-precision solves only (for profiler captures)")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# CPU legs (the oracle is test infrastructure: used here only as the baseline)
+# ---------------------------------------------------------------------------
+def _cpu_solve_worker(q):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    from thunderegg_gb300 import problems as PB
+
+    levels, f, _ = PB.config2()
+    cfg = orc.gmg_config(scheme=1, smoother=0, tol=1e-10)
+    O = orc.Oracle("teo")
+    t = time.perf_counter()
+    u, its, res, rc = O.solve(levels, f, cfg)
+    q.put((time.perf_counter() - t, its, rc))
+
+
+def cpu_solves(nproc):
+    """Run nproc independent solves in parallel processes; returns (wall, [times])."""
+    import multiprocessing as mp
+
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    orc.build()
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    procs = [ctx.Process(target=_cpu_solve_worker, args=(q,)) for _ in range(nproc)]
+    t = time.perf_counter()
+    for p in procs:
+        p.start()
+    out = [q.get() for _ in procs]
+    for p in procs:
+        p.join()
+    return time.perf_counter() - t, out
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    steps, warm = max(1, args.steps), max(0, args.warmup)
+    # bounded: each step is one round of `cores` parallel solves; cap total rounds
+    rounds = min(steps, 3)
+    for _ in range(min(warm, 1)):
+        cpu_solves(cores)
+    walls, its = [], None
+    for _ in range(rounds):
+        w, out = cpu_solves(cores)
+        walls.append(w)
+        its = out[0][1]
+    total = sum(walls)
+    value = rounds * cores / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
+        "steps": rounds, "warmup": min(warm, 1), "ms_per_step": 1000 * total / rounds,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": WORKLOAD, "outer_iterations": its},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{rounds} rounds of {cores} independent full solves, one process per core"},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+class Clocks:
+    def __init__(self, index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import thunderegg_gb300 as te
+    from thunderegg_gb300 import build as tb
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    tb.build()
+    L = te.capi.lib()
+    levels, f_np, exact = PB.config2()
+    mixed = GmgSolver(levels, GmgOptions(scheme=1, smoother=0, tol=1e-10, cycle_dtype=te.TE_F32, bicgstab_flags=1))
+    fp64 = GmgSolver(levels, GmgOptions(scheme=1, smoother=0, tol=1e-10, cycle_dtype=te.TE_F64, bicgstab_flags=1))
+    dom = mixed.finest
+    f = te.Vector.from_numpy(dom, f_np)
+    u = te.Vector(dom)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed_solves(solver, k, warm, host=False):
+        hf = torch.from_numpy(f_np).pin_memory() if host else None
+        hu = torch.empty(f_np.shape, dtype=torch.float64).pin_memory() if host else None
+        times, its, res = [], [], []
+        for i in range(warm + k):
+            flush.fill_(i & 0xFF)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            if host:
+                f.t.copy_(hf, non_blocking=True)
+            u.t.zero_()
+            n = solver.solve(f, u)
+            if host:
+                hu.copy_(u.t, non_blocking=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i >= warm:
+                times.append(e0.elapsed_time(e1) / 1000.0)
+                its.append(n)
+        res = solver.residual(f, u)
+        return times, its, res
+
+    barrier()
+    launches0 = L.te_kernel_launch_count()
+    clk = Clocks(local)
+    t_wall = time.perf_counter()
+    times, its, res = timed_solves(mixed, args.steps, args.warmup)
+    t_wall = time.perf_counter() - t_wall
+    clocks = clk.stop()
+    launches = (L.te_kernel_launch_count() - launches0) * args.steps // (args.steps + args.warmup)
+    barrier()
+    total = sum(times)
+    if world > 1:
+        tt = torch.tensor([total], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        total = float(tt.item())
+    value = world * args.steps / total
+    err = float(np.abs(PB.interior_view(levels[0], u.numpy()) - PB.interior_view(levels[0], exact)).max())
+    if args.only_mixed:
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "solves/s", "ms_per_step": 1000 * total / args.steps,
+                              "outer_iterations": its[-1], "final_rel_residual_fp64": res,
+                              "gpu_launches": int(launches), "clocks": clocks}), flush=True)
+        return
+
+    # e2e through the C ABI from pinned host memory
+    e_times, _, e_res = timed_solves(mixed, max(3, args.steps // 2), 1, host=True)
+    e2e = world * len(e_times) / sum(e_times)
+
+    # plain FP64 drop-in on the same GPU
+    d_times, d_its, d_res = timed_solves(fp64, args.fp64_steps, 1)
+
+    # dominant kernel: FP64 star operator apply on the finest level, timed alone
+    r = te.Vector(dom)
+    for _ in range(3):
+        fp64.ops[0].apply(u, r)
+    nrep = 50
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(nrep):
+        fp64.ops[0].apply(u, r)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    apply_s = e0.elapsed_time(e1) / 1000.0 / nrep
+    cells = levels[0].num_cells
+    n = levels[0].ns[0]
+    alg_bytes = 8 * cells * (2 + 4 / n)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / apply_s / 1e9
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        w, out = cpu_solves(1)
+        cpu = {"value": 1.0 / out[0][0], "unit": "solves/s", "cores": 1, "kind": "port",
+               "sample": "one full FP64 solve of the same workload by the CPU restatement, 1 core"}
+
+    lat = sorted(times)
+    p50 = statistics.median(lat)
+    p99 = lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 V-cycle + f64 Krylov", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "patches": levels[0].num_patches, "levels": len(levels),
+                   "cells": cells, "l2": "flushed between steps (256 MiB write), outside step timing",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "latency_ms": {"p50": 1000 * p50, "p99": 1000 * p99},
+        "outer_iterations": its[-1], "final_rel_residual_fp64": res, "max_err_vs_exact": err,
+        "fp64_dropin": {"value": len(d_times) / sum(d_times), "unit": "solves/s",
+                        "latency_ms_p50": 1000 * statistics.median(d_times), "outer_iterations": d_its[-1],
+                        "final_rel_residual_fp64": d_res},
+        "speedup_mixed_vs_fp64_dropin": value / world / (len(d_times) / sum(d_times)),
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(f_np.nbytes),
+                "d2h_bytes_per_step": int(f_np.nbytes), "final_rel_residual_fp64": e_res},
+        "gpu_launches": int(launches),
+        "roofline": {"kernel": "FP64 ghost fill + star apply, finest level (timed alone)", "bound": "hbm",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": None, "peak_source": "measured" if peaks else "fallback"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "wall_s_timed": t_wall,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

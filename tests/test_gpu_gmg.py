@@ -74,3 +74,88 @@ def test_solve_reaches_tolerance(te, idx, cycle_dtype):
     its = s.solve(fv, uv)
     assert its < 40
     assert s.residual(fv, uv) <= 1e-10
+
+
+@pytest.mark.parametrize("opts", [dict(extrapolate_boundary_ghosts=True),
+                                  dict(pre_sweeps=0, post_sweeps=2, coarse_sweeps=2),
+                                  dict(pre_sweeps=2, post_sweeps=0, coarse_sweeps=1)])
+def test_vcycle_options(te, oracle, opts):
+    """Cycle options and the unfused residual path (ghost extrapolation on)."""
+    from oracle import gmg_config
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels = M.circle_mesh(n=8, lo=2, hi=5)
+    o = GmgOptions(scheme=1, smoother=0, **opts)
+    s = GmgSolver(levels, o)
+    cfg = gmg_config(scheme=1, smoother=0, pre_sweeps=o.pre_sweeps, post_sweeps=o.post_sweeps,
+                     coarse_sweeps=o.coarse_sweeps, extrapolate_boundary_ghosts=int(o.extrapolate_boundary_ghosts))
+    f = np.random.default_rng(40).standard_normal(levels[0].padded_shape(1))
+    want = oracle.vcycle(levels, f, cfg)
+    for dt, tol in ((te.TE_F64, 1e-11), (te.TE_F32, 5e-5)):
+        s2 = GmgSolver(levels, GmgOptions(scheme=1, smoother=0, cycle_dtype=dt, **opts))
+        fv = te.Vector.from_numpy(s2.finest, f)
+        uv = te.Vector(s2.finest)
+        for _ in range(2):  # second application replays the captured graph
+            s2.cycle.apply(fv, uv)
+            g = levels[0].num_ghost
+            inner = (Ellipsis, slice(g, -g), slice(g, -g))
+            assert rel_err(uv.numpy()[inner], want[inner]) <= tol, (dt, opts)
+
+
+def test_solve_no_preconditioner(te, oracle):
+    from oracle import gmg_config
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels = M.uniform_mesh(2, 1, 8)
+    s = GmgSolver(levels, GmgOptions(scheme=0, smoother=0, tol=1e-9))
+    f = np.random.default_rng(41).standard_normal(levels[0].padded_shape(1))
+    u_o, its_o, _, rc = oracle.solve(levels, f, gmg_config(scheme=0, tol=1e-9, use_precond=0))
+    fv, uv = te.Vector.from_numpy(s.finest, f), te.Vector(s.finest)
+    its = s.solve(fv, uv, precondition=False)
+    assert abs(its - its_o) <= 1
+    inner = (Ellipsis, slice(1, -1), slice(1, -1))
+    assert rel_err(uv.numpy()[inner], u_o[inner]) <= 1e-7
+
+
+def test_solve_repeated_and_launch_count(te):
+    """Repeated solves replay cached graphs and give identical results."""
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels = M.circle_mesh(n=8, lo=2, hi=5)
+    s = GmgSolver(levels, GmgOptions(scheme=1, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1))
+    f = np.random.default_rng(42).standard_normal(levels[0].padded_shape(1))
+    fv = te.Vector.from_numpy(s.finest, f)
+    outs = []
+    for _ in range(3):
+        uv = te.Vector(s.finest)
+        n0 = te.capi.lib().te_kernel_launch_count()
+        its = s.solve(fv, uv)
+        assert te.capi.lib().te_kernel_launch_count() - n0 > 10 * its
+        outs.append(uv.numpy())
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
+
+
+@pytest.mark.parametrize("idx", range(3))
+@pytest.mark.parametrize("cycle_dtype", ("f64", "f32"))
+def test_fused_cycle_matches_unfused(te, idx, cycle_dtype, monkeypatch):
+    """The fused per-level kernels give the same V-cycle as the unfused sequence
+    (ghost fill, apply, residual, restrict, interpolate, ghost fill, smooth)."""
+    name, levels, scheme = meshes()[idx]
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    dt = te.TE_F64 if cycle_dtype == "f64" else te.TE_F32
+    f = np.random.default_rng(50 + idx).standard_normal(levels[0].padded_shape(1))
+    outs = []
+    for nofuse in ("0", "1"):
+        monkeypatch.setenv("TE_NO_FUSION", nofuse)
+        s = GmgSolver(levels, GmgOptions(scheme=scheme, smoother=0, cycle_dtype=dt))
+        fv, uv = te.Vector.from_numpy(s.finest, f), te.Vector(s.finest)
+        s.cycle.apply(fv, uv)
+        outs.append(uv.numpy())
+    g = levels[0].num_ghost
+    inner = (Ellipsis,) + tuple(slice(g, -g) for _ in range(levels[0].dim))
+    tol = 1e-12 if cycle_dtype == "f64" else 2e-5
+    assert rel_err(outs[0][inner], outs[1][inner]) <= tol

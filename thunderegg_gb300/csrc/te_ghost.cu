@@ -16,7 +16,7 @@
 #include <array>
 #include <cstring>
 
-#include "te_ghost.cuh"
+#include "te_ghost_dev.cuh"
 
 namespace te {
 
@@ -78,147 +78,6 @@ FaceTable make_face_table(const Layout& L) {
   return t;
 }
 
-// ---------------------------------------------------------------------------
-// device: gather formulas
-// ---------------------------------------------------------------------------
-template <class T>
-struct K {
-  static constexpr T third = T(1.0 / 3.0);
-  static constexpr T two3 = T(2.0 / 3.0);
-  static constexpr T four3 = T(4.0 / 3.0);
-};
-
-// value of the interior slice (depth `dep` along every side of the face) of a patch
-template <class T>
-__device__ __forceinline__ T sv(const T* p, const FaceGeom& g, int dep, int i, int j) {
-  int idx = g.ibase + i * g.tstride[0] + j * g.tstride[1];
-  for (int k = 0; k < g.nsides; k++) idx += dep * g.inward[k];
-  return p[idx];
-}
-
-// ---- BiLinear / TriLinear edges: own Coarse term on a 1-D ghost line
-// (BiLinearGhostFiller.cpp:118-134, TriLinearGhostFiller.cpp:172-195)
-template <class T>
-__device__ __forceinline__ T lin_own_coarse_1d(T v, const T* p, const FaceGeom& g, int j, int n, int off) {
-  if (j - 1 >= 0 && ((j - 1 + off) % 2 == 0)) v += -K<T>::third * sv(p, g, 0, j - 1, 0);
-  v += K<T>::two3 * sv(p, g, 0, j, 0);
-  if (j + 1 < n && ((j + 1 + off) % 2 != 0)) v += -K<T>::third * sv(p, g, 0, j + 1, 0);
-  return v;
-}
-
-template <class T, int SCHEME>
-__device__ T own_term(T v, const T* p, const FaceGeom& g, int M, int D, int type, int orth, int i, int j) {
-  if (type == TE_NBR_NORMAL || type < 0) return v;
-  const T third = K<T>::third;
-  if (M == 0) {  // corners
-    if (SCHEME == TE_GHOST_BIQUADRATIC) {
-      // BiQuadraticGhostFiller.cpp:176-204
-      if (type == TE_NBR_COARSE) return v + (T(2) * sv(p, g, 0, 0, 0) * third - sv(p, g, 1, 0, 0) * T(0.2));
-      return v + (-sv(p, g, 0, 0, 0) * T(1.0 / 15.0));
-    }
-    // BiLinear :207-264, TriLinear :349-364
-    if (type == TE_NBR_COARSE) return v + sv(p, g, 0, 0, 0) * third;
-    return v + (-sv(p, g, 0, 0, 0) * third);
-  }
-  if (M == 1 && D == 3) {  // TriLinear edges
-    int n = g.nt[0];
-    if (type == TE_NBR_COARSE) return lin_own_coarse_1d(v, p, g, i, n, orth == 1 ? n : 0);
-    return v + (-third * sv(p, g, 0, i, 0));
-  }
-  if (D == 2) {  // sides, 2D
-    int n = g.nt[0];
-    if (SCHEME == TE_GHOST_BILINEAR) {
-      if (type == TE_NBR_COARSE) return lin_own_coarse_1d(v, p, g, i, n, orth == 1 ? n : 0);
-      return v + (-third * sv(p, g, 0, i, 0));
-    }
-    // BiQuadratic: FillGhostForLocalWithCoarseNbr / WithFineNbr (:34-58)
-    if (type == TE_NBR_COARSE) return v + (T(2) * sv(p, g, 0, i, 0) * third - sv(p, g, 1, i, 0) * T(0.2));
-    const T c10 = T(0.1), c15 = T(1.0 / 15.0), c30 = T(1.0 / 30.0);
-    if (i == 0) return v + (-sv(p, g, 0, 0, 0) * c10 + sv(p, g, 0, 1, 0) * c15 - sv(p, g, 0, 2, 0) * c30);
-    if (i == n - 1)
-      return v + (-sv(p, g, 0, n - 1, 0) * c10 + sv(p, g, 0, n - 2, 0) * c15 - sv(p, g, 0, n - 3, 0) * c30);
-    return v + (-sv(p, g, 0, i - 1, 0) * c30 - sv(p, g, 0, i + 1, 0) * c30);
-  }
-  // TriLinear sides (:100-122, :74-82)
-  if (type == TE_NBR_COARSE) {
-    int si = (orth & 1) ? g.nt[0] : 0, sj = (orth & 2) ? g.nt[1] : 0;
-    int oi = (i + si) % 2 == 0 ? i + 1 : i - 1;
-    int oj = (j + sj) % 2 == 0 ? j + 1 : j - 1;
-    const T sixth = T(1.0 / 6.0);
-    v += T(5.0 / 6.0) * sv(p, g, 0, i, j);
-    v -= sixth * sv(p, g, 0, oi, j);
-    v -= sixth * sv(p, g, 0, i, oj);
-    v -= sixth * sv(p, g, 0, oi, oj);
-    return v;
-  }
-  return v - third * sv(p, g, 0, i, j);
-}
-
-// contribution of one incoming call (caller patch q, caller face geometry gq)
-template <class T, int SCHEME>
-__device__ T call_term(T v, const T* q, const FaceGeom& gq, int M, int D, int type, int orth, int i, int j) {
-  if (type == TE_NBR_NORMAL) return sv(q, gq, 0, i, j);  // plain copy, an assignment
-  const T third = K<T>::third;
-  if (M == 0) {
-    if (SCHEME == TE_GHOST_BIQUADRATIC) {  // :150-175
-      if (type == TE_NBR_COARSE)
-        return v + (T(2) * sv(q, gq, 0, 0, 0) * third + T(2) * sv(q, gq, 1, 0, 0) * T(0.2));
-      return v + T(8) * sv(q, gq, 0, 0, 0) * T(1.0 / 15.0);
-    }
-    if (type == TE_NBR_COARSE) return v + T(4) * sv(q, gq, 0, 0, 0) * third;
-    return v + T(2) * sv(q, gq, 0, 0, 0) * third;
-  }
-  if (M == 1) {  // 2D sides (BiLinear/BiQuadratic) or 3D edges (TriLinear)
-    int n = gq.nt[0];
-    int off = orth == 1 ? n : 0;
-    if (SCHEME == TE_GHOST_BIQUADRATIC && D == 2) {
-      if (type == TE_NBR_COARSE) {  // caller finer: CoarseNbrLower/Upper (:81-105)
-        for (int idx = 2 * i - off; idx <= 2 * i + 1 - off; idx++)
-          if (idx >= 0 && idx < n) v += sv(q, gq, 0, idx, 0) * third + sv(q, gq, 1, idx, 0) * T(0.2);
-        return v;
-      }
-      // caller coarser: FineNbrLower/Upper (:106-148)
-      const T c12 = T(1.0 / 12.0), c20 = T(0.05), c30 = T(1.0 / 30.0);
-      if (orth == 0) {
-        if (i == 0)
-          return v + (T(0.75) * sv(q, gq, 0, 0, 0) - T(0.3) * sv(q, gq, 0, 1, 0) + sv(q, gq, 0, 2, 0) * c12);
-        if (i == 1)
-          return v + (T(0.35) * sv(q, gq, 0, 0, 0) + T(7) * sv(q, gq, 0, 1, 0) * c30 - sv(q, gq, 0, 2, 0) * c20);
-        int k = i / 2;
-        if (i % 2 == 0)
-          return v + (sv(q, gq, 0, k - 1, 0) * c12 + sv(q, gq, 0, k, 0) * T(0.5) - sv(q, gq, 0, k + 1, 0) * c20);
-        return v + (-sv(q, gq, 0, k - 1, 0) * c20 + sv(q, gq, 0, k, 0) * T(0.5) + sv(q, gq, 0, k + 1, 0) * c12);
-      }
-      if (i < n - 2) {
-        int k = (i + n) / 2;
-        if ((i + n) % 2 == 0)
-          return v + (sv(q, gq, 0, k - 1, 0) * c12 + sv(q, gq, 0, k, 0) * T(0.5) - sv(q, gq, 0, k + 1, 0) * c20);
-        return v + (-sv(q, gq, 0, k - 1, 0) * c20 + sv(q, gq, 0, k, 0) * T(0.5) + sv(q, gq, 0, k + 1, 0) * c12);
-      }
-      if (i == n - 2)
-        return v + (T(0.35) * sv(q, gq, 0, n - 1, 0) + T(7) * sv(q, gq, 0, n - 2, 0) * c30 -
-                    sv(q, gq, 0, n - 3, 0) * c20);
-      return v + (T(0.75) * sv(q, gq, 0, n - 1, 0) - T(0.3) * sv(q, gq, 0, n - 2, 0) + sv(q, gq, 0, n - 3, 0) * c12);
-    }
-    // BiLinear sides (:61-105) and TriLinear edges (:140-171)
-    if (type == TE_NBR_COARSE) {
-      for (int idx = 2 * i - off; idx <= 2 * i + 1 - off; idx++)
-        if (idx >= 0 && idx < n) v += K<T>::two3 * sv(q, gq, 0, idx, 0);
-      return v;
-    }
-    return v + K<T>::two3 * sv(q, gq, 0, (i + off) / 2, 0);
-  }
-  // TriLinear sides (:58-99); offsets from getOffset (:28-44)
-  int oi = (orth & 1) ? gq.nt[0] : 0, oj = (orth & 2) ? gq.nt[1] : 0;
-  if (type == TE_NBR_COARSE) {
-    for (int jj = 2 * j - oj; jj <= 2 * j + 1 - oj; jj++)
-      for (int ii = 2 * i - oi; ii <= 2 * i + 1 - oi; ii++)
-        if (ii >= 0 && ii < gq.nt[0] && jj >= 0 && jj < gq.nt[1]) v += third * sv(q, gq, 0, ii, jj);
-    return v;
-  }
-  return v + K<T>::two3 * sv(q, gq, 0, (i + oi) / 2, (j + oj) / 2);
-}
-
 constexpr int GHOST_THREADS = 128;
 
 template <class T, int SCHEME>
@@ -254,18 +113,9 @@ __global__ void __launch_bounds__(GHOST_THREADS)
     }
     for (int e = threadIdx.x; e < cnt; e += blockDim.x) {
       int c = e / per_c, t = e % per_c, i = t % ni, j = t / ni;
-      const T* pu = u + p * ps + (long long)c * L.cs;
       T* gp = u + p * ps + (long long)c * L.cs + g.gbase + i * g.tstride[0] + j * g.tstride[1];
-      T v = sl.zero ? T(0) : *gp;
-      v = own_term<T, SCHEME>(v, pu, g, sl.M, D, sl.own_type, sl.own_orth, i, j);
-      for (int k = 0; k < sl.ncalls; k++) {
-        GCall cl = calls[sl.call0 + k];
-        const FaceGeom& gq =
-            ft.f[sl.M == D - 1 ? (D == 2 ? 4 : 20) + cl.src_face : (sl.M == 0 ? cl.src_face : 8 + cl.src_face)];
-        const T* q = u + cl.src * ps + (long long)c * L.cs;
-        v = call_term<T, SCHEME>(v, q, gq, sl.M, D, cl.type, cl.orth, i, j);
-      }
-      *gp = v;
+      PlainAcc<T> acc{u, ps, (long long)c * L.cs};
+      *gp = gather_ghost<T, SCHEME>(acc, p, sl, g, ft, calls, D, i, j, sl.zero ? T(0) : *gp);
     }
   }
 }

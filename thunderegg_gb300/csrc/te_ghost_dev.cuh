@@ -1,0 +1,232 @@
+// te_ghost_dev.cuh -- device-side gather formulas of the three ghost schemes.
+// Included by the ghost-fill kernel and by fused kernels that gather ghosts
+// on the fly.
+#pragma once
+#include "te_ghost.cuh"
+
+namespace te {
+
+// ---------------------------------------------------------------------------
+// device: gather formulas
+// ---------------------------------------------------------------------------
+template <class T>
+struct K {
+  static constexpr T third = T(1.0 / 3.0);
+  static constexpr T two3 = T(2.0 / 3.0);
+  static constexpr T four3 = T(4.0 / 3.0);
+};
+
+// Accessors return the value of cell `idx` (index within one padded
+// component) of patch q.  PlainAcc reads a level buffer; other accessors
+// (e.g. "u + interpolated coarse correction") let fused kernels gather
+// ghosts of values that are never stored.
+template <class T>
+struct PlainAcc {
+  const T* u;
+  long long ps;  // patch stride
+  long long co;  // component offset
+  __device__ __forceinline__ T operator()(int q, int idx) const { return u[q * ps + co + idx]; }
+};
+
+// value of the interior slice (depth `dep` along every side of the face) of patch q
+template <class T, class Acc>
+__device__ __forceinline__ T sv(const Acc& acc, int q, const FaceGeom& g, int dep, int i, int j) {
+  int idx = g.ibase + i * g.tstride[0] + j * g.tstride[1];
+  for (int k = 0; k < g.nsides; k++) idx += dep * g.inward[k];
+  return acc(q, idx);
+}
+
+// ---- BiLinear / TriLinear edges: own Coarse term on a 1-D ghost line
+// (BiLinearGhostFiller.cpp:118-134, TriLinearGhostFiller.cpp:172-195)
+template <class T, class Acc>
+__device__ __forceinline__ T lin_own_coarse_1d(T v, const Acc& p, int pq, const FaceGeom& g, int j, int n, int off) {
+  if (j - 1 >= 0 && ((j - 1 + off) % 2 == 0)) v += -K<T>::third * sv<T>(p, pq, g, 0, j - 1, 0);
+  v += K<T>::two3 * sv<T>(p, pq, g, 0, j, 0);
+  if (j + 1 < n && ((j + 1 + off) % 2 != 0)) v += -K<T>::third * sv<T>(p, pq, g, 0, j + 1, 0);
+  return v;
+}
+
+template <class T, int SCHEME, class Acc>
+__device__ T own_term(T v, const Acc& p, int pq, const FaceGeom& g, int M, int D, int type, int orth, int i, int j) {
+  if (type == TE_NBR_NORMAL || type < 0) return v;
+  const T third = K<T>::third;
+  if (M == 0) {  // corners
+    if (SCHEME == TE_GHOST_BIQUADRATIC) {
+      // BiQuadraticGhostFiller.cpp:176-204
+      if (type == TE_NBR_COARSE) return v + (T(2) * sv<T>(p, pq, g, 0, 0, 0) * third - sv<T>(p, pq, g, 1, 0, 0) * T(0.2));
+      return v + (-sv<T>(p, pq, g, 0, 0, 0) * T(1.0 / 15.0));
+    }
+    // BiLinear :207-264, TriLinear :349-364
+    if (type == TE_NBR_COARSE) return v + sv<T>(p, pq, g, 0, 0, 0) * third;
+    return v + (-sv<T>(p, pq, g, 0, 0, 0) * third);
+  }
+  if (M == 1 && D == 3) {  // TriLinear edges
+    int n = g.nt[0];
+    if (type == TE_NBR_COARSE) return lin_own_coarse_1d<T>(v, p, pq, g, i, n, orth == 1 ? n : 0);
+    return v + (-third * sv<T>(p, pq, g, 0, i, 0));
+  }
+  if (D == 2) {  // sides, 2D
+    int n = g.nt[0];
+    if (SCHEME == TE_GHOST_BILINEAR) {
+      if (type == TE_NBR_COARSE) return lin_own_coarse_1d<T>(v, p, pq, g, i, n, orth == 1 ? n : 0);
+      return v + (-third * sv<T>(p, pq, g, 0, i, 0));
+    }
+    // BiQuadratic: FillGhostForLocalWithCoarseNbr / WithFineNbr (:34-58)
+    if (type == TE_NBR_COARSE) return v + (T(2) * sv<T>(p, pq, g, 0, i, 0) * third - sv<T>(p, pq, g, 1, i, 0) * T(0.2));
+    const T c10 = T(0.1), c15 = T(1.0 / 15.0), c30 = T(1.0 / 30.0);
+    if (i == 0) return v + (-sv<T>(p, pq, g, 0, 0, 0) * c10 + sv<T>(p, pq, g, 0, 1, 0) * c15 - sv<T>(p, pq, g, 0, 2, 0) * c30);
+    if (i == n - 1)
+      return v + (-sv<T>(p, pq, g, 0, n - 1, 0) * c10 + sv<T>(p, pq, g, 0, n - 2, 0) * c15 - sv<T>(p, pq, g, 0, n - 3, 0) * c30);
+    return v + (-sv<T>(p, pq, g, 0, i - 1, 0) * c30 - sv<T>(p, pq, g, 0, i + 1, 0) * c30);
+  }
+  // TriLinear sides (:100-122, :74-82)
+  if (type == TE_NBR_COARSE) {
+    int si = (orth & 1) ? g.nt[0] : 0, sj = (orth & 2) ? g.nt[1] : 0;
+    int oi = (i + si) % 2 == 0 ? i + 1 : i - 1;
+    int oj = (j + sj) % 2 == 0 ? j + 1 : j - 1;
+    const T sixth = T(1.0 / 6.0);
+    v += T(5.0 / 6.0) * sv<T>(p, pq, g, 0, i, j);
+    v -= sixth * sv<T>(p, pq, g, 0, oi, j);
+    v -= sixth * sv<T>(p, pq, g, 0, i, oj);
+    v -= sixth * sv<T>(p, pq, g, 0, oi, oj);
+    return v;
+  }
+  return v - third * sv<T>(p, pq, g, 0, i, j);
+}
+
+// contribution of one incoming call (caller patch q, caller face geometry gq)
+template <class T, int SCHEME, class Acc>
+__device__ T call_term(T v, const Acc& q, int qq, const FaceGeom& gq, int M, int D, int type, int orth, int i, int j) {
+  if (type == TE_NBR_NORMAL) return sv<T>(q, qq, gq, 0, i, j);  // plain copy, an assignment
+  const T third = K<T>::third;
+  if (M == 0) {
+    if (SCHEME == TE_GHOST_BIQUADRATIC) {  // :150-175
+      if (type == TE_NBR_COARSE)
+        return v + (T(2) * sv<T>(q, qq, gq, 0, 0, 0) * third + T(2) * sv<T>(q, qq, gq, 1, 0, 0) * T(0.2));
+      return v + T(8) * sv<T>(q, qq, gq, 0, 0, 0) * T(1.0 / 15.0);
+    }
+    if (type == TE_NBR_COARSE) return v + T(4) * sv<T>(q, qq, gq, 0, 0, 0) * third;
+    return v + T(2) * sv<T>(q, qq, gq, 0, 0, 0) * third;
+  }
+  if (M == 1) {  // 2D sides (BiLinear/BiQuadratic) or 3D edges (TriLinear)
+    int n = gq.nt[0];
+    int off = orth == 1 ? n : 0;
+    if (SCHEME == TE_GHOST_BIQUADRATIC && D == 2) {
+      if (type == TE_NBR_COARSE) {  // caller finer: CoarseNbrLower/Upper (:81-105)
+        for (int idx = 2 * i - off; idx <= 2 * i + 1 - off; idx++)
+          if (idx >= 0 && idx < n) v += sv<T>(q, qq, gq, 0, idx, 0) * third + sv<T>(q, qq, gq, 1, idx, 0) * T(0.2);
+        return v;
+      }
+      // caller coarser: FineNbrLower/Upper (:106-148)
+      const T c12 = T(1.0 / 12.0), c20 = T(0.05), c30 = T(1.0 / 30.0);
+      if (orth == 0) {
+        if (i == 0)
+          return v + (T(0.75) * sv<T>(q, qq, gq, 0, 0, 0) - T(0.3) * sv<T>(q, qq, gq, 0, 1, 0) + sv<T>(q, qq, gq, 0, 2, 0) * c12);
+        if (i == 1)
+          return v + (T(0.35) * sv<T>(q, qq, gq, 0, 0, 0) + T(7) * sv<T>(q, qq, gq, 0, 1, 0) * c30 - sv<T>(q, qq, gq, 0, 2, 0) * c20);
+        int k = i / 2;
+        if (i % 2 == 0)
+          return v + (sv<T>(q, qq, gq, 0, k - 1, 0) * c12 + sv<T>(q, qq, gq, 0, k, 0) * T(0.5) - sv<T>(q, qq, gq, 0, k + 1, 0) * c20);
+        return v + (-sv<T>(q, qq, gq, 0, k - 1, 0) * c20 + sv<T>(q, qq, gq, 0, k, 0) * T(0.5) + sv<T>(q, qq, gq, 0, k + 1, 0) * c12);
+      }
+      if (i < n - 2) {
+        int k = (i + n) / 2;
+        if ((i + n) % 2 == 0)
+          return v + (sv<T>(q, qq, gq, 0, k - 1, 0) * c12 + sv<T>(q, qq, gq, 0, k, 0) * T(0.5) - sv<T>(q, qq, gq, 0, k + 1, 0) * c20);
+        return v + (-sv<T>(q, qq, gq, 0, k - 1, 0) * c20 + sv<T>(q, qq, gq, 0, k, 0) * T(0.5) + sv<T>(q, qq, gq, 0, k + 1, 0) * c12);
+      }
+      if (i == n - 2)
+        return v + (T(0.35) * sv<T>(q, qq, gq, 0, n - 1, 0) + T(7) * sv<T>(q, qq, gq, 0, n - 2, 0) * c30 -
+                    sv<T>(q, qq, gq, 0, n - 3, 0) * c20);
+      return v + (T(0.75) * sv<T>(q, qq, gq, 0, n - 1, 0) - T(0.3) * sv<T>(q, qq, gq, 0, n - 2, 0) + sv<T>(q, qq, gq, 0, n - 3, 0) * c12);
+    }
+    // BiLinear sides (:61-105) and TriLinear edges (:140-171)
+    if (type == TE_NBR_COARSE) {
+      for (int idx = 2 * i - off; idx <= 2 * i + 1 - off; idx++)
+        if (idx >= 0 && idx < n) v += K<T>::two3 * sv<T>(q, qq, gq, 0, idx, 0);
+      return v;
+    }
+    return v + K<T>::two3 * sv<T>(q, qq, gq, 0, (i + off) / 2, 0);
+  }
+  // TriLinear sides (:58-99); offsets from getOffset (:28-44)
+  int oi = (orth & 1) ? gq.nt[0] : 0, oj = (orth & 2) ? gq.nt[1] : 0;
+  if (type == TE_NBR_COARSE) {
+    for (int jj = 2 * j - oj; jj <= 2 * j + 1 - oj; jj++)
+      for (int ii = 2 * i - oi; ii <= 2 * i + 1 - oi; ii++)
+        if (ii >= 0 && ii < gq.nt[0] && jj >= 0 && jj < gq.nt[1]) v += third * sv<T>(q, qq, gq, 0, ii, jj);
+    return v;
+  }
+  return v + K<T>::two3 * sv<T>(q, qq, gq, 0, (i + oi) / 2, (j + oj) / 2);
+}
+
+
+// Value of ghost cell (i, j) of slab `sl` of patch p: zero (or the current
+// value), the patch's own terms, then the incoming calls in reference order.
+template <class T, int SCHEME, class Acc>
+__device__ __forceinline__ T gather_ghost(const Acc& acc, int p, const GSlab& sl, const FaceGeom& g,
+                                          const FaceTable& ft, const GCall* __restrict__ calls, int D, int i, int j,
+                                          T start) {
+  T v = sl.zero ? T(0) : start;
+  v = own_term<T, SCHEME>(v, acc, p, g, sl.M, D, sl.own_type, sl.own_orth, i, j);
+  for (int k = 0; k < sl.ncalls; k++) {
+    GCall cl = calls[sl.call0 + k];
+    const FaceGeom& gq =
+        ft.f[sl.M == D - 1 ? (D == 2 ? 4 : 20) + cl.src_face : (sl.M == 0 ? cl.src_face : 8 + cl.src_face)];
+    v = call_term<T, SCHEME>(v, acc, cl.src, gq, sl.M, D, cl.type, cl.orth, i, j);
+  }
+  return v;
+}
+
+// Face (side) ghosts of up to NP patches into shared memory: for patch slot
+// q, G[q * 2D * gstride + side * gstride + j*nt0 + i], for every side slab with
+// a neighbour (the only ghosts a star stencil or the internal-boundary RHS
+// terms read).  Sides without a neighbour are left alone.  All slabs of all
+// patches are processed in one flattened loop; `sl_buf` is shared scratch
+// for up to NP * 6 slab records.  Contains __syncthreads: call from all threads.
+template <class T, int SCHEME, class Acc>
+__device__ void side_ghosts_to_smem(const Acc& acc, const int* pq, int NP, const GSlab* __restrict__ slabs,
+                                    const GCall* __restrict__ calls, const int* __restrict__ slab_start,
+                                    const FaceTable& ft, int D, T* G, int gstride, GSlab* sl_buf, int* sl_q,
+                                    int* n_sl) {
+  if (threadIdx.x == 0) {
+    int n = 0;
+    for (int q = 0; q < NP; q++) {
+      int p = pq[q];
+      if (p < 0) continue;
+      for (int s = slab_start[p]; s < slab_start[p + 1]; s++) {
+        GSlab sl = slabs[s];
+        if (sl.M != D - 1 || !sl.zero) continue;
+        sl_buf[n] = sl;
+        sl_q[n] = q;
+        n++;
+      }
+    }
+    *n_sl = n;
+  }
+  __syncthreads();
+  const int ns = *n_sl;
+  const int side0 = D == 2 ? 4 : 20;
+  // every side slab of one dimension has the same size (n^(D-1) for cubes; take each slab's own)
+  int total = 0;
+  for (int k = 0; k < ns; k++) {
+    const FaceGeom& g = ft.f[side0 + sl_buf[k].face];
+    total += g.nt[0] * g.nt[1];
+  }
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    int k = 0, r = e;
+    for (;;) {
+      const FaceGeom& g = ft.f[side0 + sl_buf[k].face];
+      int c = g.nt[0] * g.nt[1];
+      if (r < c) break;
+      r -= c;
+      k++;
+    }
+    const GSlab sl = sl_buf[k];
+    const FaceGeom& g = ft.f[side0 + sl.face];
+    int i = r % g.nt[0], j = r / g.nt[0];
+    G[sl_q[k] * 2 * D * gstride + sl.face * gstride + r] =
+        gather_ghost<T, SCHEME>(acc, sl.patch, sl, g, ft, calls, D, i, j, T(0));
+  }
+}
+
+}  // namespace te

@@ -9,27 +9,10 @@
 //   Iterative::BiCGStab::solve (Iterative/BiCGStab.h:111-203).
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
-#include "te_ops.cuh"
-
-struct te_restrictor {
-  const te_domain* fine = nullptr;
-  const te_domain* coarse = nullptr;
-  int extrapolate = 0;
-  // children of each coarse patch, in fine-patch order
-  te::DevBuf<int> child_start;  // [Pc+1]
-  te::DevBuf<int> child;        // fine local index
-  te::DevBuf<int> child_orth;   // orth_on_parent (-1 = copied patch)
-  te::DevBuf<int8_t> child_corner_nbr;  // fine patch has a neighbour at Corner(orth)
-};
-
-struct te_interpolator {
-  const te_domain* coarse = nullptr;
-  const te_domain* fine = nullptr;
-  te::DevBuf<int> parent;  // coarse local index of each fine patch
-  te::DevBuf<int> orth;    // orth_on_parent of each fine patch
-};
+#include "te_gmg.cuh"
 
 namespace te {
 
@@ -161,6 +144,230 @@ __global__ void interpolate_kernel(Layout F, Layout C, int nc, const int* __rest
   }
 }
 
+// Cycle::restrict fused: r = f - A u on the fine level (Poisson or VarPoisson
+// star stencil, boundary ghosts -u / +u as enforceBoundaryConditions) is
+// formed in registers and averaged straight into the coarse cell
+// (restrictToCoarserParent / copyToParent).  u's ghosts across faces with a
+// neighbour must already be filled.  Used when ghost extrapolation is off.
+template <class T, int KIND>
+__global__ void residual_restrict_kernel(Layout F, Layout C, int nc, const int* __restrict__ cstart,
+                                         const int* __restrict__ child, const int* __restrict__ corth,
+                                         const int8_t* __restrict__ fntype, int FS, const T* __restrict__ fsp,
+                                         int neumann, const T* __restrict__ coeff, const T* __restrict__ fu,
+                                         const T* __restrict__ ff, T* __restrict__ coarse) {
+  const int cp = blockIdx.x;
+  const int D = C.D;
+  const T wD = T(1.0 / (1 << D));
+  const int k0 = cstart[cp], k1 = cstart[cp + 1];
+  const int py = C.n1 + 2 * C.g;
+  const int side0 = D == 2 ? 4 : 20;
+  const long long fps = F.pstride(nc), cps = C.pstride(nc);
+  const int tot = C.cs * nc;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    int c = e / C.cs, k = e - c * C.cs;
+    int cc[3];
+    cc[0] = k % C.sy - C.g;
+    int q = k / C.sy;
+    cc[1] = q % py - C.g;
+    cc[2] = q / py - (D == 3 ? C.g : 0);
+    bool interior = cc[0] >= 0 && cc[0] < C.n0 && cc[1] >= 0 && cc[1] < C.n1 && cc[2] >= 0 && cc[2] < C.n2;
+    T v = T(0);
+    if (interior) {
+      for (int qq = k0; qq < k1; qq++) {
+        const int fp = child[qq], o = corth[qq];
+        const T* u = fu + fp * fps + (long long)c * F.cs;
+        const T* f = ff + fp * fps + (long long)c * F.cs;
+        const T* cf = KIND ? coeff + (long long)fp * F.cs : nullptr;
+        T inv[3];
+        int hasn[6];
+        for (int a = 0; a < 3; a++) inv[a] = fsp[(size_t)fp * 6 + (KIND ? 3 : 0) + a];
+        for (int sd = 0; sd < 2 * D; sd++) hasn[sd] = fntype[(size_t)fp * FS + side0 + sd] >= 0;
+        int lo[3], hi[3];
+        for (int a = 0; a < 3; a++) {
+          if (a >= D) {
+            lo[a] = hi[a] = 0;
+          } else if (o < 0) {
+            lo[a] = hi[a] = cc[a];
+          } else {
+            int st = ((o >> a) & 1) ? C.n(a) : 0;
+            lo[a] = max(2 * cc[a] - st, 0);
+            hi[a] = min(2 * cc[a] + 1 - st, F.n(a) - 1);
+          }
+        }
+        for (int z = lo[2]; z <= hi[2]; z++)
+          for (int y = lo[1]; y <= hi[1]; y++)
+            for (int x = lo[0]; x <= hi[0]; x++) {
+              int fk = F.at(x, y, z);
+              int fc[3] = {x, y, z};
+              T mid = u[fk];
+              T au = T(0);
+              for (int a = 0; a < D; a++) {
+                int st = F.stride(a);
+                T lov, hiv;
+                if (fc[a] == 0 && !hasn[2 * a])
+                  lov = neumann ? mid : -mid;
+                else
+                  lov = u[fk - st];
+                if (fc[a] == F.n(a) - 1 && !hasn[2 * a + 1])
+                  hiv = neumann ? mid : -mid;
+                else
+                  hiv = u[fk + st];
+                if (KIND == 0) {
+                  au += ((hiv - T(2) * mid) + lov) * inv[a];
+                } else {
+                  T cl = cf[fk - st], cm = cf[fk], cu = cf[fk + st];
+                  au += ((cu + cm) * (hiv - mid) - (cl + cm) * (mid - lov)) * inv[a];
+                }
+              }
+              T r = au * T(-1) + f[fk];
+              if (o < 0)
+                v += r;
+              else
+                v += r * wD;
+            }
+      }
+    }
+    coarse[cp * cps + e] = v;
+  }
+}
+
+// Even patch sizes: every coarse cell has exactly one contributing child (or
+// is a copy), so the children's metadata is staged in shared memory once and
+// each thread does one coarse cell without searching.
+template <class T, int KIND>
+__global__ void __launch_bounds__(256)
+    residual_restrict_even_kernel(Layout F, Layout C, int nc, const int* __restrict__ by_orth,
+                                  const int* __restrict__ copy_of, const int8_t* __restrict__ fntype, int FS,
+                                  const T* __restrict__ finv, int neumann, const T* __restrict__ coeff,
+                                  const T* __restrict__ fu, const T* __restrict__ ff, T* __restrict__ coarse) {
+  const int cp = blockIdx.x;
+  const int D = C.D;
+  const int NCH = 1 << D;
+  __shared__ int s_fp[8];
+  __shared__ int s_has[8];
+  __shared__ T s_inv[8][3];
+  const int copy = copy_of[cp];
+  if (threadIdx.x < NCH) {
+    int q = threadIdx.x;
+    int fp = copy >= 0 ? (q == 0 ? copy : -1) : by_orth[cp * NCH + q];
+    s_fp[q] = fp;
+    int m = 0;
+    if (fp >= 0) {
+      const int side0 = D == 2 ? 4 : 20;
+      for (int sd = 0; sd < 2 * D; sd++) m |= (fntype[(size_t)fp * FS + side0 + sd] >= 0) << sd;
+      for (int a2 = 0; a2 < 3; a2++) s_inv[q][a2] = finv[(size_t)fp * 6 + (KIND ? 3 : 0) + a2];
+    }
+    s_has[q] = m;
+  }
+  __syncthreads();
+  const T wD = T(1.0 / (1 << D));
+  const int py = C.n1 + 2 * C.g;
+  const long long fps = F.pstride(nc), cps = C.pstride(nc);
+  const int tot = C.cs * nc;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    int c = e / C.cs, k = e - c * C.cs;
+    int cc[3];
+    cc[0] = k % C.sy - C.g;
+    int q = k / C.sy;
+    cc[1] = q % py - C.g;
+    cc[2] = q / py - (D == 3 ? C.g : 0);
+    bool interior = cc[0] >= 0 && cc[0] < C.n0 && cc[1] >= 0 && cc[1] < C.n1 && cc[2] >= 0 && cc[2] < C.n2;
+    T v = T(0);
+    if (interior) {
+      int o = 0, lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+      if (copy >= 0) {
+        for (int a2 = 0; a2 < D; a2++) lo[a2] = hi[a2] = cc[a2];
+      } else {
+        for (int a2 = 0; a2 < D; a2++) {
+          int up = 2 * cc[a2] >= C.n(a2);
+          o |= up << a2;
+          lo[a2] = 2 * cc[a2] - (up ? C.n(a2) : 0);
+          hi[a2] = lo[a2] + 1;
+        }
+      }
+      const int fp = s_fp[o];
+      if (fp >= 0) {
+        const int hasn = s_has[o];
+        const T* u = fu + fp * fps + (long long)c * F.cs;
+        const T* f = ff + fp * fps + (long long)c * F.cs;
+        const T* cf = KIND ? coeff + (long long)fp * F.cs : nullptr;
+        for (int z = lo[2]; z <= hi[2]; z++)
+          for (int y = lo[1]; y <= hi[1]; y++)
+            for (int x = lo[0]; x <= hi[0]; x++) {
+              int fk = F.at(x, y, z);
+              int fc[3] = {x, y, z};
+              T mid = u[fk];
+              T au = T(0);
+              for (int a2 = 0; a2 < D; a2++) {
+                int st = F.stride(a2);
+                T lov = (fc[a2] == 0 && !((hasn >> (2 * a2)) & 1)) ? (neumann ? mid : -mid) : u[fk - st];
+                T hiv = (fc[a2] == F.n(a2) - 1 && !((hasn >> (2 * a2 + 1)) & 1)) ? (neumann ? mid : -mid)
+                                                                               : u[fk + st];
+                if (KIND == 0) {
+                  au += ((hiv - T(2) * mid) + lov) * s_inv[o][a2];
+                } else {
+                  T cl = cf[fk - st], cm = cf[fk], cu = cf[fk + st];
+                  au += ((cu + cm) * (hiv - mid) - (cl + cm) * (mid - lov)) * s_inv[o][a2];
+                }
+              }
+              T r = au * T(-1) + f[fk];
+              v += copy >= 0 ? r : r * wD;
+            }
+      }
+    }
+    coarse[cp * cps + e] = v;
+  }
+}
+
+void residual_restrict(const te_restrictor* r, const te_operator* op, int nc, int dtype, const void* f,
+                       const void* u, void* coarse, cudaStream_t s) {
+  const te_domain* fd = r->fine;
+  const Layout &F = fd->lay, &C = r->coarse->lay;
+  int threads = C.cs * nc >= 256 ? 256 : 128;
+  if (r->even) {
+#define TE_RRE(T, K, INV, CO)                                                                                  \
+  residual_restrict_even_kernel<T, K><<<C.P, 256, 0, s>>>(F, C, nc, r->by_orth.p, r->copy_of.p, fd->d_nbr_type.p, \
+                                                           fd->F, INV, op->neumann, CO, (const T*)u, (const T*)f,  \
+                                                           (T*)coarse)
+    if (dtype == TE_F64) {
+      if (op->kind == 0)
+        TE_RRE(double, 0, fd->d_inv.p, nullptr);
+      else
+        TE_RRE(double, 1, fd->d_inv.p, op->coeffs.p);
+    } else {
+      if (op->kind == 0)
+        TE_RRE(float, 0, fd->d_inv_f.p, nullptr);
+      else
+        TE_RRE(float, 1, fd->d_inv_f.p, op->coeffs_f.p);
+    }
+#undef TE_RRE
+    count_launch();
+    TE_LAUNCH_CHECK();
+    return;
+  }
+  if (dtype == TE_F64) {
+    if (op->kind == 0)
+      residual_restrict_kernel<double, 0><<<C.P, threads, 0, s>>>(
+          F, C, nc, r->child_start.p, r->child.p, r->child_orth.p, fd->d_nbr_type.p, fd->F, fd->d_inv.p,
+          op->neumann, nullptr, (const double*)u, (const double*)f, (double*)coarse);
+    else
+      residual_restrict_kernel<double, 1><<<C.P, threads, 0, s>>>(
+          F, C, nc, r->child_start.p, r->child.p, r->child_orth.p, fd->d_nbr_type.p, fd->F, fd->d_inv.p, 0,
+          op->coeffs.p, (const double*)u, (const double*)f, (double*)coarse);
+  } else {
+    if (op->kind == 0)
+      residual_restrict_kernel<float, 0><<<C.P, threads, 0, s>>>(
+          F, C, nc, r->child_start.p, r->child.p, r->child_orth.p, fd->d_nbr_type.p, fd->F, fd->d_inv_f.p,
+          op->neumann, nullptr, (const float*)u, (const float*)f, (float*)coarse);
+    else
+      residual_restrict_kernel<float, 1><<<C.P, threads, 0, s>>>(
+          F, C, nc, r->child_start.p, r->child.p, r->child_orth.p, fd->d_nbr_type.p, fd->F, fd->d_inv_f.p, 0,
+          op->coeffs_f.p, (const float*)u, (const float*)f, (float*)coarse);
+  }
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
 void restrict_level(const te_restrictor* r, int nc, int dtype, const void* fine, void* coarse, cudaStream_t s) {
   const Layout &F = r->fine->lay, &C = r->coarse->lay;
   if (dtype == TE_F64)
@@ -203,7 +410,7 @@ __global__ void residual_kernel(Layout L, int nc, long long n, const T* __restri
   }
 }
 
-static void residual(const te_domain* d, int nc, int dtype, const void* f, void* r, cudaStream_t s) {
+void residual(const te_domain* d, int nc, int dtype, const void* f, void* r, cudaStream_t s) {
   long long n = (long long)d->lay.P * nc * d->lay.interior();
   int grid = (int)std::min<long long>((n + 255) / 256, 152 * 16);
   if (dtype == TE_F64)
@@ -213,108 +420,6 @@ static void residual(const te_domain* d, int nc, int dtype, const void* f, void*
   count_launch();
   TE_LAUNCH_CHECK();
 }
-
-}  // namespace te
-
-// ---------------------------------------------------------------------------
-// V-cycle
-// ---------------------------------------------------------------------------
-struct te_cycle {
-  std::vector<te_cycle_level> levels;
-  te_cycle_opts opts{1, 1, 1, 1};
-  int dtype = TE_F64;
-  int nc = 1;
-  cudaStream_t stream = nullptr;
-  // per-level work buffers in the cycle's precision
-  std::vector<te::DevBuf<char>> f, u, r;
-  size_t esize() const { return dtype == TE_F64 ? 8 : 4; }
-  const te_domain* dom(int k) const { return levels[k].op->dom; }
-  size_t bytes(int k) const { return (size_t)dom(k)->lay.P * dom(k)->lay.pstride(nc) * esize(); }
-  void ensure(int nc_in) {
-    if (nc_in == nc && !f.empty()) return;
-    nc = nc_in;
-    size_t L = levels.size();
-    f.clear();
-    u.clear();
-    r.clear();
-    f.resize(L);
-    u.resize(L);
-    r.resize(L);
-    for (size_t k = 0; k < L; k++) {
-      r[k].alloc(bytes(k));
-      if (k > 0 || dtype != TE_F64) {
-        f[k].alloc(bytes(k));
-        u[k].alloc(bytes(k));
-      }
-    }
-  }
-  void smooth(int k, const void* fk, void* uk, int times) const {
-    for (int i = 0; i < times; i++) te::patch_smooth(levels[k].smoother, nc, dtype, fk, uk, false, stream);
-  }
-  // VCycle::visit (GMG/VCycle.h:46-70)
-  void visit(int k, const void* fk, void* uk) const {
-    int last = (int)levels.size() - 1;
-    if (k == last) {
-      smooth(k, fk, uk, opts.coarse_sweeps);
-      return;
-    }
-    smooth(k, fk, uk, opts.pre_sweeps);
-    // Cycle::restrict (GMG/Cycle.h:57-65): r = f - A u, then restrict(r)
-    void* rk = r[k].p;
-    te::operator_apply(levels[k].op, nc, dtype, uk, rk, stream);
-    te::residual(dom(k), nc, dtype, fk, rk, stream);
-    void* fc = f[k + 1].p;
-    void* uc = u[k + 1].p;
-    te::restrict_level(levels[k].restrictor, nc, dtype, rk, fc, stream);
-    TE_CUDA(cudaMemsetAsync(uc, 0, bytes(k + 1), stream));
-    visit(k + 1, fc, uc);
-    te::interpolate_level(levels[k + 1].interpolator, nc, dtype, uc, uk, stream);
-    smooth(k, fk, uk, opts.post_sweeps);
-  }
-  // Cycle::apply (GMG/Cycle.h:94-98); f and u are FP64 finest-level buffers
-  void apply(const void* f64, void* u64) const {
-    if (dtype == TE_F64) {
-      TE_CUDA(cudaMemsetAsync(u64, 0, bytes(0), stream));
-      visit(0, f64, u64);
-    } else {
-      te::convert_level(dom(0), nc, dtype, f[0].p, TE_F64, f64, stream);
-      TE_CUDA(cudaMemsetAsync(u[0].p, 0, bytes(0), stream));
-      visit(0, f[0].p, u[0].p);
-      te::convert_level(dom(0), nc, TE_F64, u64, dtype, u[0].p, stream);
-    }
-  }
-};
-
-// ---------------------------------------------------------------------------
-// outer BiCGStab, FP64, device vectors, host scalars (as the reference)
-// ---------------------------------------------------------------------------
-namespace te {
-
-struct Krylov {
-  const te_domain* d;
-  int nc;
-  cudaStream_t s;
-  DevBuf<double> res;
-  double* h = nullptr;
-  Krylov(const te_domain* d, int nc) : d(d), nc(nc), s(d->stream), res(8) {
-    TE_CUDA(cudaMallocHost(&h, 8 * sizeof(double)));
-  }
-  ~Krylov() {
-    if (h) cudaFreeHost(h);
-  }
-  // launch up to 8 dot products, read them back with one synchronisation
-  void dots(int n, const void* const* a, const void* const* b, double* out) {
-    for (int i = 0; i < n; i++) reduce_dot(d, nc, TE_F64, a[i], b[i], res.p + i, s);
-    TE_CUDA(cudaMemcpyAsync(h, res.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
-    TE_CUDA(cudaStreamSynchronize(s));
-    for (int i = 0; i < n; i++) out[i] = h[i];
-  }
-  double dot(const void* a, const void* b) {
-    double o;
-    dots(1, &a, &b, &o);
-    return o;
-  }
-};
 
 }  // namespace te
 
@@ -348,7 +453,27 @@ int te_linear_restrictor_create(const te_domain* fine, const te_domain* coarse, 
       }
     }
     start[Pc] = (int)child.size();
+    // even patch sizes: one child per coarse cell (by orthant) or a copied patch
+    const Layout& FL = fine->lay;
+    bool even = FL.n0 % 2 == 0 && FL.n1 % 2 == 0 && FL.n2 % 2 == 0 || (FL.D == 2 && FL.n0 % 2 == 0 && FL.n1 % 2 == 0);
+    int NCH = 1 << FL.D;
+    std::vector<int> by_orth((size_t)Pc * NCH, -1), copy_of(Pc, -1);
+    for (int c = 0; c < Pc && even; c++) {
+      auto& ks = kids[c];
+      if (ks.size() == 1 && fine->orth_on_parent[ks[0]] < 0) {
+        copy_of[c] = ks[0];
+        continue;
+      }
+      for (int p : ks) {
+        int o = fine->orth_on_parent[p];
+        if (o < 0 || by_orth[(size_t)c * NCH + o] >= 0) even = false;
+        else by_orth[(size_t)c * NCH + o] = p;
+      }
+    }
+    r->even = even;
     cudaStream_t s = fine->stream;
+    r->by_orth.upload(by_orth, s);
+    r->copy_of.upload(copy_of, s);
     r->child_start.upload(start, s);
     r->child.upload(child, s);
     r->child_orth.upload(orth, s);
@@ -410,6 +535,21 @@ int te_vcycle_create(const te_cycle_level* levels, int num_levels, te_cycle_opts
       if (k > 0) require(levels[k].interpolator != nullptr, "missing interpolator");
     }
     c->stream = levels[0].op->dom->stream;
+    static std::atomic<unsigned long long> serials{1};
+    c->serial = serials.fetch_add(1);
+    const char* ng = getenv("TE_NO_GRAPH");
+    c->use_graph = !(ng && ng[0] == '1');
+    bool fz = num_levels >= 2 && opts.pre_sweeps == 1 && opts.post_sweeps == 1 && opts.coarse_sweeps == 1;
+    const char* nf = getenv("TE_NO_FUSION");
+    if (nf && nf[0] == '1') fz = false;
+    for (int k = 0; k < num_levels && fz; k++) {
+      fz &= levels[k].smoother->kind == 0;
+      if (k + 1 < num_levels) fz &= levels[k].restrictor->even && !levels[k].restrictor->extrapolate;
+    }
+    c->fusable = fz;
+    TE_CUDA(cudaStreamCreateWithFlags(&c->cap, cudaStreamNonBlocking));
+    TE_CUDA(cudaEventCreateWithFlags(&c->ev_in, cudaEventDisableTiming));
+    TE_CUDA(cudaEventCreateWithFlags(&c->ev_out, cudaEventDisableTiming));
     c->ensure(1);
     *out = c.release();
   });
@@ -423,101 +563,10 @@ int te_cycle_destroy(te_cycle* c) {
 int te_cycle_apply(const te_cycle* c, int nc, const void* f, void* u) {
   return guard([&] {
     require(c && f && u, "null argument");
-    const_cast<te_cycle*>(c)->ensure(nc);
-    c->apply(f, u);
+    te_cycle* m = const_cast<te_cycle*>(c);
+    m->ensure(nc);
+    m->apply_on(f, u, m->stream);
   });
-}
-
-int te_bicgstab_solve(const te_operator* A, int nc, void* x, const void* b, const te_cycle* M, double tol,
-                      int max_iterations, int flags, int* iterations, double* final_residual) {
-  int status = TE_OK;
-  int rc = guard([&] {
-    require(A && x && b, "null argument");
-    const te_domain* d = A->dom;
-    cudaStream_t s = d->stream;
-    size_t bytes = (size_t)d->lay.P * d->lay.pstride(nc) * sizeof(double);
-    auto zero = [&]() {
-      DevBuf<double> v(bytes / sizeof(double));
-      TE_CUDA(cudaMemsetAsync(v.p, 0, bytes, s));
-      return v;
-    };
-    Krylov K(d, nc);
-    if (M) const_cast<te_cycle*>(M)->ensure(nc);
-    DevBuf<double> resid = zero(), ms, mp;
-    if (M) {
-      ms = zero();
-      mp = zero();
-    }
-    operator_apply(A, nc, TE_F64, x, resid.p, s);
-    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, resid.p, b, nullptr, -1, 0, 0);
-    double r0 = std::sqrt(K.dot(b, b));
-    DevBuf<double> rhat(bytes / 8), p(bytes / 8), ap = zero(), as = zero(), sv = zero();
-    TE_CUDA(cudaMemcpyAsync(rhat.p, resid.p, bytes, cudaMemcpyDeviceToDevice, s));
-    TE_CUDA(cudaMemcpyAsync(p.p, resid.p, bytes, cudaMemcpyDeviceToDevice, s));
-    double rho = K.dot(rhat.p, resid.p);
-    int its = 0;
-    double residual = std::sqrt(K.dot(resid.p, resid.p)) / r0;
-    if (final_residual) *final_residual = residual;
-    if (r0 == 0) {
-      *iterations = 0;
-      return;
-    }
-    while (residual > tol && its < max_iterations) {
-      if (rho == 0) {
-        status = TE_ERR_BREAKDOWN;
-        set_error("BiCGStab broke down, rho was 0 on iteration " + std::to_string(its));
-        break;
-      }
-      if (M) {
-        M->apply(p.p, mp.p);
-        operator_apply(A, nc, TE_F64, mp.p, ap.p, s);
-      } else {
-        operator_apply(A, nc, TE_F64, p.p, ap.p, s);
-      }
-      double alpha = rho / K.dot(rhat.p, ap.p);
-      vec_dispatch(d, nc, TE_F64, OP_COPY, sv.p, resid.p, nullptr, 0, 0, 0);
-      vec_dispatch(d, nc, TE_F64, OP_ADD_SCALED, sv.p, ap.p, nullptr, -alpha, 0, 0);
-      double snorm = std::sqrt(K.dot(sv.p, sv.p)) / r0;
-      if (snorm <= tol) {
-        // the reference adds alpha * p even when preconditioned (BiCGStab.h:163);
-        // flag bit 0 selects the preconditioned update alpha * M p instead
-        const void* dir = (M && (flags & 1)) ? (const void*)mp.p : (const void*)p.p;
-        vec_dispatch(d, nc, TE_F64, OP_ADD_SCALED, x, dir, nullptr, alpha, 0, 0);
-        if (final_residual) *final_residual = snorm;
-        break;
-      }
-      if (M) {
-        M->apply(sv.p, ms.p);
-        operator_apply(A, nc, TE_F64, ms.p, as.p, s);
-      } else {
-        operator_apply(A, nc, TE_F64, sv.p, as.p, s);
-      }
-      const void* da[2] = {as.p, as.p};
-      const void* db[2] = {sv.p, as.p};
-      double w[2];
-      K.dots(2, da, db, w);
-      double omega = w[0] / w[1];
-      if (M)
-        vec_dispatch(d, nc, TE_F64, OP_ADD_SCALED2, x, mp.p, ms.p, alpha, omega, 0);
-      else
-        vec_dispatch(d, nc, TE_F64, OP_ADD_SCALED2, x, p.p, sv.p, alpha, omega, 0);
-      vec_dispatch(d, nc, TE_F64, OP_ADD_SCALED2, resid.p, ap.p, as.p, -alpha, -omega, 0);
-      const void* ra[2] = {resid.p, resid.p};
-      const void* rb[2] = {rhat.p, resid.p};
-      double rr[2];
-      K.dots(2, ra, rb, rr);
-      double rho_new = rr[0];
-      double beta = rho_new * alpha / (rho * omega);
-      vec_dispatch(d, nc, TE_F64, OP_ADD_SCALED, p.p, ap.p, nullptr, -omega, 0, 0);
-      vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, p.p, resid.p, nullptr, beta, 0, 0);
-      its++;
-      rho = rho_new;
-      residual = std::sqrt(rr[1]) / r0;
-      if (final_residual) *final_residual = residual;
-    }
-    *iterations = its;
-  });
-  return rc != TE_OK ? rc : status;
 }
 
 }  // extern "C"

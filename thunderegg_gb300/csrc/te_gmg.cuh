@@ -1,0 +1,211 @@
+// te_gmg.cuh -- transfer and cycle handles (internal).
+#pragma once
+#include <map>
+#include <utility>
+
+#include "te_ops.cuh"
+
+struct te_restrictor {
+  const te_domain* fine = nullptr;
+  const te_domain* coarse = nullptr;
+  int extrapolate = 0;
+  // children of each coarse patch, in fine-patch order
+  te::DevBuf<int> child_start;  // [Pc+1]
+  te::DevBuf<int> child;        // fine local index
+  te::DevBuf<int> child_orth;   // orth_on_parent (-1 = copied patch)
+  te::DevBuf<int8_t> child_corner_nbr;  // fine patch has a neighbour at Corner(orth)
+  // even patch sizes: child by orthant per coarse patch, or the copied fine patch
+  bool even = false;
+  te::DevBuf<int> by_orth;   // [Pc * 2^D]
+  te::DevBuf<int> copy_of;   // [Pc]
+};
+
+struct te_interpolator {
+  const te_domain* coarse = nullptr;
+  const te_domain* fine = nullptr;
+  te::DevBuf<int> parent;  // coarse local index of each fine patch
+  te::DevBuf<int> orth;    // orth_on_parent of each fine patch
+};
+
+namespace te {
+void restrict_level(const te_restrictor* r, int nc, int dtype, const void* fine, void* coarse, cudaStream_t s);
+void interpolate_level(const te_interpolator* in, int nc, int dtype, const void* coarse, void* fine,
+                       cudaStream_t s);
+void residual_restrict(const te_restrictor* r, const te_operator* op, int nc, int dtype, const void* f,
+                       const void* u, void* coarse, cudaStream_t s);
+void residual(const te_domain* d, int nc, int dtype, const void* f, void* r, cudaStream_t s);
+// fused per-level kernels of the DFT-smoother V-cycle (te_fused.cu)
+template <class T, class TF>
+void vc_pre(const te_patch_solver* ps, const TF* f, T* out, cudaStream_t s);
+template <class T, class TF>
+void vc_restrict(const te_restrictor* r, const te_operator* op, const T* u, const TF* f, T* coarse,
+                 cudaStream_t s);
+template <class T, class TF, class TO>
+void vc_post(const te_patch_solver* ps, const te_interpolator* in, const T* A, const T* uc, const TF* f, TO* out,
+             cudaStream_t s);
+}  // namespace te
+
+// ---------------------------------------------------------------------------
+// V-cycle
+// ---------------------------------------------------------------------------
+// The launch sequence of one cycle application is fixed, so it is captured
+// once per (f, u) buffer pair into a CUDA graph on a private stream and
+// replayed; the caller's stream is ordered around it with events.
+// Set TE_NO_GRAPH=1 in the environment to launch eagerly instead.
+struct te_cycle {
+  std::vector<te_cycle_level> levels;
+  te_cycle_opts opts{1, 1, 1, 1};
+  int dtype = TE_F64;
+  int nc = 1;
+  cudaStream_t stream = nullptr;  // caller's stream (that of the level handles)
+  cudaStream_t cap = nullptr;     // private capture stream
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  bool use_graph = true;
+  unsigned long long serial = 0;      // unique per cycle object
+  unsigned long long generation = 0;  // bumped whenever the work buffers are reallocated
+  struct G {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t x = nullptr;
+    long long launches = 0;
+  };
+  std::map<std::pair<const void*, void*>, G> graphs;
+  // per-level work buffers in the cycle's precision
+  std::vector<te::DevBuf<char>> f, u, r;
+  // fused path: every level smooths with the DFT solver, one pre/post sweep,
+  // even patch sizes, no ghost extrapolation, one component
+  bool fusable = false;
+  bool fused() const { return fusable && nc == 1; }
+  ~te_cycle() {
+    clear_graphs();
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (cap) cudaStreamDestroy(cap);
+  }
+  void clear_graphs() {
+    for (auto& kv : graphs) {
+      if (kv.second.x) cudaGraphExecDestroy(kv.second.x);
+      if (kv.second.g) cudaGraphDestroy(kv.second.g);
+    }
+    graphs.clear();
+  }
+  size_t esize() const { return dtype == TE_F64 ? 8 : 4; }
+  const te_domain* dom(int k) const { return levels[k].op->dom; }
+  size_t bytes(int k) const { return (size_t)dom(k)->lay.P * dom(k)->lay.pstride(nc) * esize(); }
+  void ensure(int nc_in) {
+    if (nc_in == nc && !f.empty()) return;
+    clear_graphs();
+    generation++;
+    nc = nc_in;
+    size_t L = levels.size();
+    f.clear();
+    u.clear();
+    r.clear();
+    f.resize(L);
+    u.resize(L);
+    r.resize(L);
+    for (size_t k = 0; k < L; k++) {
+      r[k].alloc(bytes(k));
+      u[k].alloc(bytes(k));
+      if (k > 0 || dtype != TE_F64) f[k].alloc(bytes(k));
+    }
+  }
+  // Fused V-cycle: A = u[k] holds the pre-smoothed iterate, r[k] the post-smoothed
+  // one (the level's result); returns the buffer holding the level's result.
+  template <class T, class TF, class TO>
+  const T* vfused(int k, const TF* fk, TO* out, cudaStream_t s) const {
+    int last = (int)levels.size() - 1;
+    T* A = (T*)u[k].p;
+    te::vc_pre<T, TF>(levels[k].smoother, fk, A, s);
+    if (k == last) return A;
+    T* fc = (T*)f[k + 1].p;
+    te::vc_restrict<T, TF>(levels[k].restrictor, levels[k].op, A, fk, fc, s);
+    const T* uc = vfused<T, T, T>(k + 1, fc, (T*)r[k + 1].p, s);
+    te::vc_post<T, TF, TO>(levels[k].smoother, levels[k + 1].interpolator, A, uc, fk, out, s);
+    return (const T*)out;
+  }
+  // `fresh`: u is known to be zero (ghosts included) before the first sweep
+  void smooth(int k, const void* fk, void* uk, int times, bool fresh, cudaStream_t s) const {
+    for (int i = 0; i < times; i++) te::patch_smooth(levels[k].smoother, nc, dtype, fk, uk, fresh && i == 0, s);
+  }
+  // VCycle::visit (GMG/VCycle.h:46-70); u enters as zero at every level
+  void visit(int k, const void* fk, void* uk, cudaStream_t s) const {
+    int last = (int)levels.size() - 1;
+    if (k == last) {
+      smooth(k, fk, uk, opts.coarse_sweeps, true, s);
+      return;
+    }
+    smooth(k, fk, uk, opts.pre_sweeps, true, s);
+    void* fc = f[k + 1].p;
+    void* uc = u[k + 1].p;
+    const te_restrictor* R = levels[k].restrictor;
+    if (!R->extrapolate && opts.pre_sweeps > 0) {
+      // Cycle::restrict (GMG/Cycle.h:57-65) fused: fill ghosts, then r = f - A u restricted
+      te::ghost_fill(levels[k].op->gf, nc, dtype, uk, s);
+      te::residual_restrict(R, levels[k].op, nc, dtype, fk, uk, fc, s);
+    } else {
+      void* rk = r[k].p;
+      te::operator_apply(levels[k].op, nc, dtype, uk, rk, s);
+      te::residual(dom(k), nc, dtype, fk, rk, s);
+      te::restrict_level(R, nc, dtype, rk, fc, s);
+    }
+    // the coarse iterate starts at zero: its first sweep writes every cell
+    if (opts.pre_sweeps == 0 && (int)k + 1 != last) TE_CUDA(cudaMemsetAsync(uc, 0, bytes(k + 1), s));
+    if ((int)k + 1 == last && opts.coarse_sweeps == 0) TE_CUDA(cudaMemsetAsync(uc, 0, bytes(k + 1), s));
+    visit(k + 1, fc, uc, s);
+    te::interpolate_level(levels[k + 1].interpolator, nc, dtype, uc, uk, s);
+    smooth(k, fk, uk, opts.post_sweeps, false, s);
+  }
+  void body(const void* f64, void* u64, cudaStream_t s) const {
+    // Cycle::apply (GMG/Cycle.h:94-98): u.setWithGhost(0); visit(finest, f, u)
+    if (fused()) {
+      if (dtype == TE_F64)
+        vfused<double, double, double>(0, (const double*)f64, (double*)u64, s);
+      else
+        vfused<float, double, double>(0, (const double*)f64, (double*)u64, s);
+      return;
+    }
+    if (dtype == TE_F64) {
+      if (opts.pre_sweeps == 0 || levels.size() == 1) TE_CUDA(cudaMemsetAsync(u64, 0, bytes(0), s));
+      visit(0, f64, u64, s);
+    } else {
+      te::convert_level(dom(0), nc, dtype, f[0].p, TE_F64, f64, s);
+      if (opts.pre_sweeps == 0 || levels.size() == 1) TE_CUDA(cudaMemsetAsync(u[0].p, 0, bytes(0), s));
+      visit(0, f[0].p, u[0].p, s);
+      te::convert_level(dom(0), nc, TE_F64, u64, dtype, u[0].p, s);
+    }
+  }
+  // run on stream s (which may itself be capturing)
+  void apply_on(const void* f64, void* u64, cudaStream_t s) {
+    if (!use_graph) {
+      body(f64, u64, s);
+      return;
+    }
+    auto key = std::make_pair(f64, u64);
+    auto it = graphs.find(key);
+    if (it == graphs.end()) {
+      G g;
+      long long l0 = te::g_launches.load();
+      TE_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal));
+      try {
+        body(f64, u64, cap);
+      } catch (...) {
+        cudaGraph_t junk;
+        cudaStreamEndCapture(cap, &junk);
+        if (junk) cudaGraphDestroy(junk);
+        throw;
+      }
+      TE_CUDA(cudaStreamEndCapture(cap, &g.g));
+      TE_CUDA(cudaGraphInstantiate(&g.x, g.g, 0));
+      g.launches = te::g_launches.load() - l0;
+      te::g_launches.fetch_sub(g.launches);
+      it = graphs.emplace(key, g).first;
+    }
+    TE_CUDA(cudaEventRecord(ev_in, s));
+    TE_CUDA(cudaStreamWaitEvent(cap, ev_in, 0));
+    TE_CUDA(cudaGraphLaunch(it->second.x, cap));
+    te::count_launch((int)it->second.launches);
+    TE_CUDA(cudaEventRecord(ev_out, cap));
+    TE_CUDA(cudaStreamWaitEvent(s, ev_out, 0));
+  }
+};
+

@@ -129,6 +129,11 @@ struct te_domain {
   te::DevBuf<int> d_nbr_local;     // [P*F*4]
   te::DevBuf<double> d_spacings;   // [P*D]
   te::DevBuf<float> d_spacings_f;  // [P*D]
+  // per patch and axis: 1/h^2 (Poisson) and 1/(2 h^2) (VarPoisson), [P*6], in both precisions
+  te::DevBuf<double> d_inv;
+  te::DevBuf<float> d_inv_f;
+  template <class T>
+  const T* inv() const;
   // reduction scratch: per-block partials + completion counter + result
   te::DevBuf<double> d_partials;
   te::DevBuf<unsigned int> d_counter;
@@ -138,6 +143,11 @@ struct te_domain {
   bool has_nbr_slot(int p, int slot) const { return nbr_type[(size_t)p * F + slot] >= 0; }
   ~te_domain();
 };
+
+template <>
+inline const double* te_domain::inv<double>() const { return d_inv.p; }
+template <>
+inline const float* te_domain::inv<float>() const { return d_inv_f.p; }
 
 namespace te {
 enum VecOp {

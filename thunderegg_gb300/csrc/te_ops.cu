@@ -17,6 +17,7 @@
 #include <map>
 #include <tuple>
 
+#include "te_dft.cuh"
 #include "te_ops.cuh"
 
 namespace te {
@@ -81,7 +82,7 @@ __device__ __forceinline__ T stencil(const Layout& L, const T* u, const T* c, in
 
 template <class T, int KIND>
 __global__ void __launch_bounds__(256)
-    apply_kernel(Layout L, int nc, const int8_t* __restrict__ ntype, int F, const double* __restrict__ sp,
+    apply_kernel(Layout L, int nc, const int8_t* __restrict__ ntype, int F, const T* __restrict__ sp,
                  int neumann, const T* __restrict__ coeff, T* u, T* __restrict__ f) {
   int p = blockIdx.x;
   long long ps = L.pstride(nc);
@@ -91,19 +92,18 @@ __global__ void __launch_bounds__(256)
   enforce_bc<T>(L, ntype, F, p, nc, neumann != 0, false, up);
   __syncthreads();
   T inv[3];
-  for (int a = 0; a < 3; a++) {
-    double h = a < L.D ? sp[(size_t)p * L.D + a] : 1.0;
-    inv[a] = (T)(KIND == 0 ? 1.0 / (h * h) : 1.0 / (2.0 * h * h));
-  }
-  int py = L.n1 + 2 * L.g;
-  for (long long e = threadIdx.x; e < ps; e += blockDim.x) {
-    int c = (int)(e / L.cs), k = (int)(e % L.cs);
+  for (int a = 0; a < 3; a++) inv[a] = sp[(size_t)p * 6 + (KIND ? 3 : 0) + a];
+  const int py = L.n1 + 2 * L.g;
+  const int tot = L.cs * nc;
+  for (int e = threadIdx.x; e < tot; e += blockDim.x) {
+    int c = e / L.cs, k = e - c * L.cs;
     int x = k % L.sy - L.g;
-    int y = (k / L.sy) % py - L.g;
-    int z = L.D == 3 ? k / L.sz - L.g : 0;
+    int q = k / L.sy;
+    int y = q % py - L.g;
+    int z = q / py - (L.D == 3 ? L.g : 0);
     bool interior = x >= 0 && x < L.n0 && y >= 0 && y < L.n1 && z >= 0 && z < L.n2;
     T v = T(0);
-    if (interior) v = stencil<T, KIND>(L, up + (long long)c * L.cs, cp, k, inv);
+    if (interior) v = stencil<T, KIND>(L, up + c * L.cs, cp, k, inv);
     fp[e] = v;
   }
 }
@@ -130,14 +130,11 @@ __device__ __forceinline__ T modify_cell(const Layout& L, const int8_t* ntype, i
 
 template <class T, int KIND>
 __global__ void modify_rhs_kernel(Layout L, int nc, const int8_t* __restrict__ ntype, int F,
-                                  const double* __restrict__ sp, const T* __restrict__ coeff, const T* u, T* f) {
+                                  const T* __restrict__ sp, const T* __restrict__ coeff, const T* u, T* f) {
   int p = blockIdx.x;
   long long ps = L.pstride(nc);
   T inv[3];
-  for (int a = 0; a < 3; a++) {
-    double h = a < L.D ? sp[(size_t)p * L.D + a] : 1.0;
-    inv[a] = (T)(KIND == 0 ? 1.0 / (h * h) : 1.0 / (2.0 * h * h));
-  }
+  for (int a = 0; a < 3; a++) inv[a] = sp[(size_t)p * 6 + (KIND ? 3 : 0) + a];
   int N = L.interior();
   const T* cp = KIND ? coeff + (long long)p * L.cs : nullptr;
   for (int e = threadIdx.x; e < N * nc; e += blockDim.x) {
@@ -156,17 +153,17 @@ void operator_apply(const te_operator* op, int nc, int dtype, void* u, void* f, 
   dim3 grid(d->lay.P), block(256);
   if (dtype == TE_F64) {
     if (op->kind == 0)
-      apply_kernel<double, 0><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_spacings.p,
+      apply_kernel<double, 0><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv.p,
                                                       op->neumann, nullptr, (double*)u, (double*)f);
     else
-      apply_kernel<double, 1><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_spacings.p, 0,
+      apply_kernel<double, 1><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv.p, 0,
                                                       op->coeffs.p, (double*)u, (double*)f);
   } else {
     if (op->kind == 0)
-      apply_kernel<float, 0><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_spacings.p,
+      apply_kernel<float, 0><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv_f.p,
                                                      op->neumann, nullptr, (float*)u, (float*)f);
     else
-      apply_kernel<float, 1><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_spacings.p, 0,
+      apply_kernel<float, 1><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv_f.p, 0,
                                                      op->coeffs_f.p, (float*)u, (float*)f);
   }
   count_launch();
@@ -213,84 +210,50 @@ static std::vector<double> transform_matrix(int type, int n) {
   return m;
 }
 
-constexpr int DFT_THREADS = 256;
-
-// one axis pass: out[e] = sum_j M[i][j] in[e with coord_a = j], M stored transposed (MT[j*n+i])
-template <class T>
-__device__ __forceinline__ void dft_axis(const Layout& L, int a, const T* MT, const T* in, T* out) {
-  int N = L.interior();
-  int n = L.n(a);
-  int st = a == 0 ? 1 : (a == 1 ? L.n0 : L.n0 * L.n1);
-  for (int e = threadIdx.x; e < N; e += blockDim.x) {
-    int i = (e / st) % n;
-    int base = e - i * st;
-    T acc = T(0);
-    for (int j = 0; j < n; j++) acc += MT[j * n + i] * in[base + j * st];
-    out[e] = acc;
-  }
-}
-
-template <class T, int KIND>
-__global__ void __launch_bounds__(DFT_THREADS)
-    dft_kernel(Layout L, const int8_t* __restrict__ ntype, int F, const double* __restrict__ sp,
-               const T* __restrict__ coeff, const int* __restrict__ plan_of_patch, const int* __restrict__ plan_mats,
-               const T* __restrict__ mats, const int* __restrict__ mat_off, const T* __restrict__ inv_eig,
-               const int* __restrict__ zero_mode, const T* __restrict__ f, T* u) {
-  extern __shared__ unsigned char smraw[];
+// DFTPatchSolver::solveSinglePatch for one patch per CTA.  UZERO: the
+// iterate is known to be zero (first sweep after u.setWithGhost(0)), so the
+// internal-boundary RHS terms vanish and u is not read; u's ghosts are zeroed.
+template <class T, int KIND, bool UZERO>
+__global__ void __launch_bounds__(1024) dft_kernel(Layout L, int ti_max, const int8_t* __restrict__ ntype, int F, const T* __restrict__ sp, T scale,
+                           const T* __restrict__ coeff, const int* __restrict__ plan_of_patch,
+                           const int* __restrict__ plan_mats, const T* __restrict__ mats,
+                           const int* __restrict__ mat_off, const T* __restrict__ inv_eig,
+                           const int* __restrict__ zero_mode, const T* __restrict__ f, T* u) {
+  extern __shared__ __align__(16) unsigned char smraw[];
   T* sm = reinterpret_cast<T*>(smraw);
-  int p = blockIdx.x;
-  int N = L.interior();
-  int nmax = max(L.n0, max(L.n1, L.n2));
+  const SmemLay S = smem_lay(L);
+  const int p = blockIdx.x;
+  const int N = L.interior();
+  const int D = L.D;
   T* A = sm;
-  T* B = A + N;
-  T* MT = B + N;  // nmax * nmax
-  long long ps = L.pstride(1);
+  T* B = A + S.size;
+  const long long ps = L.pstride(1);
   const T* fp = f + p * ps;
   T* up = u + p * ps;
   const T* cp = KIND ? coeff + (long long)p * L.cs : nullptr;
+  const int plan = plan_of_patch[p];
+  const T* MT[6];
+  dft_mat_ptrs<T>(L, plan, plan_mats, mats, mat_off, MT);
   T inv[3];
-  for (int a = 0; a < 3; a++) {
-    double h = a < L.D ? sp[(size_t)p * L.D + a] : 1.0;
-    inv[a] = (T)(KIND == 0 ? 1.0 / (h * h) : 1.0 / (2.0 * h * h));
-  }
+  for (int a = 0; a < 3; a++) inv[a] = sp[(size_t)p * 6 + (KIND ? 3 : 0) + a];
   // f_copy with the internal boundary conditions folded in (modifyRHS)
+#pragma unroll 2
   for (int e = threadIdx.x; e < N; e += blockDim.x) {
-    int x, y, z;
-    decompose(L, e, x, y, z);
+    int x = e % L.n0, r = e / L.n0, y = r % L.n1, z = r / L.n1;
     int k = L.at(x, y, z);
-    A[e] = modify_cell<T, KIND>(L, ntype, F, p, up, cp, x, y, z, k, fp[k], inv);
-  }
-  int plan = plan_of_patch[p];
-  T* cur = A;
-  T* nxt = B;
-  for (int pass = 0; pass < 2; pass++) {
-    for (int a = 0; a < L.D; a++) {
-      int n = L.n(a);
-      const T* M = mats + mat_off[plan_mats[plan * 6 + pass * 3 + a]];
-      __syncthreads();
-      for (int e = threadIdx.x; e < n * n; e += blockDim.x) MT[e] = M[e];
-      __syncthreads();
-      dft_axis<T>(L, a, MT, cur, nxt);
-      T* t = cur;
-      cur = nxt;
-      nxt = t;
-    }
-    if (pass == 0) {
-      __syncthreads();
-      const T* ie = inv_eig + (long long)plan * N;
-      for (int e = threadIdx.x; e < N; e += blockDim.x) cur[e] *= ie[e];
-      __syncthreads();
-      if (zero_mode[p] && threadIdx.x == 0) cur[0] = T(0);
-    }
+    T v = fp[k];
+    if (!UZERO) v = modify_cell<T, KIND>(L, ntype, F, p, up, cp, x, y, z, k, v, inv);
+    A[x + y * S.sy + z * S.sz] = v;
   }
   __syncthreads();
-  T scale = T(1);
-  for (int a = 0; a < L.D; a++) scale *= T(2.0 / L.n(a));
-  (void)nmax;
+  T* cur = dft_solve_smem<T>(L, S, MT, inv_eig + (long long)plan * N, zero_mode[p] != 0, A, B, ti_max);
+  if (UZERO) {
+    for (int k = threadIdx.x; k < L.cs; k += blockDim.x) up[k] = T(0);
+    __syncthreads();
+  }
   for (int e = threadIdx.x; e < N; e += blockDim.x) {
-    int x, y, z;
-    decompose(L, e, x, y, z);
-    up[L.at(x, y, z)] = cur[e] * scale;
+    int x = e % L.n0, r = e / L.n0, y = r % L.n1, z = r / L.n1;
+    up[L.at(x, y, z)] = cur[x + y * S.sy + z * S.sz] * scale;
   }
 }
 
@@ -351,7 +314,7 @@ __device__ void patch_apply(const Layout& L, const int8_t* ntype, int F, int p, 
 
 template <class T, int KIND>
 __global__ void __launch_bounds__(BCG_THREADS)
-    bicgstab_patch_kernel(Layout L, const int8_t* __restrict__ ntype, int F, const double* __restrict__ sp,
+    bicgstab_patch_kernel(Layout L, const int8_t* __restrict__ ntype, int F, const T* __restrict__ sp,
                           int neumann, const T* __restrict__ coeff, const T* __restrict__ f, T* u, double tol,
                           int max_it, int cont, bool use_smem, T* gscratch, unsigned long long* its_out,
                           int* status) {
@@ -365,10 +328,7 @@ __global__ void __launch_bounds__(BCG_THREADS)
   T* up = u + (long long)p * cs;
   const T* cp = KIND ? coeff + (long long)p * cs : nullptr;
   T inv[3];
-  for (int a = 0; a < 3; a++) {
-    double h = a < L.D ? sp[(size_t)p * L.D + a] : 1.0;
-    inv[a] = (T)(KIND == 0 ? 1.0 / (h * h) : 1.0 / (2.0 * h * h));
-  }
+  for (int a = 0; a < 3; a++) inv[a] = sp[(size_t)p * 6 + (KIND ? 3 : 0) + a];
   // x = u (all cells); b = f_copy (zero ghosts, modifyRHS applied); others zero
   for (int e = threadIdx.x; e < cs; e += blockDim.x) {
     x[e] = up[e];
@@ -437,25 +397,53 @@ __global__ void __launch_bounds__(BCG_THREADS)
 }
 
 static size_t dft_smem(const Layout& L, int tsize) {
-  int N = L.interior();
-  int nmax = std::max(L.n0, std::max(L.n1, L.n2));
-  return (size_t)(2 * N + nmax * nmax) * tsize;
+  SmemLay S = smem_lay(L);
+  return ((size_t)S.mats + smem_mat_elems(L)) * tsize;
+}
+
+static int dft_threads(const Layout& L) {
+  int best = 32;
+  for (int a = 0; a < L.D; a++) {
+    int n = L.n(a);
+    int ti = n % 8 == 0 ? 8 : (n % 4 == 0 ? 4 : (n % 2 == 0 ? 2 : 1));
+    int tasks = (L.interior() / n) * (n / ti);
+    best = std::max(best, tasks);
+  }
+  best = (best + 31) / 32 * 32;
+  return std::min(best, 256);
 }
 
 template <class T>
 static void launch_dft(const te_patch_solver* ps, const T* f, T* u, const T* coeff, const T* mats,
-                       const T* ie, cudaStream_t s) {
+                       const T* ie, bool uzero, cudaStream_t s) {
   const te_domain* d = ps->op->dom;
   size_t smem = dft_smem(d->lay, sizeof(T));
-  auto k0 = dft_kernel<T, 0>;
-  auto k1 = dft_kernel<T, 1>;
-  auto kern = ps->op->kind == 0 ? k0 : k1;
-  if (smem > 48 * 1024) TE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<d->lay.P, DFT_THREADS, smem, s>>>(d->lay, d->d_nbr_type.p, d->F, d->d_spacings.p, coeff,
-                                             ps->plan_of_patch.p, ps->plan_mats.p, mats, ps->mat_off.p, ie,
-                                             ps->zero_mode.p, f, u);
+  int ti_max, threads;
+  dft_launch_shape(d->lay, ti_max, threads);
+  auto kern = ps->op->kind == 0 ? (uzero ? dft_kernel<T, 0, true> : dft_kernel<T, 0, false>)
+                                : (uzero ? dft_kernel<T, 1, true> : dft_kernel<T, 1, false>);
+  double scale = 1.0;
+  for (int a = 0; a < d->lay.D; a++) scale *= 2.0 / d->lay.n(a);
+  kern<<<d->lay.P, threads, smem, s>>>(d->lay, ti_max, d->d_nbr_type.p, d->F, d->template inv<T>(), (T)scale, coeff,
+                                        ps->plan_of_patch.p, ps->plan_mats.p, mats, ps->mat_off.p, ie,
+                                        ps->zero_mode.p, f, u);
   count_launch();
   TE_LAUNCH_CHECK();
+}
+
+// raise the dynamic shared-memory limit of every DFT kernel instance once
+static void dft_set_smem_limits(size_t smem64, size_t smem32) {
+  auto set = [](const void* k, size_t sm) {
+    if (sm > 48 * 1024) TE_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  };
+  set((const void*)dft_kernel<double, 0, true>, smem64);
+  set((const void*)dft_kernel<double, 0, false>, smem64);
+  set((const void*)dft_kernel<double, 1, true>, smem64);
+  set((const void*)dft_kernel<double, 1, false>, smem64);
+  set((const void*)dft_kernel<float, 0, true>, smem32);
+  set((const void*)dft_kernel<float, 0, false>, smem32);
+  set((const void*)dft_kernel<float, 1, true>, smem32);
+  set((const void*)dft_kernel<float, 1, false>, smem32);
 }
 
 template <class T>
@@ -464,21 +452,34 @@ static void launch_bcg(const te_patch_solver* ps, const T* f, T* u, const T* coe
   const Layout& L = d->lay;
   size_t need = (size_t)8 * L.cs * sizeof(T);
   bool use_smem = need <= 200 * 1024;
-  T* scratch = nullptr;
-  if (!use_smem) {
-    size_t bytes = (size_t)L.P * need;
-    if (ps->scratch.n < bytes) ps->scratch.alloc(bytes);
-    scratch = reinterpret_cast<T*>(ps->scratch.p);
-  }
+  T* scratch = use_smem ? nullptr : reinterpret_cast<T*>(ps->scratch.p);
   size_t smem = use_smem ? need : 0;
-  auto k0 = bicgstab_patch_kernel<T, 0>;
-  auto k1 = bicgstab_patch_kernel<T, 1>;
-  auto kern = ps->op->kind == 0 ? k0 : k1;
-  if (smem > 48 * 1024) TE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<L.P, BCG_THREADS, smem, s>>>(L, d->d_nbr_type.p, d->F, d->d_spacings.p, ps->op->neumann, coeff, f, u,
+  auto kern = ps->op->kind == 0 ? bicgstab_patch_kernel<T, 0> : bicgstab_patch_kernel<T, 1>;
+  kern<<<L.P, BCG_THREADS, smem, s>>>(L, d->d_nbr_type.p, d->F, d->template inv<T>(), ps->op->neumann, coeff, f, u,
                                        ps->tol, ps->max_it, ps->cont, use_smem, scratch, ps->its.p, ps->status.p);
   count_launch();
   TE_LAUNCH_CHECK();
+}
+
+// shared-memory limits and global scratch are set up when the solver is
+// created, so that launches can be captured into CUDA graphs
+static void bcg_prepare(te_patch_solver* ps) {
+  const Layout& L = ps->op->dom->lay;
+  auto setup = [&](auto tag, const void* k0, const void* k1) {
+    using T = decltype(tag);
+    size_t need = (size_t)8 * L.cs * sizeof(T);
+    if (need <= 200 * 1024) {
+      if (need > 48 * 1024) {
+        TE_CUDA(cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+        TE_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+      }
+    } else {
+      size_t bytes = (size_t)L.P * need;
+      if (ps->scratch.n < bytes) ps->scratch.alloc(bytes);
+    }
+  };
+  setup(double(0), (const void*)bicgstab_patch_kernel<double, 0>, (const void*)bicgstab_patch_kernel<double, 1>);
+  setup(float(0), (const void*)bicgstab_patch_kernel<float, 0>, (const void*)bicgstab_patch_kernel<float, 1>);
 }
 
 void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, void* u, bool zero_first,
@@ -486,6 +487,15 @@ void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, v
   const te_operator* op = ps->op;
   const te_domain* d = op->dom;
   require(nc == 1, "patch solvers support one component", TE_ERR_UNSUPPORTED);
+  if (ps->kind == 0 && zero_first) {
+    // PatchSolver::apply / a first sweep on u.setWithGhost(0): with u == 0 the
+    // ghost fill and the RHS modification contribute exactly zero
+    if (dtype == TE_F64)
+      launch_dft<double>(ps, (const double*)f, (double*)u, op->coeffs.p, ps->mats.p, ps->inv_eig.p, true, s);
+    else
+      launch_dft<float>(ps, (const float*)f, (float*)u, op->coeffs_f.p, ps->mats_f.p, ps->inv_eig_f.p, true, s);
+    return;
+  }
   if (zero_first) {
     // PatchSolver::apply: u.setWithGhost(0) (PatchSolver.h:118)
     TE_CUDA(cudaMemsetAsync(u, 0, (size_t)d->lay.P * d->lay.pstride(nc) * (dtype == TE_F64 ? 8 : 4), s));
@@ -494,9 +504,9 @@ void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, v
   }
   if (ps->kind == 0) {
     if (dtype == TE_F64)
-      launch_dft<double>(ps, (const double*)f, (double*)u, op->coeffs.p, ps->mats.p, ps->inv_eig.p, s);
+      launch_dft<double>(ps, (const double*)f, (double*)u, op->coeffs.p, ps->mats.p, ps->inv_eig.p, false, s);
     else
-      launch_dft<float>(ps, (const float*)f, (float*)u, op->coeffs_f.p, ps->mats_f.p, ps->inv_eig_f.p, s);
+      launch_dft<float>(ps, (const float*)f, (float*)u, op->coeffs_f.p, ps->mats_f.p, ps->inv_eig_f.p, false, s);
   } else {
     if (dtype == TE_F64)
       launch_bcg<double>(ps, (const double*)f, (double*)u, op->coeffs.p, s);
@@ -572,17 +582,17 @@ int te_operator_modify_rhs(const te_operator* op, int nc, int dtype, const void*
     cudaStream_t s = d->stream;
     if (dtype == TE_F64) {
       if (op->kind == 0)
-        modify_rhs_kernel<double, 0><<<d->lay.P, 256, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_spacings.p,
+        modify_rhs_kernel<double, 0><<<d->lay.P, 256, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv.p,
                                                               nullptr, (const double*)u, (double*)f);
       else
-        modify_rhs_kernel<double, 1><<<d->lay.P, 256, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_spacings.p,
+        modify_rhs_kernel<double, 1><<<d->lay.P, 256, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv.p,
                                                               op->coeffs.p, (const double*)u, (double*)f);
     } else {
       if (op->kind == 0)
-        modify_rhs_kernel<float, 0><<<d->lay.P, 256, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_spacings.p,
+        modify_rhs_kernel<float, 0><<<d->lay.P, 256, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv_f.p,
                                                              nullptr, (const float*)u, (float*)f);
       else
-        modify_rhs_kernel<float, 1><<<d->lay.P, 256, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_spacings.p,
+        modify_rhs_kernel<float, 1><<<d->lay.P, 256, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv_f.p,
                                                              op->coeffs_f.p, (const float*)u, (float*)f);
     }
     count_launch();
@@ -598,6 +608,7 @@ int te_dft_patch_solver_create(const te_operator* op, int neumann_mask, te_patch
     int D = L.D, P = L.P, N = L.interior();
     size_t smem = dft_smem(L, sizeof(double));
     require(smem <= 220 * 1024, "patch too large for the DFT patch solver", TE_ERR_UNSUPPORTED);
+    dft_set_smem_limits(smem, dft_smem(L, sizeof(float)));
     auto ps = std::make_unique<te_patch_solver>();
     ps->op = op;
     ps->kind = 0;
@@ -705,6 +716,7 @@ int te_bicgstab_patch_solver_create(const te_operator* op, double tol, int max_i
     ps->cont = cont;
     ps->its.alloc(1);
     ps->status.alloc(1);
+    bcg_prepare(ps.get());
     TE_CUDA(cudaMemsetAsync(ps->its.p, 0, sizeof(unsigned long long), op->dom->stream));
     TE_CUDA(cudaMemsetAsync(ps->status.p, 0, sizeof(int), op->dom->stream));
     TE_CUDA(cudaStreamSynchronize(op->dom->stream));

@@ -1,5 +1,8 @@
 // te_ops.cuh -- operator and patch-solver handles (internal).
 #pragma once
+#include <map>
+#include <memory>
+
 #include "te_ghost.cuh"
 
 struct te_operator {
@@ -10,6 +13,8 @@ struct te_operator {
   te::DevBuf<double> coeffs;    // VarPoisson: ghost-filled coefficient level buffer (1 component)
   te::DevBuf<float> coeffs_f;   // FP32 copy for the mixed-precision cycle
   te::FaceTable faces;
+  // work vectors of te_bicgstab_solve with this operator, per component count
+  mutable std::map<int, std::shared_ptr<void>> krylov;
   const void* coeff_ptr(int dtype) const {
     return kind == 0 ? nullptr : (dtype == TE_F64 ? (const void*)coeffs.p : (const void*)coeffs_f.p);
   }

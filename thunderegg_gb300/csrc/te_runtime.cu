@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <mutex>
 
 #include "te_internal.cuh"
@@ -48,38 +49,41 @@ cudaStream_t current_stream() { return g_stream; }
 template <class T>
 struct Elem;
 
-// one thread per interior cell of (P x nc) padded patches
-__device__ __forceinline__ long long interior_index(const Layout& L, int nc, long long i) {
-  int x = (int)(i % L.n0);
-  long long r = i / L.n0;
-  int y = (int)(r % L.n1);
-  r /= L.n1;
-  int z = (int)(r % L.n2);
-  r /= L.n2;  // r = p * nc + c
-  return r * L.cs + L.at(x, y, z);
+// Interior cells are visited one padded (patch, component) block at a time:
+// block b handles blocks pc = b, b + gridDim.x, ...; threads walk its interior
+// cells with 32-bit index arithmetic.
+__device__ __forceinline__ int interior_offset(const Layout& L, int e) {
+  int x = e % L.n0;
+  int r = e / L.n0;
+  int y = r % L.n1;
+  int z = r / L.n1;
+  return L.at(x, y, z);
 }
 
 template <class T, int OP>
-__global__ void vec_kernel(Layout L, int nc, long long n, T* x, const T* a, const T* b, double alpha,
-                           double beta, double gamma) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    long long k = interior_index(L, nc, i);
-    T xv = x[k];
-    if (OP == OP_SET) xv = (T)alpha;
-    if (OP == OP_SCALE) xv *= (T)alpha;
-    if (OP == OP_SHIFT) xv += (T)alpha;
-    if (OP == OP_COPY) xv = a[k];
-    if (OP == OP_ADD) xv += a[k];
-    // reference: view += b_view * alpha  (Vector.h:495)
-    if (OP == OP_ADD_SCALED) xv += a[k] * (T)alpha;
-    // view += a * alpha + b * beta  (Vector.h:507-511)
-    if (OP == OP_ADD_SCALED2) xv += a[k] * (T)alpha + b[k] * (T)beta;
-    // view = view * alpha + b  (Vector.h:523)
-    if (OP == OP_SCALE_THEN_ADD) xv = xv * (T)alpha + a[k];
-    if (OP == OP_SCALE_THEN_ADD_SCALED) xv = xv * (T)alpha + a[k] * (T)beta;
-    if (OP == OP_SCALE_THEN_ADD_SCALED2) xv = xv * (T)alpha + a[k] * (T)beta + b[k] * (T)gamma;
-    x[k] = xv;
+__global__ void vec_kernel(Layout L, int npc, T* x, const T* a, const T* b, double alpha, double beta,
+                           double gamma) {
+  const int N = L.interior();
+  for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
+    long long base = (long long)pc * L.cs;
+    for (int e = threadIdx.x; e < N; e += blockDim.x) {
+      long long k = base + interior_offset(L, e);
+      T xv = x[k];
+      if (OP == OP_SET) xv = (T)alpha;
+      if (OP == OP_SCALE) xv *= (T)alpha;
+      if (OP == OP_SHIFT) xv += (T)alpha;
+      if (OP == OP_COPY) xv = a[k];
+      if (OP == OP_ADD) xv += a[k];
+      // reference: view += b_view * alpha  (Vector.h:495)
+      if (OP == OP_ADD_SCALED) xv += a[k] * (T)alpha;
+      // view += a * alpha + b * beta  (Vector.h:507-511)
+      if (OP == OP_ADD_SCALED2) xv += a[k] * (T)alpha + b[k] * (T)beta;
+      // view = view * alpha + b  (Vector.h:523)
+      if (OP == OP_SCALE_THEN_ADD) xv = xv * (T)alpha + a[k];
+      if (OP == OP_SCALE_THEN_ADD_SCALED) xv = xv * (T)alpha + a[k] * (T)beta;
+      if (OP == OP_SCALE_THEN_ADD_SCALED2) xv = xv * (T)alpha + a[k] * (T)beta + b[k] * (T)gamma;
+      x[k] = xv;
+    }
   }
 }
 
@@ -106,12 +110,12 @@ static int grid_for(long long n, int block = 256) {
 template <class T>
 static void launch_vec(const te_domain* d, int nc, int op, T* x, const T* a, const T* b, double al,
                        double be, double ga, cudaStream_t s) {
-  long long n = (long long)d->lay.P * nc * d->lay.interior();
-  if (n == 0) return;
-  int grid = grid_for(n);
+  int npc = d->lay.P * nc;
+  if (npc == 0) return;
+  int grid = npc < 152 * 8 ? npc : 152 * 8;
 #define TE_VEC_CASE(OPV)                                                                   \
   case OPV:                                                                                \
-    vec_kernel<T, OPV><<<grid, 256, 0, s>>>(d->lay, nc, n, x, a, b, al, be, ga);          \
+    vec_kernel<T, OPV><<<grid, 256, 0, s>>>(d->lay, npc, x, a, b, al, be, ga);            \
     break;
   switch (op) {
     TE_VEC_CASE(OP_SET)
@@ -173,16 +177,19 @@ __device__ double block_reduce(double v) {
 
 // MODE 0: dot(x, y); MODE 1: max(x) with 0 floor (Vector::infNorm, Vector.h:568-578)
 template <class T, int MODE>
-__global__ void reduce_kernel(Layout L, int nc, long long n, const T* x, const T* y, double* partials,
+__global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double* partials,
                               unsigned int* counter, double* out) {
   double acc = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    long long k = interior_index(L, nc, i);
-    if (MODE == 0)
-      acc += (double)x[k] * (double)y[k];
-    else
-      acc = fmax((double)x[k], acc);
+  const int N = L.interior();
+  for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
+    long long base = (long long)pc * L.cs;
+    for (int e = threadIdx.x; e < N; e += blockDim.x) {
+      long long k = base + interior_offset(L, e);
+      if (MODE == 0)
+        acc += (double)x[k] * (double)y[k];
+      else
+        acc = fmax((double)x[k], acc);
+    }
   }
   double b = block_reduce<MODE == 1>(acc);
   __shared__ bool last;
@@ -210,21 +217,21 @@ __global__ void reduce_kernel(Layout L, int nc, long long n, const T* x, const T
 
 static void reduce_launch(const te_domain* d, int nc, int dtype, const void* x, const void* y, int mode,
                           double* d_out, cudaStream_t s) {
-  long long n = (long long)d->lay.P * nc * d->lay.interior();
-  int grid = d->red_blocks;
+  int npc = d->lay.P * nc;
+  int grid = std::min(d->red_blocks, npc);
   if (dtype == TE_F64) {
     if (mode == 0)
-      reduce_kernel<double, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, nc, n, (const double*)x, (const double*)y,
+      reduce_kernel<double, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, (const double*)y,
                                                             d->d_partials.p, d->d_counter.p, d_out);
     else
-      reduce_kernel<double, 1><<<grid, RED_THREADS, 0, s>>>(d->lay, nc, n, (const double*)x, nullptr,
+      reduce_kernel<double, 1><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, nullptr,
                                                             d->d_partials.p, d->d_counter.p, d_out);
   } else {
     if (mode == 0)
-      reduce_kernel<float, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, nc, n, (const float*)x, (const float*)y,
+      reduce_kernel<float, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const float*)x, (const float*)y,
                                                            d->d_partials.p, d->d_counter.p, d_out);
     else
-      reduce_kernel<float, 1><<<grid, RED_THREADS, 0, s>>>(d->lay, nc, n, (const float*)x, nullptr,
+      reduce_kernel<float, 1><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const float*)x, nullptr,
                                                            d->d_partials.p, d->d_counter.p, d_out);
   }
   count_launch();
@@ -354,6 +361,15 @@ int te_domain_create(const te_level_desc* desc, te_domain** out) {
     d->d_spacings.upload(d->spacings, st);
     std::vector<float> spf(d->spacings.begin(), d->spacings.end());
     d->d_spacings_f.upload(spf, st);
+    std::vector<double> inv((size_t)P * 6, 1.0);
+    for (int p = 0; p < P; p++)
+      for (int a = 0; a < D; a++) {
+        double h = d->spacings[(size_t)p * D + a];
+        inv[(size_t)p * 6 + a] = 1.0 / (h * h);
+        inv[(size_t)p * 6 + 3 + a] = 1.0 / (2.0 * h * h);
+      }
+    d->d_inv.upload(inv, st);
+    d->d_inv_f.upload(std::vector<float>(inv.begin(), inv.end()), st);
     d->red_blocks = 152 * 2;
     d->d_partials.alloc(d->red_blocks);
     d->d_counter.alloc(1);
