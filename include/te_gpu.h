@@ -214,6 +214,24 @@ int te_bicgstab_solve(const te_operator* A, int ncomp, void* x, const void* b, c
                       double tol, int max_iterations, int flags, int* iterations,
                       double* final_residual);
 
+/* ---- dot product without allocation ---------------------------------------
+ * No counterpart in the reference (ThunderEgg reduces on the host).
+ * For callers that cannot call cudaMalloc when they need a reduction: code
+ * running while a stream is captured into a CUDA graph, hosts whose device
+ * memory belongs to another allocator, or callers that must not trigger the
+ * device-wide synchronisation an allocation can cause.  Computes the
+ * interior dot product of two level buffers of the given layout (the same
+ * result as te_vec_dot) and allocates nothing: its scratch is a fixed device
+ * array of TE_NOALLOC_MAX_PARTIALS + 1 doubles that every GPU using this
+ * library holds until exit.  num_patches * ncomp above TE_NOALLOC_MAX_PARTIALS
+ * is rejected with TE_ERR_UNSUPPORTED.  Calls share the array: calls that
+ * overlap on the GPU race, so serialise them.  The first call on a device
+ * looks up the array's device address; make it before any stream capture.
+ * Synchronises `cuda_stream` (NULL = legacy default stream) to return *out. */
+#define TE_NOALLOC_MAX_PARTIALS 65536
+int te_level_dot_noalloc(int dim, const int* ns, int num_ghost, int num_patches, int ncomp, int dtype,
+                         const void* x, const void* y, double* out, void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

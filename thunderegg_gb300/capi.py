@@ -17,6 +17,7 @@ TE_ERR_UNSUPPORTED, TE_ERR_BUDGET, TE_ERR_TIMEOUT, TE_ERR_NOT_CONVERGED = 4, 5, 
 TE_F64, TE_F32 = 0, 1
 TE_GHOST_BILINEAR, TE_GHOST_BIQUADRATIC, TE_GHOST_TRILINEAR = 0, 1, 2
 TE_FILL_FACES, TE_FILL_EDGES, TE_FILL_CORNERS = 0, 1, 2
+TE_NOALLOC_MAX_PARTIALS = 65536
 
 _ip = ctypes.POINTER(ctypes.c_int)
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -103,6 +104,7 @@ _SIGS = {
     "te_cycle_destroy": (_I, [_V]),
     "te_cycle_apply": (_I, [_V, _I, _V, _V]),
     "te_bicgstab_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, _I, _ip, _dp]),
+    "te_level_dot_noalloc": (_I, [_I, _ip, _I, _I, _I, _I, _V, _V, _dp, _V]),
 }
 
 _lib = None
