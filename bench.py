@@ -6,8 +6,10 @@ Workload (one "step" = one complete solve to a 1e-10 relative FP64 residual):
   balanced (1444 leaves, 8 GMG levels), 32x32-cell patches, u = exp(xy),
   Dirichlet data from u; BiQuadratic ghost filling, DFT patch smoother,
   V(1,1) cycle, BiCGStab outer solver.
-  value: mixed precision (FP32 V-cycle, FP64 BiCGStab/residuals), inputs
-         resident in HBM.  The plain FP64 drop-in is reported beside it.
+  value: mixed precision (FP32 V-cycle, FP64 BiCGStab/residuals), served as
+         a batch of --batch independent solves per step (one right-hand side
+         each), inputs resident in HBM.  Single-solve latency and the plain
+         FP64 drop-in (one solve at a time) are reported beside it.
   e2e:   the same solve through the C ABI from pinned host buffers: f copied
          host->device and u device->host inside the timed region.
   L2: flushed (256 MiB write) between timed steps, outside the step timing.
@@ -41,6 +43,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--fp64-steps", type=int, default=5)
+    ap.add_argument("--batch", type=int, default=16, help="solves served per step")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--only-mixed", action="store_true",
                     help="time the mixed-precision solves only (for profiler captures)")
@@ -159,6 +162,25 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def _phase_bytes(name, levels, dtype_bytes):
+    """Algorithmic bytes of one launch of a fused V-cycle phase on level k
+    ("Measurement"): interior cells only, each value read or
+    written once; ghost gathers count 2D/n reads per cell."""
+    k = int(name.split()[0][1:])
+    lv = levels[k]
+    cells = lv.num_cells
+    D, n = lv.dim, lv.ns[0]
+    w = dtype_bytes
+    wf = 8 if k == 0 else w  # the finest level reads FP64 f and writes FP64 u
+    wo = 8 if k == 0 else w
+    ghost = w * 2 * D / n
+    if "pre-smooth" in name:
+        return cells * (wf + w)
+    if "restrict" in name:
+        return cells * (w + wf + ghost + w / (1 << D))
+    return cells * (w + w / (1 << D) + wf + ghost + wo)
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -171,17 +193,29 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     import thunderegg_gb300 as te
     from thunderegg_gb300 import build as tb
+    from thunderegg_gb300 import mesh as M
     from thunderegg_gb300 import problems as PB
     from thunderegg_gb300.gmg import GmgOptions, GmgSolver
 
     tb.build()
     L = te.capi.lib()
+    B = args.batch
     levels, f_np, exact = PB.config2()
-    mixed = GmgSolver(levels, GmgOptions(scheme=1, smoother=0, tol=1e-10, cycle_dtype=te.TE_F32, bicgstab_flags=1))
-    fp64 = GmgSolver(levels, GmgOptions(scheme=1, smoother=0, tol=1e-10, cycle_dtype=te.TE_F64, bicgstab_flags=1))
-    dom = mixed.finest
-    f = te.Vector.from_numpy(dom, f_np)
-    u = te.Vector(dom)
+    rng = np.random.default_rng(2024)
+    # B independent right-hand sides on the same mesh: the benchmark problem plus
+    # seeded sine-mode perturbations (each solve is a full, distinct solve)
+    fs = [f_np] + [f_np + 0.1 * PB.sine_modes_rhs(levels[0], rng) for _ in range(B - 1)]
+    mixed_opts = GmgOptions(scheme=1, smoother=0, tol=1e-10, cycle_dtype=te.TE_F32, bicgstab_flags=1)
+    fp64_opts = GmgOptions(scheme=1, smoother=0, tol=1e-10, cycle_dtype=te.TE_F64, bicgstab_flags=1)
+    blevels, offsets = M.union_hierarchy([levels] * B)
+    served = GmgSolver(blevels, mixed_opts)
+    single = GmgSolver(levels, mixed_opts)
+    fp64 = GmgSolver(levels, fp64_opts)
+    fB_np = np.concatenate(fs, axis=0)
+    fB = te.Vector.from_numpy(served.finest, fB_np)
+    uB = te.Vector(served.finest)
+    f1 = te.Vector.from_numpy(single.finest, f_np)
+    u1 = te.Vector(single.finest)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
 
@@ -190,34 +224,30 @@ def run_gpu(args):
         if world > 1:
             torch.distributed.barrier()
 
-    def timed_solves(solver, k, warm, host=False):
-        hf = torch.from_numpy(f_np).pin_memory() if host else None
-        hu = torch.empty(f_np.shape, dtype=torch.float64).pin_memory() if host else None
-        times, its, res = [], [], []
+    def timed(step, k, warm):
+        times, out = [], None
         for i in range(warm + k):
             flush.fill_(i & 0xFF)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            if host:
-                f.t.copy_(hf, non_blocking=True)
-            u.t.zero_()
-            n = solver.solve(f, u)
-            if host:
-                hu.copy_(u.t, non_blocking=True)
+            out = step()
             e1.record(stream)
             torch.cuda.synchronize()
             if i >= warm:
                 times.append(e0.elapsed_time(e1) / 1000.0)
-                its.append(n)
-        res = solver.residual(f, u)
-        return times, its, res
+        return times, out
 
+    def served_step():
+        uB.t.zero_()
+        return served.solve_batched(fB, uB, offsets[0])
+
+    # ---- headline: mixed precision, B solves served per step, inputs in HBM
     barrier()
     launches0 = L.te_kernel_launch_count()
     clk = Clocks(local)
     t_wall = time.perf_counter()
-    times, its, res = timed_solves(mixed, args.steps, args.warmup)
+    times, (its, res, st) = timed(served_step, args.steps, args.warmup)
     t_wall = time.perf_counter() - t_wall
     clocks = clk.stop()
     launches = (L.te_kernel_launch_count() - launches0) * args.steps // (args.steps + args.warmup)
@@ -227,45 +257,64 @@ def run_gpu(args):
         tt = torch.tensor([total], device="cuda")
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         total = float(tt.item())
-    value = world * args.steps / total
-    err = float(np.abs(PB.interior_view(levels[0], u.numpy()) - PB.interior_view(levels[0], exact)).max())
+    value = world * B * args.steps / total
+    true_res = []
+    uB_np = uB.numpy()
+    for b in range(B):
+        sl = slice(offsets[0][b], offsets[0][b + 1])
+        uu = te.Vector.from_numpy(single.finest, uB_np[sl])
+        ff = te.Vector.from_numpy(single.finest, fB_np[sl])
+        true_res.append(single.residual(ff, uu))
+    err = float(np.abs(PB.interior_view(levels[0], uB_np[:levels[0].num_patches])
+                       - PB.interior_view(levels[0], exact)).max())
+
     if args.only_mixed:
         if rank == 0:
-            print(json.dumps({"metric": METRIC, "value": value, "unit": "solves/s", "ms_per_step": 1000 * total / args.steps,
-                              "outer_iterations": its[-1], "final_rel_residual_fp64": res,
-                              "gpu_launches": int(launches), "clocks": clocks}), flush=True)
+            print(json.dumps({"metric": METRIC, "value": value, "unit": "solves/s", "batch": B,
+                              "ms_per_step": 1000 * total / args.steps, "outer_iterations": max(its),
+                              "max_true_rel_residual": max(true_res), "gpu_launches": int(launches),
+                              "clocks": clocks}), flush=True)
         return
 
-    # e2e through the C ABI from pinned host memory
-    e_times, _, e_res = timed_solves(mixed, max(3, args.steps // 2), 1, host=True)
-    e2e = world * len(e_times) / sum(e_times)
+    # ---- one solve at a time (latency), mixed and plain FP64 drop-in
+    def single_step(s, f, u):
+        def run():
+            u.t.zero_()
+            return s.solve(f, u)
+        return run
 
-    # plain FP64 drop-in on the same GPU
-    d_times, d_its, d_res = timed_solves(fp64, args.fp64_steps, 1)
+    lat, its1 = timed(single_step(single, f1, u1), args.steps, 2)
+    d_times, d_its = timed(single_step(fp64, f1, u1), args.fp64_steps, 1)
+    d_res = fp64.residual(f1, u1)
 
-    # dominant kernel: FP64 star operator apply on the finest level, timed alone
-    r = te.Vector(dom)
-    for _ in range(3):
-        fp64.ops[0].apply(u, r)
-    nrep = 50
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(nrep):
-        fp64.ops[0].apply(u, r)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    apply_s = e0.elapsed_time(e1) / 1000.0 / nrep
-    cells = levels[0].num_cells
-    n = levels[0].ns[0]
-    alg_bytes = 8 * cells * (2 + 4 / n)
+    # ---- e2e: the served step through the C ABI from pinned host memory
+    hf = torch.from_numpy(fB_np).pin_memory()
+    hu = torch.empty(fB_np.shape, dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        fB.t.copy_(hf, non_blocking=True)
+        uB.t.zero_()
+        out = served.solve_batched(fB, uB, offsets[0])
+        hu.copy_(uB.t, non_blocking=True)
+        return out
+
+    e_times, _ = timed(e2e_step, max(3, args.steps // 2), 1)
+    e2e = world * B * len(e_times) / sum(e_times)
+
+    # ---- dominant kernel: per-phase device times of one V-cycle of the served batch
+    mp = te.Vector(served.finest)
+    phases = served.cycle.timings(fB, mp)
+    phases.sort(key=lambda x: -x[1])
+    top_name, top_ms = phases[0]
+    alg = _phase_bytes(top_name, blevels, 4)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    achieved = alg_bytes / apply_s / 1e9
+    achieved = alg / (top_ms / 1000.0) / 1e9
+    cyc_total = sum(t for _, t in phases)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -273,28 +322,36 @@ def run_gpu(args):
         cpu = {"value": 1.0 / out[0][0], "unit": "solves/s", "cores": 1, "kind": "port",
                "sample": "one full FP64 solve of the same workload by the CPU restatement, 1 core"}
 
-    lat = sorted(times)
-    p50 = statistics.median(lat)
-    p99 = lat[min(len(lat) - 1, int(round(0.99 * (len(lat) - 1))))]
+    def pct(v, q):
+        v = sorted(v)
+        return v[min(len(v) - 1, int(round(q * (len(v) - 1))))]
+
     line = {
         "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 V-cycle + f64 Krylov", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "patches": levels[0].num_patches, "levels": len(levels),
-                   "cells": cells, "l2": "flushed between steps (256 MiB write), outside step timing",
+        "config": {"workload": WORKLOAD, "served_batch": B, "patches_per_solve": levels[0].num_patches,
+                   "levels": len(levels), "cells_per_solve": levels[0].num_cells,
+                   "rhs": "benchmark RHS + seeded sine-mode perturbations (one per solve)",
+                   "l2": "flushed between steps (256 MiB write), outside step timing",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "latency_ms": {"p50": 1000 * p50, "p99": 1000 * p99},
-        "outer_iterations": its[-1], "final_rel_residual_fp64": res, "max_err_vs_exact": err,
+        "latency_ms": {"served_batch_p50": 1000 * pct(times, 0.5), "served_batch_p99": 1000 * pct(times, 0.99),
+                       "single_solve_p50": 1000 * pct(lat, 0.5), "single_solve_p99": 1000 * pct(lat, 0.99)},
+        "single_solve_mixed": {"value": len(lat) / sum(lat), "unit": "solves/s", "outer_iterations": its1},
+        "outer_iterations": max(its), "max_true_rel_residual_fp64": max(true_res), "max_err_vs_exact": err,
         "fp64_dropin": {"value": len(d_times) / sum(d_times), "unit": "solves/s",
-                        "latency_ms_p50": 1000 * statistics.median(d_times), "outer_iterations": d_its[-1],
+                        "latency_ms_p50": 1000 * pct(d_times, 0.5), "outer_iterations": d_its,
                         "final_rel_residual_fp64": d_res},
-        "speedup_mixed_vs_fp64_dropin": value / world / (len(d_times) / sum(d_times)),
-        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(f_np.nbytes),
-                "d2h_bytes_per_step": int(f_np.nbytes), "final_rel_residual_fp64": e_res},
+        "speedup_served_vs_fp64_dropin": value / world / (len(d_times) / sum(d_times)),
+        "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(fB_np.nbytes),
+                "d2h_bytes_per_step": int(fB_np.nbytes)},
         "gpu_launches": int(launches),
-        "roofline": {"kernel": "FP64 ghost fill + star apply, finest level (timed alone)", "bound": "hbm",
+        "roofline": {"kernel": f"{top_name} (fused V-cycle phase, served batch)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "traffic": None, "peak_source": "measured" if peaks else "fallback"},
+                     "traffic": None, "peak_source": "measured" if peaks else "fallback",
+                     "launch_ms": top_ms, "algorithmic_bytes": alg,
+                     "share_of_vcycle": top_ms / cyc_total if cyc_total else None},
+        "vcycle_phases_ms": [[n, round(t, 4)] for n, t in phases[:6]],
         "cpu_baseline": cpu,
         "clocks": clocks,
         "wall_s_timed": t_wall,

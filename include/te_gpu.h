@@ -201,6 +201,14 @@ int te_cycle_destroy(te_cycle* c);
 /* u = M f  (u.setWithGhost(0); visit(finest, f, u)); f and u are FP64 */
 int te_cycle_apply(const te_cycle* c, int ncomp, const void* f, void* u);
 
+/* Per-kernel device times of one eager application of the cycle (the GPU
+ * counterpart of the reference's per-level Timer, Timer.h:60-202): fills up to
+ * max_entries names (32 chars each, "L<k> <phase>") and milliseconds measured
+ * with CUDA events between consecutive kernels.  Only the fused DFT-smoother
+ * cycle records phases; *count = 0 otherwise. */
+int te_cycle_timings(const te_cycle* c, int ncomp, const void* f, void* u, int max_entries, char* names,
+                     double* ms, int* count);
+
 /* ---- Iterative::BiCGStab (Iterative/BiCGStab.h:111-203) ------------------- */
 /* Right-preconditioned BiCGStab in FP64 on device vectors of A's domain.
  * M may be NULL.  Stops when ||r||/||b|| <= tol.  Returns TE_ERR_BREAKDOWN
@@ -213,6 +221,18 @@ enum { TE_BICGSTAB_PRECONDITIONED_EXIT = 1 };
 int te_bicgstab_solve(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M,
                       double tol, int max_iterations, int flags, int* iterations,
                       double* final_residual);
+
+/* Batched form: num_solves independent systems whose finest-level patches
+ * are the contiguous ranges [patch_offsets[i], patch_offsets[i+1]) of A's
+ * domain (a union of meshes of equal depth; M a V-cycle on the union).  Each
+ * solve keeps its own scalars, stops on its own tolerance and reports its own
+ * iterations, residual and status (TE_OK / TE_ERR_BREAKDOWN).  A solve's
+ * result does not depend on the other solves in the batch.  No counterpart in
+ * the reference (one solve per BiCGStab::solve call). */
+int te_bicgstab_solve_batched(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M,
+                              double tol, int max_iterations, int flags, int num_solves,
+                              const int* patch_offsets, int* iterations, double* final_residuals,
+                              int* statuses);
 
 /* ---- dot product without allocation ---------------------------------------
  * No counterpart in the reference (ThunderEgg reduces on the host).

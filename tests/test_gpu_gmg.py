@@ -159,3 +159,35 @@ def test_fused_cycle_matches_unfused(te, idx, cycle_dtype, monkeypatch):
     inner = (Ellipsis,) + tuple(slice(g, -g) for _ in range(levels[0].dim))
     tol = 1e-12 if cycle_dtype == "f64" else 2e-5
     assert rel_err(outs[0][inner], outs[1][inner]) <= tol
+
+
+def test_batched_solves_match_alone(te):
+    """A batch of independent solves: each solve's result is bit-identical to
+    the same solve alone (batch of one) and to the single-solve entry point."""
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    hiers = [M.circle_mesh(n=8, lo=2, hi=5) for _ in range(3)]
+    rng = np.random.default_rng(60)
+    fs = [PB.sine_modes_rhs(h[0], rng) for h in hiers]
+    opts = GmgOptions(scheme=1, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1)
+    levels, offsets = M.union_hierarchy(hiers)
+    s = GmgSolver(levels, opts)
+    fv = te.Vector.from_numpy(s.finest, np.concatenate(fs, axis=0))
+    uv = te.Vector(s.finest)
+    its, res, st = s.solve_batched(fv, uv, offsets[0])
+    assert st == [0, 0, 0] and all(r <= 1e-10 for r in res)
+    mixed = uv.numpy()
+    for b in range(3):
+        one = GmgSolver(hiers[b], opts)
+        f1 = te.Vector.from_numpy(one.finest, fs[b])
+        u1 = te.Vector(one.finest)
+        its1, _, _ = one.solve_batched(f1, u1, [0, hiers[b][0].num_patches])
+        assert its1[0] == its[b]
+        part = mixed[offsets[0][b]:offsets[0][b + 1]]
+        inner = (Ellipsis, slice(1, -1), slice(1, -1))
+        assert np.array_equal(part[inner], u1.numpy()[inner])
+        u2 = te.Vector(one.finest)
+        assert one.solve(f1, u2) == its[b]
+        assert np.array_equal(u2.numpy()[inner], part[inner])

@@ -358,6 +358,15 @@ class Cycle(_Handle):
     def apply(self, f: Vector, u: Vector):
         check(lib().te_cycle_apply(self.h, u.ncomp, f.ptr, u.ptr))
 
+    def timings(self, f: Vector, u: Vector, max_entries=128):
+        """[(phase name, milliseconds)] of one eager application (device events)."""
+        names = ctypes.create_string_buffer(32 * max_entries)
+        ms = (ctypes.c_double * max_entries)()
+        n = ctypes.c_int(0)
+        check(lib().te_cycle_timings(self.h, u.ncomp, f.ptr, u.ptr, max_entries, names, ms, ctypes.byref(n)))
+        raw = names.raw
+        return [(raw[32 * i:32 * i + 32].split(b"\0")[0].decode(), ms[i]) for i in range(n.value)]
+
 
 class CycleBuilder:
     """GMG::CycleBuilder (GMG/CycleBuilder.h:86-192)."""

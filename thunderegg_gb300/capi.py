@@ -103,7 +103,9 @@ _SIGS = {
     "te_vcycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, ctypes.POINTER(_V)]),
     "te_cycle_destroy": (_I, [_V]),
     "te_cycle_apply": (_I, [_V, _I, _V, _V]),
+    "te_cycle_timings": (_I, [_V, _I, _V, _V, _I, ctypes.c_char_p, _dp, _ip]),
     "te_bicgstab_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, _I, _ip, _dp]),
+    "te_bicgstab_solve_batched": (_I, [_V, _I, _V, _V, _V, _D, _I, _I, _I, _ip, _ip, _dp, _ip]),
     "te_level_dot_noalloc": (_I, [_I, _ip, _I, _I, _I, _I, _V, _V, _dp, _V]),
 }
 

@@ -555,6 +555,40 @@ int te_vcycle_create(const te_cycle_level* levels, int num_levels, te_cycle_opts
   });
 }
 
+int te_cycle_timings(const te_cycle* c, int nc, const void* f, void* u, int max_entries, char* names,
+                     double* ms, int* count) {
+  return guard([&] {
+    require(c && f && u && names && ms && count, "null argument");
+    te_cycle* m = const_cast<te_cycle*>(c);
+    m->ensure(nc);
+    std::vector<te_cycle::Mark> marks;
+    cudaStream_t s = m->stream;
+    TE_CUDA(cudaStreamSynchronize(s));
+    m->marks = &marks;
+    try {
+      m->mark("start", s);
+      m->body(f, u, s);
+      m->mark("end", s);
+    } catch (...) {
+      m->marks = nullptr;
+      for (auto& mk : marks) cudaEventDestroy(mk.ev);
+      throw;
+    }
+    m->marks = nullptr;
+    TE_CUDA(cudaStreamSynchronize(s));
+    int n = 0;
+    for (size_t i = 1; i + 1 < marks.size() && n < max_entries; i++, n++) {
+      float t = 0;
+      TE_CUDA(cudaEventElapsedTime(&t, marks[i - 1].ev, marks[i].ev));
+      ms[n] = t;
+      std::strncpy(names + 32 * n, marks[i].name.c_str(), 31);
+      names[32 * n + 31] = 0;
+    }
+    for (auto& mk : marks) cudaEventDestroy(mk.ev);
+    *count = n;
+  });
+}
+
 int te_cycle_destroy(te_cycle* c) {
   delete c;
   return TE_OK;

@@ -1,6 +1,7 @@
 // te_gmg.cuh -- transfer and cycle handles (internal).
 #pragma once
 #include <map>
+#include <string>
 #include <utility>
 
 #include "te_ops.cuh"
@@ -71,6 +72,19 @@ struct te_cycle {
   std::map<std::pair<const void*, void*>, G> graphs;
   // per-level work buffers in the cycle's precision
   std::vector<te::DevBuf<char>> f, u, r;
+  // optional per-kernel timing of one eager application (te_cycle_timings)
+  struct Mark {
+    std::string name;
+    cudaEvent_t ev;
+  };
+  mutable std::vector<Mark>* marks = nullptr;
+  void mark(const std::string& name, cudaStream_t s) const {
+    if (!marks) return;
+    cudaEvent_t e;
+    TE_CUDA(cudaEventCreate(&e));
+    TE_CUDA(cudaEventRecord(e, s));
+    marks->push_back({name, e});
+  }
   // fused path: every level smooths with the DFT solver, one pre/post sweep,
   // even patch sizes, no ghost extrapolation, one component
   bool fusable = false;
@@ -116,11 +130,14 @@ struct te_cycle {
     int last = (int)levels.size() - 1;
     T* A = (T*)u[k].p;
     te::vc_pre<T, TF>(levels[k].smoother, fk, A, s);
+    mark("L" + std::to_string(k) + " pre-smooth", s);
     if (k == last) return A;
     T* fc = (T*)f[k + 1].p;
     te::vc_restrict<T, TF>(levels[k].restrictor, levels[k].op, A, fk, fc, s);
+    mark("L" + std::to_string(k) + " residual+restrict", s);
     const T* uc = vfused<T, T, T>(k + 1, fc, (T*)r[k + 1].p, s);
     te::vc_post<T, TF, TO>(levels[k].smoother, levels[k + 1].interpolator, A, uc, fk, out, s);
+    mark("L" + std::to_string(k) + " interpolate+post-smooth", s);
     return (const T*)out;
   }
   // `fresh`: u is known to be zero (ghosts included) before the first sweep

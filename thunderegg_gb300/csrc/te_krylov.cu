@@ -1,13 +1,19 @@
-// te_krylov.cu -- the outer Iterative::BiCGStab (Iterative/BiCGStab.h:111-203) in FP64.
+// te_krylov.cu -- the outer Iterative::BiCGStab (Iterative/BiCGStab.h:111-203) in FP64,
+// for one solve or a batch of independent solves sharing one level buffer.
 //
 // The reference keeps alpha, omega, rho and beta on the host and reduces with
-// MPI_Allreduce after every dot product.  Here all scalars live in device
-// memory: each vector update is fused with the dot products that follow it,
-// the last block of each reduction finalises the scalars in a fixed order,
-// and the host reads the scalars back once per iteration to test for
-// convergence or breakdown.  One iteration (two preconditioner applications,
-// two operator applications, five fused kernels) is captured into a CUDA
-// graph per (x, b, M) and replayed.
+// MPI_Allreduce after every dot product.  Here every solve's scalars live in
+// device memory: each vector update is fused with the dot products that
+// follow it, and the last block of each solve's reduction finalises that
+// solve's scalars.  The host reads all scalars back once per iteration to test
+// convergence and breakdown per solve; converged solves are masked out of the
+// updates.  One iteration (two preconditioner applications, two operator
+// applications, five fused kernels) is captured into a CUDA graph and replayed.
+//
+// A batch is a union of solves whose finest-level patches are contiguous
+// ranges [offs[b], offs[b+1]).  A solve's reductions are split into a fixed
+// number of chunks that depends only on its own patch count, and summed in a
+// fixed order, so a solve gives bit-identical results alone or in any batch.
 //
 // Arithmetic per element follows the reference's operation order:
 //   s = r + ap*(-alpha); x += mp*alpha + ms*omega; r += ap*(-alpha) + as*(-omega);
@@ -17,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <tuple>
 
 #include "te_gmg.cuh"
 
@@ -40,6 +47,17 @@ enum Slot {
 };
 
 constexpr int KT = 256;
+constexpr int MAX_CHUNKS = 1024;
+
+// chunks of one solve's reductions: a function of its own patch count only
+inline int chunks_for(int patches) { return patches < MAX_CHUNKS ? patches : MAX_CHUNKS; }
+
+struct Batch {
+  int B;              // solves
+  const int* offs;    // [B+1] patch ranges
+  const int* nch;     // [B] chunks of each solve
+  const int* active;  // [B] 1 while the solve iterates
+};
 
 __device__ __forceinline__ int k_interior_offset(const Layout& L, int e) {
   int x = e % L.n0;
@@ -49,10 +67,27 @@ __device__ __forceinline__ int k_interior_offset(const Layout& L, int e) {
   return L.at(x, y, z);
 }
 
+// iterate the interior cells of chunk `ch` of solve `b`
+#define TE_CHUNK_LOOP(BT, L, nc, b, ch, k, body)                                       \
+  {                                                                                    \
+    const int _N = (L).interior();                                                     \
+    const long long _ps = (L).pstride(nc);                                             \
+    for (int _p = (BT).offs[b] + (ch); _p < (BT).offs[(b) + 1]; _p += (BT).nch[b])     \
+      for (int _c = 0; _c < (nc); _c++) {                                              \
+        const long long _base = _p * _ps + (long long)_c * (L).cs;                     \
+        _Pragma("unroll 4") for (int _e = threadIdx.x; _e < _N; _e += blockDim.x) {    \
+          const long long k = _base + k_interior_offset((L), _e);                      \
+          body;                                                                        \
+        }                                                                              \
+      }                                                                                \
+  }
+
+// Per-block sums -> part; the last block of solve b sums its chunks in a
+// fixed order into S[b][slot0 ...] and finalises scalars.
+// finalize_kind: 1 alpha, 2 omega, 3 beta + rho commit, 4 initial r0, 5 early-exit test
 template <int NV>
-__device__ void k_reduce(double (&v)[NV], double* part, unsigned int* counter, double* S, int slot0,
-                         int finalize_kind, double tol) {
-  // finalize_kind: 1 alpha, 2 omega, 3 beta + rho commit, 4 initial r0, 5 early-exit test
+__device__ void k_reduce(double (&v)[NV], const Batch& bt, int b, int ch, double* part, unsigned int* counter,
+                         double* S, int slot0, int finalize_kind, double tol) {
   __shared__ double red[NV][KT / 32];
   __shared__ double fin[NV][KT];
   __shared__ bool last;
@@ -63,24 +98,23 @@ __device__ void k_reduce(double (&v)[NV], double* part, unsigned int* counter, d
     if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = x;
   }
   __syncthreads();
+  const int CH = bt.nch[b];
   if (threadIdx.x == 0) {
     for (int i = 0; i < NV; i++) {
       double s = 0;
       for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[i][w];
-      part[(size_t)i * gridDim.x + blockIdx.x] = s;
+      part[((size_t)i * bt.B + b) * MAX_CHUNKS + ch] = s;
     }
     __threadfence();
-    unsigned int done = atomicAdd(counter, 1u);
-    last = done == gridDim.x - 1;
+    unsigned int done = atomicAdd(&counter[b], 1u);
+    last = done == (unsigned)(CH - 1);
   }
   __syncthreads();
   if (!last) return;
   __threadfence();
-  // fixed-order final sum over the block partials: strided per-thread sums,
-  // then a fixed tree (blockDim.x is a power of two)
   for (int i = 0; i < NV; i++) {
     double s = 0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) s += __ldcg(&part[(size_t)i * gridDim.x + b]);
+    for (int c = threadIdx.x; c < CH; c += blockDim.x) s += __ldcg(&part[((size_t)i * bt.B + b) * MAX_CHUNKS + c]);
     fin[i][threadIdx.x] = s;
   }
   __syncthreads();
@@ -90,128 +124,117 @@ __device__ void k_reduce(double (&v)[NV], double* part, unsigned int* counter, d
     __syncthreads();
   }
   if (threadIdx.x == 0) {
+    double* Sb = S + (size_t)b * S_NSLOTS;
     double tot[NV];
     for (int i = 0; i < NV; i++) {
       tot[i] = fin[i][0];
-      S[slot0 + i] = tot[i];
+      Sb[slot0 + i] = tot[i];
     }
     if (finalize_kind == 1) {  // alpha = rho / (rhat . ap)
-      S[S_ALPHA] = S[S_RHO] / tot[0];
+      Sb[S_ALPHA] = Sb[S_RHO] / tot[0];
     } else if (finalize_kind == 2) {  // omega = (as . s) / (as . as)
-      S[S_OMEGA] = tot[0] / tot[1];
+      Sb[S_OMEGA] = tot[0] / tot[1];
     } else if (finalize_kind == 3) {  // beta = rho_new * alpha / (rho * omega); rho = rho_new
-      if (S[S_DONE] == 0.0) {
-        S[S_BETA] = S[S_R_RHAT] * S[S_ALPHA] / (S[S_RHO] * S[S_OMEGA]);
-        S[S_RHO] = S[S_R_RHAT];
+      if (Sb[S_DONE] == 0.0) {
+        Sb[S_BETA] = Sb[S_R_RHAT] * Sb[S_ALPHA] / (Sb[S_RHO] * Sb[S_OMEGA]);
+        Sb[S_RHO] = Sb[S_R_RHAT];
       }
-    } else if (finalize_kind == 4) {  // initial: r0 = ||b||
-      S[S_R0] = sqrt(S[S_BB]);
     } else if (finalize_kind == 5) {  // ||s|| / ||b|| <= tol (BiCGStab.h:162)
-      S[S_DONE] = sqrt(tot[0]) / S[S_R0] <= tol ? 1.0 : 0.0;
+      Sb[S_DONE] = sqrt(tot[0]) / Sb[S_R0] <= tol ? 1.0 : 0.0;
     }
-    *counter = 0u;
+    counter[b] = 0u;
   }
 }
 
-// dots of up to three pairs into S[slot0 ...]
+#define TE_BLOCK_SOLVE(bt)                  \
+  const int b = blockIdx.x / MAX_CHUNKS;    \
+  const int ch = blockIdx.x % MAX_CHUNKS;   \
+  if (ch >= (bt).nch[b] || !(bt).active[b]) return;
+
+// dots of up to three pairs into S[b][slot0 ...]
 template <int NV>
-__global__ void __launch_bounds__(KT) k_dots(Layout L, int npc, const double* a0, const double* b0, const double* a1,
-                                             const double* b1, const double* a2, const double* b2, double* part,
-                                             unsigned int* counter, double* S, int slot0, int fin) {
+__global__ void __launch_bounds__(KT) k_dots(Layout L, int nc, Batch bt, const double* a0, const double* b0,
+                                             const double* a1, const double* b1, const double* a2, const double* b2,
+                                             double* part, unsigned int* counter, double* S, int slot0, int fin) {
+  TE_BLOCK_SOLVE(bt);
   double v[NV];
   for (int i = 0; i < NV; i++) v[i] = 0;
-  const int N = L.interior();
-  for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    long long base = (long long)pc * L.cs;
-#pragma unroll 4
-    for (int e = threadIdx.x; e < N; e += blockDim.x) {
-      long long k = base + k_interior_offset(L, e);
-      v[0] += a0[k] * b0[k];
-      if (NV > 1) v[1] += a1[k] * b1[k];
-      if (NV > 2) v[2] += a2[k] * b2[k];
-    }
-  }
-  k_reduce<NV>(v, part, counter, S, slot0, fin, 0);
+  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
+    v[0] += a0[k] * b0[k];
+    if (NV > 1) v[1] += a1[k] * b1[k];
+    if (NV > 2) v[2] += a2[k] * b2[k];
+  });
+  k_reduce<NV>(v, bt, b, ch, part, counter, S, slot0, fin, 0);
 }
 
 // s = r + ap * (-alpha);  S_SS = s . s; S_DONE = (||s|| / ||b|| <= tol)
-__global__ void __launch_bounds__(KT) k_s(Layout L, int npc, double tol, const double* r, const double* ap,
+__global__ void __launch_bounds__(KT) k_s(Layout L, int nc, Batch bt, double tol, const double* r, const double* ap,
                                           double* s, double* part, unsigned int* counter, double* S) {
-  const double alpha = S[S_ALPHA];
+  TE_BLOCK_SOLVE(bt);
+  const double alpha = S[(size_t)b * S_NSLOTS + S_ALPHA];
   double v[1] = {0};
-  const int N = L.interior();
-  for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    long long base = (long long)pc * L.cs;
-#pragma unroll 4
-    for (int e = threadIdx.x; e < N; e += blockDim.x) {
-      long long k = base + k_interior_offset(L, e);
-      double sv = r[k];
-      sv += ap[k] * -alpha;
-      s[k] = sv;
-      v[0] += sv * sv;
-    }
-  }
-  k_reduce<1>(v, part, counter, S, S_SS, 5, tol);
+  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
+    double sv = r[k];
+    sv += ap[k] * -alpha;
+    s[k] = sv;
+    v[0] += sv * sv;
+  });
+  k_reduce<1>(v, bt, b, ch, part, counter, S, S_SS, 5, tol);
 }
 
 // early exit when ||s|| / ||b|| <= tol: x += dir * alpha (reference: dir = p);
-// otherwise x += mp*alpha + ms*omega, r += ap*(-alpha) + as*(-omega) and
-// the dots r.rhat, r.r; the last block forms beta and commits rho.
-__global__ void __launch_bounds__(KT) k_xr(Layout L, int npc, double* x, double* r, const double* mp,
+// otherwise x += mp*alpha + ms*omega, r += ap*(-alpha) + as*(-omega) and the
+// dots r.r, r.rhat; the last block forms beta and commits rho.
+__global__ void __launch_bounds__(KT) k_xr(Layout L, int nc, Batch bt, double* x, double* r, const double* mp,
                                            const double* ms, const double* ap, const double* as, const double* rhat,
                                            const double* dir, double* part, unsigned int* counter, double* S) {
-  const double alpha = S[S_ALPHA], omega = S[S_OMEGA];
-  const bool done = S[S_DONE] != 0.0;
+  TE_BLOCK_SOLVE(bt);
+  const double* Sb = S + (size_t)b * S_NSLOTS;
+  const double alpha = Sb[S_ALPHA], omega = Sb[S_OMEGA];
+  const bool done = Sb[S_DONE] != 0.0;
   double v[2] = {0, 0};
-  const int N = L.interior();
-  for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    long long base = (long long)pc * L.cs;
-#pragma unroll 4
-    for (int e = threadIdx.x; e < N; e += blockDim.x) {
-      long long k = base + k_interior_offset(L, e);
-      if (done) {
-        x[k] += dir[k] * alpha;
-      } else {
-        x[k] += mp[k] * alpha + ms[k] * omega;
-        double rv = r[k];
-        rv += ap[k] * -alpha + as[k] * -omega;
-        r[k] = rv;
-        v[0] += rv * rv;
-        v[1] += rv * rhat[k];
-      }
+  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
+    if (done) {
+      x[k] += dir[k] * alpha;
+    } else {
+      x[k] += mp[k] * alpha + ms[k] * omega;
+      double rv = r[k];
+      rv += ap[k] * -alpha + as[k] * -omega;
+      r[k] = rv;
+      v[0] += rv * rv;
+      v[1] += rv * rhat[k];
     }
-  }
-  k_reduce<2>(v, part, counter, S, S_RR, 3, 0);
+  });
+  k_reduce<2>(v, bt, b, ch, part, counter, S, S_RR, 3, 0);
 }
 
 // p += ap*(-omega); p = p*beta + r
-__global__ void __launch_bounds__(KT) k_p(Layout L, int npc, double* p, const double* ap, const double* r,
+__global__ void __launch_bounds__(KT) k_p(Layout L, int nc, Batch bt, double* p, const double* ap, const double* r,
                                           const double* S) {
-  if (S[S_DONE] != 0.0) return;
-  const double omega = S[S_OMEGA], beta = S[S_BETA];
-  const int N = L.interior();
-  for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    long long base = (long long)pc * L.cs;
-#pragma unroll 4
-    for (int e = threadIdx.x; e < N; e += blockDim.x) {
-      long long k = base + k_interior_offset(L, e);
-      double pv = p[k];
-      pv += ap[k] * -omega;
-      p[k] = pv * beta + r[k];
-    }
-  }
+  TE_BLOCK_SOLVE(bt);
+  const double* Sb = S + (size_t)b * S_NSLOTS;
+  if (Sb[S_DONE] != 0.0) return;
+  const double omega = Sb[S_OMEGA], beta = Sb[S_BETA];
+  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
+    double pv = p[k];
+    pv += ap[k] * -omega;
+    p[k] = pv * beta + r[k];
+  });
 }
 
 struct KrylovWork {
   const te_domain* d;
   int nc;
+  int B;
   size_t n;
+  std::vector<int> h_offs, h_nch;
   DevBuf<double> resid, rhat, p, ap, as, s, ms, mp, S, part;
   DevBuf<unsigned int> counter;
+  DevBuf<int> offs, nch, active;
   double* h = nullptr;
+  int* h_active = nullptr;
   cudaStream_t cap = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
-  int grid = 1;
   struct G {
     cudaGraph_t g = nullptr;
     cudaGraphExec_t x = nullptr;
@@ -219,19 +242,24 @@ struct KrylovWork {
   };
   // keyed by x, b, the cycle's serial number and buffer generation, tol, flags
   std::map<std::tuple<void*, const void*, unsigned long long, unsigned long long, double, int>, G> graphs;
-  KrylovWork(const te_domain* d, int nc) : d(d), nc(nc) {
+  KrylovWork(const te_domain* d, int nc, const std::vector<int>& offsets) : d(d), nc(nc) {
+    B = (int)offsets.size() - 1;
+    h_offs = offsets;
+    for (int b = 0; b < B; b++) h_nch.push_back(chunks_for(offsets[b + 1] - offsets[b]));
     n = (size_t)d->lay.P * d->lay.pstride(nc);
-    for (auto* b : {&resid, &rhat, &p, &ap, &as, &s, &ms, &mp}) {
-      b->alloc(n);
-      TE_CUDA(cudaMemsetAsync(b->p, 0, n * sizeof(double), d->stream));
+    for (auto* buf : {&resid, &rhat, &p, &ap, &as, &s, &ms, &mp}) {
+      buf->alloc(n);
+      TE_CUDA(cudaMemsetAsync(buf->p, 0, n * sizeof(double), d->stream));
     }
-    S.alloc(S_NSLOTS);
-    grid = std::min(d->lay.P * nc, 152 * 8);
-    part.alloc((size_t)3 * grid);
-    counter.alloc(1);
-    TE_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned int), d->stream));
-    TE_CUDA(cudaMemsetAsync(S.p, 0, S_NSLOTS * sizeof(double), d->stream));
-    TE_CUDA(cudaMallocHost(&h, S_NSLOTS * sizeof(double)));
+    S.alloc((size_t)B * S_NSLOTS);
+    part.alloc((size_t)3 * B * MAX_CHUNKS);
+    counter.alloc(B);
+    TE_CUDA(cudaMemsetAsync(counter.p, 0, B * sizeof(unsigned int), d->stream));
+    offs.upload(h_offs, d->stream);
+    nch.upload(h_nch, d->stream);
+    active.alloc(B);
+    TE_CUDA(cudaMallocHost(&h, (size_t)B * S_NSLOTS * sizeof(double)));
+    TE_CUDA(cudaMallocHost(&h_active, (size_t)B * sizeof(int)));
     TE_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     TE_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
     TE_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
@@ -242,26 +270,32 @@ struct KrylovWork {
       if (kv.second.g) cudaGraphDestroy(kv.second.g);
     }
     if (h) cudaFreeHost(h);
+    if (h_active) cudaFreeHost(h_active);
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
     if (cap) cudaStreamDestroy(cap);
   }
+  Batch batch() const { return Batch{B, offs.p, nch.p, active.p}; }
+  int grid() const { return B * MAX_CHUNKS; }
   void read_scalars(cudaStream_t st) {
-    TE_CUDA(cudaMemcpyAsync(h, S.p, S_NSLOTS * sizeof(double), cudaMemcpyDeviceToHost, st));
+    TE_CUDA(cudaMemcpyAsync(h, S.p, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyDeviceToHost, st));
     TE_CUDA(cudaStreamSynchronize(st));
+  }
+  void push_active(cudaStream_t st) {
+    TE_CUDA(cudaMemcpyAsync(active.p, h_active, (size_t)B * sizeof(int), cudaMemcpyHostToDevice, st));
   }
 };
 
 static void launch_dots(KrylovWork& W, int nv, const double* a0, const double* b0, const double* a1, const double* b1,
                         const double* a2, const double* b2, int slot0, int fin, cudaStream_t st) {
   const Layout& L = W.d->lay;
-  int npc = L.P * W.nc;
+  Batch bt = W.batch();
   if (nv == 1)
-    k_dots<1><<<W.grid, KT, 0, st>>>(L, npc, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
+    k_dots<1><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
   else if (nv == 2)
-    k_dots<2><<<W.grid, KT, 0, st>>>(L, npc, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
+    k_dots<2><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
   else
-    k_dots<3><<<W.grid, KT, 0, st>>>(L, npc, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
+    k_dots<3><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
   count_launch();
   TE_LAUNCH_CHECK();
 }
@@ -270,26 +304,147 @@ static void launch_dots(KrylovWork& W, int nv, const double* a0, const double* b
 static void iteration(KrylovWork& W, const te_operator* A, te_cycle* M, double* x, double tol, int flags,
                       cudaStream_t st) {
   const Layout& L = W.d->lay;
-  int nc = W.nc, npc = L.P * nc;
+  int nc = W.nc;
+  Batch bt = W.batch();
   double* mp = M ? W.mp.p : W.p.p;
   double* ms = M ? W.ms.p : W.s.p;
   if (M) M->body(W.p.p, W.mp.p, st);
   operator_apply(A, nc, TE_F64, mp, W.ap.p, st);
   launch_dots(W, 1, W.rhat.p, W.ap.p, nullptr, nullptr, nullptr, nullptr, S_RHAT_AP, 1, st);
-  k_s<<<W.grid, KT, 0, st>>>(L, npc, tol, W.resid.p, W.ap.p, W.s.p, W.part.p, W.counter.p, W.S.p);
+  k_s<<<W.grid(), KT, 0, st>>>(L, nc, bt, tol, W.resid.p, W.ap.p, W.s.p, W.part.p, W.counter.p, W.S.p);
   count_launch();
   TE_LAUNCH_CHECK();
   if (M) M->body(W.s.p, W.ms.p, st);
   operator_apply(A, nc, TE_F64, ms, W.as.p, st);
   launch_dots(W, 2, W.as.p, W.s.p, W.as.p, W.as.p, nullptr, nullptr, S_AS_S, 2, st);
   const double* dir = (M && (flags & TE_BICGSTAB_PRECONDITIONED_EXIT)) ? W.mp.p : W.p.p;
-  k_xr<<<W.grid, KT, 0, st>>>(L, npc, x, W.resid.p, mp, ms, W.ap.p, W.as.p, W.rhat.p, dir, W.part.p,
-                              W.counter.p, W.S.p);
+  k_xr<<<W.grid(), KT, 0, st>>>(L, nc, bt, x, W.resid.p, mp, ms, W.ap.p, W.as.p, W.rhat.p, dir, W.part.p,
+                                W.counter.p, W.S.p);
   count_launch();
   TE_LAUNCH_CHECK();
-  k_p<<<W.grid, KT, 0, st>>>(L, npc, W.p.p, W.ap.p, W.resid.p, W.S.p);
+  k_p<<<W.grid(), KT, 0, st>>>(L, nc, bt, W.p.p, W.ap.p, W.resid.p, W.S.p);
   count_launch();
   TE_LAUNCH_CHECK();
+}
+
+static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv, const te_cycle* Mc, double tol,
+                         int max_iterations, int flags, const std::vector<int>& offsets, int* iterations,
+                         double* final_residuals, int* statuses) {
+  const te_domain* d = A->dom;
+  cudaStream_t st = d->stream;
+  const int B = (int)offsets.size() - 1;
+  // the solver's work vectors live with the operator (freed with it), per component count and batch layout
+  auto& slot = A->krylov[std::make_pair(nc, offsets)];
+  if (!slot) slot = std::make_shared<KrylovWork>(d, nc, offsets);
+  KrylovWork& W = *std::static_pointer_cast<KrylovWork>(slot);
+  te_cycle* M = const_cast<te_cycle*>(Mc);
+  if (M) M->ensure(nc);
+  double* x = (double*)xv;
+  const double* b = (const double*)bv;
+  size_t bytes = W.n * sizeof(double);
+  // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
+  operator_apply(A, nc, TE_F64, x, W.resid.p, st);
+  vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.resid.p, b, nullptr, -1, 0, 0);
+  TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+  TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+  TE_CUDA(cudaMemsetAsync(W.S.p, 0, (size_t)B * S_NSLOTS * sizeof(double), st));
+  for (int i = 0; i < B; i++) W.h_active[i] = 1;
+  W.push_active(st);
+  launch_dots(W, 3, b, b, W.rhat.p, W.resid.p, W.resid.p, W.resid.p, S_BB, 0, st);
+  W.read_scalars(st);
+  std::vector<double> rho(B), r0(B), residual(B);
+  std::vector<int> its(B, 0);
+  int nactive = 0;
+  for (int i = 0; i < B; i++) {
+    double* h = W.h + (size_t)i * S_NSLOTS;
+    double bb = h[S_BB], rh = h[S_BB + 1], rr = h[S_BB + 2];
+    r0[i] = std::sqrt(bb);
+    rho[i] = rh;
+    residual[i] = std::sqrt(rr) / r0[i];
+    statuses[i] = TE_OK;
+    for (int k = 0; k < S_NSLOTS; k++) h[k] = 0.0;
+    h[S_RHO] = rho[i];
+    h[S_R0] = r0[i];
+    if (final_residuals) final_residuals[i] = residual[i];
+    // zero right-hand side or already converged: no iterations (BiCGStab.h:140-144)
+    W.h_active[i] = (r0[i] != 0 && residual[i] > tol && max_iterations > 0) ? 1 : 0;
+    if (W.h_active[i] && rho[i] == 0) {  // BiCGStab.h:149-151
+      statuses[i] = TE_ERR_BREAKDOWN;
+      W.h_active[i] = 0;
+    }
+    nactive += W.h_active[i];
+  }
+  TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
+  W.push_active(st);
+  const char* ng = getenv("TE_NO_GRAPH");
+  bool use_graph = !(ng && ng[0] == '1');
+  auto gkey = std::make_tuple((void*)x, (const void*)b, M ? M->serial : 0ull, M ? M->generation : 0ull, tol, flags);
+  while (nactive > 0) {
+    if (use_graph) {
+      auto it = W.graphs.find(gkey);
+      if (it == W.graphs.end()) {
+        KrylovWork::G g;
+        long long l0 = g_launches.load();
+        TE_CUDA(cudaStreamBeginCapture(W.cap, cudaStreamCaptureModeThreadLocal));
+        try {
+          iteration(W, A, M, x, tol, flags, W.cap);
+        } catch (...) {
+          cudaGraph_t junk = nullptr;
+          cudaStreamEndCapture(W.cap, &junk);
+          if (junk) cudaGraphDestroy(junk);
+          throw;
+        }
+        TE_CUDA(cudaStreamEndCapture(W.cap, &g.g));
+        TE_CUDA(cudaGraphInstantiate(&g.x, g.g, 0));
+        g.launches = g_launches.load() - l0;
+        g_launches.fetch_sub(g.launches);
+        it = W.graphs.emplace(gkey, g).first;
+      }
+      TE_CUDA(cudaEventRecord(W.ev_in, st));
+      TE_CUDA(cudaStreamWaitEvent(W.cap, W.ev_in, 0));
+      TE_CUDA(cudaGraphLaunch(it->second.x, W.cap));
+      count_launch((int)it->second.launches);
+      TE_CUDA(cudaEventRecord(W.ev_out, W.cap));
+      TE_CUDA(cudaStreamWaitEvent(st, W.ev_out, 0));
+    } else {
+      iteration(W, A, M, x, tol, flags, st);
+    }
+    W.read_scalars(st);
+    bool changed = false;
+    for (int i = 0; i < B; i++) {
+      if (!W.h_active[i]) continue;
+      const double* h = W.h + (size_t)i * S_NSLOTS;
+      if (h[S_DONE] != 0.0) {  // ||s|| / ||b|| <= tol: x updated, stop (BiCGStab.h:162-168)
+        if (final_residuals) final_residuals[i] = std::sqrt(h[S_SS]) / r0[i];
+        W.h_active[i] = 0;
+        changed = true;
+        continue;
+      }
+      its[i]++;
+      rho[i] = h[S_RHO];
+      residual[i] = std::sqrt(h[S_RR]) / r0[i];
+      if (final_residuals) final_residuals[i] = residual[i];
+      if (residual[i] <= tol || its[i] >= max_iterations) {
+        W.h_active[i] = 0;
+        changed = true;
+      } else if (rho[i] == 0) {  // BiCGStab.h:149-151
+        statuses[i] = TE_ERR_BREAKDOWN;
+        W.h_active[i] = 0;
+        changed = true;
+      }
+    }
+    if (changed) {
+      nactive = 0;
+      for (int i = 0; i < B; i++) nactive += W.h_active[i];
+      W.push_active(st);
+    }
+  }
+  for (int i = 0; i < B; i++) iterations[i] = its[i];
+  TE_CUDA(cudaStreamSynchronize(st));
+  int worst = TE_OK;
+  for (int i = 0; i < B; i++)
+    if (statuses[i] != TE_OK) worst = statuses[i];
+  return worst;
 }
 
 }  // namespace te
@@ -303,89 +458,27 @@ int te_bicgstab_solve(const te_operator* A, int nc, void* xv, const void* bv, co
   int status = TE_OK;
   int rc = guard([&] {
     require(A && xv && bv && iterations, "null argument");
-    const te_domain* d = A->dom;
-    cudaStream_t st = d->stream;
-    // the solver's work vectors live with the operator (freed with it)
-    auto& slot = A->krylov[nc];
-    if (!slot) slot = std::make_shared<KrylovWork>(d, nc);
-    KrylovWork& W = *std::static_pointer_cast<KrylovWork>(slot);
-    te_cycle* M = const_cast<te_cycle*>(Mc);
-    if (M) M->ensure(nc);
-    double* x = (double*)xv;
-    const double* b = (const double*)bv;
-    size_t bytes = W.n * sizeof(double);
-    // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
-    operator_apply(A, nc, TE_F64, x, W.resid.p, st);
-    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.resid.p, b, nullptr, -1, 0, 0);
-    TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-    TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-    TE_CUDA(cudaMemsetAsync(W.S.p, 0, S_NSLOTS * sizeof(double), st));
-    launch_dots(W, 3, b, b, W.rhat.p, W.resid.p, W.resid.p, W.resid.p, S_BB, 0, st);
-    // S_BB, S_RHO? slots: S_BB = b.b, S_BB+1 and S_BB+2 are scratch; copy into place
-    W.read_scalars(st);
-    double bb = W.h[S_BB], rho = W.h[S_BB + 1], rr = W.h[S_BB + 2];
-    double r0 = std::sqrt(bb);
-    for (int i = 0; i < S_NSLOTS; i++) W.h[i] = 0.0;
-    W.h[S_RHO] = rho;
-    W.h[S_R0] = r0;
-    TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
-    int its = 0;
-    double residual = std::sqrt(rr) / r0;
-    if (final_residual) *final_residual = residual;
-    if (r0 == 0) {
-      TE_CUDA(cudaStreamSynchronize(st));
-      *iterations = 0;
-      return;
-    }
-    const char* ng = getenv("TE_NO_GRAPH");
-    bool use_graph = !(ng && ng[0] == '1');
-    auto gkey = std::make_tuple((void*)x, (const void*)b, M ? M->serial : 0ull, M ? M->generation : 0ull, tol, flags);
-    while (residual > tol && its < max_iterations) {
-      if (rho == 0) {
-        status = TE_ERR_BREAKDOWN;
-        set_error("BiCGStab broke down, rho was 0 on iteration " + std::to_string(its));
-        break;
-      }
-      if (use_graph) {
-        auto it = W.graphs.find(gkey);
-        if (it == W.graphs.end()) {
-          KrylovWork::G g;
-          long long l0 = g_launches.load();
-          TE_CUDA(cudaStreamBeginCapture(W.cap, cudaStreamCaptureModeThreadLocal));
-          try {
-            iteration(W, A, M, x, tol, flags, W.cap);
-          } catch (...) {
-            cudaGraph_t junk = nullptr;
-            cudaStreamEndCapture(W.cap, &junk);
-            if (junk) cudaGraphDestroy(junk);
-            throw;
-          }
-          TE_CUDA(cudaStreamEndCapture(W.cap, &g.g));
-          TE_CUDA(cudaGraphInstantiate(&g.x, g.g, 0));
-          g.launches = g_launches.load() - l0;
-          g_launches.fetch_sub(g.launches);
-          it = W.graphs.emplace(gkey, g).first;
-        }
-        TE_CUDA(cudaEventRecord(W.ev_in, st));
-        TE_CUDA(cudaStreamWaitEvent(W.cap, W.ev_in, 0));
-        TE_CUDA(cudaGraphLaunch(it->second.x, W.cap));
-        count_launch((int)it->second.launches);
-        TE_CUDA(cudaEventRecord(W.ev_out, W.cap));
-        TE_CUDA(cudaStreamWaitEvent(st, W.ev_out, 0));
-      } else {
-        iteration(W, A, M, x, tol, flags, st);
-      }
-      W.read_scalars(st);
-      if (W.h[S_DONE] != 0.0) {  // ||s|| / ||b|| <= tol: x updated, stop (BiCGStab.h:162-168)
-        if (final_residual) *final_residual = std::sqrt(W.h[S_SS]) / r0;
-        break;
-      }
-      its++;
-      rho = W.h[S_RHO];
-      residual = std::sqrt(W.h[S_RR]) / r0;
-      if (final_residual) *final_residual = residual;
-    }
-    *iterations = its;
+    std::vector<int> offs = {0, A->dom->lay.P};
+    int st = TE_OK;
+    status = solve_batched(A, nc, xv, bv, Mc, tol, max_iterations, flags, offs, iterations, final_residual, &st);
+    if (status == TE_ERR_BREAKDOWN)
+      set_error("BiCGStab broke down, rho was 0 on iteration " + std::to_string(*iterations));
+  });
+  return rc != TE_OK ? rc : status;
+}
+
+int te_bicgstab_solve_batched(const te_operator* A, int nc, void* xv, const void* bv, const te_cycle* Mc, double tol,
+                              int max_iterations, int flags, int num_solves, const int* patch_offsets,
+                              int* iterations, double* final_residuals, int* statuses) {
+  int status = TE_OK;
+  int rc = guard([&] {
+    require(A && xv && bv && patch_offsets && iterations && statuses, "null argument");
+    require(num_solves >= 1, "num_solves must be >= 1");
+    std::vector<int> offs(patch_offsets, patch_offsets + num_solves + 1);
+    require(offs[0] == 0 && offs[num_solves] == A->dom->lay.P, "patch_offsets must span the finest level");
+    for (int i = 0; i < num_solves; i++) require(offs[i + 1] > offs[i], "every solve needs at least one patch");
+    status = solve_batched(A, nc, xv, bv, Mc, tol, max_iterations, flags, offs, iterations, final_residuals, statuses);
+    if (status == TE_ERR_BREAKDOWN) set_error("BiCGStab broke down in at least one solve of the batch");
   });
   return rc != TE_OK ? rc : status;
 }

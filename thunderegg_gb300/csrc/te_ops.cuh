@@ -13,8 +13,9 @@ struct te_operator {
   te::DevBuf<double> coeffs;    // VarPoisson: ghost-filled coefficient level buffer (1 component)
   te::DevBuf<float> coeffs_f;   // FP32 copy for the mixed-precision cycle
   te::FaceTable faces;
-  // work vectors of te_bicgstab_solve with this operator, per component count
-  mutable std::map<int, std::shared_ptr<void>> krylov;
+  // work vectors of te_bicgstab_solve(_batched) with this operator, per
+  // component count and batch layout (patch offsets of the solves)
+  mutable std::map<std::pair<int, std::vector<int>>, std::shared_ptr<void>> krylov;
   const void* coeff_ptr(int dtype) const {
     return kind == 0 ? nullptr : (dtype == TE_F64 ? (const void*)coeffs.p : (const void*)coeffs_f.p);
   }

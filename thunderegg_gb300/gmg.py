@@ -81,6 +81,26 @@ class GmgSolver:
     def solve(self, f: Vector, u: Vector, precondition=True):
         return self.krylov.solve(self.ops[0], u, f, self.cycle if precondition else None)
 
+    def solve_batched(self, f: Vector, u: Vector, patch_offsets, precondition=True):
+        """Independent solves whose finest patches are the ranges of patch_offsets
+        (see mesh.union_hierarchy).  Returns (iterations, residuals, statuses)."""
+        import ctypes
+
+        from .capi import check, lib
+
+        B = len(patch_offsets) - 1
+        offs = (ctypes.c_int * (B + 1))(*patch_offsets)
+        its = (ctypes.c_int * B)()
+        res = (ctypes.c_double * B)()
+        st = (ctypes.c_int * B)()
+        rc = lib().te_bicgstab_solve_batched(self.ops[0].h, u.ncomp, u.ptr, f.ptr,
+                                             self.cycle.h if precondition else None, float(self.opts.tol),
+                                             int(self.opts.max_it), int(self.opts.bicgstab_flags), B, offs, its, res,
+                                             st)
+        if rc not in (0, 3):
+            check(rc)
+        return list(its), list(res), list(st)
+
     def residual(self, f: Vector, u: Vector):
         """||f - A u|| / ||f|| in FP64 on the device."""
         r = f.getZeroClone()

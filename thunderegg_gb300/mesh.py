@@ -640,3 +640,60 @@ def cell_centers(lvl: MeshLevel):
         sl[dim - a] = slice(None)
         out[..., a] = np.broadcast_to(g[tuple(sl)], shape)
     return out
+
+
+# ---------------------------------------------------------------------------
+# batches: several independent hierarchies as one
+# ---------------------------------------------------------------------------
+def union_hierarchy(hierarchies):
+    """Concatenate the levels of several hierarchies of equal depth.
+
+    Patches of solve b come after those of solve b-1 on every level, and every
+    id is shifted by the sum of the previous solves' id ranges, so the union
+    is a valid hierarchy of disconnected meshes.  Returns (levels, offsets)
+    with offsets[k] the patch offsets of the solves on level k."""
+    depth = len(hierarchies[0])
+    if any(len(h) != depth for h in hierarchies):
+        raise ValueError("hierarchies in one batch must have the same number of levels")
+    shifts, acc = [], 0
+    for h in hierarchies:
+        shifts.append(acc)
+        acc += int(max(int(lv.id.max()) for lv in h)) + 1
+
+    def shift(a, s, valid=None):
+        a = np.array(a, copy=True)
+        mask = a >= 0 if valid is None else valid
+        a[mask] += s
+        return a
+
+    levels, offsets = [], []
+    for k in range(depth):
+        parts = [h[k] for h in hierarchies]
+        d0 = parts[0]
+        for p in parts:
+            if p.dim != d0.dim or tuple(p.ns) != tuple(d0.ns) or p.num_ghost != d0.num_ghost:
+                raise ValueError("hierarchies in one batch must share patch shape")
+        F = num_face_slots(d0.dim)
+        lv = _empty_level(d0.dim, sum(p.num_patches for p in parts), d0.ns, d0.num_ghost)
+        fields = {n: [] for n in ("id", "refine_level", "parent_id", "orth_on_parent", "child_ids", "starts",
+                                  "spacings", "nbr_type", "nbr_ids", "nbr_orth")}
+        off = [0]
+        for p, s in zip(parts, shifts):
+            fields["id"].append(p.id + s)
+            fields["refine_level"].append(p.refine_level)
+            fields["parent_id"].append(shift(p.parent_id, s))
+            fields["orth_on_parent"].append(p.orth_on_parent)
+            fields["child_ids"].append(shift(p.child_ids, s))
+            fields["starts"].append(p.starts)
+            fields["spacings"].append(p.spacings)
+            fields["nbr_type"].append(p.nbr_type)
+            valid = np.repeat((p.nbr_type >= 0)[:, :, None], 4, axis=2) & (p.nbr_ids >= 0)
+            fields["nbr_ids"].append(shift(p.nbr_ids, s, valid))
+            fields["nbr_orth"].append(p.nbr_orth)
+            off.append(off[-1] + p.num_patches)
+        for n, v in fields.items():
+            setattr(lv, n, np.concatenate(v, axis=0))
+        assert lv.nbr_type.shape[1] == F
+        levels.append(lv)
+        offsets.append(off)
+    return levels, offsets
