@@ -163,9 +163,9 @@ class Clocks:
 
 
 def _phase_bytes(name, levels, dtype_bytes):
-    """Algorithmic bytes of one launch of a fused V-cycle phase on level k
-    ("Measurement"): interior cells only, each value read or
-    written once; ghost gathers count 2D/n reads per cell."""
+    """Algorithmic bytes of one launch of a fused V-cycle phase on level k:
+    interior cells only, each value read or written once; ghost gathers count
+    2D/n reads per cell (one face row of neighbour values per patch side)."""
     k = int(name.split()[0][1:])
     lv = levels[k]
     cells = lv.num_cells
