@@ -178,6 +178,8 @@ def _phase_bytes(name, levels, dtype_bytes):
         return cells * (wf + w)
     if "restrict" in name:
         return cells * (w + wf + ghost + w / (1 << D))
+    if name.endswith("post-smooth") and "interpolate" not in name:
+        return cells * (wo + wo)  # tensor-core solve in place: read the right-hand side, write u
     return cells * (w + w / (1 << D) + wf + ghost + wo)
 
 

@@ -168,6 +168,11 @@ int te_patch_solver_destroy(te_patch_solver* s);
 int te_patch_solver_smooth(const te_patch_solver* s, int ncomp, int dtype, const void* f, void* u);
 /* apply: u.setWithGhost(0), then solveSinglePatch on every patch */
 int te_patch_solver_apply(const te_patch_solver* s, int ncomp, int dtype, const void* f, void* u);
+/* *out = 1 when the FP32 DFT solves of this solver run on the tensor cores
+ * (3xTF32 tcgen05 contractions: cubic patches, n = 16, 32 or 64 in 2D or 16 in
+ * 3D, one set of transform matrices for the level; TE_NO_TC=1 at creation
+ * turns it off).  No counterpart in the reference. */
+int te_patch_solver_uses_tensor_cores(const te_patch_solver* s, int* out);
 
 /* ---- GMG transfers -------------------------------------------------------- */
 /* GMG::LinearRestrictor (GMG/LinearRestrictor.h:166-191, MPIRestrictor.h:55-83)

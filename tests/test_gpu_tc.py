@@ -1,0 +1,160 @@
+"""The tensor-core (3xTF32 tcgen05) DFT patch solve against the CPU oracle.
+
+Tolerances (infinity-norm relative to the FP64 oracle):
+  FP32 DFT patch solve on the tensor cores: 2e-5 (FP32 data, ~22-bit products)
+  FP32 V-cycle with tensor-core solves on every level: 5e-5
+  tensor-core vs SIMT FP32 V-cycle: 2e-5
+  GMG-preconditioned BiCGStab with the tensor-core cycle: 1e-10 FP64 residual
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _meshes():
+    from thunderegg_gb300 import mesh as M
+
+    return {
+        "2d_uniform_n16": (M.uniform_mesh(2, 2, 16), 0),
+        "2d_uniform_n32": (M.uniform_mesh(2, 2, 32), 1),
+        "2d_uniform_n64": (M.uniform_mesh(2, 1, 64), 1),
+        "2d_circle_n16": (M.circle_mesh(n=16, lo=2, hi=4), 1),
+        "2d_random_n32": (M.random_mesh(7, n=32, lo=1, hi=3), 0),
+        "3d_uniform_n16": (M.uniform_mesh(3, 1, 16), 2),
+        "3d_random_n16": (M.random_mesh(8, n=16, dim=3, lo=1, hi=2), 2),
+    }
+
+
+MESHES = None
+
+
+def meshes():
+    global MESHES
+    if MESHES is None:
+        MESHES = _meshes()
+    return MESHES
+
+
+def _filler(te, scheme):
+    return [te.BiLinearGhostFiller, te.BiQuadraticGhostFiller, te.TriLinearGhostFiller][scheme]
+
+
+def _inner(lv):
+    g = lv.num_ghost
+    return (Ellipsis,) + tuple(slice(g, -g) for _ in range(lv.dim))
+
+
+@pytest.mark.parametrize("name", sorted(["2d_uniform_n16", "2d_uniform_n32", "2d_uniform_n64", "2d_circle_n16",
+                                         "2d_random_n32", "3d_uniform_n16", "3d_random_n16"]))
+def test_tc_patch_solve(te, oracle, name):
+    """PatchSolver::apply in FP32 runs on the tensor cores and matches the FP64 oracle."""
+    levels, sc = meshes()[name]
+    lv = levels[0]
+    dom = te.Domain(lv)
+    op = te.PoissonStarPatchOperator(dom, _filler(te, sc)(dom))
+    ps = te.DFTPatchSolver(op)
+    assert ps.uses_tensor_cores
+    rng = np.random.default_rng(11)
+    f = rng.standard_normal(lv.padded_shape(1))
+    u = rng.standard_normal(lv.padded_shape(1))
+    want, _ = oracle.patch_solver(lv, f, u, sc, smoother=0, mode=1)
+    f32 = te.Vector.from_numpy(dom, f, dtype=te.TE_F32)
+    u32 = te.Vector.from_numpy(dom, u, dtype=te.TE_F32)
+    ps.apply(f32, u32)
+    got = u32.numpy()
+    inner = _inner(lv)
+    assert rel_err(got[inner], want[inner]) <= 2e-5
+    # apply zeroes the ghost cells (u.setWithGhost(0))
+    ghosts = np.ones(got.shape, bool)
+    ghosts[inner] = False
+    assert np.all(got[ghosts] == 0)
+
+
+def test_tc_patch_solve_large_level(te, oracle):
+    """Many CTA passes over patch groups (persistent loop), including a partial last group."""
+    from thunderegg_gb300 import mesh as M
+
+    lv = M.random_mesh(12, n=32, lo=3, hi=6)[0]
+    dom = te.Domain(lv)
+    op = te.PoissonStarPatchOperator(dom, te.BiQuadraticGhostFiller(dom))
+    ps = te.DFTPatchSolver(op)
+    assert ps.uses_tensor_cores
+    f = np.random.default_rng(12).standard_normal(lv.padded_shape(1))
+    want, _ = oracle.patch_solver(lv, f, np.zeros_like(f), 1, smoother=0, mode=1)
+    f32 = te.Vector.from_numpy(dom, f, dtype=te.TE_F32)
+    u32 = te.Vector(dom, dtype=te.TE_F32)
+    ps.apply(f32, u32)
+    inner = _inner(lv)
+    assert rel_err(u32.numpy()[inner], want[inner]) <= 2e-5
+
+
+def test_tc_off_switch(te):
+    from thunderegg_gb300 import mesh as M
+
+    lv = M.uniform_mesh(2, 1, 32)[0]
+    dom = te.Domain(lv)
+    op = te.PoissonStarPatchOperator(dom, te.BiLinearGhostFiller(dom))
+    os.environ["TE_NO_TC"] = "1"
+    try:
+        assert not te.DFTPatchSolver(op).uses_tensor_cores
+    finally:
+        del os.environ["TE_NO_TC"]
+    assert te.DFTPatchSolver(op).uses_tensor_cores
+    # sizes without a tensor-core shape fall back to the SIMT transforms
+    lv8 = M.uniform_mesh(2, 1, 8)[0]
+    d8 = te.Domain(lv8)
+    assert not te.DFTPatchSolver(te.PoissonStarPatchOperator(d8, te.BiLinearGhostFiller(d8))).uses_tensor_cores
+
+
+@pytest.mark.parametrize("name", ["2d_circle_n16", "2d_random_n32", "3d_uniform_n16"])
+def test_tc_vcycle(te, oracle, name):
+    """The FP32 fused V-cycle with tensor-core solves on every level against the FP64 oracle cycle,
+    and against the same cycle with SIMT FP32 transforms."""
+    from oracle import gmg_config
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels, sc = meshes()[name]
+    f = np.random.default_rng(13).standard_normal(levels[0].padded_shape(1))
+    want = oracle.vcycle(levels, f, gmg_config(scheme=sc, smoother=0))
+    inner = _inner(levels[0])
+    s = GmgSolver(levels, GmgOptions(scheme=sc, smoother=0, cycle_dtype=te.TE_F32))
+    assert all(ps.uses_tensor_cores for ps in s.smoothers)
+    fv = te.Vector.from_numpy(s.finest, f)
+    uv = te.Vector(s.finest)
+    for _ in range(2):  # the second application replays the captured graph
+        s.cycle.apply(fv, uv)
+        got = uv.numpy()
+        assert rel_err(got[inner], want[inner]) <= 5e-5
+    os.environ["TE_NO_TC"] = "1"
+    try:
+        s2 = GmgSolver(levels, GmgOptions(scheme=sc, smoother=0, cycle_dtype=te.TE_F32))
+    finally:
+        del os.environ["TE_NO_TC"]
+    assert not any(ps.uses_tensor_cores for ps in s2.smoothers)
+    uv2 = te.Vector(s2.finest)
+    s2.cycle.apply(te.Vector.from_numpy(s2.finest, f), uv2)
+    assert rel_err(got[inner], uv2.numpy()[inner]) <= 2e-5
+
+
+@pytest.mark.parametrize("name", ["2d_circle_n16", "3d_uniform_n16"])
+def test_tc_solve_reaches_tolerance(te, oracle, name):
+    """Mixed precision (tensor-core FP32 cycle, FP64 BiCGStab) reaches 1e-10 and matches the FP64 oracle solve."""
+    from oracle import gmg_config
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels, sc = meshes()[name]
+    f = np.random.default_rng(14).standard_normal(levels[0].padded_shape(1))
+    u_o, its_o, _, rc = oracle.solve(levels, f, gmg_config(scheme=sc, smoother=0, tol=1e-12))
+    s = GmgSolver(levels, GmgOptions(scheme=sc, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1))
+    fv, uv = te.Vector.from_numpy(s.finest, f), te.Vector(s.finest)
+    its = s.solve(fv, uv)
+    assert its <= its_o + 3
+    assert s.residual(fv, uv) <= 1e-10
+    inner = _inner(levels[0])
+    # solution error <= cond(A) * relative residual; cond ~ 1e3 here (random right-hand side)
+    assert rel_err(uv.numpy()[inner], u_o[inner]) <= 1e-6

@@ -296,6 +296,13 @@ class DFTPatchSolver(_PatchSolver):
         self.op = op
         check(lib().te_dft_patch_solver_create(op.h, int(neumann_mask), ctypes.byref(self.h)))
 
+    @property
+    def uses_tensor_cores(self) -> bool:
+        """True when the FP32 solves run as 3xTF32 tcgen05 contractions."""
+        v = ctypes.c_int(0)
+        check(lib().te_patch_solver_uses_tensor_cores(self.h, ctypes.byref(v)))
+        return bool(v.value)
+
 
 class BiCGStabPatchSolver(_PatchSolver):
     """Iterative::PatchSolver with an inner Iterative::BiCGStab (Iterative/PatchSolver.h:121-175)."""

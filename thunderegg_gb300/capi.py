@@ -94,6 +94,7 @@ _SIGS = {
     "te_patch_solver_destroy": (_I, [_V]),
     "te_patch_solver_smooth": (_I, [_V, _I, _I, _V, _V]),
     "te_patch_solver_apply": (_I, [_V, _I, _I, _V, _V]),
+    "te_patch_solver_uses_tensor_cores": (_I, [_V, _ip]),
     "te_linear_restrictor_create": (_I, [_V, _V, _I, ctypes.POINTER(_V)]),
     "te_restrictor_destroy": (_I, [_V]),
     "te_restrict": (_I, [_V, _I, _I, _V, _V]),

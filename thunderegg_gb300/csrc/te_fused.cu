@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(1024)
 }
 
 // ---------------------------------------------------------------------------
-template <class T, class TF, class TO, int KIND, int SCHEME>
+template <class T, class TF, class TO, int KIND, int SCHEME, bool SOLVE>
 __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int ti_max, const int* __restrict__ parent, const int* __restrict__ porth,
                                const int8_t* __restrict__ ntype, int FS, const T* __restrict__ inv_tab,
                                const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int t
   const int p = blockIdx.x, N = F.interior(), D = F.D;
   T* Ab = reinterpret_cast<T*>(smraw);
   T* Bb = Ab + S.size;
-  T* G = Ab + S.mats;  // [2D][gstride]
+  T* G = SOLVE ? Ab + S.mats : Ab;  // [2D][gstride]
   const int plan = plan_of_patch[p];
   const T* MT[6];
   dft_mat_ptrs<T>(F, plan, plan_mats, mats, mat_off, MT);
@@ -254,8 +254,12 @@ __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int t
         v -= (gv + uv) * (cp[k] + cp[gk]) * inv[a];
       }
     }
-    Ab[x + y * S.sy + z * S.sz] = v;
+    if (SOLVE)
+      Ab[x + y * S.sy + z * S.sz] = v;
+    else
+      out[(long long)p * F.cs + k] = (TO)v;
   }
+  if (!SOLVE) return;  // the right-hand side goes to the tensor-core solve
   __syncthreads();
   T* cur = dft_solve_smem<T>(F, S, MT, inv_eig + (long long)plan * N, zero_mode[p] != 0, Ab, Bb, ti_max);
   TO* op = out + (long long)p * F.cs;
@@ -297,7 +301,7 @@ static int threads_for(const Layout& L) {
 
 template <class K>
 static void raise_smem(K kern, size_t bytes) {
-  if (bytes > 48 * 1024)
+  if (bytes > 40 * 1024)  // leave room for the static shared memory
     TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
 }
 
@@ -377,17 +381,19 @@ void vc_restrict(const te_restrictor* r, const te_operator* op, const T* u, cons
 
 template <class T, class TF, class TO, int KIND, int SCHEME>
 static void vc_post_t(const te_patch_solver* ps, const te_interpolator* in, const T* A, const T* uc, const TF* f,
-                      TO* out, cudaStream_t s) {
+                      TO* out, cudaStream_t s, bool solve) {
   const te_operator* op = ps->op;
   const te_domain* d = op->dom;
   const Layout &F = d->lay, &C = in->coarse->lay;
   const te_ghost_filler* g = op->gf;
   int gs = gstride_of(F);
-  size_t smem = dft_bytes(F, sizeof(T)) + (size_t)2 * F.D * gs * sizeof(T);
-  auto kern = vc_post_kernel<T, TF, TO, KIND, SCHEME>;
+  size_t gbytes = (size_t)2 * F.D * gs * sizeof(T);
+  size_t smem = solve ? dft_bytes(F, sizeof(T)) + gbytes : gbytes;
+  auto kern = solve ? vc_post_kernel<T, TF, TO, KIND, SCHEME, true> : vc_post_kernel<T, TF, TO, KIND, SCHEME, false>;
   raise_smem(kern, smem);
   int ti_max, threads;
   dft_launch_shape(F, ti_max, threads);
+  if (!solve) threads = std::min(256, (F.interior() + 31) / 32 * 32);
   kern<<<F.P, threads, smem, s>>>(F, C, ti_max, in->parent.p, in->orth.p, d->d_nbr_type.p, d->F,
                                           d->template inv<T>(), coeff_of<T>(op), g->faces, g->d_slabs.p,
                                           g->d_calls.p, g->d_slab_start.p, gs, ps->plan_of_patch.p,
@@ -399,10 +405,10 @@ static void vc_post_t(const te_patch_solver* ps, const te_interpolator* in, cons
 
 template <class T, class TF, class TO>
 void vc_post(const te_patch_solver* ps, const te_interpolator* in, const T* A, const T* uc, const TF* f, TO* out,
-             cudaStream_t s) {
+             cudaStream_t s, bool solve) {
   const te_operator* op = ps->op;
   int sc = op->gf->scheme;
-#define TE_VP(K, S) vc_post_t<T, TF, TO, K, S>(ps, in, A, uc, f, out, s)
+#define TE_VP(K, S) vc_post_t<T, TF, TO, K, S>(ps, in, A, uc, f, out, s, solve)
   if (op->kind == 0) {
     if (sc == TE_GHOST_BILINEAR) TE_VP(0, TE_GHOST_BILINEAR);
     else if (sc == TE_GHOST_BIQUADRATIC) TE_VP(0, TE_GHOST_BIQUADRATIC);
@@ -425,10 +431,10 @@ template void vc_restrict<float, double>(const te_restrictor*, const te_operator
 template void vc_restrict<float, float>(const te_restrictor*, const te_operator*, const float*, const float*,
                                         float*, cudaStream_t);
 template void vc_post<double, double, double>(const te_patch_solver*, const te_interpolator*, const double*,
-                                              const double*, const double*, double*, cudaStream_t);
+                                              const double*, const double*, double*, cudaStream_t, bool);
 template void vc_post<float, double, double>(const te_patch_solver*, const te_interpolator*, const float*,
-                                             const float*, const double*, double*, cudaStream_t);
+                                             const float*, const double*, double*, cudaStream_t, bool);
 template void vc_post<float, float, float>(const te_patch_solver*, const te_interpolator*, const float*,
-                                           const float*, const float*, float*, cudaStream_t);
+                                           const float*, const float*, float*, cudaStream_t, bool);
 
 }  // namespace te

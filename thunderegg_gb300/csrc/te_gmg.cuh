@@ -43,7 +43,7 @@ void vc_restrict(const te_restrictor* r, const te_operator* op, const T* u, cons
                  cudaStream_t s);
 template <class T, class TF, class TO>
 void vc_post(const te_patch_solver* ps, const te_interpolator* in, const T* A, const T* uc, const TF* f, TO* out,
-             cudaStream_t s);
+             cudaStream_t s, bool solve = true);
 }  // namespace te
 
 // ---------------------------------------------------------------------------
@@ -89,6 +89,9 @@ struct te_cycle {
   // even patch sizes, no ghost extrapolation, one component
   bool fusable = false;
   bool fused() const { return fusable && nc == 1; }
+  // the FP32 fused cycle runs the DFT solves of level k on the tensor cores
+  bool tc_enabled = true;
+  bool use_tc(int k) const { return tc_enabled && dtype == TE_F32 && levels[k].smoother->tc_ok; }
   ~te_cycle() {
     clear_graphs();
     if (ev_in) cudaEventDestroy(ev_in);
@@ -129,15 +132,28 @@ struct te_cycle {
   const T* vfused(int k, const TF* fk, TO* out, cudaStream_t s) const {
     int last = (int)levels.size() - 1;
     T* A = (T*)u[k].p;
-    te::vc_pre<T, TF>(levels[k].smoother, fk, A, s);
+    const te_patch_solver* ps = levels[k].smoother;
+    const bool tc = use_tc(k);
+    if (tc)
+      te::dft_tc<TF, T>(ps, fk, A, s);
+    else
+      te::vc_pre<T, TF>(ps, fk, A, s);
     mark("L" + std::to_string(k) + " pre-smooth", s);
     if (k == last) return A;
     T* fc = (T*)f[k + 1].p;
     te::vc_restrict<T, TF>(levels[k].restrictor, levels[k].op, A, fk, fc, s);
     mark("L" + std::to_string(k) + " residual+restrict", s);
     const T* uc = vfused<T, T, T>(k + 1, fc, (T*)r[k + 1].p, s);
-    te::vc_post<T, TF, TO>(levels[k].smoother, levels[k + 1].interpolator, A, uc, fk, out, s);
-    mark("L" + std::to_string(k) + " interpolate+post-smooth", s);
+    if (tc) {
+      // right-hand side with the corrected iterate's boundary terms into `out`, then solve in place
+      te::vc_post<T, TF, TO>(ps, levels[k + 1].interpolator, A, uc, fk, out, s, false);
+      mark("L" + std::to_string(k) + " interpolate+post-rhs", s);
+      te::dft_tc<TO, TO>(ps, out, out, s);
+      mark("L" + std::to_string(k) + " post-smooth", s);
+    } else {
+      te::vc_post<T, TF, TO>(ps, levels[k + 1].interpolator, A, uc, fk, out, s);
+      mark("L" + std::to_string(k) + " interpolate+post-smooth", s);
+    }
     return (const T*)out;
   }
   // `fresh`: u is known to be zero (ghosts included) before the first sweep

@@ -441,6 +441,12 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
   }
   for (int i = 0; i < B; i++) iterations[i] = its[i];
   TE_CUDA(cudaStreamSynchronize(st));
+  if (M)
+    for (const te_cycle_level& lv : M->levels)
+      if (lv.smoother && dft_tc_error(lv.smoother, st)) {
+        TE_CUDA(cudaMemsetAsync(lv.smoother->tc_err.p, 0, sizeof(int), st));
+        throw Error(TE_ERR_TIMEOUT, "tensor-core DFT: an MMA completion wait timed out; results are invalid");
+      }
   int worst = TE_OK;
   for (int i = 0; i < B; i++)
     if (statuses[i] != TE_OK) worst = statuses[i];

@@ -434,7 +434,7 @@ static void launch_dft(const te_patch_solver* ps, const T* f, T* u, const T* coe
 // raise the dynamic shared-memory limit of every DFT kernel instance once
 static void dft_set_smem_limits(size_t smem64, size_t smem32) {
   auto set = [](const void* k, size_t sm) {
-    if (sm > 48 * 1024) TE_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (sm > 40 * 1024) TE_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   };
   set((const void*)dft_kernel<double, 0, true>, smem64);
   set((const void*)dft_kernel<double, 0, false>, smem64);
@@ -469,7 +469,7 @@ static void bcg_prepare(te_patch_solver* ps) {
     using T = decltype(tag);
     size_t need = (size_t)8 * L.cs * sizeof(T);
     if (need <= 200 * 1024) {
-      if (need > 48 * 1024) {
+      if (need > 40 * 1024) {
         TE_CUDA(cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
         TE_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
       }
@@ -492,6 +492,8 @@ void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, v
     // ghost fill and the RHS modification contribute exactly zero
     if (dtype == TE_F64)
       launch_dft<double>(ps, (const double*)f, (double*)u, op->coeffs.p, ps->mats.p, ps->inv_eig.p, true, s);
+    else if (ps->tc_ok)
+      dft_tc<float, float>(ps, (const float*)f, (float*)u, s);
     else
       launch_dft<float>(ps, (const float*)f, (float*)u, op->coeffs_f.p, ps->mats_f.p, ps->inv_eig_f.p, true, s);
     return;
@@ -698,6 +700,7 @@ int te_dft_patch_solver_create(const te_operator* op, int neumann_mask, te_patch
     ps->inv_eig.upload(eig_inv, st);
     ps->inv_eig_f.upload(std::vector<float>(eig_inv.begin(), eig_inv.end()), st);
     ps->zero_mode.upload(zero, st);
+    dft_tc_prepare(ps.get(), mats, plan_mats, st);
     TE_CUDA(cudaStreamSynchronize(st));
     *out = ps.release();
   });
@@ -751,6 +754,12 @@ int te_patch_solver_smooth(const te_patch_solver* s, int nc, int dtype, const vo
 }
 int te_patch_solver_apply(const te_patch_solver* s, int nc, int dtype, const void* f, void* u) {
   return solver_call(s, nc, dtype, f, u, true);
+}
+int te_patch_solver_uses_tensor_cores(const te_patch_solver* s, int* out) {
+  return guard([&] {
+    require(s && out, "null argument");
+    *out = s->tc_ok ? 1 : 0;
+  });
 }
 
 }  // extern "C"

@@ -2,6 +2,7 @@
 #pragma once
 #include <map>
 #include <memory>
+#include <vector>
 
 #include "te_ghost.cuh"
 
@@ -42,10 +43,22 @@ struct te_patch_solver {
   te::DevBuf<unsigned long long> its;  // total inner iterations (statistics)
   te::DevBuf<int> status;              // breakdown flag
   mutable te::DevBuf<char> scratch;    // global-memory fallback for large patches
+  // tensor-core DFT (te_dft_tc.cu): usable when every patch shares the transform matrices
+  bool tc_ok = false;
+  int tc_pass_mat[6] = {0, 0, 0, 0, 0, 0};
+  int tc_nmat = 0;
+  te::DevBuf<float> tc_bmat;  // [tc_nmat][2][n*n] TF32 hi/lo parts, row-major
+  te::DevBuf<int> tc_err;     // set when an MMA wait timed out
 };
 
 namespace te {
 void operator_apply(const te_operator* op, int nc, int dtype, void* u, void* f, cudaStream_t s);
 void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, void* u, bool zero_first,
                   cudaStream_t s);
+// tensor-core DFT solve of every patch: out = DFT-solve(in) (in == out allowed)
+void dft_tc_prepare(te_patch_solver* ps, const std::vector<std::vector<double>>& mats_t,
+                    const std::vector<int>& plan_mats, cudaStream_t st);
+template <class TI, class TO>
+void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s);
+int dft_tc_error(const te_patch_solver* ps, cudaStream_t s);
 }  // namespace te
