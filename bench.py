@@ -178,8 +178,13 @@ def _phase_bytes(name, levels, dtype_bytes):
         return cells * (wf + w)
     if "restrict" in name:
         return cells * (w + wf + ghost + w / (1 << D))
+    face = 2 * D / n  # side-face cells per cell
+    if "post-corrections" in name:
+        # corrections written; own two boundary layers, the neighbours' two face layers and the
+        # coarse values under them read (FP32)
+        return cells * 4 * face * (1 + 2 + 2 + 1)
     if name.endswith("post-smooth") and "interpolate" not in name:
-        return cells * (wo + wo)  # tensor-core solve in place: read the right-hand side, write u
+        return cells * (wf + 4 * face + wo)  # tensor-core solve: f and the corrections in, u out
     return cells * (w + w / (1 << D) + wf + ghost + wo)
 
 

@@ -45,6 +45,7 @@ struct DftTcArgs {
   const int* plan_of_patch;  // [P]
   const float* inv_eig;      // [nplans][n^D]
   const int* zero_mode;      // [P]
+  const float* corr;         // optional [P][2D][n^(D-1)]: right-hand-side corrections per side face
   int* err;
 };
 
@@ -96,6 +97,9 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
   constexpr int CS = DIM == 3 ? SY * SY * SY : SY * SY;  // padded cells per patch
   constexpr int PER = S::G * S::NCELL / S::ROWS;          // interior cells per thread per group
   constexpr int OP = NN + 1;                               // row pitch (floats) of the output staging
+  constexpr int NF = S::RPP;                               // cells of one side face
+  constexpr int CPER = S::G * 2 * DIM * NF / S::ROWS;      // corrections per thread per group
+  static_assert(S::G * 2 * DIM * NF % S::ROWS == 0, "corrections must split evenly over the threads");
   extern __shared__ uint8_t dsm[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base;
@@ -107,9 +111,12 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
   uint8_t* Alo = sm + S::ATILE;
   uint8_t* Bm = sm + 2 * S::ATILE;
   float* stage = reinterpret_cast<float*>(sm);  // output staging over both A tiles: [ROWS][OP]
+  float* cbuf = reinterpret_cast<float*>(Bm + a.nmat * 2 * S::BTILE);  // [G][2D][NF] corrections
+  const bool has_corr = a.corr != nullptr;
 
   // the first group's right-hand sides, in flight while the CTA sets up
   TI pf[PER];
+  float cpf[CPER];
   auto prefetch = [&](int grp) {
     const int p0 = grp * S::G;
 #pragma unroll
@@ -118,6 +125,14 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
       int i = e / S::NCELL, c = e % S::NCELL;
       int p = p0 + i;
       pf[k] = p < P ? __ldg(in + (long long)p * CS + interior_offset<DIM, NN>(c)) : TI(0);
+    }
+    if (has_corr) {
+#pragma unroll
+      for (int k = 0; k < CPER; k++) {
+        int e = t + k * S::ROWS;
+        int p = p0 + e / (2 * DIM * NF);
+        cpf[k] = p < P ? __ldg(a.corr + (long long)p0 * 2 * DIM * NF + e) : 0.f;
+      }
     }
   };
   prefetch(blockIdx.x);
@@ -144,12 +159,28 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
 
   for (int grp = blockIdx.x; grp < a.ngroups && !abort; grp += gridDim.x) {
     const int p0 = grp * S::G;
+    if (has_corr) {
+#pragma unroll
+      for (int k = 0; k < CPER; k++) cbuf[t + k * S::ROWS] = cpf[k];
+      __syncthreads();
+    }
     // right-hand sides into the operand tiles of the x pass: line (i, y[, z]), k = x
 #pragma unroll
     for (int k = 0; k < PER; k++) {
       int e = t + k * S::ROWS;
       int i = e / S::NCELL, c = e % S::NCELL;
       float v = (float)pf[k];
+      if (has_corr) {
+        // f_copy = f - corrections of the cell's sides, in side order
+        const float* cb = cbuf + i * 2 * DIM * NF;
+        const int x = c % NN, y = (c / NN) % NN, z = DIM == 3 ? c / (NN * NN) : 0;
+        if (x == 0) v -= cb[0 * NF + y + NN * z];
+        if (x == NN - 1) v -= cb[1 * NF + y + NN * z];
+        if (y == 0) v -= cb[2 * NF + x + NN * z];
+        if (y == NN - 1) v -= cb[3 * NF + x + NN * z];
+        if (DIM == 3 && z == 0) v -= cb[4 * NF + x + NN * y];
+        if (DIM == 3 && z == NN - 1) v -= cb[5 * NF + x + NN * y];
+      }
       float hi = tc::to_tf32(v), lo = v - hi;
       uint32_t off = tc::tile_offset(i * S::RPP + c / NN, c % NN, S::ROWS, NN);
       *reinterpret_cast<float*>(Ahi + off) = hi;
@@ -289,7 +320,7 @@ float tf32_round_host(float x) {
 template <int DIM, int NN>
 size_t tc_smem_bytes(int nmat) {
   using S = TcShape<DIM, NN>;
-  return 1024 + 2 * (size_t)S::ATILE + (size_t)nmat * 2 * S::BTILE;
+  return 1024 + 2 * (size_t)S::ATILE + (size_t)nmat * 2 * S::BTILE + (size_t)S::G * 2 * DIM * S::RPP * 4;
 }
 
 }  // namespace
@@ -346,7 +377,7 @@ void dft_tc_prepare(te_patch_solver* ps, const std::vector<std::vector<double>>&
 }
 
 template <class TI, class TO, int DIM, int NN>
-static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s) {
+static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr) {
   using S = TcShape<DIM, NN>;
   const Layout& L = ps->op->dom->lay;
   DftTcArgs a;
@@ -358,6 +389,7 @@ static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStrea
   a.plan_of_patch = ps->plan_of_patch.p;
   a.inv_eig = ps->inv_eig_f.p;
   a.zero_mode = ps->zero_mode.p;
+  a.corr = corr;
   a.err = ps->tc_err.p;
   auto kern = dft_tc_kernel<TI, TO, DIM, NN>;
   size_t smem = tc_smem_bytes<DIM, NN>(a.nmat);
@@ -391,17 +423,17 @@ static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStrea
 }
 
 template <class TI, class TO>
-void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s) {
+void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr) {
   const Layout& L = ps->op->dom->lay;
   require(ps->tc_ok, "tensor-core DFT not prepared for this solver", TE_ERR_UNSUPPORTED);
   if (L.D == 2 && L.n0 == 16)
-    dft_tc_t<TI, TO, 2, 16>(ps, in, out, s);
+    dft_tc_t<TI, TO, 2, 16>(ps, in, out, s, corr);
   else if (L.D == 2 && L.n0 == 32)
-    dft_tc_t<TI, TO, 2, 32>(ps, in, out, s);
+    dft_tc_t<TI, TO, 2, 32>(ps, in, out, s, corr);
   else if (L.D == 2 && L.n0 == 64)
-    dft_tc_t<TI, TO, 2, 64>(ps, in, out, s);
+    dft_tc_t<TI, TO, 2, 64>(ps, in, out, s, corr);
   else
-    dft_tc_t<TI, TO, 3, 16>(ps, in, out, s);
+    dft_tc_t<TI, TO, 3, 16>(ps, in, out, s, corr);
 }
 
 int dft_tc_error(const te_patch_solver* ps, cudaStream_t s) {
@@ -412,8 +444,8 @@ int dft_tc_error(const te_patch_solver* ps, cudaStream_t s) {
   return e;
 }
 
-template void dft_tc<double, float>(const te_patch_solver*, const double*, float*, cudaStream_t);
-template void dft_tc<float, float>(const te_patch_solver*, const float*, float*, cudaStream_t);
-template void dft_tc<double, double>(const te_patch_solver*, const double*, double*, cudaStream_t);
+template void dft_tc<double, float>(const te_patch_solver*, const double*, float*, cudaStream_t, const float*);
+template void dft_tc<float, float>(const te_patch_solver*, const float*, float*, cudaStream_t, const float*);
+template void dft_tc<double, double>(const te_patch_solver*, const double*, double*, cudaStream_t, const float*);
 
 }  // namespace te

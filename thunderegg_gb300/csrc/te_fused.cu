@@ -203,7 +203,7 @@ __global__ void __launch_bounds__(1024)
 }
 
 // ---------------------------------------------------------------------------
-template <class T, class TF, class TO, int KIND, int SCHEME, bool SOLVE>
+template <class T, class TF, class TO, int KIND, int SCHEME>
 __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int ti_max, const int* __restrict__ parent, const int* __restrict__ porth,
                                const int8_t* __restrict__ ntype, int FS, const T* __restrict__ inv_tab,
                                const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
@@ -218,7 +218,7 @@ __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int t
   const int p = blockIdx.x, N = F.interior(), D = F.D;
   T* Ab = reinterpret_cast<T*>(smraw);
   T* Bb = Ab + S.size;
-  T* G = SOLVE ? Ab + S.mats : Ab;  // [2D][gstride]
+  T* G = Ab + S.mats;  // [2D][gstride]
   const int plan = plan_of_patch[p];
   const T* MT[6];
   dft_mat_ptrs<T>(F, plan, plan_mats, mats, mat_off, MT);
@@ -254,12 +254,8 @@ __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int t
         v -= (gv + uv) * (cp[k] + cp[gk]) * inv[a];
       }
     }
-    if (SOLVE)
-      Ab[x + y * S.sy + z * S.sz] = v;
-    else
-      out[(long long)p * F.cs + k] = (TO)v;
+    Ab[x + y * S.sy + z * S.sz] = v;
   }
-  if (!SOLVE) return;  // the right-hand side goes to the tensor-core solve
   __syncthreads();
   T* cur = dft_solve_smem<T>(F, S, MT, inv_eig + (long long)plan * N, zero_mode[p] != 0, Ab, Bb, ti_max);
   TO* op = out + (long long)p * F.cs;
@@ -269,6 +265,64 @@ __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int t
     bool in = x >= 0 && x < F.n0 && y >= 0 && y < F.n1 && z >= 0 && z < F.n2;
     op[k] = in ? (TO)(cur[x + y * S.sy + z * S.sz] * scale) : TO(0);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Boundary corrections of the post-smooth right-hand side
+// (modifyRHSForInternalBoundaryConditions, Poisson/StarPatchOperator.h:145-180,
+// VarPoisson/StarPatchOperator.h:150-186) for the corrected iterate
+// u = A + P u_coarse, which is never stored: one thread per cell of a side
+// face that has a neighbour computes the ghost value (the filler's gather on
+// the fly) and the correction c = (ghost + u_boundary) / h^2 (Poisson) or
+// (ghost + u_boundary) (c_in + c_ghost) / (2 h^2) (VarPoisson).  The solve
+// then subtracts the corrections of a cell's sides in side order:
+// f_copy = f - c_side0 - c_side1 ...  Faces without a neighbour get 0.
+// corr is [P][2D][gs], gs = the largest face size.
+template <int KIND, int SCHEME, int DIM>
+__global__ void __launch_bounds__(256)
+    vc_corr_kernel(Layout F, Layout C, const int* __restrict__ parent, const int* __restrict__ porth,
+                   const float* __restrict__ inv_tab, const float* __restrict__ coeff, FaceTable ft,
+                   const GSlab* __restrict__ slabs, const GCall* __restrict__ calls,
+                   const int* __restrict__ side_slab, int gs, const float* __restrict__ A,
+                   const float* __restrict__ uc, float* __restrict__ corr) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)F.P * 2 * DIM * gs;
+  if (e >= total) return;
+  const int r = (int)(e % gs);
+  const int s = (int)((e / gs) % (2 * DIM));
+  const int p = (int)(e / ((long long)gs * 2 * DIM));
+  const int a = s >> 1, upr = s & 1;
+  const int side0 = DIM == 2 ? 4 : 20;
+  const FaceGeom& g = ft.f[side0 + s];
+  if (r >= g.nt[0] * g.nt[1]) return;
+  const int si = side_slab[p * 2 * DIM + s];
+  float c = 0.f;
+  if (si >= 0) {
+    InterpAcc<float> acc{A, uc, parent, porth, F, C};
+    const GSlab sl = slabs[si];
+    const int i = r % g.nt[0], j = r / g.nt[0];
+    const float gv = gather_ghost<float, SCHEME>(acc, p, sl, g, ft, calls, DIM, i, j, 0.f);
+    const int coord = upr ? F.n(a) - 1 : 0;
+    int x, y, z;
+    if (a == 0) {
+      x = coord; y = i; z = j;
+    } else if (a == 1) {
+      x = i; y = coord; z = j;
+    } else {
+      x = i; y = j; z = coord;
+    }
+    const int k = F.at(x, y, z);
+    const float uv = acc(p, k);
+    const float inv = inv_tab[(size_t)p * 6 + (KIND ? 3 : 0) + a];
+    if (KIND == 0) {
+      c = (gv + uv) * inv;
+    } else {
+      const float* cp = coeff + (long long)p * F.cs;
+      const int gk = k + (upr ? F.stride(a) : -F.stride(a));
+      c = (gv + uv) * (cp[k] + cp[gk]) * inv;
+    }
+  }
+  corr[e] = c;
 }
 
 // ---------------------------------------------------------------------------
@@ -381,19 +435,17 @@ void vc_restrict(const te_restrictor* r, const te_operator* op, const T* u, cons
 
 template <class T, class TF, class TO, int KIND, int SCHEME>
 static void vc_post_t(const te_patch_solver* ps, const te_interpolator* in, const T* A, const T* uc, const TF* f,
-                      TO* out, cudaStream_t s, bool solve) {
+                      TO* out, cudaStream_t s) {
   const te_operator* op = ps->op;
   const te_domain* d = op->dom;
   const Layout &F = d->lay, &C = in->coarse->lay;
   const te_ghost_filler* g = op->gf;
   int gs = gstride_of(F);
-  size_t gbytes = (size_t)2 * F.D * gs * sizeof(T);
-  size_t smem = solve ? dft_bytes(F, sizeof(T)) + gbytes : gbytes;
-  auto kern = solve ? vc_post_kernel<T, TF, TO, KIND, SCHEME, true> : vc_post_kernel<T, TF, TO, KIND, SCHEME, false>;
+  size_t smem = dft_bytes(F, sizeof(T)) + (size_t)2 * F.D * gs * sizeof(T);
+  auto kern = vc_post_kernel<T, TF, TO, KIND, SCHEME>;
   raise_smem(kern, smem);
   int ti_max, threads;
   dft_launch_shape(F, ti_max, threads);
-  if (!solve) threads = std::min(256, (F.interior() + 31) / 32 * 32);
   kern<<<F.P, threads, smem, s>>>(F, C, ti_max, in->parent.p, in->orth.p, d->d_nbr_type.p, d->F,
                                           d->template inv<T>(), coeff_of<T>(op), g->faces, g->d_slabs.p,
                                           g->d_calls.p, g->d_slab_start.p, gs, ps->plan_of_patch.p,
@@ -405,10 +457,10 @@ static void vc_post_t(const te_patch_solver* ps, const te_interpolator* in, cons
 
 template <class T, class TF, class TO>
 void vc_post(const te_patch_solver* ps, const te_interpolator* in, const T* A, const T* uc, const TF* f, TO* out,
-             cudaStream_t s, bool solve) {
+             cudaStream_t s) {
   const te_operator* op = ps->op;
   int sc = op->gf->scheme;
-#define TE_VP(K, S) vc_post_t<T, TF, TO, K, S>(ps, in, A, uc, f, out, s, solve)
+#define TE_VP(K, S) vc_post_t<T, TF, TO, K, S>(ps, in, A, uc, f, out, s)
   if (op->kind == 0) {
     if (sc == TE_GHOST_BILINEAR) TE_VP(0, TE_GHOST_BILINEAR);
     else if (sc == TE_GHOST_BIQUADRATIC) TE_VP(0, TE_GHOST_BIQUADRATIC);
@@ -421,6 +473,43 @@ void vc_post(const te_patch_solver* ps, const te_interpolator* in, const T* A, c
 #undef TE_VP
 }
 
+int corr_stride(const Layout& L) { return gstride_of(L); }
+
+template <int KIND, int SCHEME>
+static void vc_corr_t(const te_patch_solver* ps, const te_interpolator* in, const float* A, const float* uc,
+                      float* corr, cudaStream_t s) {
+  const te_operator* op = ps->op;
+  const te_domain* d = op->dom;
+  const Layout &F = d->lay, &C = in->coarse->lay;
+  const te_ghost_filler* g = op->gf;
+  const int gs = gstride_of(F);
+  const long long total = (long long)F.P * 2 * F.D * gs;
+  const int threads = 256;
+  const unsigned blocks = (unsigned)((total + threads - 1) / threads);
+  auto kern = F.D == 2 ? vc_corr_kernel<KIND, SCHEME, 2> : vc_corr_kernel<KIND, SCHEME, 3>;
+  kern<<<blocks, threads, 0, s>>>(F, C, in->parent.p, in->orth.p, d->template inv<float>(), op->coeffs_f.p,
+                                  g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, gs, A, uc, corr);
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
+void vc_corr(const te_patch_solver* ps, const te_interpolator* in, const float* A, const float* uc, float* corr,
+             cudaStream_t s) {
+  const te_operator* op = ps->op;
+  int sc = op->gf->scheme;
+#define TE_VC(K, S) vc_corr_t<K, S>(ps, in, A, uc, corr, s)
+  if (op->kind == 0) {
+    if (sc == TE_GHOST_BILINEAR) TE_VC(0, TE_GHOST_BILINEAR);
+    else if (sc == TE_GHOST_BIQUADRATIC) TE_VC(0, TE_GHOST_BIQUADRATIC);
+    else TE_VC(0, TE_GHOST_TRILINEAR);
+  } else {
+    if (sc == TE_GHOST_BILINEAR) TE_VC(1, TE_GHOST_BILINEAR);
+    else if (sc == TE_GHOST_BIQUADRATIC) TE_VC(1, TE_GHOST_BIQUADRATIC);
+    else TE_VC(1, TE_GHOST_TRILINEAR);
+  }
+#undef TE_VC
+}
+
 template void vc_pre<double, double>(const te_patch_solver*, const double*, double*, cudaStream_t);
 template void vc_pre<float, double>(const te_patch_solver*, const double*, float*, cudaStream_t);
 template void vc_pre<float, float>(const te_patch_solver*, const float*, float*, cudaStream_t);
@@ -431,10 +520,10 @@ template void vc_restrict<float, double>(const te_restrictor*, const te_operator
 template void vc_restrict<float, float>(const te_restrictor*, const te_operator*, const float*, const float*,
                                         float*, cudaStream_t);
 template void vc_post<double, double, double>(const te_patch_solver*, const te_interpolator*, const double*,
-                                              const double*, const double*, double*, cudaStream_t, bool);
+                                              const double*, const double*, double*, cudaStream_t);
 template void vc_post<float, double, double>(const te_patch_solver*, const te_interpolator*, const float*,
-                                             const float*, const double*, double*, cudaStream_t, bool);
+                                             const float*, const double*, double*, cudaStream_t);
 template void vc_post<float, float, float>(const te_patch_solver*, const te_interpolator*, const float*,
-                                           const float*, const float*, float*, cudaStream_t, bool);
+                                           const float*, const float*, float*, cudaStream_t);
 
 }  // namespace te

@@ -243,7 +243,13 @@ int te_ghost_filler_create(const te_domain* d, int scheme, int fill_type, te_gho
         }
     }
     g->h_slab_start[P] = (int)g->h_slabs.size();
+    std::vector<int> side_slab((size_t)P * 2 * D, -1);
+    for (size_t k = 0; k < g->h_slabs.size(); k++) {
+      const GSlab& s = g->h_slabs[k];
+      if (s.M == D - 1 && s.zero) side_slab[(size_t)s.patch * 2 * D + s.face] = (int)k;
+    }
     cudaStream_t st = d->stream;
+    g->d_side_slab.upload(side_slab, st);
     g->d_slabs.upload(g->h_slabs, st);
     g->d_calls.upload(hc, st);
     g->d_slab_start.upload(g->h_slab_start, st);

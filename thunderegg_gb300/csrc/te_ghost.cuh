@@ -56,6 +56,7 @@ struct te_ghost_filler {
   te::DevBuf<te::GSlab> d_slabs;
   te::DevBuf<te::GCall> d_calls;
   te::DevBuf<int> d_slab_start;
+  te::DevBuf<int> d_side_slab;  // [P * 2D]: the side slab with a neighbour, or -1
   te::FaceTable faces;
 };
 

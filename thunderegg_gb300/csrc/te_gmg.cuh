@@ -43,7 +43,11 @@ void vc_restrict(const te_restrictor* r, const te_operator* op, const T* u, cons
                  cudaStream_t s);
 template <class T, class TF, class TO>
 void vc_post(const te_patch_solver* ps, const te_interpolator* in, const T* A, const T* uc, const TF* f, TO* out,
-             cudaStream_t s, bool solve = true);
+             cudaStream_t s);
+// boundary corrections of the post-smooth right-hand side (FP32), [P][2D][face cells]
+void vc_corr(const te_patch_solver* ps, const te_interpolator* in, const float* A, const float* uc, float* corr,
+             cudaStream_t s);
+int corr_stride(const Layout& L);
 }  // namespace te
 
 // ---------------------------------------------------------------------------
@@ -72,6 +76,7 @@ struct te_cycle {
   std::map<std::pair<const void*, void*>, G> graphs;
   // per-level work buffers in the cycle's precision
   std::vector<te::DevBuf<char>> f, u, r;
+  std::vector<te::DevBuf<char>> corr;  // tensor-core post-smooth: right-hand-side corrections per level
   // optional per-kernel timing of one eager application (te_cycle_timings)
   struct Mark {
     std::string name;
@@ -117,13 +122,19 @@ struct te_cycle {
     f.clear();
     u.clear();
     r.clear();
+    corr.clear();
     f.resize(L);
     u.resize(L);
     r.resize(L);
+    corr.resize(L);
     for (size_t k = 0; k < L; k++) {
       r[k].alloc(bytes(k));
       u[k].alloc(bytes(k));
       if (k > 0 || dtype != TE_F64) f[k].alloc(bytes(k));
+      if (use_tc((int)k)) {
+        const te::Layout& Lk = dom(k)->lay;
+        corr[k].alloc((size_t)Lk.P * 2 * Lk.D * te::corr_stride(Lk) * sizeof(float));
+      }
     }
   }
   // Fused V-cycle: A = u[k] holds the pre-smoothed iterate, r[k] the post-smoothed
@@ -145,10 +156,11 @@ struct te_cycle {
     mark("L" + std::to_string(k) + " residual+restrict", s);
     const T* uc = vfused<T, T, T>(k + 1, fc, (T*)r[k + 1].p, s);
     if (tc) {
-      // right-hand side with the corrected iterate's boundary terms into `out`, then solve in place
-      te::vc_post<T, TF, TO>(ps, levels[k + 1].interpolator, A, uc, fk, out, s, false);
-      mark("L" + std::to_string(k) + " interpolate+post-rhs", s);
-      te::dft_tc<TO, TO>(ps, out, out, s);
+      // boundary corrections of the corrected iterate (never stored), then the solve from f
+      float* cr = (float*)corr[k].p;
+      te::vc_corr(ps, levels[k + 1].interpolator, (const float*)A, (const float*)uc, cr, s);
+      mark("L" + std::to_string(k) + " interpolate+post-corrections", s);
+      te::dft_tc<TF, TO>(ps, fk, out, s, cr);
       mark("L" + std::to_string(k) + " post-smooth", s);
     } else {
       te::vc_post<T, TF, TO>(ps, levels[k + 1].interpolator, A, uc, fk, out, s);

@@ -58,7 +58,8 @@ void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, v
 // tensor-core DFT solve of every patch: out = DFT-solve(in) (in == out allowed)
 void dft_tc_prepare(te_patch_solver* ps, const std::vector<std::vector<double>>& mats_t,
                     const std::vector<int>& plan_mats, cudaStream_t st);
+// corr (optional, FP32 [P][2D][n^(D-1)]): per-side right-hand-side corrections subtracted while staging
 template <class TI, class TO>
-void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s);
+void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr = nullptr);
 int dft_tc_error(const te_patch_solver* ps, cudaStream_t s);
 }  // namespace te
