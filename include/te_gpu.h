@@ -215,14 +215,23 @@ int te_cycle_timings(const te_cycle* c, int ncomp, const void* f, void* u, int m
                      double* ms, int* count);
 
 /* ---- Iterative::BiCGStab (Iterative/BiCGStab.h:111-203) ------------------- */
-/* Right-preconditioned BiCGStab in FP64 on device vectors of A's domain.
+/* Right-preconditioned BiCGStab on FP64 device vectors of A's domain.
  * M may be NULL.  Stops when ||r||/||b|| <= tol.  Returns TE_ERR_BREAKDOWN
  * when rho == 0 (the reference throws BreakdownError).
+ * With an FP32 cycle as M (mixed precision) the iteration runs in float-float
+ * arithmetic (pairs of FP32 numbers, ~48 significant bits) on the FP32 pipes;
+ * the initial residual and x in and out stay FP64.  When the float-float
+ * recurrence has converged, every solve's true residual b - A x is computed
+ * in FP64; a solve still above tol restarts from it (residual replacement),
+ * and the final residual reported is that FP64 residual.  With an FP64 cycle
+ * or no preconditioner the iteration runs in FP64.
  * flags: 0 = the reference's update rule exactly; TE_BICGSTAB_PRECONDITIONED_EXIT
  * = on the early exit (||s|| small) add alpha * M p instead of alpha * p
  * (the reference adds alpha * p, BiCGStab.h:160-168, which leaves the true
- * residual of a preconditioned solve well above tol). */
-enum { TE_BICGSTAB_PRECONDITIONED_EXIT = 1 };
+ * residual of a preconditioned solve well above tol); TE_BICGSTAB_FP64_OUTER
+ * = run the iteration in FP64 even with an FP32 cycle (no counterpart in the
+ * reference). */
+enum { TE_BICGSTAB_PRECONDITIONED_EXIT = 1, TE_BICGSTAB_FP64_OUTER = 2 };
 int te_bicgstab_solve(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M,
                       double tol, int max_iterations, int flags, int* iterations,
                       double* final_residual);

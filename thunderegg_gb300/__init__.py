@@ -423,9 +423,11 @@ class CycleBuilder:
 
 
 class BiCGStab:
-    """Iterative::BiCGStab (Iterative/BiCGStab.h:40-204); FP64 on the GPU."""
+    """Iterative::BiCGStab (Iterative/BiCGStab.h:40-204) on the GPU: FP64, or
+    float-float (pairs of FP32 numbers) when the preconditioner is an FP32 cycle."""
 
     PRECONDITIONED_EXIT = 1
+    FP64_OUTER = 2
 
     def __init__(self, tolerance=1e-12, max_iterations=1000, flags=0):
         self.tolerance, self.max_iterations, self.flags = tolerance, max_iterations, flags

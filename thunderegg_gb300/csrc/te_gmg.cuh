@@ -219,6 +219,16 @@ struct te_cycle {
       te::convert_level(dom(0), nc, TE_F64, u64, dtype, u[0].p, s);
     }
   }
+  // FP32 in and out (dtype TE_F32): the float-float outer Krylov loop passes the
+  // hi half of its vectors and takes an FP32 result
+  void body_f32(const float* f32, float* u32, cudaStream_t s) const {
+    if (fused()) {
+      vfused<float, float, float>(0, f32, u32, s);
+      return;
+    }
+    if (opts.pre_sweeps == 0 || levels.size() == 1) TE_CUDA(cudaMemsetAsync(u32, 0, bytes(0), s));
+    visit(0, f32, u32, s);
+  }
   // run on stream s (which may itself be capturing)
   void apply_on(const void* f64, void* u64, cudaStream_t s) {
     if (!use_graph) {

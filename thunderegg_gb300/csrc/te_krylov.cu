@@ -25,6 +25,8 @@
 #include <string>
 #include <tuple>
 
+#include "te_df64.cuh"
+#include "te_ghost_dev.cuh"
 #include "te_gmg.cuh"
 
 namespace te {
@@ -43,6 +45,7 @@ enum Slot {
   S_BETA,
   S_DONE,
   S_BB,
+  S_TRUE = 15,  // float-float loop: ||b - A x||^2 in FP64 after convergence
   S_NSLOTS = 16
 };
 
@@ -222,6 +225,209 @@ __global__ void __launch_bounds__(KT) k_p(Layout L, int nc, Batch bt, double* p,
   });
 }
 
+// ---------------------------------------------------------------------------
+// Float-float outer loop (mixed precision: FP32 V-cycle preconditioner).
+// The same recurrences and operation order as the FP64 kernels above, with
+// every Krylov vector a float-float pair stored as hi and lo FP32 arrays and
+// the preconditioner results mp, ms plain FP32 (they are FP32 values).
+// ---------------------------------------------------------------------------
+struct DV {
+  float* hi;
+  float* lo;
+};
+struct CV {
+  const float* hi;
+  const float* lo;  // null: the vector is FP32 (lo = 0)
+};
+__host__ __device__ __forceinline__ CV as_cv(const DV& v) { return CV{v.hi, v.lo}; }
+__device__ __forceinline__ df64 ldv(const CV& v, long long k) { return df64(v.hi[k], v.lo ? v.lo[k] : 0.f); }
+__device__ __forceinline__ void stv(const DV& v, long long k, df64 x) {
+  v.hi[k] = x.hi;
+  v.lo[k] = x.lo;
+}
+
+template <int NV>
+__global__ void __launch_bounds__(KT) kd_dots(Layout L, int nc, Batch bt, CV a0, CV b0, CV a1, CV b1, CV a2, CV b2,
+                                              double* part, unsigned int* counter, double* S, int slot0, int fin) {
+  TE_BLOCK_SOLVE(bt);
+  df64 v[NV];
+  for (int i = 0; i < NV; i++) v[i] = df64(0.f, 0.f);
+  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
+    v[0] += ldv(a0, k) * ldv(b0, k);
+    if (NV > 1) v[1] += ldv(a1, k) * ldv(b1, k);
+    if (NV > 2) v[2] += ldv(a2, k) * ldv(b2, k);
+  });
+  double d[NV];
+  for (int i = 0; i < NV; i++) d[i] = df_to_double(v[i]);
+  k_reduce<NV>(d, bt, b, ch, part, counter, S, slot0, fin, 0);
+}
+
+__global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double tol, CV r, CV ap, DV s, double* part,
+                                           unsigned int* counter, double* S) {
+  TE_BLOCK_SOLVE(bt);
+  const df64 nalpha(-S[(size_t)b * S_NSLOTS + S_ALPHA]);
+  df64 v = df64(0.f, 0.f);
+  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
+    df64 sv = ldv(r, k) + ldv(ap, k) * nalpha;
+    stv(s, k, sv);
+    v += sv * sv;
+  });
+  double d[1] = {df_to_double(v)};
+  k_reduce<1>(d, bt, b, ch, part, counter, S, S_SS, 5, tol);
+}
+
+__global__ void __launch_bounds__(KT) kd_xr(Layout L, int nc, Batch bt, DV x, DV r, const float* mp, const float* ms,
+                                            CV ap, CV as, CV rhat, CV dir, double* part, unsigned int* counter,
+                                            double* S) {
+  TE_BLOCK_SOLVE(bt);
+  const double* Sb = S + (size_t)b * S_NSLOTS;
+  const df64 alpha(Sb[S_ALPHA]), omega(Sb[S_OMEGA]);
+  const df64 nalpha = -alpha, nomega = -omega;
+  const bool done = Sb[S_DONE] != 0.0;
+  df64 v0 = df64(0.f, 0.f), v1 = df64(0.f, 0.f);
+  const CV xc = as_cv(x), rc = as_cv(r);
+  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
+    if (done) {
+      stv(x, k, ldv(xc, k) + ldv(dir, k) * alpha);
+    } else {
+      stv(x, k, ldv(xc, k) + (alpha * mp[k] + omega * ms[k]));
+      df64 rv = ldv(rc, k) + (ldv(ap, k) * nalpha + ldv(as, k) * nomega);
+      stv(r, k, rv);
+      v0 += rv * rv;
+      v1 += rv * ldv(rhat, k);
+    }
+  });
+  double d[2] = {df_to_double(v0), df_to_double(v1)};
+  k_reduce<2>(d, bt, b, ch, part, counter, S, S_RR, 3, 0);
+}
+
+__global__ void __launch_bounds__(KT) kd_p(Layout L, int nc, Batch bt, DV p, CV ap, CV r, const double* S) {
+  TE_BLOCK_SOLVE(bt);
+  const double* Sb = S + (size_t)b * S_NSLOTS;
+  if (Sb[S_DONE] != 0.0) return;
+  const df64 nomega(-Sb[S_OMEGA]), beta(Sb[S_BETA]);
+  const CV pc = as_cv(p);
+  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
+    df64 pv = ldv(pc, k) + ldv(ap, k) * nomega;
+    stv(p, k, pv * beta + ldv(r, k));
+  });
+}
+
+__global__ void kd_split(const double* src, DV dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    stv(dst, i, df64(src[i]));
+}
+__global__ void kd_join(CV src, double* dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = df_to_double(ldv(src, i));
+}
+
+// FP32 values of a level buffer, read as float-float numbers
+struct F32Acc {
+  const float* u;
+  long long ps;
+  __device__ __forceinline__ df64 operator()(int q, int idx) const { return df64(u[q * ps + idx], 0.f); }
+};
+
+// f = A u for an FP32 level buffer u (ghosts not filled), in float-float:
+// the side ghosts of every face with a neighbour are gathered with the ghost
+// filler's formulas (te_ghost_dev.cuh) into shared memory, physical-boundary
+// ghosts are -u (Dirichlet) or +u (Neumann) (enforceBoundaryConditions), and
+// the star stencil runs in the reference's operation order.  u is not
+// modified.  One CTA per patch; f's ghost cells are set to 0.
+template <int KIND, int SCHEME, int DIM>
+__global__ void __launch_bounds__(256)
+    apply_df_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const double* __restrict__ inv64,
+                    int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
+                    const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gs,
+                    const float* __restrict__ u, DV f) {
+  extern __shared__ df64 G[];  // [2D][gs]
+  __shared__ df64 inv[3];
+  __shared__ int has[6];
+  const int p = blockIdx.x;
+  const int side0 = DIM == 2 ? 4 : 20;
+  const F32Acc acc{u, (long long)L.cs};
+  for (int e = threadIdx.x; e < 2 * DIM * gs; e += blockDim.x) {
+    const int s = e / gs, r = e % gs;
+    const FaceGeom& g = ft.f[side0 + s];
+    if (r >= g.nt[0] * g.nt[1]) continue;
+    const int si = side_slab[p * 2 * DIM + s];
+    if (si < 0) continue;
+    const GSlab sl = slabs[si];
+    G[e] = gather_ghost<df64, SCHEME>(acc, p, sl, g, ft, calls, DIM, r % g.nt[0], r / g.nt[0], df64(0.f, 0.f));
+  }
+  if (threadIdx.x < 3) inv[threadIdx.x] = df64(inv64[(size_t)p * 6 + (KIND ? 3 : 0) + threadIdx.x]);
+  if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
+  __syncthreads();
+  const float* up = u + (long long)p * L.cs;
+  const long long base = (long long)p * L.cs;
+  const int py = L.n1 + 2 * L.g;
+  for (int e = threadIdx.x; e < L.cs; e += blockDim.x) {
+    const int c0 = e % L.sy - L.g, q = e / L.sy;
+    const int c1 = q % py - L.g, c2 = q / py - (DIM == 3 ? L.g : 0);
+    const bool interior = c0 >= 0 && c0 < L.n0 && c1 >= 0 && c1 < L.n1 && c2 >= 0 && c2 < L.n2;
+    df64 res(0.f, 0.f);
+    if (interior) {
+      const int cc[3] = {c0, c1, c2};
+      const df64 mid(up[e], 0.f);
+#pragma unroll
+      for (int a = 0; a < DIM; a++) {
+        const int st = L.stride(a);
+        const int tan = a == 0 ? c1 + c2 * L.n1 : (a == 1 ? c0 + c2 * L.n0 : c0 + c1 * L.n0);
+        df64 lo, hi;
+        if (cc[a] == 0)
+          lo = has[2 * a] ? G[(2 * a) * gs + tan] : (neumann ? mid : -mid);
+        else
+          lo = df64(up[e - st], 0.f);
+        if (cc[a] == L.n(a) - 1)
+          hi = has[2 * a + 1] ? G[(2 * a + 1) * gs + tan] : (neumann ? mid : -mid);
+        else
+          hi = df64(up[e + st], 0.f);
+        if (KIND == 0) {
+          res += ((hi - df64(2.0) * mid) + lo) * inv[a];
+        } else {
+          const df64 cl = ldv(coeff, base + e - st), cm = ldv(coeff, base + e), cu = ldv(coeff, base + e + st);
+          res += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
+        }
+      }
+    }
+    stv(f, base + e, res);
+  }
+}
+
+template <int KIND, int SCHEME>
+static void apply_df_t(const te_operator* A, const float* u, DV f, cudaStream_t st) {
+  const te_domain* d = A->dom;
+  const Layout& L = d->lay;
+  const te_ghost_filler* g = A->gf;
+  const int gs = corr_stride(L);
+  const size_t smem = (size_t)2 * L.D * gs * sizeof(df64);
+  const long long n = (long long)L.P * L.cs;
+  CV coeff{KIND ? A->coeffs_df.p : nullptr, KIND ? A->coeffs_df.p + n : nullptr};
+  auto kern = L.D == 2 ? apply_df_kernel<KIND, SCHEME, 2> : apply_df_kernel<KIND, SCHEME, 3>;
+  if (smem > 40 * 1024)
+    TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, d->d_inv.p, A->neumann, coeff, g->faces, g->d_slabs.p,
+                               g->d_calls.p, g->d_side_slab.p, gs, u, f);
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
+static void apply_df(const te_operator* A, const float* u, DV f, cudaStream_t st) {
+  const int sc = A->gf->scheme;
+#define TE_AD(K, S) apply_df_t<K, S>(A, u, f, st)
+  if (A->kind == 0) {
+    if (sc == TE_GHOST_BILINEAR) TE_AD(0, TE_GHOST_BILINEAR);
+    else if (sc == TE_GHOST_BIQUADRATIC) TE_AD(0, TE_GHOST_BIQUADRATIC);
+    else TE_AD(0, TE_GHOST_TRILINEAR);
+  } else {
+    if (sc == TE_GHOST_BILINEAR) TE_AD(1, TE_GHOST_BILINEAR);
+    else if (sc == TE_GHOST_BIQUADRATIC) TE_AD(1, TE_GHOST_BIQUADRATIC);
+    else TE_AD(1, TE_GHOST_TRILINEAR);
+  }
+#undef TE_AD
+}
+
 struct KrylovWork {
   const te_domain* d;
   int nc;
@@ -229,6 +435,7 @@ struct KrylovWork {
   size_t n;
   std::vector<int> h_offs, h_nch;
   DevBuf<double> resid, rhat, p, ap, as, s, ms, mp, S, part;
+  DevBuf<double> xdf;  // float-float outer loop: the iterate (allocated on first use)
   DevBuf<unsigned int> counter;
   DevBuf<int> offs, nch, active;
   double* h = nullptr;
@@ -276,6 +483,10 @@ struct KrylovWork {
     if (cap) cudaStreamDestroy(cap);
   }
   Batch batch() const { return Batch{B, offs.p, nch.p, active.p}; }
+  // float-float views of the work buffers: hi in the first n floats, lo in the next n
+  DV dv(DevBuf<double>& v) const { return DV{(float*)v.p, (float*)v.p + n}; }
+  CV cv(const DevBuf<double>& v) const { return CV{(const float*)v.p, (const float*)v.p + n}; }
+  float* f32(DevBuf<double>& v) const { return (float*)v.p; }
   int grid() const { return B * MAX_CHUNKS; }
   void read_scalars(cudaStream_t st) {
     TE_CUDA(cudaMemcpyAsync(h, S.p, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -327,6 +538,46 @@ static void iteration(KrylovWork& W, const te_operator* A, te_cycle* M, double* 
   TE_LAUNCH_CHECK();
 }
 
+// one float-float iteration; M is an FP32 cycle
+static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, double tol, int flags, cudaStream_t st) {
+  const Layout& L = W.d->lay;
+  const int nc = W.nc;
+  Batch bt = W.batch();
+  const CV none{nullptr, nullptr};
+  M->body_f32(W.f32(W.p), W.f32(W.mp), st);
+  apply_df(A, W.f32(W.mp), W.dv(W.ap), st);
+  kd_dots<1><<<W.grid(), KT, 0, st>>>(L, nc, bt, W.cv(W.rhat), W.cv(W.ap), none, none, none, none, W.part.p,
+                                      W.counter.p, W.S.p, S_RHAT_AP, 1);
+  count_launch();
+  TE_LAUNCH_CHECK();
+  kd_s<<<W.grid(), KT, 0, st>>>(L, nc, bt, tol, W.cv(W.resid), W.cv(W.ap), W.dv(W.s), W.part.p, W.counter.p,
+                                W.S.p);
+  count_launch();
+  TE_LAUNCH_CHECK();
+  M->body_f32(W.f32(W.s), W.f32(W.ms), st);
+  apply_df(A, W.f32(W.ms), W.dv(W.as), st);
+  kd_dots<2><<<W.grid(), KT, 0, st>>>(L, nc, bt, W.cv(W.as), W.cv(W.s), W.cv(W.as), W.cv(W.as), none, none,
+                                      W.part.p, W.counter.p, W.S.p, S_AS_S, 2);
+  count_launch();
+  TE_LAUNCH_CHECK();
+  const CV dir = (flags & TE_BICGSTAB_PRECONDITIONED_EXIT) ? CV{W.f32(W.mp), nullptr} : W.cv(W.p);
+  kd_xr<<<W.grid(), KT, 0, st>>>(L, nc, bt, W.dv(W.xdf), W.dv(W.resid), W.f32(W.mp), W.f32(W.ms), W.cv(W.ap),
+                                 W.cv(W.as), W.cv(W.rhat), dir, W.part.p, W.counter.p, W.S.p);
+  count_launch();
+  TE_LAUNCH_CHECK();
+  kd_p<<<W.grid(), KT, 0, st>>>(L, nc, bt, W.dv(W.p), W.cv(W.ap), W.cv(W.resid), W.S.p);
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
+// the float-float outer loop runs when the preconditioner is an FP32 cycle
+static bool use_df(const te_operator* A, int nc, const te_cycle* M, int flags) {
+  if (!M || M->dtype != TE_F32 || nc != 1 || (flags & TE_BICGSTAB_FP64_OUTER)) return false;
+  if (A->kind == 1 && !A->coeffs_df.p) return false;
+  const char* e = getenv("TE_KRYLOV_FP64");
+  return !(e && e[0] == '1');
+}
+
 static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv, const te_cycle* Mc, double tol,
                          int max_iterations, int flags, const std::vector<int>& offsets, int* iterations,
                          double* final_residuals, int* statuses) {
@@ -342,15 +593,31 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
   double* x = (double*)xv;
   const double* b = (const double*)bv;
   size_t bytes = W.n * sizeof(double);
-  // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
-  operator_apply(A, nc, TE_F64, x, W.resid.p, st);
-  vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.resid.p, b, nullptr, -1, 0, 0);
-  TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-  TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+  const bool df = use_df(A, nc, M, flags);
+  const long long nvals = (long long)W.n;
   TE_CUDA(cudaMemsetAsync(W.S.p, 0, (size_t)B * S_NSLOTS * sizeof(double), st));
   for (int i = 0; i < B; i++) W.h_active[i] = 1;
   W.push_active(st);
-  launch_dots(W, 3, b, b, W.rhat.p, W.resid.p, W.resid.p, W.resid.p, S_BB, 0, st);
+  if (df) {
+    // resid = b - A x in FP64, then split into float-float; rhat = p = resid (BiCGStab.h:113-131)
+    if (!W.xdf.p) W.xdf.alloc(W.n);
+    operator_apply(A, nc, TE_F64, x, W.ap.p, st);
+    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.ap.p, b, nullptr, -1, 0, 0);
+    launch_dots(W, 3, b, b, W.ap.p, W.ap.p, W.ap.p, W.ap.p, S_BB, 0, st);
+    kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
+    kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
+    count_launch(2);
+    TE_LAUNCH_CHECK();
+    TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+    TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+  } else {
+    // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
+    operator_apply(A, nc, TE_F64, x, W.resid.p, st);
+    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.resid.p, b, nullptr, -1, 0, 0);
+    TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+    TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+    launch_dots(W, 3, b, b, W.rhat.p, W.resid.p, W.resid.p, W.resid.p, S_BB, 0, st);
+  }
   W.read_scalars(st);
   std::vector<double> rho(B), r0(B), residual(B);
   std::vector<int> its(B, 0);
@@ -378,7 +645,9 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
   W.push_active(st);
   const char* ng = getenv("TE_NO_GRAPH");
   bool use_graph = !(ng && ng[0] == '1');
-  auto gkey = std::make_tuple((void*)x, (const void*)b, M ? M->serial : 0ull, M ? M->generation : 0ull, tol, flags);
+  auto gkey = std::make_tuple((void*)x, (const void*)b, M ? M->serial : 0ull, M ? M->generation : 0ull, tol,
+                              flags | (df ? 1 << 30 : 0));
+  auto run = [&]() {
   while (nactive > 0) {
     if (use_graph) {
       auto it = W.graphs.find(gkey);
@@ -387,7 +656,10 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
         long long l0 = g_launches.load();
         TE_CUDA(cudaStreamBeginCapture(W.cap, cudaStreamCaptureModeThreadLocal));
         try {
-          iteration(W, A, M, x, tol, flags, W.cap);
+          if (df)
+            iteration_df(W, A, M, tol, flags, W.cap);
+          else
+            iteration(W, A, M, x, tol, flags, W.cap);
         } catch (...) {
           cudaGraph_t junk = nullptr;
           cudaStreamEndCapture(W.cap, &junk);
@@ -406,6 +678,8 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
       count_launch((int)it->second.launches);
       TE_CUDA(cudaEventRecord(W.ev_out, W.cap));
       TE_CUDA(cudaStreamWaitEvent(st, W.ev_out, 0));
+    } else if (df) {
+      iteration_df(W, A, M, tol, flags, st);
     } else {
       iteration(W, A, M, x, tol, flags, st);
     }
@@ -437,6 +711,49 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
       nactive = 0;
       for (int i = 0; i < B; i++) nactive += W.h_active[i];
       W.push_active(st);
+    }
+  }
+  };
+  run();
+  if (df) {
+    // Residual replacement: the float-float recurrence keeps ~1e-14 of the
+    // initial residual, so check every solve's true residual b - A x in FP64
+    // and restart the ones above tol from it (at most a few times).
+    for (int restart = 0;; restart++) {
+      kd_join<<<1216, 256, 0, st>>>(W.cv(W.xdf), x, nvals);
+      count_launch();
+      TE_LAUNCH_CHECK();
+      if (restart == 8) break;
+      for (int i = 0; i < B; i++) W.h_active[i] = statuses[i] == TE_OK ? 1 : 0;
+      W.push_active(st);
+      operator_apply(A, nc, TE_F64, x, W.ap.p, st);
+      vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.ap.p, b, nullptr, -1, 0, 0);
+      launch_dots(W, 1, W.ap.p, W.ap.p, nullptr, nullptr, nullptr, nullptr, S_TRUE, 0, st);
+      W.read_scalars(st);
+      nactive = 0;
+      for (int i = 0; i < B; i++) {
+        double* h = W.h + (size_t)i * S_NSLOTS;
+        const bool ok = statuses[i] == TE_OK && r0[i] != 0;
+        const double tr = ok ? std::sqrt(h[S_TRUE]) / r0[i] : 0.0;
+        if (ok && final_residuals) final_residuals[i] = tr;
+        W.h_active[i] = (ok && tr > tol && its[i] < max_iterations) ? 1 : 0;
+        const double rr = h[S_TRUE];
+        for (int k = 0; k < S_NSLOTS; k++) h[k] = 0.0;
+        h[S_RHO] = rr;  // rhat = r
+        h[S_R0] = r0[i];
+        rho[i] = rr;
+        nactive += W.h_active[i];
+      }
+      if (nactive == 0) break;
+      kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
+      kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
+      count_launch(2);
+      TE_LAUNCH_CHECK();
+      TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+      TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+      TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
+      W.push_active(st);
+      run();
     }
   }
   for (int i = 0; i < B; i++) iterations[i] = its[i];

@@ -523,6 +523,16 @@ __global__ void cast_kernel(T* dst, const double* src, long long n) {
     dst[i] = (T)src[i];
 }
 
+// nearest float-float split: hi = fl32(v), lo = fl32(v - hi)
+__global__ void split_df_kernel(float* hi, float* lo, const double* src, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double v = src[i];
+    float h = (float)v;
+    hi[i] = h;
+    lo[i] = (float)(v - (double)h);
+  }
+}
+
 }  // namespace te
 
 using namespace te;
@@ -548,6 +558,10 @@ static int make_operator(const te_domain* d, const te_ghost_filler* g, int kind,
       ghost_fill(g, 1, TE_F64, op->coeffs.p, d->stream);  // VarPoisson ctor (:70)
       op->coeffs_f.alloc(n);
       cast_kernel<float><<<304, 256, 0, d->stream>>>(op->coeffs_f.p, op->coeffs.p, n);
+      count_launch();
+      TE_LAUNCH_CHECK();
+      op->coeffs_df.alloc(2 * n);
+      split_df_kernel<<<304, 256, 0, d->stream>>>(op->coeffs_df.p, op->coeffs_df.p + n, op->coeffs.p, n);
       count_launch();
       TE_LAUNCH_CHECK();
       TE_CUDA(cudaStreamSynchronize(d->stream));

@@ -13,6 +13,7 @@ struct te_operator {
   int neumann = 0;
   te::DevBuf<double> coeffs;    // VarPoisson: ghost-filled coefficient level buffer (1 component)
   te::DevBuf<float> coeffs_f;   // FP32 copy for the mixed-precision cycle
+  te::DevBuf<float> coeffs_df;  // float-float split [2 * size]: hi, then lo (mixed-precision outer Krylov)
   te::FaceTable faces;
   // work vectors of te_bicgstab_solve(_batched) with this operator, per
   // component count and batch layout (patch offsets of the solves)
