@@ -158,3 +158,35 @@ def test_tc_solve_reaches_tolerance(te, oracle, name):
     inner = _inner(levels[0])
     # solution error <= cond(A) * relative residual; cond ~ 1e3 here (random right-hand side)
     assert rel_err(uv.numpy()[inner], u_o[inner]) <= 1e-6
+
+
+_CYCLE_SCRIPT = r"""
+import sys, numpy as np
+sys.path.insert(0, {root!r})
+import thunderegg_gb300 as te
+from thunderegg_gb300 import mesh as M
+from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+levels = {mesh}
+s = GmgSolver(levels, GmgOptions(scheme={scheme}, smoother=0, cycle_dtype=te.TE_F32))
+f = np.random.default_rng(31).standard_normal(levels[0].padded_shape(1))
+fv, uv = te.Vector.from_numpy(s.finest, f), te.Vector(s.finest)
+s.cycle.apply(fv, uv)
+np.save({out!r}, uv.numpy())
+"""
+
+
+@pytest.mark.parametrize("mesh,scheme", [("M.circle_mesh(n=32, lo=2, hi=4)", 1), ("M.uniform_mesh(3, 2, 16)", 2)])
+def test_fine_restrict_matches_coarse_centric(tmp_path, mesh, scheme):
+    """The fine-patch-centric residual+restriction gives the same cycle as the coarse-patch-centric kernel."""
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = []
+    for off in ("0", "1"):
+        out = str(tmp_path / f"u{off}.npy")
+        env = dict(os.environ, TE_NO_FINE_RESTRICT=off)
+        code = _CYCLE_SCRIPT.format(root=root, mesh=mesh, scheme=scheme, out=out)
+        subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=300)
+        outs.append(np.load(out))
+    assert rel_err(outs[0], outs[1]) <= 1e-6

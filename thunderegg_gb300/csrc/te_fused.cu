@@ -19,6 +19,9 @@
 // The finest level reads f in FP64 and writes u in FP64 even when the cycle
 // computes in FP32, so no conversion passes are needed.
 
+#include <cstdlib>
+#include <type_traits>
+
 #include "te_dft.cuh"
 #include "te_ghost_dev.cuh"
 #include "te_gmg.cuh"
@@ -97,7 +100,7 @@ __global__ void __launch_bounds__(1024)
     vc_restrict_kernel(Layout F, Layout C, const int* __restrict__ by_orth, const int* __restrict__ copy_of,
                        const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
                        const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                       const GCall* __restrict__ calls, const int* __restrict__ slab_start, int gstride,
+                       const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gstride,
                        const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* G = reinterpret_cast<T*>(smraw);  // [2^D][2D][gstride]
@@ -122,10 +125,7 @@ __global__ void __launch_bounds__(1024)
   }
   __syncthreads();
   PlainAcc<T> acc{u, (long long)F.cs, 0};
-  __shared__ GSlab sl_buf[48];
-  __shared__ int sl_q[48];
-  __shared__ int n_sl;
-  side_ghosts_to_smem<T, SCHEME>(acc, s_fp, NCH, slabs, calls, slab_start, ft, D, G, gstride, sl_buf, sl_q, &n_sl);
+  side_ghosts_table<T, SCHEME>(acc, s_fp, NCH, slabs, calls, side_slab, ft, D, G, gstride);
   __syncthreads();
   const T wD = T(1.0 / (1 << D));
   const int py = C.n1 + 2 * C.g;
@@ -207,7 +207,7 @@ template <class T, class TF, class TO, int KIND, int SCHEME>
 __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int ti_max, const int* __restrict__ parent, const int* __restrict__ porth,
                                const int8_t* __restrict__ ntype, int FS, const T* __restrict__ inv_tab,
                                const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                               const GCall* __restrict__ calls, const int* __restrict__ slab_start, int gstride,
+                               const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gstride,
                                const int* __restrict__ plan_of_patch, const int* __restrict__ plan_mats,
                                const T* __restrict__ mats, const int* __restrict__ mat_off,
                                const T* __restrict__ inv_eig, const int* __restrict__ zero_mode, T scale,
@@ -223,11 +223,8 @@ __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int t
   const T* MT[6];
   dft_mat_ptrs<T>(F, plan, plan_mats, mats, mat_off, MT);
   InterpAcc<T> acc{A, uc, parent, porth, F, C};
-  __shared__ GSlab sl_buf[6];
-  __shared__ int sl_q[6];
-  __shared__ int n_sl;
   int pself[1] = {p};
-  side_ghosts_to_smem<T, SCHEME>(acc, pself, 1, slabs, calls, slab_start, ft, D, G, gstride, sl_buf, sl_q, &n_sl);
+  side_ghosts_table<T, SCHEME>(acc, pself, 1, slabs, calls, side_slab, ft, D, G, gstride);
   __syncthreads();
   // f_copy with modifyRHSForInternalBoundaryConditions, sides in Side order
   const int side0 = D == 2 ? 4 : 20;
@@ -411,7 +408,7 @@ static void vc_restrict_t(const te_restrictor* r, const te_operator* op, const T
   int threads = C.P >= 2 * 152 ? 256 : 1024;
   kern<<<C.P, threads, smem, s>>>(F, C, r->by_orth.p, r->copy_of.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(),
                                op->neumann, coeff_of<T>(op), g->faces, g->d_slabs.p, g->d_calls.p,
-                               g->d_slab_start.p, gs, u, f, coarse);
+                               g->d_side_slab.p, gs, u, f, coarse);
   count_launch();
   TE_LAUNCH_CHECK();
 }
@@ -419,6 +416,13 @@ static void vc_restrict_t(const te_restrictor* r, const te_operator* op, const T
 template <class T, class TF>
 void vc_restrict(const te_restrictor* r, const te_operator* op, const T* u, const TF* f, T* coarse,
                  cudaStream_t s) {
+  if constexpr (std::is_same<T, float>::value) {
+    static const bool off = [] {
+      const char* e = getenv("TE_NO_FINE_RESTRICT");
+      return e && e[0] == '1';
+    }();
+    if (!off && vc_restrict_fine<T, TF>(r, op, u, f, coarse, s)) return;
+  }
   int sc = op->gf->scheme;
 #define TE_VR(K, S) vc_restrict_t<T, TF, K, S>(r, op, u, f, coarse, s)
   if (op->kind == 0) {
@@ -448,7 +452,7 @@ static void vc_post_t(const te_patch_solver* ps, const te_interpolator* in, cons
   dft_launch_shape(F, ti_max, threads);
   kern<<<F.P, threads, smem, s>>>(F, C, ti_max, in->parent.p, in->orth.p, d->d_nbr_type.p, d->F,
                                           d->template inv<T>(), coeff_of<T>(op), g->faces, g->d_slabs.p,
-                                          g->d_calls.p, g->d_slab_start.p, gs, ps->plan_of_patch.p,
+                                          g->d_calls.p, g->d_side_slab.p, gs, ps->plan_of_patch.p,
                                           ps->plan_mats.p, mats_of<T>(ps), ps->mat_off.p, ie_of<T>(ps),
                                           ps->zero_mode.p, (T)dft_scale(F), A, uc, f, out);
   count_launch();

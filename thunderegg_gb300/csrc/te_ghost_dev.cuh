@@ -177,55 +177,28 @@ __device__ __forceinline__ T gather_ghost(const Acc& acc, int p, const GSlab& sl
   return v;
 }
 
-// Face (side) ghosts of up to NP patches into shared memory: for patch slot
-// q, G[q * 2D * gstride + side * gstride + j*nt0 + i], for every side slab with
-// a neighbour (the only ghosts a star stencil or the internal-boundary RHS
-// terms read).  Sides without a neighbour are left alone.  All slabs of all
-// patches are processed in one flattened loop; `sl_buf` is shared scratch
-// for up to NP * 6 slab records.  Contains __syncthreads: call from all threads.
+// Face (side) ghosts of up to NP patches into shared memory,
+// G[(q * 2D + side) * gstride + j*nt0 + i] for patch slot q, for every side
+// with a neighbour; side_slab[p * 2D + side] names that side's slab (-1: none,
+// the entry is left alone).  Every thread takes whole ghost values; there is
+// no barrier inside: the caller synchronises before reading G.
 template <class T, int SCHEME, class Acc>
-__device__ void side_ghosts_to_smem(const Acc& acc, const int* pq, int NP, const GSlab* __restrict__ slabs,
-                                    const GCall* __restrict__ calls, const int* __restrict__ slab_start,
-                                    const FaceTable& ft, int D, T* G, int gstride, GSlab* sl_buf, int* sl_q,
-                                    int* n_sl) {
-  if (threadIdx.x == 0) {
-    int n = 0;
-    for (int q = 0; q < NP; q++) {
-      int p = pq[q];
-      if (p < 0) continue;
-      for (int s = slab_start[p]; s < slab_start[p + 1]; s++) {
-        GSlab sl = slabs[s];
-        if (sl.M != D - 1 || !sl.zero) continue;
-        sl_buf[n] = sl;
-        sl_q[n] = q;
-        n++;
-      }
-    }
-    *n_sl = n;
-  }
-  __syncthreads();
-  const int ns = *n_sl;
+__device__ __forceinline__ void side_ghosts_table(const Acc& acc, const int* pq, int NP,
+                                                  const GSlab* __restrict__ slabs, const GCall* __restrict__ calls,
+                                                  const int* __restrict__ side_slab, const FaceTable& ft, int D,
+                                                  T* G, int gstride) {
   const int side0 = D == 2 ? 4 : 20;
-  // every side slab of one dimension has the same size (n^(D-1) for cubes; take each slab's own)
-  int total = 0;
-  for (int k = 0; k < ns; k++) {
-    const FaceGeom& g = ft.f[side0 + sl_buf[k].face];
-    total += g.nt[0] * g.nt[1];
-  }
-  for (int e = threadIdx.x; e < total; e += blockDim.x) {
-    int k = 0, r = e;
-    for (;;) {
-      const FaceGeom& g = ft.f[side0 + sl_buf[k].face];
-      int c = g.nt[0] * g.nt[1];
-      if (r < c) break;
-      r -= c;
-      k++;
-    }
-    const GSlab sl = sl_buf[k];
-    const FaceGeom& g = ft.f[side0 + sl.face];
-    int i = r % g.nt[0], j = r / g.nt[0];
-    G[sl_q[k] * 2 * D * gstride + sl.face * gstride + r] =
-        gather_ghost<T, SCHEME>(acc, sl.patch, sl, g, ft, calls, D, i, j, T(0));
+  const int per = 2 * D * gstride;
+  for (int e = threadIdx.x; e < NP * per; e += blockDim.x) {
+    const int q = e / per, rem = e - q * per, s = rem / gstride, r = rem - s * gstride;
+    const int p = pq[q];
+    if (p < 0) continue;
+    const FaceGeom& g = ft.f[side0 + s];
+    if (r >= g.nt[0] * g.nt[1]) continue;
+    const int si = side_slab[p * 2 * D + s];
+    if (si < 0) continue;
+    const GSlab sl = slabs[si];
+    G[e] = gather_ghost<T, SCHEME>(acc, p, sl, g, ft, calls, D, r % g.nt[0], r / g.nt[0], T(0));
   }
 }
 

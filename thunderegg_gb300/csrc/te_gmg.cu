@@ -471,7 +471,19 @@ int te_linear_restrictor_create(const te_domain* fine, const te_domain* coarse, 
       }
     }
     r->even = even;
+    bool complete = even;
+    for (int c = 0; c < Pc && complete; c++)
+      if (copy_of[c] < 0)
+        for (int o = 0; o < NCH; o++) complete = complete && by_orth[(size_t)c * NCH + o] >= 0;
+    r->complete = complete;
+    std::vector<int> fpar(fine->lay.P), forth(fine->lay.P);
+    for (int p = 0; p < fine->lay.P; p++) {
+      fpar[p] = pm[p];
+      forth[p] = fine->orth_on_parent[p];
+    }
     cudaStream_t s = fine->stream;
+    r->fine_parent.upload(fpar, s);
+    r->fine_orth.upload(forth, s);
     r->by_orth.upload(by_orth, s);
     r->copy_of.upload(copy_of, s);
     r->child_start.upload(start, s);

@@ -19,6 +19,11 @@ struct te_restrictor {
   bool even = false;
   te::DevBuf<int> by_orth;   // [Pc * 2^D]
   te::DevBuf<int> copy_of;   // [Pc]
+  // every coarse patch is a copy or has all 2^D children: each fine patch
+  // writes its quadrant of the parent (fine-patch-centric kernels)
+  bool complete = false;
+  te::DevBuf<int> fine_parent;  // [Pf] coarse local index
+  te::DevBuf<int> fine_orth;    // [Pf] orth_on_parent, -1 for a copied patch
 };
 
 struct te_interpolator {
@@ -48,6 +53,10 @@ void vc_post(const te_patch_solver* ps, const te_interpolator* in, const T* A, c
 void vc_corr(const te_patch_solver* ps, const te_interpolator* in, const float* A, const float* uc, float* corr,
              cudaStream_t s);
 int corr_stride(const Layout& L);
+// fine-patch-centric residual + restriction (te_restrict.cu); false when the hierarchy does not qualify
+template <class T, class TF>
+bool vc_restrict_fine(const te_restrictor* r, const te_operator* op, const T* u, const TF* f, T* coarse,
+                      cudaStream_t s);
 }  // namespace te
 
 // ---------------------------------------------------------------------------

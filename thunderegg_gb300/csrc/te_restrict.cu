@@ -1,0 +1,209 @@
+// te_restrict.cu -- the fused residual + restriction of the FP32 V-cycle,
+// fine-patch-centric (Cycle::restrict, GMG/Cycle.h:57-65: r = f - A u, then
+// LinearRestrictor::restrictToCoarserParent, GMG/LinearRestrictor.h:115-127).
+//
+// One CTA per fine patch and one thread per 2x2(x2) block of fine cells,
+// i.e. per cell of the patch's quadrant in its parent.  The padded patch is
+// staged into shared memory with 16-byte loads; its side ghost ring is
+// replaced by the ghost filler's values gathered from the neighbours
+// (te_ghost_dev.cuh) or, on the physical boundary, by -u (Dirichlet) / +u
+// (Neumann).  Each thread then evaluates the star-stencil residual of its
+// fine cells from shared memory, in the reference's operation order, sums
+// them in z, y, x order with weight 2^-D and writes one coarse cell.  A
+// copied patch (its own parent) writes its residual cell by cell.  The
+// orthant-0 child (or the copy) zeroes the parent's ghost cells.
+//
+// Used when every coarse patch is a copy or has all 2^D children, the
+// patches are cubic with n = 16, 32 or 64 (2D) or 8 or 16 (3D) and one ghost
+// layer; other hierarchies use the coarse-patch-centric kernel in te_fused.cu.
+
+#include "te_ghost_dev.cuh"
+#include "te_gmg.cuh"
+
+namespace te {
+
+template <int DIM, int NN>
+struct RShape {
+  static constexpr int SY = NN + 2;
+  static constexpr int SZ = DIM == 3 ? SY * SY : 0;
+  static constexpr int CS = DIM == 3 ? SY * SY * SY : SY * SY;
+  static constexpr int H = NN / 2;
+  static constexpr int NT = DIM == 3 ? H * H * H : H * H;  // threads: coarse cells of one quadrant
+  static constexpr int NF = DIM == 3 ? NN * NN : NN;       // cells of one side face
+};
+
+template <class T, class TF, int KIND, int SCHEME, int DIM, int NN>
+__global__ void __launch_bounds__(RShape<DIM, NN>::NT)
+    vc_restrict_fine_kernel(const int* __restrict__ fparent, const int* __restrict__ forth,
+                            const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
+                            const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
+                            const GCall* __restrict__ calls, const int* __restrict__ side_slab,
+                            const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse) {
+  using S = RShape<DIM, NN>;
+  __shared__ __align__(16) T tile[S::CS];
+  __shared__ T s_inv[3];
+  __shared__ int s_has;
+  const int p = blockIdx.x, t = threadIdx.x;
+  const int side0 = DIM == 2 ? 4 : 20;
+  const T* up = u + (long long)p * S::CS;
+  // 1. the padded patch (its ghosts are replaced below)
+  if ((S::CS * sizeof(T)) % 16 == 0) {
+    constexpr int V = 16 / sizeof(T);
+    const float4* src = reinterpret_cast<const float4*>(up);
+    float4* dst = reinterpret_cast<float4*>(tile);
+    for (int e = t; e < S::CS / V; e += S::NT) dst[e] = __ldg(src + e);
+  } else {
+    for (int e = t; e < S::CS; e += S::NT) tile[e] = up[e];
+  }
+  if (t < 3) s_inv[t] = finv[(size_t)p * 6 + (KIND ? 3 : 0) + t];
+  if (t == 0) {
+    int m = 0;
+    for (int sd = 0; sd < 2 * DIM; sd++) m |= (fntype[(size_t)p * FS + side0 + sd] >= 0) << sd;
+    s_has = m;
+  }
+  __syncthreads();
+  // 2. the side ghost ring
+  const PlainAcc<T> acc{u, (long long)S::CS, 0};
+  for (int e = t; e < 2 * DIM * S::NF; e += S::NT) {
+    const int s = e / S::NF, r = e % S::NF;
+    const int a = s >> 1, upr = s & 1;
+    const int i = r % NN, j = r / NN;
+    const int edge = upr ? NN - 1 : 0;
+    int x, y, z;
+    if (a == 0) {
+      x = edge; y = i; z = j;
+    } else if (a == 1) {
+      x = i; y = edge; z = j;
+    } else {
+      x = i; y = j; z = edge;
+    }
+    const int in = (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0);
+    const int st = a == 0 ? 1 : (a == 1 ? S::SY : S::SZ);
+    T v;
+    if ((s_has >> s) & 1) {
+      const GSlab sl = slabs[side_slab[p * 2 * DIM + s]];
+      v = gather_ghost<T, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, i, j, T(0));
+    } else {
+      v = neumann ? tile[in] : -tile[in];
+    }
+    tile[in + (upr ? st : -st)] = v;
+  }
+  __syncthreads();
+  // 3. residuals of this thread's fine cells, restricted
+  const TF* ff = f + (long long)p * S::CS;
+  const T* cf = KIND ? coeff + (long long)p * S::CS : nullptr;
+  const T i0 = s_inv[0], i1 = s_inv[1], i2 = s_inv[2];
+  auto resid = [&](int x, int y, int z) -> T {
+    const int k = (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0);
+    const T mid = tile[k];
+    T au = T(0);
+#pragma unroll
+    for (int a = 0; a < DIM; a++) {
+      const int st = a == 0 ? 1 : (a == 1 ? S::SY : S::SZ);
+      const T inv = a == 0 ? i0 : (a == 1 ? i1 : i2);
+      const T lov = tile[k - st], hiv = tile[k + st];
+      if (KIND == 0) {
+        au += ((hiv - T(2) * mid) + lov) * inv;
+      } else {
+        const T cl = cf[k - st], cm = cf[k], cu = cf[k + st];
+        au += ((cu + cm) * (hiv - mid) - (cl + cm) * (mid - lov)) * inv;
+      }
+    }
+    return au * T(-1) + (T)ff[k];
+  };
+  const int o = forth[p];
+  T* cp = coarse + (long long)fparent[p] * S::CS;
+  const int bx = t % S::H, by = (t / S::H) % S::H, bz = DIM == 3 ? t / (S::H * S::H) : 0;
+  if (o >= 0) {
+    const T wD = T(1.0 / (1 << DIM));
+    T v = T(0);
+#pragma unroll
+    for (int dz = 0; dz < (DIM == 3 ? 2 : 1); dz++)
+#pragma unroll
+      for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+        for (int dx = 0; dx < 2; dx++) v += resid(2 * bx + dx, 2 * by + dy, 2 * bz + dz) * wD;
+    const int cx = bx + ((o & 1) ? S::H : 0), cy = by + ((o & 2) ? S::H : 0), cz = bz + ((o & 4) ? S::H : 0);
+    cp[(cx + 1) + (cy + 1) * S::SY + (DIM == 3 ? (cz + 1) * S::SZ : 0)] = v;
+  } else {
+#pragma unroll
+    for (int dz = 0; dz < (DIM == 3 ? 2 : 1); dz++)
+#pragma unroll
+      for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+        for (int dx = 0; dx < 2; dx++) {
+          const int x = 2 * bx + dx, y = 2 * by + dy, z = 2 * bz + dz;
+          cp[(x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0)] = resid(x, y, z);
+        }
+  }
+  if (o <= 0) {
+    for (int e = t; e < S::CS; e += S::NT) {
+      const int x = e % S::SY - 1, r2 = e / S::SY;
+      const int y = r2 % S::SY - 1, z = DIM == 3 ? r2 / S::SY - 1 : 0;
+      const bool inner = x >= 0 && x < NN && y >= 0 && y < NN && z >= 0 && z < NN;
+      if (!inner) cp[e] = T(0);
+    }
+  }
+}
+
+template <class T, class TF, int KIND, int SCHEME, int DIM, int NN>
+static void launch_fine(const te_restrictor* r, const te_operator* op, const T* u, const TF* f, T* coarse,
+                        cudaStream_t s) {
+  using S = RShape<DIM, NN>;
+  const te_domain* fd = r->fine;
+  const te_ghost_filler* g = op->gf;
+  const T* coeff = KIND ? (const T*)op->coeff_ptr(sizeof(T) == 8 ? TE_F64 : TE_F32) : nullptr;
+  vc_restrict_fine_kernel<T, TF, KIND, SCHEME, DIM, NN><<<fd->lay.P, S::NT, 0, s>>>(
+      r->fine_parent.p, r->fine_orth.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(), op->neumann, coeff, g->faces,
+      g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, u, f, coarse);
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
+template <class T, class TF, int KIND, int SCHEME>
+static bool try_fine_k(const te_restrictor* r, const te_operator* op, const T* u, const TF* f, T* coarse,
+                       cudaStream_t s) {
+  const Layout& L = r->fine->lay;
+  if (L.D == 2) {
+    if constexpr (SCHEME == TE_GHOST_TRILINEAR) {
+      return false;
+    } else {
+      if (L.n0 == 16) launch_fine<T, TF, KIND, SCHEME, 2, 16>(r, op, u, f, coarse, s);
+      else if (L.n0 == 32) launch_fine<T, TF, KIND, SCHEME, 2, 32>(r, op, u, f, coarse, s);
+      else if (L.n0 == 64) launch_fine<T, TF, KIND, SCHEME, 2, 64>(r, op, u, f, coarse, s);
+      else return false;
+      return true;
+    }
+  }
+  if constexpr (SCHEME != TE_GHOST_TRILINEAR) {
+    return false;
+  } else {
+    if (L.n0 == 8) launch_fine<T, TF, KIND, SCHEME, 3, 8>(r, op, u, f, coarse, s);
+    else if (L.n0 == 16) launch_fine<T, TF, KIND, SCHEME, 3, 16>(r, op, u, f, coarse, s);
+    else return false;
+    return true;
+  }
+}
+
+template <class T, class TF>
+bool vc_restrict_fine(const te_restrictor* r, const te_operator* op, const T* u, const TF* f, T* coarse,
+                      cudaStream_t s) {
+  const Layout& L = r->fine->lay;
+  if (!r->complete || L.g != 1 || L.n1 != L.n0 || (L.D == 3 && L.n2 != L.n0)) return false;
+  const int sc = op->gf->scheme;
+  if (op->kind == 0) {
+    if (sc == TE_GHOST_BILINEAR) return try_fine_k<T, TF, 0, TE_GHOST_BILINEAR>(r, op, u, f, coarse, s);
+    if (sc == TE_GHOST_BIQUADRATIC) return try_fine_k<T, TF, 0, TE_GHOST_BIQUADRATIC>(r, op, u, f, coarse, s);
+    return try_fine_k<T, TF, 0, TE_GHOST_TRILINEAR>(r, op, u, f, coarse, s);
+  }
+  if (sc == TE_GHOST_BILINEAR) return try_fine_k<T, TF, 1, TE_GHOST_BILINEAR>(r, op, u, f, coarse, s);
+  if (sc == TE_GHOST_BIQUADRATIC) return try_fine_k<T, TF, 1, TE_GHOST_BIQUADRATIC>(r, op, u, f, coarse, s);
+  return try_fine_k<T, TF, 1, TE_GHOST_TRILINEAR>(r, op, u, f, coarse, s);
+}
+
+template bool vc_restrict_fine<float, float>(const te_restrictor*, const te_operator*, const float*, const float*,
+                                             float*, cudaStream_t);
+template bool vc_restrict_fine<float, double>(const te_restrictor*, const te_operator*, const float*,
+                                              const double*, float*, cudaStream_t);
+
+}  // namespace te
