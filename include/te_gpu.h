@@ -210,7 +210,9 @@ int te_cycle_apply(const te_cycle* c, int ncomp, const void* f, void* u);
  * counterpart of the reference's per-level Timer, Timer.h:60-202): fills up to
  * max_entries names (32 chars each, "L<k> <phase>") and milliseconds measured
  * with CUDA events between consecutive kernels.  Only the fused DFT-smoother
- * cycle records phases; *count = 0 otherwise. */
+ * cycle records phases; *count = 0 otherwise.  An FP32 cycle is timed as the
+ * mixed-precision BiCGStab runs it, with FP32 input and output (f is
+ * converted before the first event and the result into u after the last). */
 int te_cycle_timings(const te_cycle* c, int ncomp, const void* f, void* u, int max_entries, char* names,
                      double* ms, int* count);
 

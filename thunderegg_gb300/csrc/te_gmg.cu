@@ -576,10 +576,16 @@ int te_cycle_timings(const te_cycle* c, int nc, const void* f, void* u, int max_
     std::vector<te_cycle::Mark> marks;
     cudaStream_t s = m->stream;
     TE_CUDA(cudaStreamSynchronize(s));
+    // an FP32 fused cycle is timed the way the mixed-precision solve runs it: FP32 in and out
+    const bool f32 = m->dtype == TE_F32 && m->fused();
+    if (f32) convert_level(m->dom(0), nc, TE_F32, m->f[0].p, TE_F64, f, s);
     m->marks = &marks;
     try {
       m->mark("start", s);
-      m->body(f, u, s);
+      if (f32)
+        m->body_f32((const float*)m->f[0].p, (float*)m->r[0].p, s);
+      else
+        m->body(f, u, s);
       m->mark("end", s);
     } catch (...) {
       m->marks = nullptr;
@@ -587,6 +593,7 @@ int te_cycle_timings(const te_cycle* c, int nc, const void* f, void* u, int max_
       throw;
     }
     m->marks = nullptr;
+    if (f32) convert_level(m->dom(0), nc, TE_F64, u, TE_F32, m->r[0].p, s);
     TE_CUDA(cudaStreamSynchronize(s));
     int n = 0;
     for (size_t i = 1; i + 1 < marks.size() && n < max_entries; i++, n++) {
