@@ -46,6 +46,7 @@ struct DftTcArgs {
   const float* inv_eig;      // [nplans][n^D]
   const int* zero_mode;      // [P]
   const float* corr;         // optional [P][2D][n^(D-1)]: right-hand-side corrections per side face
+  float scale;               // prod 2/n, applied to the last pass's result
   int* err;
 };
 
@@ -238,7 +239,7 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
       if (q == 2 * DIM - 1) {
         // line (i, y[, z]) with x = j: into the staging rows, then whole padded patches out
 #pragma unroll
-        for (int j = 0; j < NN; j++) stage[t * OP + j] = v[j];
+        for (int j = 0; j < NN; j++) stage[t * OP + j] = v[j] * a.scale;
         __syncthreads();
         for (int e = t; e < S::G * CS; e += S::ROWS) {
           int i = e / CS, k = e % CS;
@@ -339,13 +340,15 @@ void dft_tc_prepare(te_patch_solver* ps, const std::vector<std::vector<double>>&
   for (int pl = 1; pl < nplans; pl++)
     for (int a = 0; a < D; a++)
       if (plan_mats[pl * 6 + a] != plan_mats[a] || plan_mats[pl * 6 + 3 + a] != plan_mats[3 + a]) return;
-  // passes: forward x, y(, z), inverse (z,) y, x; the last pass carries the scale prod 2/n
+  // passes: forward x, y(, z), inverse (z,) y, x; each distinct matrix is stored once (a cube with one
+  // boundary type per axis needs two), which keeps four CTAs' shared memory on an SM
   double scale = 1.0;
   for (int ax = 0; ax < D; ax++) scale *= 2.0 / n;
-  std::vector<std::pair<int, bool>> ids;
+  ps->tc_scale = (float)scale;
+  std::vector<int> ids;
   for (int q = 0; q < 2 * D; q++) {
     int ax = q < D ? q : 2 * D - 1 - q;
-    std::pair<int, bool> key(plan_mats[(q < D ? 0 : 3) + ax], q == 2 * D - 1);
+    int key = plan_mats[(q < D ? 0 : 3) + ax];
     int slot = -1;
     for (size_t u = 0; u < ids.size(); u++)
       if (ids[u] == key) slot = (int)u;
@@ -358,13 +361,12 @@ void dft_tc_prepare(te_patch_solver* ps, const std::vector<std::vector<double>>&
   ps->tc_nmat = (int)ids.size();
   std::vector<float> b((size_t)ps->tc_nmat * 2 * n * n);
   for (int u = 0; u < ps->tc_nmat; u++) {
-    const std::vector<double>& mt = mats_t[ids[u].first];  // transposed: mt[j*n + i] = M[i][j]
-    const double sc = ids[u].second ? scale : 1.0;
+    const std::vector<double>& mt = mats_t[ids[u]];  // transposed: mt[j*n + i] = M[i][j]
     float* hi = &b[(size_t)u * 2 * n * n];
     float* lo = hi + n * n;
     for (int i = 0; i < n; i++)
       for (int j = 0; j < n; j++) {
-        double m = mt[(size_t)j * n + i] * sc;
+        double m = mt[(size_t)j * n + i];
         float h = tf32_round_host((float)m);
         hi[i * n + j] = h;
         lo[i * n + j] = tf32_round_host((float)(m - (double)h));
@@ -390,6 +392,7 @@ static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStrea
   a.inv_eig = ps->inv_eig_f.p;
   a.zero_mode = ps->zero_mode.p;
   a.corr = corr;
+  a.scale = ps->tc_scale;
   a.err = ps->tc_err.p;
   auto kern = dft_tc_kernel<TI, TO, DIM, NN>;
   size_t smem = tc_smem_bytes<DIM, NN>(a.nmat);

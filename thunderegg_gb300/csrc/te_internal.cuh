@@ -132,6 +132,7 @@ struct te_domain {
   // per patch and axis: 1/h^2 (Poisson) and 1/(2 h^2) (VarPoisson), [P*6], in both precisions
   te::DevBuf<double> d_inv;
   te::DevBuf<float> d_inv_f;
+  te::DevBuf<float> d_inv_df;  // [P*6][2]: float-float split (hi, lo) of d_inv
   template <class T>
   const T* inv() const;
   // reduction scratch: per-block partials + completion counter + result

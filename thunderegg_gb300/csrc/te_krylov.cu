@@ -88,26 +88,15 @@ __device__ __forceinline__ int k_interior_offset(const Layout& L, int e) {
 // Per-block sums -> part; the last block of solve b sums its chunks in a
 // fixed order into S[b][slot0 ...] and finalises scalars.
 // finalize_kind: 1 alpha, 2 omega, 3 beta + rho commit, 4 initial r0, 5 early-exit test
+// blk: this block's sums, valid on thread 0
 template <int NV>
-__device__ void k_reduce(double (&v)[NV], const Batch& bt, int b, int ch, double* part, unsigned int* counter,
-                         double* S, int slot0, int finalize_kind, double tol) {
-  __shared__ double red[NV][KT / 32];
+__device__ void k_reduce_blk(const double (&blk)[NV], const Batch& bt, int b, int ch, double* part,
+                             unsigned int* counter, double* S, int slot0, int finalize_kind, double tol) {
   __shared__ double fin[NV][KT];
   __shared__ bool last;
-#pragma unroll
-  for (int i = 0; i < NV; i++) {
-    double x = v[i];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-    if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = x;
-  }
-  __syncthreads();
   const int CH = bt.nch[b];
   if (threadIdx.x == 0) {
-    for (int i = 0; i < NV; i++) {
-      double s = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[i][w];
-      part[((size_t)i * bt.B + b) * MAX_CHUNKS + ch] = s;
-    }
+    for (int i = 0; i < NV; i++) part[((size_t)i * bt.B + b) * MAX_CHUNKS + ch] = blk[i];
     __threadfence();
     unsigned int done = atomicAdd(&counter[b], 1u);
     last = done == (unsigned)(CH - 1);
@@ -147,6 +136,27 @@ __device__ void k_reduce(double (&v)[NV], const Batch& bt, int b, int ch, double
     }
     counter[b] = 0u;
   }
+}
+
+template <int NV>
+__device__ void k_reduce(double (&v)[NV], const Batch& bt, int b, int ch, double* part, unsigned int* counter,
+                         double* S, int slot0, int finalize_kind, double tol) {
+  __shared__ double red[NV][KT / 32];
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    double x = v[i];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = x;
+  }
+  __syncthreads();
+  double blk[NV];
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NV; i++) {
+      double s = 0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += red[i][w];
+      blk[i] = s;
+    }
+  k_reduce_blk<NV>(blk, bt, b, ch, part, counter, S, slot0, finalize_kind, tol);
 }
 
 #define TE_BLOCK_SOLVE(bt)                  \
@@ -246,6 +256,34 @@ __device__ __forceinline__ void stv(const DV& v, long long k, df64 x) {
   v.lo[k] = x.lo;
 }
 
+// block sums of float-float accumulators (the FP64 pipe stays idle until the last block)
+template <int NV>
+__device__ void kd_reduce(df64 (&v)[NV], const Batch& bt, int b, int ch, double* part, unsigned int* counter,
+                          double* S, int slot0, int finalize_kind, double tol) {
+  __shared__ df64 red[NV][KT / 32];
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    df64 x = v[i];
+    for (int o = 16; o > 0; o >>= 1) x += df_shfl_down(x, o);
+    if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = x;
+  }
+  __syncthreads();
+  double blk[NV];
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NV; i++) {
+      df64 t = red[i][0];
+      for (int w = 1; w < (int)(blockDim.x >> 5); w++) t += red[i][w];
+      blk[i] = df_to_double(t);
+    }
+  k_reduce_blk<NV>(blk, bt, b, ch, part, counter, S, slot0, finalize_kind, tol);
+}
+
+// the solve's scalars as float-float numbers, split once per block
+__device__ __forceinline__ void kd_scalars(const double* Sb, df64* sc, int n, int s0, int s1) {
+  if (threadIdx.x < n) sc[threadIdx.x] = df64(Sb[threadIdx.x == 0 ? s0 : s1]);
+  __syncthreads();
+}
+
 template <int NV>
 __global__ void __launch_bounds__(KT) kd_dots(Layout L, int nc, Batch bt, CV a0, CV b0, CV a1, CV b1, CV a2, CV b2,
                                               double* part, unsigned int* counter, double* S, int slot0, int fin) {
@@ -257,23 +295,22 @@ __global__ void __launch_bounds__(KT) kd_dots(Layout L, int nc, Batch bt, CV a0,
     if (NV > 1) v[1] += ldv(a1, k) * ldv(b1, k);
     if (NV > 2) v[2] += ldv(a2, k) * ldv(b2, k);
   });
-  double d[NV];
-  for (int i = 0; i < NV; i++) d[i] = df_to_double(v[i]);
-  k_reduce<NV>(d, bt, b, ch, part, counter, S, slot0, fin, 0);
+  kd_reduce<NV>(v, bt, b, ch, part, counter, S, slot0, fin, 0);
 }
 
 __global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double tol, CV r, CV ap, DV s, double* part,
                                            unsigned int* counter, double* S) {
   TE_BLOCK_SOLVE(bt);
-  const df64 nalpha(-S[(size_t)b * S_NSLOTS + S_ALPHA]);
-  df64 v = df64(0.f, 0.f);
+  __shared__ df64 sc[1];
+  kd_scalars(S + (size_t)b * S_NSLOTS, sc, 1, S_ALPHA, S_ALPHA);
+  const df64 nalpha = -sc[0];
+  df64 v[1] = {df64(0.f, 0.f)};
   TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
     df64 sv = ldv(r, k) + ldv(ap, k) * nalpha;
     stv(s, k, sv);
-    v += sv * sv;
+    v[0] += sv * sv;
   });
-  double d[1] = {df_to_double(v)};
-  k_reduce<1>(d, bt, b, ch, part, counter, S, S_SS, 5, tol);
+  kd_reduce<1>(v, bt, b, ch, part, counter, S, S_SS, 5, tol);
 }
 
 __global__ void __launch_bounds__(KT) kd_xr(Layout L, int nc, Batch bt, DV x, DV r, const float* mp, const float* ms,
@@ -281,10 +318,12 @@ __global__ void __launch_bounds__(KT) kd_xr(Layout L, int nc, Batch bt, DV x, DV
                                             double* S) {
   TE_BLOCK_SOLVE(bt);
   const double* Sb = S + (size_t)b * S_NSLOTS;
-  const df64 alpha(Sb[S_ALPHA]), omega(Sb[S_OMEGA]);
+  __shared__ df64 sc[2];
+  kd_scalars(Sb, sc, 2, S_ALPHA, S_OMEGA);
+  const df64 alpha = sc[0], omega = sc[1];
   const df64 nalpha = -alpha, nomega = -omega;
   const bool done = Sb[S_DONE] != 0.0;
-  df64 v0 = df64(0.f, 0.f), v1 = df64(0.f, 0.f);
+  df64 v[2] = {df64(0.f, 0.f), df64(0.f, 0.f)};
   const CV xc = as_cv(x), rc = as_cv(r);
   TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
     if (done) {
@@ -293,19 +332,20 @@ __global__ void __launch_bounds__(KT) kd_xr(Layout L, int nc, Batch bt, DV x, DV
       stv(x, k, ldv(xc, k) + (alpha * mp[k] + omega * ms[k]));
       df64 rv = ldv(rc, k) + (ldv(ap, k) * nalpha + ldv(as, k) * nomega);
       stv(r, k, rv);
-      v0 += rv * rv;
-      v1 += rv * ldv(rhat, k);
+      v[0] += rv * rv;
+      v[1] += rv * ldv(rhat, k);
     }
   });
-  double d[2] = {df_to_double(v0), df_to_double(v1)};
-  k_reduce<2>(d, bt, b, ch, part, counter, S, S_RR, 3, 0);
+  kd_reduce<2>(v, bt, b, ch, part, counter, S, S_RR, 3, 0);
 }
 
 __global__ void __launch_bounds__(KT) kd_p(Layout L, int nc, Batch bt, DV p, CV ap, CV r, const double* S) {
   TE_BLOCK_SOLVE(bt);
   const double* Sb = S + (size_t)b * S_NSLOTS;
   if (Sb[S_DONE] != 0.0) return;
-  const df64 nomega(-Sb[S_OMEGA]), beta(Sb[S_BETA]);
+  __shared__ df64 sc[2];
+  kd_scalars(Sb, sc, 2, S_OMEGA, S_BETA);
+  const df64 nomega = -sc[0], beta = sc[1];
   const CV pc = as_cv(p);
   TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
     df64 pv = ldv(pc, k) + ldv(ap, k) * nomega;
@@ -329,74 +369,104 @@ struct F32Acc {
   __device__ __forceinline__ df64 operator()(int q, int idx) const { return df64(u[q * ps + idx], 0.f); }
 };
 
+// exact (hi - 2 mid) + lo of three FP32 values, rounded once to float-float
+__device__ __forceinline__ df64 df_second_difference(float hi, float mid, float lo) {
+  const df64 a = two_sum(hi, -2.f * mid);
+  const df64 b = two_sum(a.hi, lo);
+  return fast_two_sum(b.hi, __fadd_rn(a.lo, b.lo));
+}
+
 // f = A u for an FP32 level buffer u (ghosts not filled), in float-float:
 // the side ghosts of every face with a neighbour are gathered with the ghost
 // filler's formulas (te_ghost_dev.cuh) into shared memory, physical-boundary
 // ghosts are -u (Dirichlet) or +u (Neumann) (enforceBoundaryConditions), and
 // the star stencil runs in the reference's operation order.  u is not
-// modified.  One CTA per patch; f's ghost cells are set to 0.
-template <int KIND, int SCHEME, int DIM>
+// modified.  One CTA per patch; f's ghost cells are set to 0.  Cells away from
+// the patch boundary need no ghost and are computed while the gather runs;
+// the boundary cells follow the barrier.  NN > 0: cubic patches of NN cells
+// and one ghost layer, with the index arithmetic known at compile time.
+template <int KIND, int SCHEME, int DIM, int NN>
 __global__ void __launch_bounds__(256)
-    apply_df_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const double* __restrict__ inv64,
+    apply_df_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const float2* __restrict__ inv_df,
                     int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
                     const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gs,
                     const float* __restrict__ u, DV f) {
   extern __shared__ df64 G[];  // [2D][gs]
-  __shared__ df64 inv[3];
   __shared__ int has[6];
   const int p = blockIdx.x;
   const int side0 = DIM == 2 ? 4 : 20;
-  const F32Acc acc{u, (long long)L.cs};
+  df64 inv[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float2 v = __ldg(inv_df + (size_t)p * 6 + (KIND ? 3 : 0) + a);
+    inv[a] = df64(v.x, v.y);
+  }
+  const int n0 = NN ? NN : L.n0, n1 = NN ? NN : L.n1, n2 = DIM == 3 ? (NN ? NN : L.n2) : 1;
+  const int sy = NN ? NN + 2 : L.sy, py = NN ? NN + 2 : L.n1 + 2 * L.g;
+  const int sz = DIM == 3 ? sy * py : 0, g = NN ? 1 : L.g;
+  const int cs = NN ? (DIM == 3 ? sy * sy * sy : sy * sy) : L.cs;
+  const F32Acc acc{u, (long long)cs};
   for (int e = threadIdx.x; e < 2 * DIM * gs; e += blockDim.x) {
     const int s = e / gs, r = e % gs;
-    const FaceGeom& g = ft.f[side0 + s];
-    if (r >= g.nt[0] * g.nt[1]) continue;
+    const FaceGeom& gf = ft.f[side0 + s];
+    if (r >= gf.nt[0] * gf.nt[1]) continue;
     const int si = side_slab[p * 2 * DIM + s];
     if (si < 0) continue;
     const GSlab sl = slabs[si];
-    G[e] = gather_ghost<df64, SCHEME>(acc, p, sl, g, ft, calls, DIM, r % g.nt[0], r / g.nt[0], df64(0.f, 0.f));
+    G[e] = gather_ghost<df64, SCHEME>(acc, p, sl, gf, ft, calls, DIM, r % gf.nt[0], r / gf.nt[0], df64(0.f, 0.f));
   }
-  if (threadIdx.x < 3) inv[threadIdx.x] = df64(inv64[(size_t)p * 6 + (KIND ? 3 : 0) + threadIdx.x]);
   if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
-  __syncthreads();
-  const float* up = u + (long long)p * L.cs;
-  const long long base = (long long)p * L.cs;
-  const int py = L.n1 + 2 * L.g;
-  for (int e = threadIdx.x; e < L.cs; e += blockDim.x) {
-    const int c0 = e % L.sy - L.g, q = e / L.sy;
-    const int c1 = q % py - L.g, c2 = q / py - (DIM == 3 ? L.g : 0);
-    const bool interior = c0 >= 0 && c0 < L.n0 && c1 >= 0 && c1 < L.n1 && c2 >= 0 && c2 < L.n2;
-    df64 res(0.f, 0.f);
-    if (interior) {
-      const int cc[3] = {c0, c1, c2};
-      const df64 mid(up[e], 0.f);
+  const float* up = u + (long long)p * cs;
+  const long long base = (long long)p * cs;
+  const int nn[3] = {n0, n1, n2};
+  const int str[3] = {1, sy, sz};
+  // pass 0: cells away from the boundary (and the ghost cells of f); pass 1: boundary cells
+  for (int pass = 0; pass < 2; pass++) {
+    if (pass == 1) __syncthreads();
+    for (int e = threadIdx.x; e < cs; e += blockDim.x) {
+      const int c0 = e % sy - g, q = e / sy;
+      const int c1 = q % py - g, c2 = DIM == 3 ? q / py - g : 0;
+      const bool interior = c0 >= 0 && c0 < n0 && c1 >= 0 && c1 < n1 && c2 >= 0 && c2 < n2;
+      const bool edge = interior && (c0 == 0 || c0 == n0 - 1 || c1 == 0 || c1 == n1 - 1 ||
+                                     (DIM == 3 && (c2 == 0 || c2 == n2 - 1)));
+      if (edge != (pass == 1)) continue;
+      df64 res(0.f, 0.f);
+      if (interior && KIND == 0 && !edge) {
+        const float mid = up[e];
+        res = df_second_difference(up[e + 1], mid, up[e - 1]) * inv[0];
+        res += df_second_difference(up[e + sy], mid, up[e - sy]) * inv[1];
+        if (DIM == 3) res += df_second_difference(up[e + sz], mid, up[e - sz]) * inv[2];
+      } else if (interior) {
+        const int cc[3] = {c0, c1, c2};
+        const df64 mid(up[e], 0.f);
 #pragma unroll
-      for (int a = 0; a < DIM; a++) {
-        const int st = L.stride(a);
-        const int tan = a == 0 ? c1 + c2 * L.n1 : (a == 1 ? c0 + c2 * L.n0 : c0 + c1 * L.n0);
-        df64 lo, hi;
-        if (cc[a] == 0)
-          lo = has[2 * a] ? G[(2 * a) * gs + tan] : (neumann ? mid : -mid);
-        else
-          lo = df64(up[e - st], 0.f);
-        if (cc[a] == L.n(a) - 1)
-          hi = has[2 * a + 1] ? G[(2 * a + 1) * gs + tan] : (neumann ? mid : -mid);
-        else
-          hi = df64(up[e + st], 0.f);
-        if (KIND == 0) {
-          res += ((hi - df64(2.0) * mid) + lo) * inv[a];
-        } else {
-          const df64 cl = ldv(coeff, base + e - st), cm = ldv(coeff, base + e), cu = ldv(coeff, base + e + st);
-          res += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
+        for (int a = 0; a < DIM; a++) {
+          const int st = str[a];
+          const int tan = a == 0 ? c1 + c2 * n1 : (a == 1 ? c0 + c2 * n0 : c0 + c1 * n0);
+          df64 lo, hi;
+          if (cc[a] == 0)
+            lo = has[2 * a] ? G[(2 * a) * gs + tan] : (neumann ? mid : -mid);
+          else
+            lo = df64(up[e - st], 0.f);
+          if (cc[a] == nn[a] - 1)
+            hi = has[2 * a + 1] ? G[(2 * a + 1) * gs + tan] : (neumann ? mid : -mid);
+          else
+            hi = df64(up[e + st], 0.f);
+          if (KIND == 0) {
+            res += ((hi - df64(2.0) * mid) + lo) * inv[a];
+          } else {
+            const df64 cl = ldv(coeff, base + e - st), cm = ldv(coeff, base + e), cu = ldv(coeff, base + e + st);
+            res += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
+          }
         }
       }
+      stv(f, base + e, res);
     }
-    stv(f, base + e, res);
   }
 }
 
-template <int KIND, int SCHEME>
-static void apply_df_t(const te_operator* A, const float* u, DV f, cudaStream_t st) {
+template <int KIND, int SCHEME, int DIM, int NN>
+static void apply_df_launch(const te_operator* A, const float* u, DV f, cudaStream_t st) {
   const te_domain* d = A->dom;
   const Layout& L = d->lay;
   const te_ghost_filler* g = A->gf;
@@ -404,13 +474,29 @@ static void apply_df_t(const te_operator* A, const float* u, DV f, cudaStream_t 
   const size_t smem = (size_t)2 * L.D * gs * sizeof(df64);
   const long long n = (long long)L.P * L.cs;
   CV coeff{KIND ? A->coeffs_df.p : nullptr, KIND ? A->coeffs_df.p + n : nullptr};
-  auto kern = L.D == 2 ? apply_df_kernel<KIND, SCHEME, 2> : apply_df_kernel<KIND, SCHEME, 3>;
+  auto kern = apply_df_kernel<KIND, SCHEME, DIM, NN>;
   if (smem > 40 * 1024)
     TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, d->d_inv.p, A->neumann, coeff, g->faces, g->d_slabs.p,
-                               g->d_calls.p, g->d_side_slab.p, gs, u, f);
+  kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff,
+                               g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, gs, u, f);
   count_launch();
   TE_LAUNCH_CHECK();
+}
+
+template <int KIND, int SCHEME>
+static void apply_df_t(const te_operator* A, const float* u, DV f, cudaStream_t st) {
+  const Layout& L = A->dom->lay;
+  const bool cube = L.g == 1 && L.n1 == L.n0 && (L.D == 2 || L.n2 == L.n0);
+  if (L.D == 2) {
+    if (cube && L.n0 == 16) apply_df_launch<KIND, SCHEME, 2, 16>(A, u, f, st);
+    else if (cube && L.n0 == 32) apply_df_launch<KIND, SCHEME, 2, 32>(A, u, f, st);
+    else if (cube && L.n0 == 64) apply_df_launch<KIND, SCHEME, 2, 64>(A, u, f, st);
+    else apply_df_launch<KIND, SCHEME, 2, 0>(A, u, f, st);
+  } else {
+    if (cube && L.n0 == 8) apply_df_launch<KIND, SCHEME, 3, 8>(A, u, f, st);
+    else if (cube && L.n0 == 16) apply_df_launch<KIND, SCHEME, 3, 16>(A, u, f, st);
+    else apply_df_launch<KIND, SCHEME, 3, 0>(A, u, f, st);
+  }
 }
 
 static void apply_df(const te_operator* A, const float* u, DV f, cudaStream_t st) {

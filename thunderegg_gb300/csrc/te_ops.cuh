@@ -48,6 +48,7 @@ struct te_patch_solver {
   bool tc_ok = false;
   int tc_pass_mat[6] = {0, 0, 0, 0, 0, 0};
   int tc_nmat = 0;
+  float tc_scale = 1.f;  // prod 2/n
   te::DevBuf<float> tc_bmat;  // [tc_nmat][2][n*n] TF32 hi/lo parts, row-major
   te::DevBuf<int> tc_err;     // set when an MMA wait timed out
 };

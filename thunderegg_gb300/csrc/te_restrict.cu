@@ -4,7 +4,8 @@
 //
 // One CTA per fine patch and one thread per 2x2(x2) block of fine cells,
 // i.e. per cell of the patch's quadrant in its parent.  The padded patch is
-// staged into shared memory with 16-byte loads; its side ghost ring is
+// staged into shared memory with 16-byte loads while the right-hand-side
+// values and the neighbour-side ghosts are fetched; its side ghost ring is
 // replaced by the ghost filler's values gathered from the neighbours
 // (te_ghost_dev.cuh) or, on the physical boundary, by -u (Dirichlet) / +u
 // (Neumann).  Each thread then evaluates the star-stencil residual of its
@@ -40,12 +41,30 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
                             const GCall* __restrict__ calls, const int* __restrict__ side_slab,
                             const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse) {
   using S = RShape<DIM, NN>;
+  constexpr int NB = DIM == 3 ? 8 : 4;  // fine cells per thread
   __shared__ __align__(16) T tile[S::CS];
-  __shared__ T s_inv[3];
-  __shared__ int s_has;
+  __shared__ T gbuf[2 * DIM * S::NF];
   const int p = blockIdx.x, t = threadIdx.x;
   const int side0 = DIM == 2 ? 4 : 20;
   const T* up = u + (long long)p * S::CS;
+  const int bx = t % S::H, by = (t / S::H) % S::H, bz = DIM == 3 ? t / (S::H * S::H) : 0;
+  // this thread's right-hand-side values, in flight while the patch is staged
+  const TF* ff = f + (long long)p * S::CS;
+  TF fv[NB];
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    const int x = 2 * bx + (q & 1), y = 2 * by + ((q >> 1) & 1), z = 2 * bz + (q >> 2);
+    fv[q] = __ldg(ff + (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0));
+  }
+  const int8_t* nt = fntype + (size_t)p * FS + side0;
+  // neighbour-side ghosts (gathered from the neighbours' values, not this tile)
+  const PlainAcc<T> acc{u, (long long)S::CS, 0};
+  for (int e = t; e < 2 * DIM * S::NF; e += S::NT) {
+    const int s = e / S::NF, r = e % S::NF;
+    if (nt[s] < 0) continue;
+    const GSlab sl = slabs[side_slab[p * 2 * DIM + s]];
+    gbuf[e] = gather_ghost<T, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, r % NN, r / NN, T(0));
+  }
   // 1. the padded patch (its ghosts are replaced below)
   if ((S::CS * sizeof(T)) % 16 == 0) {
     constexpr int V = 16 / sizeof(T);
@@ -55,15 +74,10 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
   } else {
     for (int e = t; e < S::CS; e += S::NT) tile[e] = up[e];
   }
-  if (t < 3) s_inv[t] = finv[(size_t)p * 6 + (KIND ? 3 : 0) + t];
-  if (t == 0) {
-    int m = 0;
-    for (int sd = 0; sd < 2 * DIM; sd++) m |= (fntype[(size_t)p * FS + side0 + sd] >= 0) << sd;
-    s_has = m;
-  }
+  const T i0 = finv[(size_t)p * 6 + (KIND ? 3 : 0)], i1 = finv[(size_t)p * 6 + (KIND ? 3 : 0) + 1];
+  const T i2 = DIM == 3 ? finv[(size_t)p * 6 + (KIND ? 3 : 0) + 2] : T(0);
   __syncthreads();
-  // 2. the side ghost ring
-  const PlainAcc<T> acc{u, (long long)S::CS, 0};
+  // 2. the side ghost ring: gathered values, or the boundary condition
   for (int e = t; e < 2 * DIM * S::NF; e += S::NT) {
     const int s = e / S::NF, r = e % S::NF;
     const int a = s >> 1, upr = s & 1;
@@ -79,21 +93,12 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
     }
     const int in = (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0);
     const int st = a == 0 ? 1 : (a == 1 ? S::SY : S::SZ);
-    T v;
-    if ((s_has >> s) & 1) {
-      const GSlab sl = slabs[side_slab[p * 2 * DIM + s]];
-      v = gather_ghost<T, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, i, j, T(0));
-    } else {
-      v = neumann ? tile[in] : -tile[in];
-    }
-    tile[in + (upr ? st : -st)] = v;
+    tile[in + (upr ? st : -st)] = nt[s] >= 0 ? gbuf[e] : (neumann ? tile[in] : -tile[in]);
   }
   __syncthreads();
   // 3. residuals of this thread's fine cells, restricted
-  const TF* ff = f + (long long)p * S::CS;
   const T* cf = KIND ? coeff + (long long)p * S::CS : nullptr;
-  const T i0 = s_inv[0], i1 = s_inv[1], i2 = s_inv[2];
-  auto resid = [&](int x, int y, int z) -> T {
+  auto resid = [&](int x, int y, int z, TF fval) -> T {
     const int k = (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0);
     const T mid = tile[k];
     T au = T(0);
@@ -109,11 +114,10 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
         au += ((cu + cm) * (hiv - mid) - (cl + cm) * (mid - lov)) * inv;
       }
     }
-    return au * T(-1) + (T)ff[k];
+    return au * T(-1) + (T)fval;
   };
   const int o = forth[p];
   T* cp = coarse + (long long)fparent[p] * S::CS;
-  const int bx = t % S::H, by = (t / S::H) % S::H, bz = DIM == 3 ? t / (S::H * S::H) : 0;
   if (o >= 0) {
     const T wD = T(1.0 / (1 << DIM));
     T v = T(0);
@@ -122,7 +126,8 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
 #pragma unroll
       for (int dy = 0; dy < 2; dy++)
 #pragma unroll
-        for (int dx = 0; dx < 2; dx++) v += resid(2 * bx + dx, 2 * by + dy, 2 * bz + dz) * wD;
+        for (int dx = 0; dx < 2; dx++)
+          v += resid(2 * bx + dx, 2 * by + dy, 2 * bz + dz, fv[dz * 4 + dy * 2 + dx]) * wD;
     const int cx = bx + ((o & 1) ? S::H : 0), cy = by + ((o & 2) ? S::H : 0), cz = bz + ((o & 4) ? S::H : 0);
     cp[(cx + 1) + (cy + 1) * S::SY + (DIM == 3 ? (cz + 1) * S::SZ : 0)] = v;
   } else {
@@ -133,7 +138,8 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
 #pragma unroll
         for (int dx = 0; dx < 2; dx++) {
           const int x = 2 * bx + dx, y = 2 * by + dy, z = 2 * bz + dz;
-          cp[(x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0)] = resid(x, y, z);
+          cp[(x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0)] =
+              resid(x, y, z, fv[dz * 4 + dy * 2 + dx]);
         }
   }
   if (o <= 0) {

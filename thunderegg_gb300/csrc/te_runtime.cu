@@ -370,6 +370,13 @@ int te_domain_create(const te_level_desc* desc, te_domain** out) {
       }
     d->d_inv.upload(inv, st);
     d->d_inv_f.upload(std::vector<float>(inv.begin(), inv.end()), st);
+    std::vector<float> inv_df(2 * inv.size());
+    for (size_t i = 0; i < inv.size(); i++) {
+      float h = (float)inv[i];
+      inv_df[2 * i] = h;
+      inv_df[2 * i + 1] = (float)(inv[i] - (double)h);
+    }
+    d->d_inv_df.upload(inv_df, st);
     d->red_blocks = 152 * 2;
     d->d_partials.alloc(d->red_blocks);
     d->d_counter.alloc(1);
