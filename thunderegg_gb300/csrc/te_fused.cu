@@ -298,7 +298,7 @@ __global__ void __launch_bounds__(256)
     InterpAcc<float> acc{A, uc, parent, porth, F, C};
     const GSlab sl = slabs[si];
     const int i = r % g.nt[0], j = r / g.nt[0];
-    const float gv = gather_side_ghost<float, SCHEME, DIM>(acc, p, sl, g, ft, calls, i, j);
+    const float gv = gather_ghost<float, SCHEME>(acc, p, sl, g, ft, calls, DIM, i, j, 0.f);
     const int coord = upr ? F.n(a) - 1 : 0;
     int x, y, z;
     if (a == 0) {

@@ -47,8 +47,7 @@ __device__ __forceinline__ T lin_own_coarse_1d(T v, const Acc& p, int pq, const 
 }
 
 template <class T, int SCHEME, class Acc>
-__device__ __forceinline__ T own_term(T v, const Acc& p, int pq, const FaceGeom& g, int M, int D, int type, int orth,
-                                      int i, int j) {
+__device__ T own_term(T v, const Acc& p, int pq, const FaceGeom& g, int M, int D, int type, int orth, int i, int j) {
   if (type == TE_NBR_NORMAL || type < 0) return v;
   const T third = K<T>::third;
   if (M == 0) {  // corners
@@ -97,8 +96,7 @@ __device__ __forceinline__ T own_term(T v, const Acc& p, int pq, const FaceGeom&
 
 // contribution of one incoming call (caller patch q, caller face geometry gq)
 template <class T, int SCHEME, class Acc>
-__device__ __forceinline__ T call_term(T v, const Acc& q, int qq, const FaceGeom& gq, int M, int D, int type,
-                                       int orth, int i, int j) {
+__device__ T call_term(T v, const Acc& q, int qq, const FaceGeom& gq, int M, int D, int type, int orth, int i, int j) {
   if (type == TE_NBR_NORMAL) return sv<T>(q, qq, gq, 0, i, j);  // plain copy, an assignment
   const T third = K<T>::third;
   if (M == 0) {
@@ -175,22 +173,6 @@ __device__ __forceinline__ T gather_ghost(const Acc& acc, int p, const GSlab& sl
     const FaceGeom& gq =
         ft.f[sl.M == D - 1 ? (D == 2 ? 4 : 20) + cl.src_face : (sl.M == 0 ? cl.src_face : 8 + cl.src_face)];
     v = call_term<T, SCHEME>(v, acc, cl.src, gq, sl.M, D, cl.type, cl.orth, i, j);
-  }
-  return v;
-}
-
-// gather_ghost for a side slab (M = D - 1) of a D-dimensional level, with
-// the face dimension and D known at compile time: the fused kernels only
-// gather side ghosts, and the corner and edge formulas drop out of the code.
-template <class T, int SCHEME, int D, class Acc>
-__device__ __forceinline__ T gather_side_ghost(const Acc& acc, int p, const GSlab& sl, const FaceGeom& g,
-                                               const FaceTable& ft, const GCall* __restrict__ calls, int i, int j) {
-  constexpr int M = D - 1;
-  constexpr int side0 = D == 2 ? 4 : 20;
-  T v = own_term<T, SCHEME>(T(0), acc, p, g, M, D, sl.own_type, sl.own_orth, i, j);
-  for (int k = 0; k < sl.ncalls; k++) {
-    const GCall cl = calls[sl.call0 + k];
-    v = call_term<T, SCHEME>(v, acc, cl.src, ft.f[side0 + cl.src_face], M, D, cl.type, cl.orth, i, j);
   }
   return v;
 }

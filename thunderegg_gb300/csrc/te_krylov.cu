@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(256)
     const int si = side_slab[p * 2 * DIM + s];
     if (si < 0) continue;
     const GSlab sl = slabs[si];
-    G[e] = gather_side_ghost<df64, SCHEME, DIM>(acc, p, sl, gf, ft, calls, r % gf.nt[0], r / gf.nt[0]);
+    G[e] = gather_ghost<df64, SCHEME>(acc, p, sl, gf, ft, calls, DIM, r % gf.nt[0], r / gf.nt[0], df64(0.f, 0.f));
   }
   if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
   const float* up = u + (long long)p * cs;

@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
     const int s = e / S::NF, r = e % S::NF;
     if (nt[s] < 0) continue;
     const GSlab sl = slabs[side_slab[p * 2 * DIM + s]];
-    gbuf[e] = gather_side_ghost<T, SCHEME, DIM>(acc, p, sl, ft.f[side0 + s], ft, calls, r % NN, r / NN);
+    gbuf[e] = gather_ghost<T, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, r % NN, r / NN, T(0));
   }
   // 1. the padded patch (its ghosts are replaced below)
   if ((S::CS * sizeof(T)) % 16 == 0) {
