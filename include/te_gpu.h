@@ -250,6 +250,26 @@ int te_bicgstab_solve_batched(const te_operator* A, int ncomp, void* x, const vo
                               const int* patch_offsets, int* iterations, double* final_residuals,
                               int* statuses);
 
+/* A batched BiCGStab run that the caller advances a few iterations at a time
+ * (the serving loop's unit of work; no counterpart in the reference, whose
+ * Iterative::BiCGStab::solve runs to the end).  create computes the initial
+ * residuals of all solves (same arguments as te_bicgstab_solve_batched; x, b,
+ * A and M must outlive the handle); step runs up to max_iterations iterations
+ * of the solves still iterating and sets *num_running (0: every solve has
+ * finished, x holds the results); state reports per solve the iterations,
+ * the last residual (the FP64 true residual once finished in the float-float
+ * loop), the status and whether it is still iterating; sync_x writes the
+ * current iterate of every solve into x and synchronises. */
+typedef struct te_bicgstab_batch te_bicgstab_batch;
+int te_bicgstab_batch_create(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M, double tol,
+                             int max_iterations, int flags, int num_solves, const int* patch_offsets,
+                             te_bicgstab_batch** out);
+int te_bicgstab_batch_step(te_bicgstab_batch* batch, int max_iterations, int* num_running);
+int te_bicgstab_batch_state(const te_bicgstab_batch* batch, int* iterations, double* residuals, int* statuses,
+                            int* running);
+int te_bicgstab_batch_sync_x(te_bicgstab_batch* batch);
+int te_bicgstab_batch_destroy(te_bicgstab_batch* batch);
+
 /* ---- dot product without allocation ---------------------------------------
  * No counterpart in the reference (ThunderEgg reduces on the host).
  * For callers that cannot call cudaMalloc when they need a reduction: code

@@ -95,6 +95,11 @@ _SIGS = {
     "te_patch_solver_smooth": (_I, [_V, _I, _I, _V, _V]),
     "te_patch_solver_apply": (_I, [_V, _I, _I, _V, _V]),
     "te_patch_solver_uses_tensor_cores": (_I, [_V, _ip]),
+    "te_bicgstab_batch_create": (_I, [_V, _I, _V, _V, _V, ctypes.c_double, _I, _I, _I, _ip, ctypes.POINTER(_V)]),
+    "te_bicgstab_batch_step": (_I, [_V, _I, _ip]),
+    "te_bicgstab_batch_state": (_I, [_V, _ip, _dp, _ip, _ip]),
+    "te_bicgstab_batch_sync_x": (_I, [_V]),
+    "te_bicgstab_batch_destroy": (_I, [_V]),
     "te_linear_restrictor_create": (_I, [_V, _V, _I, ctypes.POINTER(_V)]),
     "te_restrictor_destroy": (_I, [_V]),
     "te_restrict": (_I, [_V, _I, _I, _V, _V]),

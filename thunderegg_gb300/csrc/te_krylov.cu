@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include <tuple>
 
 #include "te_df64.cuh"
@@ -664,77 +665,110 @@ static bool use_df(const te_operator* A, int nc, const te_cycle* M, int flags) {
   return !(e && e[0] == '1');
 }
 
-static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv, const te_cycle* Mc, double tol,
-                         int max_iterations, int flags, const std::vector<int>& offsets, int* iterations,
-                         double* final_residuals, int* statuses) {
-  const te_domain* d = A->dom;
-  cudaStream_t st = d->stream;
-  const int B = (int)offsets.size() - 1;
-  // the solver's work vectors live with the operator (freed with it), per component count and batch layout
-  auto& slot = A->krylov[std::make_pair(nc, offsets)];
-  if (!slot) slot = std::make_shared<KrylovWork>(d, nc, offsets);
-  KrylovWork& W = *std::static_pointer_cast<KrylovWork>(slot);
-  te_cycle* M = const_cast<te_cycle*>(Mc);
-  if (M) M->ensure(nc);
-  double* x = (double*)xv;
-  const double* b = (const double*)bv;
-  size_t bytes = W.n * sizeof(double);
-  const bool df = use_df(A, nc, M, flags);
-  const long long nvals = (long long)W.n;
-  TE_CUDA(cudaMemsetAsync(W.S.p, 0, (size_t)B * S_NSLOTS * sizeof(double), st));
-  for (int i = 0; i < B; i++) W.h_active[i] = 1;
-  W.push_active(st);
-  if (df) {
-    // resid = b - A x in FP64, then split into float-float; rhat = p = resid (BiCGStab.h:113-131)
-    if (!W.xdf.p) W.xdf.alloc(W.n);
-    operator_apply(A, nc, TE_F64, x, W.ap.p, st);
-    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.ap.p, b, nullptr, -1, 0, 0);
-    launch_dots(W, 3, b, b, W.ap.p, W.ap.p, W.ap.p, W.ap.p, S_BB, 0, st);
-    kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
-    kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
-    count_launch(2);
-    TE_LAUNCH_CHECK();
-    TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-    TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-  } else {
-    // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
-    operator_apply(A, nc, TE_F64, x, W.resid.p, st);
-    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.resid.p, b, nullptr, -1, 0, 0);
-    TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-    TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-    launch_dots(W, 3, b, b, W.rhat.p, W.resid.p, W.resid.p, W.resid.p, S_BB, 0, st);
+// One batched BiCGStab run as a resumable object: start() forms the initial
+// residuals, step(k) advances up to k iterations (replaying the iteration's
+// CUDA graph and testing convergence on the host after each), and the
+// float-float loop's residual-replacement check runs when every solve has
+// stopped.  solve_batched runs it to the end in one call; the serving loop
+// (te_bicgstab_batch_*) steps it a few iterations at a time.
+struct BatchRun {
+  const te_operator* A;
+  int nc;
+  const te_domain* d;
+  cudaStream_t st;
+  int B;
+  KrylovWork* Wp;
+  te_cycle* M;
+  double* x;
+  const double* b;
+  size_t bytes;
+  bool df;
+  long long nvals;
+  double tol;
+  int max_iterations, flags;
+  std::vector<double> rho, r0, residual, finals;
+  std::vector<int> its, statuses;
+  int nactive = 0, restart = 0;
+  bool done = false, use_graph = true;
+  std::tuple<void*, const void*, unsigned long long, unsigned long long, double, int> gkey;
+
+  BatchRun(const te_operator* A_, int nc_, void* xv, const void* bv, const te_cycle* Mc, double tol_, int max_it,
+           int flags_, const std::vector<int>& offsets)
+      : A(A_), nc(nc_), d(A_->dom), st(A_->dom->stream), B((int)offsets.size() - 1), x((double*)xv),
+        b((const double*)bv), tol(tol_), max_iterations(max_it), flags(flags_) {
+    // the solver's work vectors live with the operator (freed with it), per component count and batch layout
+    auto& slot = A->krylov[std::make_pair(nc, offsets)];
+    if (!slot) slot = std::make_shared<KrylovWork>(d, nc, offsets);
+    Wp = std::static_pointer_cast<KrylovWork>(slot).get();
+    M = const_cast<te_cycle*>(Mc);
+    if (M) M->ensure(nc);
+    bytes = Wp->n * sizeof(double);
+    df = use_df(A, nc, M, flags);
+    nvals = (long long)Wp->n;
+    rho.assign(B, 0.0);
+    r0.assign(B, 0.0);
+    residual.assign(B, 0.0);
+    finals.assign(B, 0.0);
+    its.assign(B, 0);
+    statuses.assign(B, TE_OK);
+    const char* ng = getenv("TE_NO_GRAPH");
+    use_graph = !(ng && ng[0] == '1');
+    gkey = std::make_tuple((void*)x, (const void*)b, M ? M->serial : 0ull, M ? M->generation : 0ull, tol,
+                           flags | (df ? 1 << 30 : 0));
   }
-  W.read_scalars(st);
-  std::vector<double> rho(B), r0(B), residual(B);
-  std::vector<int> its(B, 0);
-  int nactive = 0;
-  for (int i = 0; i < B; i++) {
-    double* h = W.h + (size_t)i * S_NSLOTS;
-    double bb = h[S_BB], rh = h[S_BB + 1], rr = h[S_BB + 2];
-    r0[i] = std::sqrt(bb);
-    rho[i] = rh;
-    residual[i] = std::sqrt(rr) / r0[i];
-    statuses[i] = TE_OK;
-    for (int k = 0; k < S_NSLOTS; k++) h[k] = 0.0;
-    h[S_RHO] = rho[i];
-    h[S_R0] = r0[i];
-    if (final_residuals) final_residuals[i] = residual[i];
-    // zero right-hand side or already converged: no iterations (BiCGStab.h:140-144)
-    W.h_active[i] = (r0[i] != 0 && residual[i] > tol && max_iterations > 0) ? 1 : 0;
-    if (W.h_active[i] && rho[i] == 0) {  // BiCGStab.h:149-151
-      statuses[i] = TE_ERR_BREAKDOWN;
-      W.h_active[i] = 0;
+
+  void start() {
+    KrylovWork& W = *Wp;
+    TE_CUDA(cudaMemsetAsync(W.S.p, 0, (size_t)B * S_NSLOTS * sizeof(double), st));
+    for (int i = 0; i < B; i++) W.h_active[i] = 1;
+    W.push_active(st);
+    if (df) {
+      // resid = b - A x in FP64, then split into float-float; rhat = p = resid (BiCGStab.h:113-131)
+      if (!W.xdf.p) W.xdf.alloc(W.n);
+      operator_apply(A, nc, TE_F64, x, W.ap.p, st);
+      vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.ap.p, b, nullptr, -1, 0, 0);
+      launch_dots(W, 3, b, b, W.ap.p, W.ap.p, W.ap.p, W.ap.p, S_BB, 0, st);
+      kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
+      kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
+      count_launch(2);
+      TE_LAUNCH_CHECK();
+      TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+      TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+    } else {
+      // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
+      operator_apply(A, nc, TE_F64, x, W.resid.p, st);
+      vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.resid.p, b, nullptr, -1, 0, 0);
+      TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+      TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+      launch_dots(W, 3, b, b, W.rhat.p, W.resid.p, W.resid.p, W.resid.p, S_BB, 0, st);
     }
-    nactive += W.h_active[i];
+    W.read_scalars(st);
+    nactive = 0;
+    for (int i = 0; i < B; i++) {
+      double* h = W.h + (size_t)i * S_NSLOTS;
+      double bb = h[S_BB], rh = h[S_BB + 1], rr = h[S_BB + 2];
+      r0[i] = std::sqrt(bb);
+      rho[i] = rh;
+      residual[i] = r0[i] != 0 ? std::sqrt(rr) / r0[i] : 0.0;
+      statuses[i] = TE_OK;
+      for (int k = 0; k < S_NSLOTS; k++) h[k] = 0.0;
+      h[S_RHO] = rho[i];
+      h[S_R0] = r0[i];
+      finals[i] = residual[i];
+      // zero right-hand side or already converged: no iterations (BiCGStab.h:140-144)
+      W.h_active[i] = (r0[i] != 0 && residual[i] > tol && max_iterations > 0) ? 1 : 0;
+      if (W.h_active[i] && rho[i] == 0) {  // BiCGStab.h:149-151
+        statuses[i] = TE_ERR_BREAKDOWN;
+        W.h_active[i] = 0;
+      }
+      nactive += W.h_active[i];
+    }
+    TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
+    W.push_active(st);
   }
-  TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
-  W.push_active(st);
-  const char* ng = getenv("TE_NO_GRAPH");
-  bool use_graph = !(ng && ng[0] == '1');
-  auto gkey = std::make_tuple((void*)x, (const void*)b, M ? M->serial : 0ull, M ? M->generation : 0ull, tol,
-                              flags | (df ? 1 << 30 : 0));
-  auto run = [&]() {
-  while (nactive > 0) {
+
+  void iterate_once() {
+    KrylovWork& W = *Wp;
     if (use_graph) {
       auto it = W.graphs.find(gkey);
       if (it == W.graphs.end()) {
@@ -775,7 +809,7 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
       if (!W.h_active[i]) continue;
       const double* h = W.h + (size_t)i * S_NSLOTS;
       if (h[S_DONE] != 0.0) {  // ||s|| / ||b|| <= tol: x updated, stop (BiCGStab.h:162-168)
-        if (final_residuals) final_residuals[i] = std::sqrt(h[S_SS]) / r0[i];
+        finals[i] = std::sqrt(h[S_SS]) / r0[i];
         W.h_active[i] = 0;
         changed = true;
         continue;
@@ -783,7 +817,7 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
       its[i]++;
       rho[i] = h[S_RHO];
       residual[i] = std::sqrt(h[S_RR]) / r0[i];
-      if (final_residuals) final_residuals[i] = residual[i];
+      finals[i] = residual[i];
       if (residual[i] <= tol || its[i] >= max_iterations) {
         W.h_active[i] = 0;
         changed = true;
@@ -799,61 +833,105 @@ static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv,
       W.push_active(st);
     }
   }
-  };
-  run();
-  if (df) {
-    // Residual replacement: the float-float recurrence keeps ~1e-14 of the
-    // initial residual, so check every solve's true residual b - A x in FP64
-    // and restart the ones above tol from it (at most a few times).
-    for (int restart = 0;; restart++) {
-      kd_join<<<1216, 256, 0, st>>>(W.cv(W.xdf), x, nvals);
-      count_launch();
-      TE_LAUNCH_CHECK();
-      if (restart == 8) break;
-      for (int i = 0; i < B; i++) W.h_active[i] = statuses[i] == TE_OK ? 1 : 0;
-      W.push_active(st);
-      operator_apply(A, nc, TE_F64, x, W.ap.p, st);
-      vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.ap.p, b, nullptr, -1, 0, 0);
-      launch_dots(W, 1, W.ap.p, W.ap.p, nullptr, nullptr, nullptr, nullptr, S_TRUE, 0, st);
-      W.read_scalars(st);
-      nactive = 0;
-      for (int i = 0; i < B; i++) {
-        double* h = W.h + (size_t)i * S_NSLOTS;
-        const bool ok = statuses[i] == TE_OK && r0[i] != 0;
-        const double tr = ok ? std::sqrt(h[S_TRUE]) / r0[i] : 0.0;
-        if (ok && final_residuals) final_residuals[i] = tr;
-        W.h_active[i] = (ok && tr > tol && its[i] < max_iterations) ? 1 : 0;
-        const double rr = h[S_TRUE];
-        for (int k = 0; k < S_NSLOTS; k++) h[k] = 0.0;
-        h[S_RHO] = rr;  // rhat = r
-        h[S_R0] = r0[i];
-        rho[i] = rr;
-        nactive += W.h_active[i];
-      }
-      if (nactive == 0) break;
-      kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
-      kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
-      count_launch(2);
-      TE_LAUNCH_CHECK();
-      TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-      TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-      TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
-      W.push_active(st);
-      run();
-    }
+
+  // float-float x into the FP64 x
+  void join_x() {
+    if (!df) return;
+    kd_join<<<1216, 256, 0, st>>>(Wp->cv(Wp->xdf), x, nvals);
+    count_launch();
+    TE_LAUNCH_CHECK();
   }
-  for (int i = 0; i < B; i++) iterations[i] = its[i];
-  TE_CUDA(cudaStreamSynchronize(st));
-  if (M)
-    for (const te_cycle_level& lv : M->levels)
-      if (lv.smoother && dft_tc_error(lv.smoother, st)) {
-        TE_CUDA(cudaMemsetAsync(lv.smoother->tc_err.p, 0, sizeof(int), st));
-        throw Error(TE_ERR_TIMEOUT, "tensor-core DFT: an MMA completion wait timed out; results are invalid");
+
+  // Residual replacement: the float-float recurrence keeps ~1e-14 of the
+  // initial residual, so check every solve's true residual b - A x in FP64
+  // and restart the ones above tol from it.  True when some solve restarted.
+  bool replacement_check() {
+    KrylovWork& W = *Wp;
+    join_x();
+    for (int i = 0; i < B; i++) W.h_active[i] = statuses[i] == TE_OK ? 1 : 0;
+    W.push_active(st);
+    operator_apply(A, nc, TE_F64, x, W.ap.p, st);
+    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.ap.p, b, nullptr, -1, 0, 0);
+    launch_dots(W, 1, W.ap.p, W.ap.p, nullptr, nullptr, nullptr, nullptr, S_TRUE, 0, st);
+    W.read_scalars(st);
+    nactive = 0;
+    for (int i = 0; i < B; i++) {
+      double* h = W.h + (size_t)i * S_NSLOTS;
+      const bool ok = statuses[i] == TE_OK && r0[i] != 0;
+      const double tr = ok ? std::sqrt(h[S_TRUE]) / r0[i] : 0.0;
+      if (ok) finals[i] = tr;
+      W.h_active[i] = (ok && tr > tol && its[i] < max_iterations) ? 1 : 0;
+      const double rr = h[S_TRUE];
+      for (int k = 0; k < S_NSLOTS; k++) h[k] = 0.0;
+      h[S_RHO] = rr;  // rhat = r
+      h[S_R0] = r0[i];
+      rho[i] = rr;
+      nactive += W.h_active[i];
+    }
+    W.push_active(st);
+    if (nactive == 0) return false;
+    kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
+    kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
+    count_launch(2);
+    TE_LAUNCH_CHECK();
+    TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+    TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
+    TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
+    return true;
+  }
+
+  void finish() {
+    join_x();
+    TE_CUDA(cudaStreamSynchronize(st));
+    done = true;
+    if (M)
+      for (const te_cycle_level& lv : M->levels)
+        if (lv.smoother && dft_tc_error(lv.smoother, st)) {
+          TE_CUDA(cudaMemsetAsync(lv.smoother->tc_err.p, 0, sizeof(int), st));
+          throw Error(TE_ERR_TIMEOUT, "tensor-core DFT: an MMA completion wait timed out; results are invalid");
+        }
+  }
+
+  // up to k iterations; returns the number of solves still iterating (0: finished, x holds the results)
+  int step(long long k) {
+    long long n = 0;
+    while (!done) {
+      if (nactive > 0) {
+        if (n >= k) break;
+        iterate_once();
+        n++;
+        continue;
       }
-  int worst = TE_OK;
-  for (int i = 0; i < B; i++)
-    if (statuses[i] != TE_OK) worst = statuses[i];
-  return worst;
+      if (df && restart < 8 && replacement_check()) {
+        restart++;
+        continue;
+      }
+      finish();
+    }
+    return done ? 0 : nactive;
+  }
+
+  int worst() const {
+    int w = TE_OK;
+    for (int i = 0; i < B; i++)
+      if (statuses[i] != TE_OK) w = statuses[i];
+    return w;
+  }
+};
+
+static int solve_batched(const te_operator* A, int nc, void* xv, const void* bv, const te_cycle* Mc, double tol,
+                         int max_iterations, int flags, const std::vector<int>& offsets, int* iterations,
+                         double* final_residuals, int* statuses) {
+  BatchRun r(A, nc, xv, bv, Mc, tol, max_iterations, flags, offsets);
+  r.start();
+  r.step(1ll << 60);
+  const int B = (int)offsets.size() - 1;
+  for (int i = 0; i < B; i++) {
+    iterations[i] = r.its[i];
+    statuses[i] = r.statuses[i];
+    if (final_residuals) final_residuals[i] = r.finals[i];
+  }
+  return r.worst();
 }
 
 }  // namespace te
@@ -890,6 +968,57 @@ int te_bicgstab_solve_batched(const te_operator* A, int nc, void* xv, const void
     if (status == TE_ERR_BREAKDOWN) set_error("BiCGStab broke down in at least one solve of the batch");
   });
   return rc != TE_OK ? rc : status;
+}
+
+int te_bicgstab_batch_create(const te_operator* A, int nc, void* xv, const void* bv, const te_cycle* Mc, double tol,
+                             int max_iterations, int flags, int num_solves, const int* patch_offsets,
+                             te_bicgstab_batch** out) {
+  return guard([&] {
+    require(A && xv && bv && patch_offsets && out, "null argument");
+    require(num_solves >= 1, "num_solves must be >= 1");
+    std::vector<int> offs(patch_offsets, patch_offsets + num_solves + 1);
+    require(offs[0] == 0 && offs[num_solves] == A->dom->lay.P, "patch_offsets must span the finest level");
+    for (int i = 0; i < num_solves; i++) require(offs[i + 1] > offs[i], "every solve needs at least one patch");
+    auto r = std::make_unique<BatchRun>(A, nc, xv, bv, Mc, tol, max_iterations, flags, offs);
+    r->start();
+    *out = reinterpret_cast<te_bicgstab_batch*>(r.release());
+  });
+}
+
+int te_bicgstab_batch_step(te_bicgstab_batch* h, int max_iterations, int* num_running) {
+  return guard([&] {
+    require(h && num_running, "null argument");
+    require(max_iterations >= 0, "max_iterations must be >= 0");
+    *num_running = reinterpret_cast<BatchRun*>(h)->step(max_iterations);
+  });
+}
+
+int te_bicgstab_batch_state(const te_bicgstab_batch* h, int* iterations, double* residuals, int* statuses,
+                            int* running) {
+  return guard([&] {
+    require(h, "null argument");
+    const BatchRun* r = reinterpret_cast<const BatchRun*>(h);
+    for (int i = 0; i < r->B; i++) {
+      if (iterations) iterations[i] = r->its[i];
+      if (residuals) residuals[i] = r->finals[i];
+      if (statuses) statuses[i] = r->statuses[i];
+      if (running) running[i] = (!r->done && r->Wp->h_active[i]) ? 1 : 0;
+    }
+  });
+}
+
+int te_bicgstab_batch_sync_x(te_bicgstab_batch* h) {
+  return guard([&] {
+    require(h, "null argument");
+    BatchRun* r = reinterpret_cast<BatchRun*>(h);
+    r->join_x();
+    TE_CUDA(cudaStreamSynchronize(r->st));
+  });
+}
+
+int te_bicgstab_batch_destroy(te_bicgstab_batch* h) {
+  delete reinterpret_cast<BatchRun*>(h);
+  return TE_OK;
 }
 
 }  // extern "C"
