@@ -93,7 +93,7 @@ class _Batch:
     def __init__(self, members, x_parts, opts):
         import torch
 
-        self.members = members
+        self.members = list(members)  # this batch's members, in patch order
         levels, offsets = M.union_hierarchy([m.req.levels for m in members])
         coeffs = None
         if members[0].req.coeffs is not None:
