@@ -1,0 +1,453 @@
+// thunderegg_gb300/adapters.hpp -- ThunderEgg's extension interfaces implemented
+// over the te_gpu C ABI, so that GPU objects drop into an existing ThunderEgg
+// solver setup (GMG::CycleBuilder, Iterative::BiCGStab) in place of the CPU
+// classes.  Header-only; include after ThunderEgg's headers are on the path
+// and link libte_gpu.so.
+//
+//   flatten(domain)            Domain<D> -> te_level_desc tables
+//   GpuDomain<D>               device-side Domain (te_domain) + device-backed Vectors
+//   GpuGhostFiller<D>          GhostFiller<D>                 (GhostFiller.h:46-53)
+//   GpuStarPatchOperator<D>    PatchOperator<D>, Poisson or VarPoisson (PatchOperator.h:61-151)
+//   GpuDFTPatchSolver<D>       PatchSolver<D> (= GMG::Smoother<D>) (PatchSolver.h:98-170)
+//   GpuLinearRestrictor<D>     GMG::Restrictor<D>             (GMG/Restrictor.h:48-54)
+//   GpuDirectInterpolator<D>   GMG::Interpolator<D>           (GMG/Interpolator.h:47-54)
+//   GpuVCycle<D>               Operator<D> applying a whole V-cycle (the Mr of BiCGStab)
+//   GpuBiCGStab<D>             Iterative::Solver<D>           (Iterative/Solver.h:47-69)
+//
+// Vectors: ThunderEgg's Vector<D> is concrete; a device-backed one is made
+// with its unmanaged constructor (Vector.h:199-215) over a GpuDomain's level
+// buffer, patches contiguous.  The adapters pass such Vectors' device
+// pointers straight to the ABI; a Vector whose patches are not contiguous is
+// rejected.  On GB300 the Grace CPU reaches HBM coherently, so ThunderEgg CPU
+// code may still read these Vectors (slowly).  The per-patch virtuals
+// (applySinglePatch, solveSinglePatch, ...) have no per-patch device entry
+// point and throw; the level-wide apply/smooth/restrict/interpolate run on the
+// GPU.  ABI failures throw ThunderEgg::RuntimeError, a Krylov breakdown throws
+// ThunderEgg::Iterative::BreakdownError.
+#pragma once
+
+#include <ThunderEgg/Domain.h>
+#include <ThunderEgg/GMG/Interpolator.h>
+#include <ThunderEgg/GMG/Restrictor.h>
+#include <ThunderEgg/GhostFiller.h>
+#include <ThunderEgg/Iterative/BreakdownError.h>
+#include <ThunderEgg/Iterative/Solver.h>
+#include <ThunderEgg/Operator.h>
+#include <ThunderEgg/PatchOperator.h>
+#include <ThunderEgg/PatchSolver.h>
+#include <ThunderEgg/RuntimeError.h>
+#include <ThunderEgg/Vector.h>
+
+#include <cuda_runtime.h>
+
+#include <array>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../te_gpu.h"
+
+namespace thunderegg_gb300 {
+
+inline void check(int rc) {
+  if (rc == TE_OK) return;
+  const char* m = te_last_error_message();
+  std::string msg = std::string("te_gpu: ") + (m ? m : "");
+  if (rc == TE_ERR_BREAKDOWN) throw ThunderEgg::Iterative::BreakdownError(msg);
+  throw ThunderEgg::RuntimeError(msg);
+}
+
+// ---------------------------------------------------------------------------
+// Domain<D> -> flat level tables (local index = position in the PatchInfo vector)
+// ---------------------------------------------------------------------------
+template <int D>
+struct LevelTables {
+  std::array<int, 3> ns{{1, 1, 1}};
+  int num_ghost = 1, P = 0;
+  std::vector<int> id, refine_level, parent_id, orth_on_parent, child_ids, nbr_type, nbr_ids, nbr_orth;
+  std::vector<double> starts, spacings;
+  te_level_desc desc() const {
+    te_level_desc d;
+    d.dim = D;
+    for (int a = 0; a < 3; a++) d.ns[a] = ns[a];
+    d.num_ghost = num_ghost;
+    d.num_patches = P;
+    d.id = id.data();
+    d.refine_level = refine_level.data();
+    d.parent_id = parent_id.data();
+    d.orth_on_parent = orth_on_parent.data();
+    d.child_ids = child_ids.data();
+    d.starts = starts.data();
+    d.spacings = spacings.data();
+    d.nbr_type = nbr_type.data();
+    d.nbr_ids = nbr_ids.data();
+    d.nbr_orth = nbr_orth.data();
+    return d;
+  }
+};
+
+constexpr int face_slots(int D) { return D == 2 ? 8 : 26; }
+
+// neighbours of one face dimension M: slot = Face<D,M>::sum_of_faces + face index (PatchInfo.h:233-290)
+template <int D, int M>
+void flatten_faces(const ThunderEgg::PatchInfo<D>& pi, int p, LevelTables<D>& t) {
+  using namespace ThunderEgg;
+  for (Face<D, M> f : Face<D, M>::getValues()) {
+    const size_t k = (size_t)p * face_slots(D) + Face<D, M>::sum_of_faces + f.getIndex();
+    if (!pi.hasNbr(f)) continue;
+    switch (pi.getNbrType(f)) {
+      case NbrType::Normal:
+        t.nbr_type[k] = TE_NBR_NORMAL;
+        t.nbr_ids[k * 4] = pi.getNormalNbrInfo(f).id;
+        break;
+      case NbrType::Coarse: {
+        const auto& ci = pi.getCoarseNbrInfo(f);
+        t.nbr_type[k] = TE_NBR_COARSE;
+        t.nbr_ids[k * 4] = ci.id;
+        t.nbr_orth[k] = (int)ci.orth_on_coarse.getIndex();
+        break;
+      }
+      case NbrType::Fine: {
+        const auto& fi = pi.getFineNbrInfo(f);
+        t.nbr_type[k] = TE_NBR_FINE;
+        for (size_t o = 0; o < fi.ids.size(); o++) t.nbr_ids[k * 4 + o] = fi.ids[o];
+        break;
+      }
+      default:
+        throw ThunderEgg::RuntimeError("unknown neighbour type");
+    }
+  }
+}
+
+template <int D>
+LevelTables<D> flatten(const ThunderEgg::Domain<D>& dom) {
+  using namespace ThunderEgg;
+  LevelTables<D> t;
+  const auto& pinfos = dom.getPatchInfoVector();
+  const int P = (int)pinfos.size(), F = face_slots(D), C = 1 << D;
+  t.P = P;
+  for (int a = 0; a < D; a++) t.ns[a] = dom.getNs()[a];
+  t.num_ghost = dom.getNumGhostCells();
+  t.id.assign(P, 0);
+  t.refine_level.assign(P, -1);
+  t.parent_id.assign(P, -1);
+  t.orth_on_parent.assign(P, -1);
+  t.child_ids.assign((size_t)P * C, -1);
+  t.starts.assign((size_t)P * D, 0.0);
+  t.spacings.assign((size_t)P * D, 1.0);
+  t.nbr_type.assign((size_t)P * F, TE_NBR_NONE);
+  t.nbr_ids.assign((size_t)P * F * 4, -1);
+  t.nbr_orth.assign((size_t)P * F, -1);
+  for (int p = 0; p < P; p++) {
+    const PatchInfo<D>& pi = pinfos[p];
+    t.id[p] = pi.id;
+    t.refine_level[p] = pi.refine_level;
+    t.parent_id[p] = pi.parent_id;
+    t.orth_on_parent[p] = pi.orth_on_parent == Orthant<D>::null() ? -1 : (int)pi.orth_on_parent.getIndex();
+    for (int c = 0; c < C; c++) t.child_ids[(size_t)p * C + c] = pi.child_ids[c];
+    for (int a = 0; a < D; a++) {
+      t.starts[(size_t)p * D + a] = pi.starts[a];
+      t.spacings[(size_t)p * D + a] = pi.spacings[a];
+    }
+    if constexpr (D == 2) {
+      flatten_faces<2, 0>(pi, p, t);
+      flatten_faces<2, 1>(pi, p, t);
+    } else {
+      flatten_faces<3, 0>(pi, p, t);
+      flatten_faces<3, 1>(pi, p, t);
+      flatten_faces<3, 2>(pi, p, t);
+    }
+  }
+  return t;
+}
+
+// ---------------------------------------------------------------------------
+// device level and device-backed Vectors
+// ---------------------------------------------------------------------------
+template <int D>
+class GpuDomain {
+ public:
+  explicit GpuDomain(const ThunderEgg::Domain<D>& dom) : dom_(dom) {
+    LevelTables<D> t = flatten(dom);
+    te_level_desc d = t.desc();
+    te_domain* h = nullptr;
+    check(te_domain_create(&d, &h));
+    h_ = std::shared_ptr<te_domain>(h, [](te_domain* x) { te_domain_destroy(x); });
+  }
+  te_domain* handle() const { return h_.get(); }
+  const ThunderEgg::Domain<D>& domain() const { return dom_; }
+  // doubles of one patch with ncomp components, ghosts included
+  long long patchStride(int ncomp) const { return te_domain_patch_stride(h_.get(), ncomp); }
+
+  // A zero-filled device level buffer and a Vector<D> over it.  The Vector does not own the
+  // memory: keep the returned object alive as long as the Vector is used.
+  struct DeviceVector {
+    std::shared_ptr<double> mem;
+    ThunderEgg::Vector<D> vec;
+  };
+  DeviceVector makeVector(int ncomp = 1) const {
+    const long long stride = patchStride(ncomp);
+    const int P = dom_.getNumLocalPatches();
+    double* p = nullptr;
+    if (cudaMalloc(&p, sizeof(double) * (size_t)stride * P) != cudaSuccess)
+      throw ThunderEgg::RuntimeError("cudaMalloc of a level buffer failed");
+    cudaMemset(p, 0, sizeof(double) * (size_t)stride * P);
+    std::shared_ptr<double> mem(p, [](double* x) { cudaFree(x); });
+    std::vector<double*> starts(P);
+    for (int i = 0; i < P; i++) starts[i] = p + (size_t)i * stride;
+    std::array<int, D + 1> strides, lengths;
+    const int g = dom_.getNumGhostCells();
+    int s = 1;
+    for (int a = 0; a < D; a++) {
+      strides[a] = s;
+      lengths[a] = dom_.getNs()[a];
+      s *= dom_.getNs()[a] + 2 * g;
+    }
+    strides[D] = s;
+    lengths[D] = ncomp;
+    return DeviceVector{mem, ThunderEgg::Vector<D>(dom_.getCommunicator(), starts, strides, lengths, g)};
+  }
+
+ private:
+  ThunderEgg::Domain<D> dom_;
+  std::shared_ptr<te_domain> h_;
+};
+
+// device pointer of a Vector's level buffer; its patches must be contiguous
+template <int D>
+void* levelPointer(const ThunderEgg::Vector<D>& v, const GpuDomain<D>& gd) {
+  const int P = v.getNumLocalPatches();
+  if (P == 0) throw ThunderEgg::RuntimeError("empty vector");
+  auto first = [&](int i) {
+    auto view = v.getPatchView(i);
+    return &view[view.getGhostStart()];
+  };
+  const double* base = first(0);
+  const long long stride = gd.patchStride(v.getNumComponents());
+  for (int i = 1; i < P; i++)
+    if (first(i) != base + (size_t)i * stride)
+      throw ThunderEgg::RuntimeError("GPU adapters need a device-backed Vector with contiguous patches");
+  return const_cast<double*>(base);
+}
+
+// ---------------------------------------------------------------------------
+// GhostFiller<D>
+// ---------------------------------------------------------------------------
+template <int D>
+class GpuGhostFiller : public ThunderEgg::GhostFiller<D> {
+ public:
+  // scheme: TE_GHOST_BILINEAR / BIQUADRATIC / TRILINEAR; fill_type: TE_FILL_*
+  GpuGhostFiller(std::shared_ptr<GpuDomain<D>> gd, int scheme, int fill_type = TE_FILL_FACES) : gd_(gd) {
+    te_ghost_filler* h = nullptr;
+    check(te_ghost_filler_create(gd->handle(), scheme, fill_type, &h));
+    h_ = std::shared_ptr<te_ghost_filler>(h, [](te_ghost_filler* x) { te_ghost_filler_destroy(x); });
+  }
+  GpuGhostFiller* clone() const override { return new GpuGhostFiller(*this); }
+  void fillGhost(const ThunderEgg::Vector<D>& u) const override {
+    check(te_ghost_fill(h_.get(), u.getNumComponents(), TE_F64, levelPointer(u, *gd_)));
+  }
+  te_ghost_filler* handle() const { return h_.get(); }
+  const std::shared_ptr<GpuDomain<D>>& gpuDomain() const { return gd_; }
+
+ private:
+  std::shared_ptr<GpuDomain<D>> gd_;
+  std::shared_ptr<te_ghost_filler> h_;
+};
+
+// ---------------------------------------------------------------------------
+// PatchOperator<D>: Poisson::StarPatchOperator or VarPoisson::StarPatchOperator
+// ---------------------------------------------------------------------------
+template <int D>
+class GpuStarPatchOperator : public ThunderEgg::PatchOperator<D> {
+ public:
+  // Poisson (coeffs == nullptr) or VarPoisson with a device coefficient Vector
+  GpuStarPatchOperator(const GpuGhostFiller<D>& gf, bool neumann = false,
+                       const ThunderEgg::Vector<D>* coeffs = nullptr)
+      : ThunderEgg::PatchOperator<D>(gf.gpuDomain()->domain(), gf), gd_(gf.gpuDomain()) {
+    te_operator* h = nullptr;
+    if (coeffs)
+      check(te_varpoisson_operator_create(gd_->handle(), gf.handle(), levelPointer(*coeffs, *gd_), &h));
+    else
+      check(te_poisson_operator_create(gd_->handle(), gf.handle(), neumann ? 1 : 0, &h));
+    h_ = std::shared_ptr<te_operator>(h, [](te_operator* x) { te_operator_destroy(x); });
+  }
+  GpuStarPatchOperator* clone() const override { return new GpuStarPatchOperator(*this); }
+  // the whole level on the GPU (PatchOperator::apply, PatchOperator.h:126-143)
+  void apply(const ThunderEgg::Vector<D>& u, ThunderEgg::Vector<D>& f) const override {
+    check(te_operator_apply(h_.get(), u.getNumComponents(), TE_F64, levelPointer(u, *gd_), levelPointer(f, *gd_)));
+  }
+  void modifyRHSForInternalBoundaryConditions(const ThunderEgg::Vector<D>& u, ThunderEgg::Vector<D>& f) const {
+    check(te_operator_modify_rhs(h_.get(), u.getNumComponents(), TE_F64, levelPointer(u, *gd_),
+                                 levelPointer(f, *gd_)));
+  }
+  void applySinglePatch(const ThunderEgg::PatchInfo<D>&, const ThunderEgg::PatchView<const double, D>&,
+                        const ThunderEgg::PatchView<double, D>&) const override {
+    throw ThunderEgg::RuntimeError("GpuStarPatchOperator runs whole levels; use apply()");
+  }
+  void modifyRHSForInternalBoundaryConditions(const ThunderEgg::PatchInfo<D>&,
+                                              const ThunderEgg::PatchView<const double, D>&,
+                                              const ThunderEgg::PatchView<double, D>&) const override {
+    throw ThunderEgg::RuntimeError("GpuStarPatchOperator runs whole levels");
+  }
+  void applySinglePatchWithInternalBoundaryConditions(const ThunderEgg::PatchInfo<D>&,
+                                                      const ThunderEgg::PatchView<const double, D>&,
+                                                      const ThunderEgg::PatchView<double, D>&) const override {
+    throw ThunderEgg::RuntimeError("GpuStarPatchOperator runs whole levels");
+  }
+  te_operator* handle() const { return h_.get(); }
+  const std::shared_ptr<GpuDomain<D>>& gpuDomain() const { return gd_; }
+
+ private:
+  std::shared_ptr<GpuDomain<D>> gd_;
+  std::shared_ptr<te_operator> h_;
+};
+
+// ---------------------------------------------------------------------------
+// PatchSolver<D> (also a GMG::Smoother<D>): the DFT patch solver
+// ---------------------------------------------------------------------------
+template <int D>
+class GpuDFTPatchSolver : public ThunderEgg::PatchSolver<D> {
+ public:
+  explicit GpuDFTPatchSolver(const GpuStarPatchOperator<D>& op, int neumann_mask = 0)
+      : ThunderEgg::PatchSolver<D>(op.gpuDomain()->domain(), op.getGhostFiller()), gd_(op.gpuDomain()) {
+    te_patch_solver* h = nullptr;
+    check(te_dft_patch_solver_create(op.handle(), neumann_mask, &h));
+    h_ = std::shared_ptr<te_patch_solver>(h, [](te_patch_solver* x) { te_patch_solver_destroy(x); });
+  }
+  GpuDFTPatchSolver* clone() const override { return new GpuDFTPatchSolver(*this); }
+  void apply(const ThunderEgg::Vector<D>& f, ThunderEgg::Vector<D>& u) const override {
+    check(te_patch_solver_apply(h_.get(), u.getNumComponents(), TE_F64, levelPointer(f, *gd_),
+                                levelPointer(u, *gd_)));
+  }
+  void smooth(const ThunderEgg::Vector<D>& f, ThunderEgg::Vector<D>& u) const override {
+    check(te_patch_solver_smooth(h_.get(), u.getNumComponents(), TE_F64, levelPointer(f, *gd_),
+                                 levelPointer(u, *gd_)));
+  }
+  void solveSinglePatch(const ThunderEgg::PatchInfo<D>&, const ThunderEgg::PatchView<const double, D>&,
+                        const ThunderEgg::PatchView<double, D>&) const override {
+    throw ThunderEgg::RuntimeError("GpuDFTPatchSolver runs whole levels; use apply() or smooth()");
+  }
+  te_patch_solver* handle() const { return h_.get(); }
+
+ private:
+  std::shared_ptr<GpuDomain<D>> gd_;
+  std::shared_ptr<te_patch_solver> h_;
+};
+
+// ---------------------------------------------------------------------------
+// GMG::Restrictor<D> and GMG::Interpolator<D>
+// ---------------------------------------------------------------------------
+template <int D>
+class GpuLinearRestrictor : public ThunderEgg::GMG::Restrictor<D> {
+ public:
+  GpuLinearRestrictor(std::shared_ptr<GpuDomain<D>> fine, std::shared_ptr<GpuDomain<D>> coarse,
+                      bool extrapolate_boundary_ghosts = false)
+      : fine_(fine), coarse_(coarse) {
+    te_restrictor* h = nullptr;
+    check(te_linear_restrictor_create(fine->handle(), coarse->handle(), extrapolate_boundary_ghosts ? 1 : 0, &h));
+    h_ = std::shared_ptr<te_restrictor>(h, [](te_restrictor* x) { te_restrictor_destroy(x); });
+  }
+  GpuLinearRestrictor* clone() const override { return new GpuLinearRestrictor(*this); }
+  // Restrictor::restrict returns a new Vector (Restrictor.h:54): a device-backed coarse Vector whose
+  // memory is kept alive by this restrictor (the most recent results are retained)
+  ThunderEgg::Vector<D> restrict(const ThunderEgg::Vector<D>& fine) const override {
+    auto out = coarse_->makeVector(fine.getNumComponents());
+    check(te_restrict(h_.get(), fine.getNumComponents(), TE_F64, levelPointer(fine, *fine_),
+                      levelPointer(out.vec, *coarse_)));
+    keep_.push_back(out.mem);
+    if (keep_.size() > 4) keep_.erase(keep_.begin());
+    return out.vec;
+  }
+
+ private:
+  std::shared_ptr<GpuDomain<D>> fine_, coarse_;
+  std::shared_ptr<te_restrictor> h_;
+  mutable std::vector<std::shared_ptr<double>> keep_;
+};
+
+template <int D>
+class GpuDirectInterpolator : public ThunderEgg::GMG::Interpolator<D> {
+ public:
+  GpuDirectInterpolator(std::shared_ptr<GpuDomain<D>> coarse, std::shared_ptr<GpuDomain<D>> fine)
+      : coarse_(coarse), fine_(fine) {
+    te_interpolator* h = nullptr;
+    check(te_direct_interpolator_create(coarse->handle(), fine->handle(), &h));
+    h_ = std::shared_ptr<te_interpolator>(h, [](te_interpolator* x) { te_interpolator_destroy(x); });
+  }
+  GpuDirectInterpolator* clone() const override { return new GpuDirectInterpolator(*this); }
+  void interpolate(const ThunderEgg::Vector<D>& coarse, ThunderEgg::Vector<D>& fine) const override {
+    check(te_interpolate(h_.get(), fine.getNumComponents(), TE_F64, levelPointer(coarse, *coarse_),
+                         levelPointer(fine, *fine_)));
+  }
+
+ private:
+  std::shared_ptr<GpuDomain<D>> coarse_, fine_;
+  std::shared_ptr<te_interpolator> h_;
+};
+
+// ---------------------------------------------------------------------------
+// The V-cycle as the right preconditioner Mr (Cycle::apply, GMG/Cycle.h:94-98)
+// ---------------------------------------------------------------------------
+template <int D>
+class GpuVCycle : public ThunderEgg::Operator<D> {
+ public:
+  struct LevelParts {
+    const GpuStarPatchOperator<D>* op;
+    const GpuDFTPatchSolver<D>* smoother;
+    te_restrictor* restrictor;      // null on the coarsest level
+    te_interpolator* interpolator;  // null on the finest level
+  };
+  // dtype TE_F32: the mixed-precision cycle (FP32 on every level, FP64 in and out)
+  GpuVCycle(std::shared_ptr<GpuDomain<D>> finest, const std::vector<LevelParts>& parts, te_cycle_opts opts,
+            int dtype = TE_F32)
+      : finest_(finest) {
+    std::vector<te_cycle_level> lv(parts.size());
+    for (size_t k = 0; k < parts.size(); k++) {
+      lv[k].op = parts[k].op->handle();
+      lv[k].smoother = parts[k].smoother->handle();
+      lv[k].restrictor = parts[k].restrictor;
+      lv[k].interpolator = parts[k].interpolator;
+    }
+    te_cycle* h = nullptr;
+    check(te_vcycle_create(lv.data(), (int)lv.size(), opts, dtype, &h));
+    h_ = std::shared_ptr<te_cycle>(h, [](te_cycle* x) { te_cycle_destroy(x); });
+  }
+  GpuVCycle* clone() const override { return new GpuVCycle(*this); }
+  void apply(const ThunderEgg::Vector<D>& f, ThunderEgg::Vector<D>& u) const override {
+    check(te_cycle_apply(h_.get(), u.getNumComponents(), levelPointer(f, *finest_), levelPointer(u, *finest_)));
+  }
+  te_cycle* handle() const { return h_.get(); }
+
+ private:
+  std::shared_ptr<GpuDomain<D>> finest_;
+  std::shared_ptr<te_cycle> h_;
+};
+
+// ---------------------------------------------------------------------------
+// Iterative::Solver<D>: BiCGStab on the GPU (Iterative/BiCGStab.h:111-203)
+// ---------------------------------------------------------------------------
+template <int D>
+class GpuBiCGStab : public ThunderEgg::Iterative::Solver<D> {
+ public:
+  double tolerance = 1e-12;
+  int max_iterations = 1000;
+  int flags = TE_BICGSTAB_PRECONDITIONED_EXIT;
+  GpuBiCGStab* clone() const override { return new GpuBiCGStab(*this); }
+  int solve(const ThunderEgg::Operator<D>& A, ThunderEgg::Vector<D>& x, const ThunderEgg::Vector<D>& b,
+            const ThunderEgg::Operator<D>* Mr = nullptr, bool output = false,
+            std::ostream& os = std::cout) const override {
+    const auto* op = dynamic_cast<const GpuStarPatchOperator<D>*>(&A);
+    if (!op) throw ThunderEgg::RuntimeError("GpuBiCGStab needs a GpuStarPatchOperator");
+    const auto* cyc = Mr ? dynamic_cast<const GpuVCycle<D>*>(Mr) : nullptr;
+    if (Mr && !cyc) throw ThunderEgg::RuntimeError("GpuBiCGStab needs a GpuVCycle (or no) preconditioner");
+    int its = 0;
+    double res = 0;
+    check(te_bicgstab_solve(op->handle(), x.getNumComponents(), levelPointer(x, *op->gpuDomain()),
+                            levelPointer(b, *op->gpuDomain()), cyc ? cyc->handle() : nullptr, tolerance,
+                            max_iterations, flags, &its, &res));
+    if (output) os << "GpuBiCGStab: " << its << " iterations, relative residual " << res << "\n";
+    return its;
+  }
+};
+
+}  // namespace thunderegg_gb300

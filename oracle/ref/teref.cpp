@@ -28,6 +28,8 @@
 #include <string>
 #include <vector>
 
+#include "thunderegg_gb300/adapters.hpp"
+
 using namespace ThunderEgg;
 
 namespace {
@@ -444,6 +446,32 @@ int teref_gmg_solve(const te_level_desc* levels, int nlevels, const teo_gmg_conf
       rc = gmg<3>(levels, nlevels, cfg, coeffs, nc, u, f, iterations, final_residual, true);
   });
   return g != TE_OK ? g : rc;
+}
+
+// Domain<D> built by ThunderEgg from the tables, flattened again by the C++
+// adapters' thunderegg_gb300::flatten (include/thunderegg_gb300/adapters.hpp):
+// the round trip the adapters rely on.  Output arrays have the input's sizes.
+int teref_flatten_roundtrip(const te_level_desc* in, int* id, int* refine_level, int* parent_id,
+                            int* orth_on_parent, int* child_ids, double* starts, double* spacings, int* nbr_type,
+                            int* nbr_ids, int* nbr_orth) {
+  return guard([&] {
+    auto out = [&](auto t) {
+      std::copy(t.id.begin(), t.id.end(), id);
+      std::copy(t.refine_level.begin(), t.refine_level.end(), refine_level);
+      std::copy(t.parent_id.begin(), t.parent_id.end(), parent_id);
+      std::copy(t.orth_on_parent.begin(), t.orth_on_parent.end(), orth_on_parent);
+      std::copy(t.child_ids.begin(), t.child_ids.end(), child_ids);
+      std::copy(t.starts.begin(), t.starts.end(), starts);
+      std::copy(t.spacings.begin(), t.spacings.end(), spacings);
+      std::copy(t.nbr_type.begin(), t.nbr_type.end(), nbr_type);
+      std::copy(t.nbr_ids.begin(), t.nbr_ids.end(), nbr_ids);
+      std::copy(t.nbr_orth.begin(), t.nbr_orth.end(), nbr_orth);
+    };
+    if (in->dim == 2)
+      out(thunderegg_gb300::flatten<2>(make_domain<2>(in)));
+    else
+      out(thunderegg_gb300::flatten<3>(make_domain<3>(in)));
+  });
 }
 
 }  // extern "C"
