@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--stream", type=int, default=40,
                     help="requests in the serving-stream measurement (0: skip)")
-    ap.add_argument("--stream-rate", type=float, default=150.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--stream-rate", type=float, default=50.0, help="Poisson arrival rate, requests/s")
     ap.add_argument("--only-mixed", action="store_true",
                     help="time the mixed-precision solves only (for profiler captures)")
     return ap.parse_args()

@@ -100,8 +100,10 @@ class _Batch:
             coeffs = [np.concatenate([m.req.coeffs[k] for m in members], axis=0) for k in range(len(levels))]
         self.solver = GmgSolver(levels, opts, coeffs)
         self.offsets = offsets[0]
-        self.x = Vector(self.solver.finest)
-        self.b = Vector(self.solver.finest)
+        shape = self.solver.finest.padded_shape(1)
+        # every patch range is written below, so the buffers need no zero fill
+        self.x = Vector(self.solver.finest, data=torch.empty(shape, dtype=torch.float64, device="cuda"))
+        self.b = Vector(self.solver.finest, data=torch.empty(shape, dtype=torch.float64, device="cuda"))
         for i, m in enumerate(members):
             lo, hi = self.offsets[i], self.offsets[i + 1]
             self.b.t[lo:hi].copy_(torch.as_tensor(m.req.f.reshape(self.b.t[lo:hi].shape)), non_blocking=False)
@@ -110,6 +112,8 @@ class _Batch:
                 self.x.t[lo:hi].copy_(src)
             elif src is not None:
                 self.x.t[lo:hi].copy_(torch.as_tensor(src.reshape(self.x.t[lo:hi].shape)))
+            else:
+                self.x.t[lo:hi].zero_()
         torch.cuda.synchronize()
         B = len(members)
         offs = (ctypes.c_int * (B + 1))(*self.offsets)
@@ -185,7 +189,9 @@ class Server:
                 a.x = req.u0
                 cls["active"].append(a)
                 cls["bytes"][rid] = nb
-                cls["dirty"] = True
+                cls["waiting"] = cls.get("waiting", 0) + 1
+                if cls["batch"] is None:
+                    cls["dirty"] = True
                 self.active_bytes += nb
                 self.stats["admitted"] += 1
             else:
@@ -214,6 +220,8 @@ class Server:
             old.close()
             cls["batch"] = None
         cls["dirty"] = False
+        cls["waiting"] = 0
+        cls["wait_rounds"] = 0
         while cls["active"]:
             members = cls["active"]
             b = _Batch(members, [m.x for m in members], members[0].req.opts)
@@ -266,10 +274,16 @@ class Server:
             b.step(self.k)
             its, res, st, run = b.state()
             stopped = len(run) - sum(run)
+            waiting = cls.get("waiting", 0)
+            if waiting:
+                cls["wait_rounds"] = cls.get("wait_rounds", 0) + 1
             if stopped == len(run):
                 self._collect(cls)
-            elif stopped and (self.queue or 4 * stopped >= len(run)):
-                # requests have stopped while others iterate: retire them (and admit) at the next round
+            elif (stopped and (self.queue or waiting or 4 * stopped >= len(run))) or \
+                    (waiting and (2 * waiting >= len(run) or cls.get("wait_rounds", 0) >= 3)):
+                # retire stopped requests and let admitted ones join: re-form at the next round.
+                # Admitted requests join a running batch once they are half its size or have
+                # waited three rounds, so that arrivals do not rebuild the batch one by one.
                 cls["dirty"] = True
         return not self.idle()
 
