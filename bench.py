@@ -191,6 +191,23 @@ def _phase_bytes(name, levels, dtype_bytes):
     return cells * (w + w / (1 << D) + wf + ghost + wo)
 
 
+def replica_throughput(local_seconds, local_solves, device="cuda"):
+    """Whole-job throughput of independent replicas (one process per GPU, no data
+    exchange): every rank's solves summed, divided by the slowest rank's time.
+    Returns (solves/s, max seconds, total solves); single process without a
+    process group: the local numbers."""
+    import torch
+    import torch.distributed as dist
+
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return local_solves / local_seconds, local_seconds, local_solves
+    t = torch.tensor([float(local_seconds)], dtype=torch.float64, device=device)
+    n = torch.tensor([float(local_solves)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(n, op=dist.ReduceOp.SUM)
+    return float(n.item()) / float(t.item()), float(t.item()), float(n.item())
+
+
 def serving_stream(args, te):
     """Config-5-style stream through the continuous-batching server: requests
     with Poisson arrivals at --stream-rate, a mix of 2D quadtrees (circle-adaptive
@@ -325,12 +342,7 @@ def run_gpu(args):
     clocks = clk.stop()
     launches = (L.te_kernel_launch_count() - launches0) * args.steps // (args.steps + args.warmup)
     barrier()
-    total = sum(times)
-    if world > 1:
-        tt = torch.tensor([total], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total = float(tt.item())
-    value = world * B * args.steps / total
+    value, total, _ = replica_throughput(sum(times), B * args.steps)
     true_res = []
     uB_np = uB.numpy()
     for b in range(B):
