@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--stream", type=int, default=40,
                     help="requests in the serving-stream measurement (0: skip)")
     ap.add_argument("--stream-rate", type=float, default=50.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--no-extra", action="store_true", help="skip the config-3 and config-4 measurements")
     ap.add_argument("--only-mixed", action="store_true",
                     help="time the mixed-precision solves only (for profiler captures)")
     return ap.parse_args()
@@ -206,6 +207,77 @@ def replica_throughput(local_seconds, local_solves, device="cuda"):
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     dist.all_reduce(n, op=dist.ReduceOp.SUM)
     return float(n.item()) / float(t.item()), float(t.item()), float(n.item())
+
+
+def config3_measure(te, reps=3):
+    """Config 3: 3D uniform octree L4 (4096 patches of 16^3, 16.8M cells), TriLinear,
+    DFT smoother, u = 0, RHS i.i.d. N(0,1) (seed 0); mixed precision (FP32 V-cycle
+    with tensor-core transforms, float-float BiCGStab) and the FP64 drop-in, both
+    to a 1e-10 FP64 residual; error of the mixed solution against the FP64 one."""
+    import numpy as np
+    import torch
+
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels, f, _ = PB.config3()
+    out = {}
+    sols = {}
+    for name, opts in (("mixed", GmgOptions(scheme=2, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1)),
+                       ("fp64", GmgOptions(scheme=2, smoother=0, cycle_dtype=te.TE_F64, bicgstab_flags=1))):
+        s = GmgSolver(levels, opts)
+        fv, uv = te.Vector.from_numpy(s.finest, f), te.Vector(s.finest)
+        times, its = [], 0
+        for r in range(reps + 1):
+            uv.t.zero_()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            its = s.solve(fv, uv)
+            torch.cuda.synchronize()
+            if r:
+                times.append(time.perf_counter() - t)
+        out[name] = {"seconds_per_solve": float(np.median(times)), "outer_iterations": its,
+                     "true_rel_residual_fp64": s.residual(fv, uv)}
+        sols[name] = uv.numpy()
+    inner = (Ellipsis, slice(1, -1), slice(1, -1), slice(1, -1))
+    d = sols["mixed"][inner] - sols["fp64"][inner]
+    out["mixed_vs_fp64_rel_err"] = float(np.abs(d).max() / np.abs(sols["fp64"][inner]).max())
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds_per_solve"] / out["mixed"]["seconds_per_solve"]
+    out["cells"] = int(levels[0].num_cells)
+    out["cell_updates_per_s_mixed"] = levels[0].num_cells * out["mixed"]["outer_iterations"] / \
+        out["mixed"]["seconds_per_solve"]
+    return out
+
+
+def config4_measure(te):
+    """Config 4: 32 variable-coefficient solves on their own random quadtrees (16^2
+    patches, BiQuadratic, BiCGStab patch smoother), FP32 V-cycle and float-float
+    BiCGStab to 1e-10, served together (the server packs solves of equal depth into
+    one launch per level)."""
+    import numpy as np
+
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions
+    from thunderegg_gb300.serve import Request, Server
+
+    probs = PB.config4()
+    opts = GmgOptions(scheme=1, smoother=1, cycle_dtype=te.TE_F32, bicgstab_flags=1)
+    reqs = [Request(lv, f, opts, coeffs=c) for lv, f, c in probs]
+    warm = Server(budget_bytes=150e9, steps_per_round=4)
+    for r in reqs[:4]:
+        warm.submit(r)
+    warm.run()
+    srv = Server(budget_bytes=150e9, steps_per_round=4)
+    t = time.perf_counter()
+    for r in reqs:
+        srv.submit(r)
+    res = srv.run()
+    wall = time.perf_counter() - t
+    return {"solves": len(reqs), "solves_per_s": len(reqs) / wall, "seconds": wall,
+            "max_rel_residual": max(r.residual for r in res.values()),
+            "mean_iterations": float(np.mean([r.iterations for r in res.values()])),
+            "depth_classes": len(srv.classes), "max_batch": srv.stats["max_batch"],
+            "patches_total": int(sum(lv[0].num_patches for lv, _, _ in probs))}
 
 
 def serving_stream(args, te):
@@ -415,6 +487,9 @@ def run_gpu(args):
     cyc_total = sum(t for _, t in phases)
 
     stream = serving_stream(args, te) if (args.stream > 0 and not args.only_mixed and rank == 0) else None
+    extra = not args.no_extra and not args.only_mixed and rank == 0
+    c3 = config3_measure(te) if extra else None
+    c4 = config4_measure(te) if extra else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -456,6 +531,8 @@ def run_gpu(args):
         "clocks": clocks,
         "wall_s_timed": t_wall,
         "serving_stream": stream,
+        "config3": c3,
+        "config4": c4,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

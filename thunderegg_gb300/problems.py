@@ -104,14 +104,26 @@ def sine_modes_rhs(lvl, rng, modes=8, kmax=8):
     return set_values(lvl, fn)
 
 
+def config4(num_solves=32, n=16, lo=2, hi=6, p=0.3):
+    """Config 4: num_solves variable-coefficient problems, solve s on its own random
+    quadtree (seed s, leaves refined with probability p from level lo to hi, 2:1
+    balanced, n x n patches), beta = 1 + 0.9 sin(4 pi x) sin(4 pi y), and RHS a
+    sum of 8 sine modes with N(0,1) amplitudes drawn from the same seed.
+    Returns [(levels, f, coeffs)]."""
+    out = []
+    for s in range(num_solves):
+        levels = M.random_mesh(s, n=n, lo=lo, hi=hi, p=p)
+        rng = np.random.default_rng(s)
+        out.append((levels, sine_modes_rhs(levels[0], rng), beta_coeffs(levels)))
+    return out
+
+
 def beta_coeffs(levels):
     """beta = 1 + 0.9 sin(4 pi x) sin(4 pi y) at cell centres and ghost centres of every level."""
     out = []
     for lvl in levels:
         v = np.zeros(lvl.padded_shape(1))
         g = lvl.num_ghost
-        for a_ in range(1):
-            pass
         D = lvl.dim
         grids = []
         for a in range(D):
