@@ -261,7 +261,9 @@ def config4_measure(te):
     from thunderegg_gb300.serve import Request, Server
 
     probs = PB.config4()
-    opts = GmgOptions(scheme=1, smoother=1, cycle_dtype=te.TE_F32, bicgstab_flags=1)
+    # the FP32 cycle's patch smoother stops at 1e-5 relative (its 1e-12 default is below FP32 resolution
+    # and would run every inner solve to its iteration limit)
+    opts = GmgOptions(scheme=1, smoother=1, cycle_dtype=te.TE_F32, bicgstab_flags=1, inner_tol=1e-5)
     reqs = [Request(lv, f, opts, coeffs=c) for lv, f, c in probs]
     warm = Server(budget_bytes=150e9, steps_per_round=4)
     for r in reqs[:4]:
@@ -276,7 +278,7 @@ def config4_measure(te):
     return {"solves": len(reqs), "solves_per_s": len(reqs) / wall, "seconds": wall,
             "max_rel_residual": max(r.residual for r in res.values()),
             "mean_iterations": float(np.mean([r.iterations for r in res.values()])),
-            "depth_classes": len(srv.classes), "max_batch": srv.stats["max_batch"],
+            "depth_classes": len(srv.classes), "max_batch": srv.stats["max_batch"], "inner_tol": 1e-5,
             "patches_total": int(sum(lv[0].num_patches for lv, _, _ in probs))}
 
 
