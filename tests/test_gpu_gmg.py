@@ -161,14 +161,16 @@ def test_fused_cycle_matches_unfused(te, idx, cycle_dtype, monkeypatch):
     assert rel_err(outs[0][inner], outs[1][inner]) <= tol
 
 
-def test_batched_solves_match_alone(te):
+@pytest.mark.parametrize("n", (8, 16))
+def test_batched_solves_match_alone(te, n):
     """A batch of independent solves: each solve's result is bit-identical to
-    the same solve alone (batch of one) and to the single-solve entry point."""
+    the same solve alone (batch of one) and to the single-solve entry point.
+    n = 16 takes the fused apply+dot kernels and the tensor-core transforms."""
     from thunderegg_gb300 import mesh as M
     from thunderegg_gb300 import problems as PB
     from thunderegg_gb300.gmg import GmgOptions, GmgSolver
 
-    hiers = [M.circle_mesh(n=8, lo=2, hi=5) for _ in range(3)]
+    hiers = [M.circle_mesh(n=n, lo=2, hi=5 if n == 8 else 4) for _ in range(3)]
     rng = np.random.default_rng(60)
     fs = [PB.sine_modes_rhs(h[0], rng) for h in hiers]
     opts = GmgOptions(scheme=1, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1)

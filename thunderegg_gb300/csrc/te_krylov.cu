@@ -139,6 +139,47 @@ __device__ void k_reduce_blk(const double (&blk)[NV], const Batch& bt, int b, in
   }
 }
 
+// Per-patch partial sums (one block per patch p of solve b): the last block of
+// the solve sums its patches' partials in patch order and finalises.  The
+// order depends only on the solve's own patches, not on the batch.
+template <int NV>
+__device__ void kp_reduce(const double (&blk)[NV], int B, int b, int first, int count, int p, double* part,
+                          int P, unsigned int* counter, double* S, int slot0, int finalize_kind) {
+  __shared__ double fin[NV][KT];
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NV; i++) part[(size_t)i * P + p] = blk[i];
+    __threadfence();
+    unsigned int done = atomicAdd(&counter[b], 1u);
+    last = done == (unsigned)(count - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int i = 0; i < NV; i++) {
+    double s = 0;
+    for (int c = threadIdx.x; c < count; c += blockDim.x) s += __ldcg(&part[(size_t)i * P + first + c]);
+    fin[i][threadIdx.x] = s;
+  }
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int i = 0; i < NV; i++) fin[i][threadIdx.x] += fin[i][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double* Sb = S + (size_t)b * S_NSLOTS;
+    double tot[NV];
+    for (int i = 0; i < NV; i++) {
+      tot[i] = fin[i][0];
+      Sb[slot0 + i] = tot[i];
+    }
+    if (finalize_kind == 1) Sb[S_ALPHA] = Sb[S_RHO] / tot[0];  // alpha = rho / (rhat . ap)
+    else if (finalize_kind == 2) Sb[S_OMEGA] = tot[0] / tot[1];  // omega = (as . s) / (as . as)
+    counter[b] = 0u;
+  }
+}
+
 template <int NV>
 __device__ void k_reduce(double (&v)[NV], const Batch& bt, int b, int ch, double* part, unsigned int* counter,
                          double* S, int slot0, int finalize_kind, double tol) {
@@ -466,6 +507,155 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// f = A u (as apply_df_kernel) fused with the dot products that follow it in
+// the iteration: NV = 1: rhat . f (-> alpha); NV = 2: f . w and f . f (-> omega).
+// Cubic patches of NN cells with one ghost layer; patches of solves that have
+// stopped are skipped.  Cells are enumerated explicitly: the (NN-2)^D cells
+// away from the patch boundary before the barrier that publishes the gathered
+// ghosts, the boundary shell after it.  f's ghost cells are not written (the
+// outer loop never reads them).
+template <int KIND, int SCHEME, int DIM, int NN, int NV>
+__global__ void __launch_bounds__(256)
+    apply_dots_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const float2* __restrict__ inv_df,
+                      int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
+                      const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gs,
+                      const float* __restrict__ u, DV f, CV w, Batch bt, const int* __restrict__ patch_solve,
+                      double* part, unsigned int* counter, double* S, int slot0, int finalize_kind) {
+  extern __shared__ df64 G[];  // [2D][gs]
+  __shared__ int has[6];
+  const int p = blockIdx.x;
+  const int b = patch_solve[p];
+  if (!bt.active[b]) return;
+  constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
+  constexpr int NF = DIM == 3 ? NN * NN : NN;
+  constexpr int NIN = DIM == 3 ? (NN - 2) * (NN - 2) * (NN - 2) : (NN - 2) * (NN - 2);
+  constexpr int NSH = (DIM == 3 ? NN * NN * NN : NN * NN) - NIN;
+  const int side0 = DIM == 2 ? 4 : 20;
+  df64 inv[3];
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    const float2 v = __ldg(inv_df + (size_t)p * 6 + (KIND ? 3 : 0) + a);
+    inv[a] = df64(v.x, v.y);
+  }
+  const F32Acc acc{u, (long long)CS};
+  for (int e = threadIdx.x; e < 2 * DIM * NF; e += blockDim.x) {
+    const int s = e / NF, r = e % NF;
+    const int si = side_slab[p * 2 * DIM + s];
+    if (si < 0) continue;
+    const GSlab sl = slabs[si];
+    G[s * gs + r] = gather_ghost<df64, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, r % NN, r / NN,
+                                               df64(0.f, 0.f));
+  }
+  if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
+  const float* up = u + (long long)p * CS;
+  const long long base = (long long)p * CS;
+  df64 v[NV];
+  for (int i = 0; i < NV; i++) v[i] = df64(0.f, 0.f);
+  auto emit = [&](int k, df64 res) {
+    stv(f, base + k, res);
+    if (NV == 1) {
+      v[0] += ldv(w, base + k) * res;
+    } else {
+      v[0] += res * ldv(w, base + k);
+      v[1] += res * res;
+    }
+  };
+  // cells away from the boundary: every neighbour is an interior FP32 value
+  for (int e = threadIdx.x; e < NIN; e += blockDim.x) {
+    const int x = e % (NN - 2) + 1, r = e / (NN - 2);
+    const int y = r % (NN - 2) + 1, z = DIM == 3 ? r / (NN - 2) + 1 : 0;
+    const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
+    df64 res;
+    if (KIND == 0) {
+      const float mid = up[k];
+      res = df_second_difference(up[k + 1], mid, up[k - 1]) * inv[0];
+      res += df_second_difference(up[k + SY], mid, up[k - SY]) * inv[1];
+      if (DIM == 3) res += df_second_difference(up[k + SZ], mid, up[k - SZ]) * inv[2];
+    } else {
+      const df64 mid(up[k], 0.f);
+      res = df64(0.f, 0.f);
+#pragma unroll
+      for (int a = 0; a < DIM; a++) {
+        const int st = a == 0 ? 1 : (a == 1 ? SY : SZ);
+        const df64 lo(up[k - st], 0.f), hi(up[k + st], 0.f);
+        const df64 cl = ldv(coeff, base + k - st), cm = ldv(coeff, base + k), cu = ldv(coeff, base + k + st);
+        res += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
+      }
+    }
+    emit(k, res);
+  }
+  __syncthreads();
+  // the boundary shell: 2D: the ring; 3D: the z = 0 and z = NN-1 planes, then the ring of every inner slice
+  for (int e = threadIdx.x; e < NSH; e += blockDim.x) {
+    int x, y, z = 0;
+    int q = e;
+    if (DIM == 3) {
+      if (q < 2 * NN * NN) {
+        z = q < NN * NN ? 0 : NN - 1;
+        q %= NN * NN;
+        x = q % NN;
+        y = q / NN;
+      } else {
+        q -= 2 * NN * NN;
+        z = q / (4 * NN - 4) + 1;
+        q %= 4 * NN - 4;
+        if (q < NN) { x = q; y = 0; }
+        else if (q < 2 * NN) { x = q - NN; y = NN - 1; }
+        else if (q < 3 * NN - 2) { x = 0; y = q - 2 * NN + 1; }
+        else { x = NN - 1; y = q - 3 * NN + 3; }
+      }
+    } else {
+      if (q < NN) { x = q; y = 0; }
+      else if (q < 2 * NN) { x = q - NN; y = NN - 1; }
+      else if (q < 3 * NN - 2) { x = 0; y = q - 2 * NN + 1; }
+      else { x = NN - 1; y = q - 3 * NN + 3; }
+    }
+    const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
+    const int cc[3] = {x, y, z};
+    const df64 mid(up[k], 0.f);
+    df64 res(0.f, 0.f);
+#pragma unroll
+    for (int a = 0; a < DIM; a++) {
+      const int st = a == 0 ? 1 : (a == 1 ? SY : SZ);
+      const int tan = a == 0 ? y + z * NN : (a == 1 ? x + z * NN : x + y * NN);
+      df64 lo, hi;
+      if (cc[a] == 0)
+        lo = has[2 * a] ? G[(2 * a) * gs + tan] : (neumann ? mid : -mid);
+      else
+        lo = df64(up[k - st], 0.f);
+      if (cc[a] == NN - 1)
+        hi = has[2 * a + 1] ? G[(2 * a + 1) * gs + tan] : (neumann ? mid : -mid);
+      else
+        hi = df64(up[k + st], 0.f);
+      if (KIND == 0) {
+        res += ((hi - df64(2.0) * mid) + lo) * inv[a];
+      } else {
+        const df64 cl = ldv(coeff, base + k - st), cm = ldv(coeff, base + k), cu = ldv(coeff, base + k + st);
+        res += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
+      }
+    }
+    emit(k, res);
+  }
+  // block sums in float-float, then this solve's patch partials in patch order
+  __shared__ df64 red[NV][256 / 32];
+#pragma unroll
+  for (int i = 0; i < NV; i++) {
+    df64 x = v[i];
+    for (int o = 16; o > 0; o >>= 1) x += df_shfl_down(x, o);
+    if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = x;
+  }
+  __syncthreads();
+  double blk[NV];
+  if (threadIdx.x == 0)
+    for (int i = 0; i < NV; i++) {
+      df64 t = red[i][0];
+      for (int q = 1; q < (int)(blockDim.x >> 5); q++) t += red[i][q];
+      blk[i] = df_to_double(t);
+    }
+  const int first = bt.offs[b];
+  kp_reduce<NV>(blk, bt.B, b, first, bt.offs[b + 1] - first, p, part, L.P, counter, S, slot0, finalize_kind);
+}
+
 template <int KIND, int SCHEME, int DIM, int NN>
 static void apply_df_launch(const te_operator* A, const float* u, DV f, cudaStream_t st) {
   const te_domain* d = A->dom;
@@ -484,20 +674,13 @@ static void apply_df_launch(const te_operator* A, const float* u, DV f, cudaStre
   TE_LAUNCH_CHECK();
 }
 
+// the general apply (any patch shape); cubic levels with the usual sizes take apply_dots
 template <int KIND, int SCHEME>
 static void apply_df_t(const te_operator* A, const float* u, DV f, cudaStream_t st) {
-  const Layout& L = A->dom->lay;
-  const bool cube = L.g == 1 && L.n1 == L.n0 && (L.D == 2 || L.n2 == L.n0);
-  if (L.D == 2) {
-    if (cube && L.n0 == 16) apply_df_launch<KIND, SCHEME, 2, 16>(A, u, f, st);
-    else if (cube && L.n0 == 32) apply_df_launch<KIND, SCHEME, 2, 32>(A, u, f, st);
-    else if (cube && L.n0 == 64) apply_df_launch<KIND, SCHEME, 2, 64>(A, u, f, st);
-    else apply_df_launch<KIND, SCHEME, 2, 0>(A, u, f, st);
-  } else {
-    if (cube && L.n0 == 8) apply_df_launch<KIND, SCHEME, 3, 8>(A, u, f, st);
-    else if (cube && L.n0 == 16) apply_df_launch<KIND, SCHEME, 3, 16>(A, u, f, st);
-    else apply_df_launch<KIND, SCHEME, 3, 0>(A, u, f, st);
-  }
+  if (A->dom->lay.D == 2)
+    apply_df_launch<KIND, SCHEME, 2, 0>(A, u, f, st);
+  else
+    apply_df_launch<KIND, SCHEME, 3, 0>(A, u, f, st);
 }
 
 static void apply_df(const te_operator* A, const float* u, DV f, cudaStream_t st) {
@@ -525,6 +708,8 @@ struct KrylovWork {
   DevBuf<double> xdf;  // float-float outer loop: the iterate (allocated on first use)
   DevBuf<unsigned int> counter;
   DevBuf<int> offs, nch, active;
+  DevBuf<int> patch_solve;  // [P] solve of each finest patch
+  DevBuf<double> part_p;    // [2][P] per-patch dot partials of the fused apply
   double* h = nullptr;
   int* h_active = nullptr;
   cudaStream_t cap = nullptr;
@@ -550,6 +735,13 @@ struct KrylovWork {
     counter.alloc(B);
     TE_CUDA(cudaMemsetAsync(counter.p, 0, B * sizeof(unsigned int), d->stream));
     offs.upload(h_offs, d->stream);
+    {
+      std::vector<int> ps(d->lay.P, 0);
+      for (int b2 = 0; b2 < B; b2++)
+        for (int q = offsets[b2]; q < offsets[b2 + 1]; q++) ps[q] = b2;
+      patch_solve.upload(ps, d->stream);
+      part_p.alloc((size_t)2 * d->lay.P);
+    }
     nch.upload(h_nch, d->stream);
     active.alloc(B);
     TE_CUDA(cudaMallocHost(&h, (size_t)B * S_NSLOTS * sizeof(double)));
@@ -625,6 +817,74 @@ static void iteration(KrylovWork& W, const te_operator* A, te_cycle* M, double* 
   TE_LAUNCH_CHECK();
 }
 
+template <int KIND, int SCHEME, int DIM, int NN, int NV>
+static void apply_dots_launch(const te_operator* A, KrylovWork& W, const float* u, DV f, CV w, int slot0, int fin,
+                              cudaStream_t st) {
+  const te_domain* d = A->dom;
+  const Layout& L = d->lay;
+  const te_ghost_filler* g = A->gf;
+  const int gs = corr_stride(L);
+  const size_t smem = (size_t)2 * L.D * gs * sizeof(df64);
+  const long long n = (long long)L.P * L.cs;
+  CV coeff{KIND ? A->coeffs_df.p : nullptr, KIND ? A->coeffs_df.p + n : nullptr};
+  auto kern = apply_dots_kernel<KIND, SCHEME, DIM, NN, NV>;
+  if (smem > 40 * 1024)
+    TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff, g->faces,
+                               g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, gs, u, f, w, W.batch(),
+                               W.patch_solve.p, W.part_p.p, W.counter.p, W.S.p, slot0, fin);
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
+template <int NV, int KIND, int SCHEME>
+static bool apply_dots_t(const te_operator* A, KrylovWork& W, const float* u, DV f, CV w, int slot0, int fin,
+                         cudaStream_t st) {
+  const Layout& L = A->dom->lay;
+  if (!(L.g == 1 && L.n1 == L.n0 && (L.D == 2 || L.n2 == L.n0))) return false;
+  if (L.D == 2) {
+    if constexpr (SCHEME == TE_GHOST_TRILINEAR) {
+      return false;
+    } else {
+      if (L.n0 == 16) apply_dots_launch<KIND, SCHEME, 2, 16, NV>(A, W, u, f, w, slot0, fin, st);
+      else if (L.n0 == 32) apply_dots_launch<KIND, SCHEME, 2, 32, NV>(A, W, u, f, w, slot0, fin, st);
+      else if (L.n0 == 64) apply_dots_launch<KIND, SCHEME, 2, 64, NV>(A, W, u, f, w, slot0, fin, st);
+      else return false;
+      return true;
+    }
+  }
+  if constexpr (SCHEME != TE_GHOST_TRILINEAR) {
+    return false;
+  } else {
+    if (L.n0 == 8) apply_dots_launch<KIND, SCHEME, 3, 8, NV>(A, W, u, f, w, slot0, fin, st);
+    else if (L.n0 == 16) apply_dots_launch<KIND, SCHEME, 3, 16, NV>(A, W, u, f, w, slot0, fin, st);
+    else return false;
+    return true;
+  }
+}
+
+// f = A u with the dots that follow it; false when the level does not qualify (the caller then
+// runs apply_df and the separate dot kernel)
+template <int NV>
+static bool apply_dots(const te_operator* A, KrylovWork& W, const float* u, DV f, CV w, int slot0, int fin,
+                       cudaStream_t st) {
+  if (W.nc != 1) return false;
+  static const bool off = [] {
+    const char* e = getenv("TE_NO_FUSED_DOTS");
+    return e && e[0] == '1';
+  }();
+  if (off) return false;
+  const int sc = A->gf->scheme;
+  if (A->kind == 0) {
+    if (sc == TE_GHOST_BILINEAR) return apply_dots_t<NV, 0, TE_GHOST_BILINEAR>(A, W, u, f, w, slot0, fin, st);
+    if (sc == TE_GHOST_BIQUADRATIC) return apply_dots_t<NV, 0, TE_GHOST_BIQUADRATIC>(A, W, u, f, w, slot0, fin, st);
+    return apply_dots_t<NV, 0, TE_GHOST_TRILINEAR>(A, W, u, f, w, slot0, fin, st);
+  }
+  if (sc == TE_GHOST_BILINEAR) return apply_dots_t<NV, 1, TE_GHOST_BILINEAR>(A, W, u, f, w, slot0, fin, st);
+  if (sc == TE_GHOST_BIQUADRATIC) return apply_dots_t<NV, 1, TE_GHOST_BIQUADRATIC>(A, W, u, f, w, slot0, fin, st);
+  return apply_dots_t<NV, 1, TE_GHOST_TRILINEAR>(A, W, u, f, w, slot0, fin, st);
+}
+
 // one float-float iteration; M is an FP32 cycle
 static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, double tol, int flags, cudaStream_t st) {
   const Layout& L = W.d->lay;
@@ -632,21 +892,25 @@ static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, doubl
   Batch bt = W.batch();
   const CV none{nullptr, nullptr};
   M->body_f32(W.f32(W.p), W.f32(W.mp), st);
-  apply_df(A, W.f32(W.mp), W.dv(W.ap), st);
-  kd_dots<1><<<W.grid(), KT, 0, st>>>(L, nc, bt, W.cv(W.rhat), W.cv(W.ap), none, none, none, none, W.part.p,
-                                      W.counter.p, W.S.p, S_RHAT_AP, 1);
-  count_launch();
-  TE_LAUNCH_CHECK();
+  if (!apply_dots<1>(A, W, W.f32(W.mp), W.dv(W.ap), W.cv(W.rhat), S_RHAT_AP, 1, st)) {
+    apply_df(A, W.f32(W.mp), W.dv(W.ap), st);
+    kd_dots<1><<<W.grid(), KT, 0, st>>>(L, nc, bt, W.cv(W.rhat), W.cv(W.ap), none, none, none, none, W.part.p,
+                                        W.counter.p, W.S.p, S_RHAT_AP, 1);
+    count_launch();
+    TE_LAUNCH_CHECK();
+  }
   kd_s<<<W.grid(), KT, 0, st>>>(L, nc, bt, tol, W.cv(W.resid), W.cv(W.ap), W.dv(W.s), W.part.p, W.counter.p,
                                 W.S.p);
   count_launch();
   TE_LAUNCH_CHECK();
   M->body_f32(W.f32(W.s), W.f32(W.ms), st);
-  apply_df(A, W.f32(W.ms), W.dv(W.as), st);
-  kd_dots<2><<<W.grid(), KT, 0, st>>>(L, nc, bt, W.cv(W.as), W.cv(W.s), W.cv(W.as), W.cv(W.as), none, none,
-                                      W.part.p, W.counter.p, W.S.p, S_AS_S, 2);
-  count_launch();
-  TE_LAUNCH_CHECK();
+  if (!apply_dots<2>(A, W, W.f32(W.ms), W.dv(W.as), W.cv(W.s), S_AS_S, 2, st)) {
+    apply_df(A, W.f32(W.ms), W.dv(W.as), st);
+    kd_dots<2><<<W.grid(), KT, 0, st>>>(L, nc, bt, W.cv(W.as), W.cv(W.s), W.cv(W.as), W.cv(W.as), none, none,
+                                        W.part.p, W.counter.p, W.S.p, S_AS_S, 2);
+    count_launch();
+    TE_LAUNCH_CHECK();
+  }
   const CV dir = (flags & TE_BICGSTAB_PRECONDITIONED_EXIT) ? CV{W.f32(W.mp), nullptr} : W.cv(W.p);
   kd_xr<<<W.grid(), KT, 0, st>>>(L, nc, bt, W.dv(W.xdf), W.dv(W.resid), W.f32(W.mp), W.f32(W.ms), W.cv(W.ap),
                                  W.cv(W.as), W.cv(W.rhat), dir, W.part.p, W.counter.p, W.S.p);
