@@ -47,6 +47,7 @@ struct DftTcArgs {
   const int* zero_mode;      // [P]
   const float* corr;         // optional [P][2D][n^(D-1)]: right-hand-side corrections per side face
   float scale;               // prod 2/n, applied to the last pass's result
+  int zero_ghosts;           // also write 0 into the output's ghost cells (PatchSolver::apply)
   int* err;
 };
 
@@ -217,8 +218,10 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
         }
         tc::commit(&bar);
       }
-      bool ok = tc::mbar_wait(&bar, phase, kWaitLimit);
-      if (__syncthreads_or(!ok)) {
+      // one thread waits for the MMAs (bounded) and tells the others at the barrier
+      int late = 0;
+      if (t == 0) late = !tc::mbar_wait(&bar, phase, kWaitLimit);
+      if (__syncthreads_or(late)) {
         abort = true;
         break;
       }
@@ -241,15 +244,24 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
 #pragma unroll
         for (int j = 0; j < NN; j++) stage[t * OP + j] = v[j] * a.scale;
         __syncthreads();
-        for (int e = t; e < S::G * CS; e += S::ROWS) {
-          int i = e / CS, k = e % CS;
-          int p = p0 + i;
-          if (p >= P) break;
-          int x = k % SY - 1, r2 = k / SY;
-          int y = r2 % SY - 1, z = DIM == 3 ? r2 / SY - 1 : 0;
-          bool inner = x >= 0 && x < NN && y >= 0 && y < NN && z >= 0 && z < NN;
-          float val = inner ? stage[(i * S::RPP + y + NN * z) * OP + x] : 0.f;
-          out[(long long)p * CS + k] = (TO)val;
+        // interior rows, coalesced: thread t writes cells t, t + ROWS, ... of the group
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+          const int e = t + k * S::ROWS;
+          const int i = e / S::NCELL, c = e % S::NCELL;
+          const int p = p0 + i;
+          if (p < P) out[(long long)p * CS + interior_offset<DIM, NN>(c)] = (TO)stage[(i * S::RPP + c / NN) * OP + c % NN];
+        }
+        if (a.zero_ghosts) {
+          for (int e = t; e < S::G * CS; e += S::ROWS) {
+            const int i = e / CS, k = e % CS;
+            const int p = p0 + i;
+            if (p >= P) break;
+            const int x = k % SY - 1, r2 = k / SY;
+            const int y = r2 % SY - 1, z = DIM == 3 ? r2 / SY - 1 : 0;
+            const bool inner = x >= 0 && x < NN && y >= 0 && y < NN && z >= 0 && z < NN;
+            if (!inner) out[(long long)p * CS + k] = TO(0);
+          }
         }
         continue;
       }
@@ -379,7 +391,8 @@ void dft_tc_prepare(te_patch_solver* ps, const std::vector<std::vector<double>>&
 }
 
 template <class TI, class TO, int DIM, int NN>
-static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr) {
+static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr,
+                     bool zero_ghosts) {
   using S = TcShape<DIM, NN>;
   const Layout& L = ps->op->dom->lay;
   DftTcArgs a;
@@ -393,6 +406,7 @@ static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStrea
   a.zero_mode = ps->zero_mode.p;
   a.corr = corr;
   a.scale = ps->tc_scale;
+  a.zero_ghosts = zero_ghosts ? 1 : 0;
   a.err = ps->tc_err.p;
   auto kern = dft_tc_kernel<TI, TO, DIM, NN>;
   size_t smem = tc_smem_bytes<DIM, NN>(a.nmat);
@@ -426,17 +440,18 @@ static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStrea
 }
 
 template <class TI, class TO>
-void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr) {
+void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr,
+            bool zero_ghosts) {
   const Layout& L = ps->op->dom->lay;
   require(ps->tc_ok, "tensor-core DFT not prepared for this solver", TE_ERR_UNSUPPORTED);
   if (L.D == 2 && L.n0 == 16)
-    dft_tc_t<TI, TO, 2, 16>(ps, in, out, s, corr);
+    dft_tc_t<TI, TO, 2, 16>(ps, in, out, s, corr, zero_ghosts);
   else if (L.D == 2 && L.n0 == 32)
-    dft_tc_t<TI, TO, 2, 32>(ps, in, out, s, corr);
+    dft_tc_t<TI, TO, 2, 32>(ps, in, out, s, corr, zero_ghosts);
   else if (L.D == 2 && L.n0 == 64)
-    dft_tc_t<TI, TO, 2, 64>(ps, in, out, s, corr);
+    dft_tc_t<TI, TO, 2, 64>(ps, in, out, s, corr, zero_ghosts);
   else
-    dft_tc_t<TI, TO, 3, 16>(ps, in, out, s, corr);
+    dft_tc_t<TI, TO, 3, 16>(ps, in, out, s, corr, zero_ghosts);
 }
 
 int dft_tc_error(const te_patch_solver* ps, cudaStream_t s) {
@@ -447,8 +462,8 @@ int dft_tc_error(const te_patch_solver* ps, cudaStream_t s) {
   return e;
 }
 
-template void dft_tc<double, float>(const te_patch_solver*, const double*, float*, cudaStream_t, const float*);
-template void dft_tc<float, float>(const te_patch_solver*, const float*, float*, cudaStream_t, const float*);
-template void dft_tc<double, double>(const te_patch_solver*, const double*, double*, cudaStream_t, const float*);
+template void dft_tc<double, float>(const te_patch_solver*, const double*, float*, cudaStream_t, const float*, bool);
+template void dft_tc<float, float>(const te_patch_solver*, const float*, float*, cudaStream_t, const float*, bool);
+template void dft_tc<double, double>(const te_patch_solver*, const double*, double*, cudaStream_t, const float*, bool);
 
 }  // namespace te

@@ -493,7 +493,7 @@ void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, v
     if (dtype == TE_F64)
       launch_dft<double>(ps, (const double*)f, (double*)u, op->coeffs.p, ps->mats.p, ps->inv_eig.p, true, s);
     else if (ps->tc_ok)
-      dft_tc<float, float>(ps, (const float*)f, (float*)u, s);
+      dft_tc<float, float>(ps, (const float*)f, (float*)u, s, nullptr, true);
     else
       launch_dft<float>(ps, (const float*)f, (float*)u, op->coeffs_f.p, ps->mats_f.p, ps->inv_eig_f.p, true, s);
     return;

@@ -61,7 +61,10 @@ void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, v
 void dft_tc_prepare(te_patch_solver* ps, const std::vector<std::vector<double>>& mats_t,
                     const std::vector<int>& plan_mats, cudaStream_t st);
 // corr (optional, FP32 [P][2D][n^(D-1)]): per-side right-hand-side corrections subtracted while staging
+// zero_ghosts: also write 0 into out's ghost cells (PatchSolver::apply's u.setWithGhost(0)); the fused
+// cycle never reads the ghosts of the solve's output and skips it
 template <class TI, class TO>
-void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr = nullptr);
+void dft_tc(const te_patch_solver* ps, const TI* in, TO* out, cudaStream_t s, const float* corr = nullptr,
+            bool zero_ghosts = false);
 int dft_tc_error(const te_patch_solver* ps, cudaStream_t s);
 }  // namespace te
