@@ -56,6 +56,30 @@ struct InterpAcc {
   }
 };
 
+// InterpAcc for cubic patches of NN cells with one ghost layer: the same
+// values, with the padded-index decode done by constant divisors
+template <class T, int DIM, int NN>
+struct InterpAccN {
+  const T* A;
+  const T* uc;
+  const int* parent;
+  const int* orth;
+  static constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
+  __device__ __forceinline__ T operator()(int q, int idx) const {
+    const int x = idx % SY - 1, r = idx / SY;
+    const int y = r % SY - 1, z = DIM == 3 ? r / SY - 1 : 0;
+    const int o = __ldg(orth + q);
+    int cidx = idx;
+    if (o >= 0) {
+      const int cx = (x + ((o & 1) ? NN : 0)) >> 1;
+      const int cy = (y + ((o & 2) ? NN : 0)) >> 1;
+      const int cz = DIM == 3 ? (z + ((o & 4) ? NN : 0)) >> 1 : 0;
+      cidx = (cx + 1) + (cy + 1) * SY + (DIM == 3 ? (cz + 1) * SZ : 0);
+    }
+    return A[(long long)q * CS + idx] + uc[(long long)__ldg(parent + q) * CS + cidx];
+  }
+};
+
 __device__ __forceinline__ int side_tangential_index(const Layout& L, int a, int x, int y, int z) {
   if (a == 0) return y + z * L.n1;
   if (a == 1) return x + z * L.n0;
@@ -322,6 +346,54 @@ __global__ void __launch_bounds__(256)
   corr[e] = c;
 }
 
+// vc_corr_kernel for cubic patches of NN cells and one ghost layer (constant index arithmetic)
+template <int KIND, int SCHEME, int DIM, int NN>
+__global__ void __launch_bounds__(256)
+    vc_corr_kernel_n(int P, const int* __restrict__ parent, const int* __restrict__ porth,
+                     const float* __restrict__ inv_tab, const float* __restrict__ coeff, FaceTable ft,
+                     const GSlab* __restrict__ slabs, const GCall* __restrict__ calls,
+                     const int* __restrict__ side_slab, const float* __restrict__ A, const float* __restrict__ uc,
+                     float* __restrict__ corr) {
+  constexpr int NF = DIM == 3 ? NN * NN : NN;
+  constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)P * 2 * DIM * NF) return;
+  const int r = (int)(e % NF);
+  const int s = (int)((e / NF) % (2 * DIM));
+  const int p = (int)(e / (NF * 2 * DIM));
+  const int si = side_slab[p * 2 * DIM + s];
+  float c = 0.f;
+  if (si >= 0) {
+    const int a = s >> 1, upr = s & 1;
+    const int side0 = DIM == 2 ? 4 : 20;
+    const InterpAccN<float, DIM, NN> acc{A, uc, parent, porth};
+    const GSlab sl = slabs[si];
+    const int i = r % NN, j = r / NN;
+    const float gv = gather_ghost<float, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, i, j, 0.f);
+    const int edge = upr ? NN - 1 : 0;
+    int x, y, z;
+    if (a == 0) {
+      x = edge; y = i; z = j;
+    } else if (a == 1) {
+      x = i; y = edge; z = j;
+    } else {
+      x = i; y = j; z = edge;
+    }
+    const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
+    const float uv = acc(p, k);
+    const float inv = inv_tab[(size_t)p * 6 + (KIND ? 3 : 0) + a];
+    if (KIND == 0) {
+      c = (gv + uv) * inv;
+    } else {
+      const float* cp = coeff + (long long)p * CS;
+      const int st = a == 0 ? 1 : (a == 1 ? SY : SZ);
+      const int gk = k + (upr ? st : -st);
+      c = (gv + uv) * (cp[k] + cp[gk]) * inv;
+    }
+  }
+  corr[e] = c;
+}
+
 // ---------------------------------------------------------------------------
 // host launchers
 // ---------------------------------------------------------------------------
@@ -490,9 +562,29 @@ static void vc_corr_t(const te_patch_solver* ps, const te_interpolator* in, cons
   const long long total = (long long)F.P * 2 * F.D * gs;
   const int threads = 256;
   const unsigned blocks = (unsigned)((total + threads - 1) / threads);
-  auto kern = F.D == 2 ? vc_corr_kernel<KIND, SCHEME, 2> : vc_corr_kernel<KIND, SCHEME, 3>;
-  kern<<<blocks, threads, 0, s>>>(F, C, in->parent.p, in->orth.p, d->template inv<float>(), op->coeffs_f.p,
-                                  g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, gs, A, uc, corr);
+  const bool cube = F.g == 1 && F.n1 == F.n0 && (F.D == 2 || F.n2 == F.n0);
+  auto fixed = [&](auto kn) {
+    kn<<<blocks, threads, 0, s>>>(F.P, in->parent.p, in->orth.p, d->template inv<float>(), op->coeffs_f.p, g->faces,
+                                  g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, A, uc, corr);
+  };
+  bool done = false;
+  if (cube && F.D == 2 && SCHEME != TE_GHOST_TRILINEAR) {
+    done = true;
+    if (F.n0 == 16) fixed(vc_corr_kernel_n<KIND, SCHEME, 2, 16>);
+    else if (F.n0 == 32) fixed(vc_corr_kernel_n<KIND, SCHEME, 2, 32>);
+    else if (F.n0 == 64) fixed(vc_corr_kernel_n<KIND, SCHEME, 2, 64>);
+    else done = false;
+  } else if (cube && F.D == 3 && SCHEME == TE_GHOST_TRILINEAR) {
+    done = true;
+    if (F.n0 == 8) fixed(vc_corr_kernel_n<KIND, SCHEME, 3, 8>);
+    else if (F.n0 == 16) fixed(vc_corr_kernel_n<KIND, SCHEME, 3, 16>);
+    else done = false;
+  }
+  if (!done) {
+    auto kern = F.D == 2 ? vc_corr_kernel<KIND, SCHEME, 2> : vc_corr_kernel<KIND, SCHEME, 3>;
+    kern<<<blocks, threads, 0, s>>>(F, C, in->parent.p, in->orth.p, d->template inv<float>(), op->coeffs_f.p,
+                                    g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, gs, A, uc, corr);
+  }
   count_launch();
   TE_LAUNCH_CHECK();
 }
