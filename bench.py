@@ -50,6 +50,8 @@ def parse():
                     help="requests in the serving-stream measurement (0: skip)")
     ap.add_argument("--stream-rate", type=float, default=50.0, help="Poisson arrival rate, requests/s")
     ap.add_argument("--no-extra", action="store_true", help="skip the config-3 and config-4 measurements")
+    ap.add_argument("--kernels", action="store_true",
+                    help="only time the drop-in level kernels against HBM (one JSON line)")
     ap.add_argument("--only-mixed", action="store_true",
                     help="time the mixed-precision solves only (for profiler captures)")
     return ap.parse_args()
@@ -190,6 +192,84 @@ def _phase_bytes(name, levels, dtype_bytes):
     if name.endswith("post-smooth") and "interpolate" not in name:
         return cells * (wf + 4 * face + wo)  # tensor-core solve: f and the corrections in, u out
     return cells * (w + w / (1 << D) + wf + ghost + wo)
+
+
+def _ghost_bytes(lv, w):
+    """Compulsory DRAM bytes of one side-ghost fill of a level at 32-byte sector
+    granularity: for every patch side with a neighbour, the ghost face is
+    written and one face of neighbour values is read.  A face across axis 0 is
+    a column (one sector per cell); the other faces are rows of n cells."""
+    import numpy as np
+
+    D, n = lv.dim, lv.ns[0]
+    side0 = 4 if D == 2 else 20
+    per = n ** (D - 1)
+    total = 0
+    for s in range(2 * D):
+        sides = int(np.count_nonzero(lv.nbr_type[:, side0 + s] >= 0))
+        total += sides * 2 * per * (32 if s // 2 == 0 else w)
+    return total
+
+
+def level_kernel_rooflines(te, solver, hbm, reps=15, warm=3):
+    """Device time of each drop-in level kernel (one ABI call on the solver's
+    finest level, or between its two finest levels), L2 flushed before every
+    call, median over `reps`, against the kernel's algorithmic bytes:
+      ghost_fill       sector-granular ghost faces written + neighbour faces read
+      operator_apply   ghost fill + u read + f written (padded: f's ghosts are set)
+      restrict         fine interior read + coarse padded written
+      interpolate      coarse interior read + fine interior read and written
+      vec_add_scaled   x, a read, x written (interior)
+      vec_dot          x, y read (interior); the call returns the value to the host"""
+    import numpy as np
+    import torch
+
+    lib = te.capi.lib()
+    f0, f1 = solver.levels[0], solver.levels[1]
+    d0, d1 = solver.domains[0], solver.domains[1]
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    rng = np.random.default_rng(7)
+    out = []
+    for dt, w in ((te.TE_F64, 8), (te.TE_F32, 4)):
+        u = te.Vector.from_numpy(d0, rng.standard_normal(f0.padded_shape(1)), dtype=dt)
+        f = te.Vector(d0, 1, dt)
+        a = te.Vector.from_numpy(d0, rng.standard_normal(f0.padded_shape(1)), dtype=dt)
+        c = te.Vector.from_numpy(d1, rng.standard_normal(f1.padded_shape(1)), dtype=dt)
+        ci = te.Vector(d1, 1, dt)
+        i0 = f0.num_cells * w
+        i1 = f1.num_cells * w
+        p0 = f0.num_patches * f0.patch_stride(1) * w
+        p1 = f1.num_patches * f1.patch_stride(1) * w
+        g = _ghost_bytes(f0, w)
+        rs, ip = solver.restrictors[0], solver.interpolators[1]
+        calls = [
+            ("ghost_fill", g, lambda: solver.fillers[0].fillGhost(u)),
+            ("operator_apply", g + 2 * p0, lambda: solver.ops[0].apply(u, f)),
+            ("restrict", i0 + p1, lambda: te.capi.check(lib.te_restrict(rs.h, 1, dt, u.ptr, ci.ptr))),
+            ("interpolate", i1 + 2 * i0, lambda: ip.interpolate(c, u)),
+            ("vec_add_scaled", 3 * i0, lambda: u.addScaled(1e-3, a)),
+            ("vec_dot", 2 * i0, lambda: u.dot(a)),
+        ]
+        for name, nbytes, fn in calls:
+            times = []
+            for i in range(warm + reps):
+                flush.fill_(i & 0xFF)
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if i >= warm:
+                    times.append(e0.elapsed_time(e1) / 1000.0)
+            t = statistics.median(times)
+            gbs = nbytes / t / 1e9
+            out.append({"kernel": name, "dtype": "f64" if w == 8 else "f32", "us": round(1e6 * t, 2),
+                        "algorithmic_bytes": int(nbytes), "achieved_gbs": round(gbs, 1),
+                        "frac": round(gbs / hbm, 3)})
+    return {"level": f"{f0.num_patches} patches of {f0.ns[0]}^{f0.dim} (+ {f1.num_patches} coarse)",
+            "peak_gbs": hbm, "l2": "flushed before every call", "kernels": out}
 
 
 def replica_throughput(local_seconds, local_solves, device="cuda"):
@@ -382,6 +462,18 @@ def run_gpu(args):
     u1 = te.Vector(single.finest)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     stream = torch.cuda.current_stream()
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    if args.kernels:
+        if rank == 0:
+            lk = level_kernel_rooflines(te, served, hbm)
+            lk["peak_source"] = "measured" if peaks else "fallback"
+            print(json.dumps({"level_kernels": lk}), flush=True)
+        return
 
     def barrier():
         torch.cuda.synchronize()
@@ -471,12 +563,6 @@ def run_gpu(args):
     phases = sorted(acc_ph.items(), key=lambda x: -x[1])
     top_name, top_ms = phases[0]
     alg = _phase_bytes(top_name, blevels, 4)
-    peaks = {}
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except Exception:
-        pass
-    hbm = peaks.get("hbm_gbs", 6800.0)
     # DRAM bytes of one launch of the phase from an ncu capture of this workload (when recorded)
     traffic = None
     try:
@@ -492,6 +578,7 @@ def run_gpu(args):
     extra = not args.no_extra and not args.only_mixed and rank == 0
     c3 = config3_measure(te) if extra else None
     c4 = config4_measure(te) if extra else None
+    lk = level_kernel_rooflines(te, served, hbm) if extra else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -535,6 +622,7 @@ def run_gpu(args):
         "serving_stream": stream,
         "config3": c3,
         "config4": c4,
+        "level_kernels": lk,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

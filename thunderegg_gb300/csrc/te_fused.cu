@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(1024)
     vc_restrict_kernel(Layout F, Layout C, const int* __restrict__ by_orth, const int* __restrict__ copy_of,
                        const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
                        const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                       const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gstride,
+                       const GCall* __restrict__ calls, const int* __restrict__ side_code, int gstride,
                        const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse) {
   extern __shared__ __align__(16) unsigned char smraw[];
   T* G = reinterpret_cast<T*>(smraw);  // [2^D][2D][gstride]
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(1024)
   }
   __syncthreads();
   PlainAcc<T> acc{u, (long long)F.cs, 0};
-  side_ghosts_table<T, SCHEME>(acc, s_fp, NCH, slabs, calls, side_slab, ft, D, G, gstride);
+  side_ghosts_table<T, SCHEME>(acc, s_fp, NCH, slabs, calls, side_code, ft, D, G, gstride);
   __syncthreads();
   const T wD = T(1.0 / (1 << D));
   const int py = C.n1 + 2 * C.g;
@@ -231,7 +231,7 @@ template <class T, class TF, class TO, int KIND, int SCHEME>
 __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int ti_max, const int* __restrict__ parent, const int* __restrict__ porth,
                                const int8_t* __restrict__ ntype, int FS, const T* __restrict__ inv_tab,
                                const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                               const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gstride,
+                               const GCall* __restrict__ calls, const int* __restrict__ side_code, int gstride,
                                const int* __restrict__ plan_of_patch, const int* __restrict__ plan_mats,
                                const T* __restrict__ mats, const int* __restrict__ mat_off,
                                const T* __restrict__ inv_eig, const int* __restrict__ zero_mode, T scale,
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(1024) vc_post_kernel(Layout F, Layout C, int t
   dft_mat_ptrs<T>(F, plan, plan_mats, mats, mat_off, MT);
   InterpAcc<T> acc{A, uc, parent, porth, F, C};
   int pself[1] = {p};
-  side_ghosts_table<T, SCHEME>(acc, pself, 1, slabs, calls, side_slab, ft, D, G, gstride);
+  side_ghosts_table<T, SCHEME>(acc, pself, 1, slabs, calls, side_code, ft, D, G, gstride);
   __syncthreads();
   // f_copy with modifyRHSForInternalBoundaryConditions, sides in Side order
   const int side0 = D == 2 ? 4 : 20;
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(256)
     vc_corr_kernel(Layout F, Layout C, const int* __restrict__ parent, const int* __restrict__ porth,
                    const float* __restrict__ inv_tab, const float* __restrict__ coeff, FaceTable ft,
                    const GSlab* __restrict__ slabs, const GCall* __restrict__ calls,
-                   const int* __restrict__ side_slab, int gs, const float* __restrict__ A,
+                   const int* __restrict__ side_code, int gs, const float* __restrict__ A,
                    const float* __restrict__ uc, float* __restrict__ corr) {
   const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long total = (long long)F.P * 2 * DIM * gs;
@@ -316,13 +316,12 @@ __global__ void __launch_bounds__(256)
   const int side0 = DIM == 2 ? 4 : 20;
   const FaceGeom& g = ft.f[side0 + s];
   if (r >= g.nt[0] * g.nt[1]) return;
-  const int si = side_slab[p * 2 * DIM + s];
+  const int code = side_code[p * 2 * DIM + s];
   float c = 0.f;
-  if (si >= 0) {
+  if (code != -1) {
     InterpAcc<float> acc{A, uc, parent, porth, F, C};
-    const GSlab sl = slabs[si];
     const int i = r % g.nt[0], j = r / g.nt[0];
-    const float gv = gather_ghost<float, SCHEME>(acc, p, sl, g, ft, calls, DIM, i, j, 0.f);
+    const float gv = side_ghost<float, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, i, j);
     const int coord = upr ? F.n(a) - 1 : 0;
     int x, y, z;
     if (a == 0) {
@@ -352,7 +351,7 @@ __global__ void __launch_bounds__(256)
     vc_corr_kernel_n(int P, const int* __restrict__ parent, const int* __restrict__ porth,
                      const float* __restrict__ inv_tab, const float* __restrict__ coeff, FaceTable ft,
                      const GSlab* __restrict__ slabs, const GCall* __restrict__ calls,
-                     const int* __restrict__ side_slab, const float* __restrict__ A, const float* __restrict__ uc,
+                     const int* __restrict__ side_code, const float* __restrict__ A, const float* __restrict__ uc,
                      float* __restrict__ corr) {
   constexpr int NF = DIM == 3 ? NN * NN : NN;
   constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
@@ -361,15 +360,13 @@ __global__ void __launch_bounds__(256)
   const int r = (int)(e % NF);
   const int s = (int)((e / NF) % (2 * DIM));
   const int p = (int)(e / (NF * 2 * DIM));
-  const int si = side_slab[p * 2 * DIM + s];
+  const int code = side_code[p * 2 * DIM + s];
   float c = 0.f;
-  if (si >= 0) {
+  if (code != -1) {
     const int a = s >> 1, upr = s & 1;
-    const int side0 = DIM == 2 ? 4 : 20;
     const InterpAccN<float, DIM, NN> acc{A, uc, parent, porth};
-    const GSlab sl = slabs[si];
     const int i = r % NN, j = r / NN;
-    const float gv = gather_ghost<float, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, i, j, 0.f);
+    const float gv = side_ghost<float, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, i, j);
     const int edge = upr ? NN - 1 : 0;
     int x, y, z;
     if (a == 0) {
@@ -411,17 +408,6 @@ static int gstride_of(const Layout& L) {
   }
   return m;
 }
-static int threads_for(const Layout& L) {
-  int best = 32;
-  for (int a = 0; a < L.D; a++) {
-    int n = L.n(a);
-    int ti = n % 8 == 0 ? 8 : (n % 4 == 0 ? 4 : (n % 2 == 0 ? 2 : 1));
-    best = std::max(best, (L.interior() / n) * (n / ti));
-  }
-  best = (best + 31) / 32 * 32;
-  return std::min(best, 256);
-}
-
 template <class K>
 static void raise_smem(K kern, size_t bytes) {
   if (bytes > 40 * 1024)  // leave room for the static shared memory
@@ -480,7 +466,7 @@ static void vc_restrict_t(const te_restrictor* r, const te_operator* op, const T
   int threads = C.P >= 2 * 152 ? 256 : 1024;
   kern<<<C.P, threads, smem, s>>>(F, C, r->by_orth.p, r->copy_of.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(),
                                op->neumann, coeff_of<T>(op), g->faces, g->d_slabs.p, g->d_calls.p,
-                               g->d_side_slab.p, gs, u, f, coarse);
+                               g->d_side_code.p, gs, u, f, coarse);
   count_launch();
   TE_LAUNCH_CHECK();
 }
@@ -524,7 +510,7 @@ static void vc_post_t(const te_patch_solver* ps, const te_interpolator* in, cons
   dft_launch_shape(F, ti_max, threads);
   kern<<<F.P, threads, smem, s>>>(F, C, ti_max, in->parent.p, in->orth.p, d->d_nbr_type.p, d->F,
                                           d->template inv<T>(), coeff_of<T>(op), g->faces, g->d_slabs.p,
-                                          g->d_calls.p, g->d_side_slab.p, gs, ps->plan_of_patch.p,
+                                          g->d_calls.p, g->d_side_code.p, gs, ps->plan_of_patch.p,
                                           ps->plan_mats.p, mats_of<T>(ps), ps->mat_off.p, ie_of<T>(ps),
                                           ps->zero_mode.p, (T)dft_scale(F), A, uc, f, out);
   count_launch();
@@ -565,7 +551,7 @@ static void vc_corr_t(const te_patch_solver* ps, const te_interpolator* in, cons
   const bool cube = F.g == 1 && F.n1 == F.n0 && (F.D == 2 || F.n2 == F.n0);
   auto fixed = [&](auto kn) {
     kn<<<blocks, threads, 0, s>>>(F.P, in->parent.p, in->orth.p, d->template inv<float>(), op->coeffs_f.p, g->faces,
-                                  g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, A, uc, corr);
+                                  g->d_slabs.p, g->d_calls.p, g->d_side_code.p, A, uc, corr);
   };
   bool done = false;
   if (cube && F.D == 2 && SCHEME != TE_GHOST_TRILINEAR) {
@@ -583,7 +569,7 @@ static void vc_corr_t(const te_patch_solver* ps, const te_interpolator* in, cons
   if (!done) {
     auto kern = F.D == 2 ? vc_corr_kernel<KIND, SCHEME, 2> : vc_corr_kernel<KIND, SCHEME, 3>;
     kern<<<blocks, threads, 0, s>>>(F, C, in->parent.p, in->orth.p, d->template inv<float>(), op->coeffs_f.p,
-                                    g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, gs, A, uc, corr);
+                                    g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_code.p, gs, A, uc, corr);
   }
   count_launch();
   TE_LAUNCH_CHECK();

@@ -13,6 +13,7 @@
 //   BiLinearGhostFiller.cpp:40-264,   BiQuadraticGhostFiller.cpp:34-334,
 //   TriLinearGhostFiller.cpp:28-370.
 
+#include <algorithm>
 #include <array>
 #include <cstring>
 
@@ -120,9 +121,79 @@ __global__ void __launch_bounds__(GHOST_THREADS)
   }
 }
 
+// ghost_fill_kernel for one ghost layer with the work of a patch spread over
+// the whole CTA: every thread takes whole ghost values of any side of NP
+// patches (the sides in side_code), then the remaining slabs (edges,
+// corners) follow slab by slab when `other` is set.  Slabs write disjoint
+// ghost cells and read only interior cells, so they need no order.
+template <class T, int SCHEME>
+__global__ void __launch_bounds__(GHOST_THREADS)
+    ghost_fill_sides_kernel(Layout L, int nc, FaceTable ft, const GSlab* __restrict__ slabs,
+                            const GCall* __restrict__ calls, const int* __restrict__ slab_start,
+                            const int* __restrict__ side_code, int NP, int gmax, int other, T* u) {
+  const int D = L.D;
+  const int side0 = D == 2 ? 4 : 20;
+  const int p0 = blockIdx.x * NP;
+  const long long ps = L.pstride(nc);
+  const int per_side = nc * gmax, per_patch = 2 * D * per_side;
+  for (int e = threadIdx.x; e < NP * per_patch; e += blockDim.x) {
+    const int q = e / per_patch, rem = e - q * per_patch, sd = rem / per_side, r2 = rem - sd * per_side;
+    const int c = r2 / gmax, r = r2 - c * gmax;
+    const int p = p0 + q;
+    if (p >= L.P) break;
+    const FaceGeom& g = ft.f[side0 + sd];
+    if (r >= g.nt[0] * g.nt[1]) continue;
+    const int code = side_code[p * 2 * D + sd];
+    if (code == -1) continue;
+    const int i = r % g.nt[0], j = r / g.nt[0];
+    PlainAcc<T> acc{u, ps, (long long)c * L.cs};
+    u[p * ps + (long long)c * L.cs + g.gbase + i * g.tstride[0] + j * g.tstride[1]] =
+        side_ghost<T, SCHEME>(acc, p, sd, code, slabs, calls, ft, D, i, j);
+  }
+  if (!other) return;
+  for (int q = 0; q < NP; q++) {
+    const int p = p0 + q;
+    if (p >= L.P) return;
+    for (int s = slab_start[p]; s < slab_start[p + 1]; s++) {
+      const GSlab sl = slabs[s];
+      if (sl.M == D - 1 && sl.zero) continue;  // filled above
+      const FaceGeom& g = ft.f[sl.M == D - 1 ? side0 + sl.face : (sl.M == 0 ? sl.face : 8 + sl.face)];
+      const int ni = g.nt[0], per_c = ni * g.nt[1];
+      for (int e = threadIdx.x; e < per_c * nc; e += blockDim.x) {
+        const int c = e / per_c, t = e - c * per_c, i = t % ni, j = t / ni;
+        T* gp = u + p * ps + (long long)c * L.cs + g.gbase + i * g.tstride[0] + j * g.tstride[1];
+        PlainAcc<T> acc{u, ps, (long long)c * L.cs};
+        *gp = gather_ghost<T, SCHEME>(acc, p, sl, g, ft, calls, D, i, j, sl.zero ? T(0) : *gp);
+      }
+    }
+  }
+}
+
+template <class T, int SCHEME>
+static void launch_fill_sides(const te_ghost_filler* gf, int nc, T* u, cudaStream_t s) {
+  const Layout& L = gf->dom->lay;
+  int gmax = 1;
+  for (int a = 0; a < L.D; a++) gmax = std::max(gmax, L.interior() / L.n(a));
+  const int per_patch = 2 * L.D * nc * gmax;
+  const int NP = std::max(1, GHOST_THREADS / per_patch);
+  ghost_fill_sides_kernel<T, SCHEME><<<(L.P + NP - 1) / NP, GHOST_THREADS, 0, s>>>(
+      L, nc, gf->faces, gf->d_slabs.p, gf->d_calls.p, gf->d_slab_start.p, gf->d_side_code.p, NP, gmax,
+      gf->other_slabs ? 1 : 0, u);
+}
+
 template <class T>
 static void launch_fill(const te_ghost_filler* gf, int nc, T* u, cudaStream_t s) {
   const Layout& L = gf->dom->lay;
+  if (L.g == 1 && !generic_level_kernels()) {
+    switch (gf->scheme) {
+      case TE_GHOST_BILINEAR: launch_fill_sides<T, TE_GHOST_BILINEAR>(gf, nc, u, s); break;
+      case TE_GHOST_BIQUADRATIC: launch_fill_sides<T, TE_GHOST_BIQUADRATIC>(gf, nc, u, s); break;
+      default: launch_fill_sides<T, TE_GHOST_TRILINEAR>(gf, nc, u, s);
+    }
+    count_launch();
+    TE_LAUNCH_CHECK();
+    return;
+  }
   dim3 grid(L.P), block(GHOST_THREADS);
   switch (gf->scheme) {
     case TE_GHOST_BILINEAR:
@@ -243,13 +314,22 @@ int te_ghost_filler_create(const te_domain* d, int scheme, int fill_type, te_gho
         }
     }
     g->h_slab_start[P] = (int)g->h_slabs.size();
-    std::vector<int> side_slab((size_t)P * 2 * D, -1);
+    std::vector<int> side_code((size_t)P * 2 * D, -1);
     for (size_t k = 0; k < g->h_slabs.size(); k++) {
       const GSlab& s = g->h_slabs[k];
-      if (s.M == D - 1 && s.zero) side_slab[(size_t)s.patch * 2 * D + s.face] = (int)k;
+      if (!(s.M == D - 1 && s.zero)) {
+        g->other_slabs = true;
+        continue;
+      }
+      int code = -2 - (int)k;
+      if (s.own_type == TE_NBR_NORMAL && s.ncalls == 1) {
+        const GCall& c = hc[s.call0];
+        if (c.type == TE_NBR_NORMAL && c.src_face == (s.face ^ 1)) code = c.src;
+      }
+      side_code[(size_t)s.patch * 2 * D + s.face] = code;
     }
     cudaStream_t st = d->stream;
-    g->d_side_slab.upload(side_slab, st);
+    g->d_side_code.upload(side_code, st);
     g->d_slabs.upload(g->h_slabs, st);
     g->d_calls.upload(hc, st);
     g->d_slab_start.upload(g->h_slab_start, st);

@@ -56,7 +56,11 @@ struct te_ghost_filler {
   te::DevBuf<te::GSlab> d_slabs;
   te::DevBuf<te::GCall> d_calls;
   te::DevBuf<int> d_slab_start;
-  te::DevBuf<int> d_side_slab;  // [P * 2D]: the side slab with a neighbour, or -1
+  // [P * 2D] per patch side: >= 0 the ghosts are a plain copy of that patch's
+  // face (a Normal neighbour and no own term), -1 no neighbour, <= -2 the
+  // side's slab is -2 - code
+  te::DevBuf<int> d_side_code;
+  bool other_slabs = false;  // slabs beyond d_side_code (edges, corners, sides without a neighbour)
   te::FaceTable faces;
 };
 

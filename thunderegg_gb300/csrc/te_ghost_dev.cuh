@@ -177,15 +177,29 @@ __device__ __forceinline__ T gather_ghost(const Acc& acc, int p, const GSlab& sl
   return v;
 }
 
+// Side ghost (i, j) of patch p on side s, from the side's code (te_ghost_filler::
+// d_side_code, not -1): a plain copy of the neighbour's face cells, or the
+// side's slab.  The copy is the value gather_ghost gives for a slab whose one
+// call is a Normal neighbour's and that has no own term.
+template <class T, int SCHEME, class Acc>
+__device__ __forceinline__ T side_ghost(const Acc& acc, int p, int s, int code, const GSlab* __restrict__ slabs,
+                                        const GCall* __restrict__ calls, const FaceTable& ft, int D, int i,
+                                        int j) {
+  const int side0 = D == 2 ? 4 : 20;
+  if (code >= 0) return sv<T>(acc, code, ft.f[side0 + (s ^ 1)], 0, i, j);
+  const GSlab sl = slabs[-2 - code];
+  return gather_ghost<T, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, D, i, j, T(0));
+}
+
 // Face (side) ghosts of up to NP patches into shared memory,
 // G[(q * 2D + side) * gstride + j*nt0 + i] for patch slot q, for every side
-// with a neighbour; side_slab[p * 2D + side] names that side's slab (-1: none,
+// with a neighbour; side_code[p * 2D + side] is that side's code (-1: none,
 // the entry is left alone).  Every thread takes whole ghost values; there is
 // no barrier inside: the caller synchronises before reading G.
 template <class T, int SCHEME, class Acc>
 __device__ __forceinline__ void side_ghosts_table(const Acc& acc, const int* pq, int NP,
                                                   const GSlab* __restrict__ slabs, const GCall* __restrict__ calls,
-                                                  const int* __restrict__ side_slab, const FaceTable& ft, int D,
+                                                  const int* __restrict__ side_code, const FaceTable& ft, int D,
                                                   T* G, int gstride) {
   const int side0 = D == 2 ? 4 : 20;
   const int per = 2 * D * gstride;
@@ -195,10 +209,9 @@ __device__ __forceinline__ void side_ghosts_table(const Acc& acc, const int* pq,
     if (p < 0) continue;
     const FaceGeom& g = ft.f[side0 + s];
     if (r >= g.nt[0] * g.nt[1]) continue;
-    const int si = side_slab[p * 2 * D + s];
-    if (si < 0) continue;
-    const GSlab sl = slabs[si];
-    G[e] = gather_ghost<T, SCHEME>(acc, p, sl, g, ft, calls, D, r % g.nt[0], r / g.nt[0], T(0));
+    const int code = side_code[p * 2 * D + s];
+    if (code == -1) continue;
+    G[e] = side_ghost<T, SCHEME>(acc, p, s, code, slabs, calls, ft, D, r % g.nt[0], r / g.nt[0]);
   }
 }
 

@@ -144,6 +144,156 @@ __global__ void interpolate_kernel(Layout F, Layout C, int nc, const int* __rest
   }
 }
 
+// interpolate_kernel for cubic patches of NN cells with one ghost layer:
+// fine += the parent's coarse cell (DirectInterpolator, GMG/DirectInterpolator.h:
+// 40-91) with constant index arithmetic.  A thread loads all of its cells
+// (fine and coarse) before it stores.
+template <class T, int DIM, int NN>
+__global__ void __launch_bounds__(256)
+    interpolate_n_kernel(int nc, const int* __restrict__ parent, const int* __restrict__ orth,
+                         const T* __restrict__ coarse, T* __restrict__ fine) {
+  constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
+  constexpr int NI = DIM == 3 ? NN * NN * NN : NN * NN;
+  constexpr int PER = (NI + 255) / 256;
+  const int fp = blockIdx.x;
+  const int o = orth[fp];
+  const T* cv = coarse + (long long)parent[fp] * CS * nc;
+  T* fv = fine + (long long)fp * CS * nc;
+  const int ox = (o >= 0 && (o & 1)) ? NN : 0, oy = (o >= 0 && (o & 2)) ? NN : 0,
+            oz = (o >= 0 && (o & 4)) ? NN : 0;
+  for (int c = 0; c < nc; c++) {
+    T a[PER], b[PER];
+#pragma unroll
+    for (int r = 0; r < PER; r++) {
+      const int e = threadIdx.x + r * 256;
+      if (NI % 256 == 0 || e < NI) {
+        const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
+        const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
+        const int kc = o < 0 ? k
+                             : ((x + ox) >> 1) + 1 + (((y + oy) >> 1) + 1) * SY +
+                                   (DIM == 3 ? (((z + oz) >> 1) + 1) * SZ : 0);
+        a[r] = fv[(long long)c * CS + k];
+        b[r] = cv[(long long)c * CS + kc];
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < PER; r++) {
+      const int e = threadIdx.x + r * 256;
+      if (NI % 256 == 0 || e < NI) {
+        const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
+        const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
+        fv[(long long)c * CS + k] = a[r] + b[r];
+      }
+    }
+  }
+}
+
+// restrict_kernel turned around for complete levels of cubic NN patches
+// without ghost extrapolation: one CTA per FINE patch writes its orthant of
+// the parent (restrictToCoarserParent, GMG/LinearRestrictor.h:101-128: the
+// average of the 2^D fine cells, summed in the reference's z, y, x order) or,
+// for a patch that is its own parent, copies its interior (copyToParent,
+// :129-147).  The coarse ghost ring is zero: the orthant-0 child (or the
+// copied patch) writes it.
+template <class T, int DIM, int NN>
+__global__ void __launch_bounds__(256)
+    restrict_n_kernel(int nc, const int* __restrict__ fparent, const int* __restrict__ forth,
+                      const T* __restrict__ fine, T* __restrict__ coarse) {
+  constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
+  constexpr int H = NN / 2;
+  constexpr int NQ = DIM == 3 ? H * H * H : H * H;  // coarse cells of one orthant
+  constexpr int NI = DIM == 3 ? NN * NN * NN : NN * NN;
+  constexpr int RING = CS - NI;
+  const int fp = blockIdx.x;
+  const int o = forth[fp];
+  const T* fv = fine + (long long)fp * CS * nc;
+  T* cv = coarse + (long long)fparent[fp] * CS * nc;
+  const T wD = T(1.0 / (1 << DIM));
+  for (int c = 0; c < nc; c++) {
+    const T* fc = fv + (long long)c * CS;
+    T* cc = cv + (long long)c * CS;
+    if (o < 0) {
+      constexpr int PER = (NI + 255) / 256;
+      T v[PER];
+#pragma unroll
+      for (int r = 0; r < PER; r++) {
+        const int e = threadIdx.x + r * 256;
+        if (NI % 256 == 0 || e < NI) {
+          const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
+          v[r] = fc[(x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0)];
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < PER; r++) {
+        const int e = threadIdx.x + r * 256;
+        if (NI % 256 == 0 || e < NI) {
+          const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
+          cc[(x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0)] = v[r];
+        }
+      }
+    } else {
+      const int ox = (o & 1) ? H : 0, oy = (o & 2) ? H : 0, oz = (o & 4) ? H : 0;
+      constexpr int PER = (NQ + 255) / 256;
+      T v[PER];
+#pragma unroll
+      for (int r = 0; r < PER; r++) {
+        const int e = threadIdx.x + r * 256;
+        if (NQ % 256 == 0 || e < NQ) {
+          const int x = e % H, y = (e / H) % H, z = DIM == 3 ? e / (H * H) : 0;
+          const int k = (2 * x + 1) + (2 * y + 1) * SY + (DIM == 3 ? (2 * z + 1) * SZ : 0);
+          T s = T(0);
+#pragma unroll
+          for (int dz = 0; dz < (DIM == 3 ? 2 : 1); dz++)
+#pragma unroll
+            for (int dy = 0; dy < 2; dy++)
+#pragma unroll
+              for (int dx = 0; dx < 2; dx++) s += fc[k + dx + dy * SY + dz * SZ] * wD;
+          v[r] = s;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < PER; r++) {
+        const int e = threadIdx.x + r * 256;
+        if (NQ % 256 == 0 || e < NQ) {
+          const int x = e % H, y = (e / H) % H, z = DIM == 3 ? e / (H * H) : 0;
+          cc[(x + ox + 1) + (y + oy + 1) * SY + (DIM == 3 ? (z + oz + 1) * SZ : 0)] = v[r];
+        }
+      }
+    }
+    if (o <= 0) {
+      // ghost ring: 2D rows 0 and SY-1, then the end cells of rows 1..NN; 3D planes
+      // 0 and SY-1, then the 2D ring of planes 1..NN
+      for (int e = threadIdx.x; e < RING; e += 256) {
+        int k;
+        if (DIM == 2) {
+          if (e < 2 * SY) {
+            k = e < SY ? e : (SY - 1) * SY + (e - SY);
+          } else {
+            const int r2 = e - 2 * SY;
+            k = (1 + (r2 >> 1)) * SY + ((r2 & 1) ? SY - 1 : 0);
+          }
+        } else {
+          constexpr int PL = SY * SY, R2 = 2 * SY + 2 * NN;
+          if (e < 2 * PL) {
+            k = e < PL ? e : (SY - 1) * PL + (e - PL);
+          } else {
+            const int q = e - 2 * PL, z = 1 + q / R2, r = q % R2;
+            int k2;
+            if (r < 2 * SY) {
+              k2 = r < SY ? r : (SY - 1) * SY + (r - SY);
+            } else {
+              const int r2 = r - 2 * SY;
+              k2 = (1 + (r2 >> 1)) * SY + ((r2 & 1) ? SY - 1 : 0);
+            }
+            k = z * PL + k2;
+          }
+        }
+        cc[k] = T(0);
+      }
+    }
+  }
+}
+
 // Cycle::restrict fused: r = f - A u on the fine level (Poisson or VarPoisson
 // star stencil, boundary ghosts -u / +u as enforceBoundaryConditions) is
 // formed in registers and averaged straight into the coarse cell
@@ -370,6 +520,22 @@ void residual_restrict(const te_restrictor* r, const te_operator* op, int nc, in
 
 void restrict_level(const te_restrictor* r, int nc, int dtype, const void* fine, void* coarse, cudaStream_t s) {
   const Layout &F = r->fine->lay, &C = r->coarse->lay;
+  if (r->complete && !r->extrapolate && F.n0 == C.n0 && F.n1 == C.n1 && F.n2 == C.n2 && F.P > 0) {
+    const bool fixed = with_cubic_size(F, [&](auto dim, auto nn) {
+      constexpr int DIM = decltype(dim)::value, NN = decltype(nn)::value;
+      if (dtype == TE_F64)
+        restrict_n_kernel<double, DIM, NN><<<F.P, 256, 0, s>>>(nc, r->fine_parent.p, r->fine_orth.p,
+                                                              (const double*)fine, (double*)coarse);
+      else
+        restrict_n_kernel<float, DIM, NN><<<F.P, 256, 0, s>>>(nc, r->fine_parent.p, r->fine_orth.p,
+                                                             (const float*)fine, (float*)coarse);
+    });
+    if (fixed) {
+      count_launch();
+      TE_LAUNCH_CHECK();
+      return;
+    }
+  }
   if (dtype == TE_F64)
     restrict_kernel<double><<<C.P, 256, 0, s>>>(F, C, nc, r->child_start.p, r->child.p, r->child_orth.p,
                                                 r->child_corner_nbr.p, r->extrapolate, (const double*)fine,
@@ -385,6 +551,22 @@ void restrict_level(const te_restrictor* r, int nc, int dtype, const void* fine,
 void interpolate_level(const te_interpolator* in, int nc, int dtype, const void* coarse, void* fine,
                        cudaStream_t s) {
   const Layout &F = in->fine->lay, &C = in->coarse->lay;
+  if (F.n0 == C.n0 && F.n1 == C.n1 && F.n2 == C.n2 && F.P > 0) {
+    const bool fixed = with_cubic_size(F, [&](auto dim, auto nn) {
+      constexpr int DIM = decltype(dim)::value, NN = decltype(nn)::value;
+      if (dtype == TE_F64)
+        interpolate_n_kernel<double, DIM, NN><<<F.P, 256, 0, s>>>(nc, in->parent.p, in->orth.p,
+                                                                 (const double*)coarse, (double*)fine);
+      else
+        interpolate_n_kernel<float, DIM, NN><<<F.P, 256, 0, s>>>(nc, in->parent.p, in->orth.p,
+                                                                (const float*)coarse, (float*)fine);
+    });
+    if (fixed) {
+      count_launch();
+      TE_LAUNCH_CHECK();
+      return;
+    }
+  }
   if (dtype == TE_F64)
     interpolate_kernel<double><<<F.P, 256, 0, s>>>(F, C, nc, in->parent.p, in->orth.p, (const double*)coarse,
                                                    (double*)fine);

@@ -5,10 +5,12 @@
 
 #include <atomic>
 #include <cstdint>
+#include <cstdlib>
 #include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "te_gpu.h"
@@ -98,6 +100,39 @@ struct Layout {
   __host__ __device__ int n(int a) const { return a == 0 ? n0 : (a == 1 ? n1 : n2); }
   __host__ __device__ int stride(int a) const { return a == 0 ? 1 : (a == 1 ? sy : sz); }
 };
+
+// Level kernels with constant index arithmetic exist for cubic patches with
+// one ghost layer of 8, 16, 32 or 64 cells (2D) and 8 or 16 cells (3D).
+// with_cubic_size calls fn(IntC<DIM>(), IntC<NN>()) for such a level and
+// returns true; otherwise it returns false and the caller launches the
+// general kernel.  TE_GENERIC_LEVEL_KERNELS=1 keeps the general kernels.
+template <int V>
+using IntC = std::integral_constant<int, V>;
+inline bool generic_level_kernels() {
+  static const bool on = [] {
+    const char* e = getenv("TE_GENERIC_LEVEL_KERNELS");
+    return e && e[0] == '1';
+  }();
+  return on;
+}
+template <class Fn>
+bool with_cubic_size(const Layout& L, Fn&& fn) {
+  if (generic_level_kernels() || L.g != 1 || L.n0 != L.n1 || (L.D == 3 && L.n1 != L.n2)) return false;
+  if (L.D == 2) {
+    switch (L.n0) {
+      case 8: fn(IntC<2>(), IntC<8>()); return true;
+      case 16: fn(IntC<2>(), IntC<16>()); return true;
+      case 32: fn(IntC<2>(), IntC<32>()); return true;
+      case 64: fn(IntC<2>(), IntC<64>()); return true;
+    }
+  } else if (L.D == 3) {
+    switch (L.n0) {
+      case 8: fn(IntC<3>(), IntC<8>()); return true;
+      case 16: fn(IntC<3>(), IntC<16>()); return true;
+    }
+  }
+  return false;
+}
 
 inline int num_slots(int D) { return D == 2 ? 8 : 26; }
 inline int sum_of_faces(int D, int M) {

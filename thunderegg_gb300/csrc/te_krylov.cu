@@ -431,7 +431,7 @@ template <int KIND, int SCHEME, int DIM, int NN>
 __global__ void __launch_bounds__(256)
     apply_df_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const float2* __restrict__ inv_df,
                     int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                    const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gs,
+                    const GCall* __restrict__ calls, const int* __restrict__ side_code, int gs,
                     const float* __restrict__ u, DV f) {
   extern __shared__ df64 G[];  // [2D][gs]
   __shared__ int has[6];
@@ -452,10 +452,9 @@ __global__ void __launch_bounds__(256)
     const int s = e / gs, r = e % gs;
     const FaceGeom& gf = ft.f[side0 + s];
     if (r >= gf.nt[0] * gf.nt[1]) continue;
-    const int si = side_slab[p * 2 * DIM + s];
-    if (si < 0) continue;
-    const GSlab sl = slabs[si];
-    G[e] = gather_ghost<df64, SCHEME>(acc, p, sl, gf, ft, calls, DIM, r % gf.nt[0], r / gf.nt[0], df64(0.f, 0.f));
+    const int code = side_code[p * 2 * DIM + s];
+    if (code == -1) continue;
+    G[e] = side_ghost<df64, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, r % gf.nt[0], r / gf.nt[0]);
   }
   if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
   const float* up = u + (long long)p * cs;
@@ -518,7 +517,7 @@ template <int KIND, int SCHEME, int DIM, int NN, int NV>
 __global__ void __launch_bounds__(256)
     apply_dots_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const float2* __restrict__ inv_df,
                       int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                      const GCall* __restrict__ calls, const int* __restrict__ side_slab, int gs,
+                      const GCall* __restrict__ calls, const int* __restrict__ side_code, int gs,
                       const float* __restrict__ u, DV f, CV w, Batch bt, const int* __restrict__ patch_solve,
                       double* part, unsigned int* counter, double* S, int slot0, int finalize_kind) {
   extern __shared__ df64 G[];  // [2D][gs]
@@ -540,11 +539,9 @@ __global__ void __launch_bounds__(256)
   const F32Acc acc{u, (long long)CS};
   for (int e = threadIdx.x; e < 2 * DIM * NF; e += blockDim.x) {
     const int s = e / NF, r = e % NF;
-    const int si = side_slab[p * 2 * DIM + s];
-    if (si < 0) continue;
-    const GSlab sl = slabs[si];
-    G[s * gs + r] = gather_ghost<df64, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, r % NN, r / NN,
-                                               df64(0.f, 0.f));
+    const int code = side_code[p * 2 * DIM + s];
+    if (code == -1) continue;
+    G[s * gs + r] = side_ghost<df64, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, r % NN, r / NN);
   }
   if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
   const float* up = u + (long long)p * CS;
@@ -669,7 +666,7 @@ static void apply_df_launch(const te_operator* A, const float* u, DV f, cudaStre
   if (smem > 40 * 1024)
     TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff,
-                               g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, gs, u, f);
+                               g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_code.p, gs, u, f);
   count_launch();
   TE_LAUNCH_CHECK();
 }
@@ -831,7 +828,7 @@ static void apply_dots_launch(const te_operator* A, KrylovWork& W, const float* 
   if (smem > 40 * 1024)
     TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff, g->faces,
-                               g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, gs, u, f, w, W.batch(),
+                               g->d_slabs.p, g->d_calls.p, g->d_side_code.p, gs, u, f, w, W.batch(),
                                W.patch_solve.p, W.part_p.p, W.counter.p, W.S.p, slot0, fin);
   count_launch();
   TE_LAUNCH_CHECK();

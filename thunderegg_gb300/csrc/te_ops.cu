@@ -147,27 +147,88 @@ __global__ void modify_rhs_kernel(Layout L, int nc, const int8_t* __restrict__ n
   }
 }
 
+// apply_kernel for cubic patches of NN cells with one ghost layer: the same
+// per-cell arithmetic with constant strides; a thread loads all of its cells'
+// stencils before it stores, so each thread keeps several loads in flight.
+template <class T, int KIND, int DIM, int SY, int SZ>
+__device__ __forceinline__ T stencil_n(const T* u, const T* c, int k, const T* inv) {
+  T r = T(0);
+#pragma unroll
+  for (int a = 0; a < DIM; a++) {
+    const int st = a == 0 ? 1 : (a == 1 ? SY : SZ);
+    T lo = u[k - st], mid = u[k], hi = u[k + st];
+    if (KIND == 0) {
+      r += ((hi - T(2) * mid) + lo) * inv[a];
+    } else {
+      T cl = c[k - st], cm = c[k], cu = c[k + st];
+      r += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
+    }
+  }
+  return r;
+}
+template <class T, int KIND, int DIM, int NN>
+__global__ void __launch_bounds__(256)
+    apply_n_kernel(Layout L, int nc, const int8_t* __restrict__ ntype, int F, const T* __restrict__ sp,
+                   int neumann, const T* __restrict__ coeff, T* u, T* __restrict__ f) {
+  constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
+  constexpr int PER = (CS + 255) / 256;
+  const int p = blockIdx.x;
+  T* up = u + (long long)p * CS * nc;
+  T* fp = f + (long long)p * CS * nc;
+  const T* cp = KIND ? coeff + (long long)p * CS : nullptr;
+  enforce_bc<T>(L, ntype, F, p, nc, neumann != 0, false, up);
+  __syncthreads();
+  T inv[DIM];
+#pragma unroll
+  for (int a = 0; a < DIM; a++) inv[a] = sp[(size_t)p * 6 + (KIND ? 3 : 0) + a];
+  for (int c = 0; c < nc; c++) {
+    const T* uc = up + (long long)c * CS;
+    T v[PER];
+#pragma unroll
+    for (int r = 0; r < PER; r++) {
+      const int k = threadIdx.x + r * 256;
+      v[r] = T(0);
+      if (k < CS) {
+        const int x = k % SY, y = (k / SY) % SY, z = DIM == 3 ? k / SZ : 1;
+        if (x >= 1 && x <= NN && y >= 1 && y <= NN && z >= 1 && z <= NN)
+          v[r] = stencil_n<T, KIND, DIM, SY, SZ>(uc, cp, k, inv);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < PER; r++) {
+      const int k = threadIdx.x + r * 256;
+      if (k < CS) fp[(long long)c * CS + k] = v[r];
+    }
+  }
+}
+template <class T, int KIND>
+static void launch_apply(const te_operator* op, int nc, const T* inv, const T* coeff, int neumann, T* u, T* f,
+                         cudaStream_t s) {
+  const te_domain* d = op->dom;
+  const Layout& L = d->lay;
+  const bool fixed = with_cubic_size(L, [&](auto dim, auto nn) {
+    apply_n_kernel<T, KIND, decltype(dim)::value, decltype(nn)::value>
+        <<<L.P, 256, 0, s>>>(L, nc, d->d_nbr_type.p, d->F, inv, neumann, coeff, u, f);
+  });
+  if (!fixed) apply_kernel<T, KIND><<<L.P, 256, 0, s>>>(L, nc, d->d_nbr_type.p, d->F, inv, neumann, coeff, u, f);
+  count_launch();
+  TE_LAUNCH_CHECK();
+}
+
 void operator_apply(const te_operator* op, int nc, int dtype, void* u, void* f, cudaStream_t s) {
   const te_domain* d = op->dom;
   ghost_fill(op->gf, nc, dtype, u, s);
-  dim3 grid(d->lay.P), block(256);
   if (dtype == TE_F64) {
     if (op->kind == 0)
-      apply_kernel<double, 0><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv.p,
-                                                      op->neumann, nullptr, (double*)u, (double*)f);
+      launch_apply<double, 0>(op, nc, d->d_inv.p, nullptr, op->neumann, (double*)u, (double*)f, s);
     else
-      apply_kernel<double, 1><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv.p, 0,
-                                                      op->coeffs.p, (double*)u, (double*)f);
+      launch_apply<double, 1>(op, nc, d->d_inv.p, op->coeffs.p, 0, (double*)u, (double*)f, s);
   } else {
     if (op->kind == 0)
-      apply_kernel<float, 0><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv_f.p,
-                                                     op->neumann, nullptr, (float*)u, (float*)f);
+      launch_apply<float, 0>(op, nc, d->d_inv_f.p, nullptr, op->neumann, (float*)u, (float*)f, s);
     else
-      apply_kernel<float, 1><<<grid, block, 0, s>>>(d->lay, nc, d->d_nbr_type.p, d->F, d->d_inv_f.p, 0,
-                                                     op->coeffs_f.p, (float*)u, (float*)f);
+      launch_apply<float, 1>(op, nc, d->d_inv_f.p, op->coeffs_f.p, 0, (float*)u, (float*)f, s);
   }
-  count_launch();
-  TE_LAUNCH_CHECK();
 }
 
 // ---------------------------------------------------------------------------
@@ -224,7 +285,6 @@ __global__ void __launch_bounds__(1024) dft_kernel(Layout L, int ti_max, const i
   const SmemLay S = smem_lay(L);
   const int p = blockIdx.x;
   const int N = L.interior();
-  const int D = L.D;
   T* A = sm;
   T* B = A + S.size;
   const long long ps = L.pstride(1);
@@ -399,18 +459,6 @@ __global__ void __launch_bounds__(BCG_THREADS)
 static size_t dft_smem(const Layout& L, int tsize) {
   SmemLay S = smem_lay(L);
   return ((size_t)S.mats + smem_mat_elems(L)) * tsize;
-}
-
-static int dft_threads(const Layout& L) {
-  int best = 32;
-  for (int a = 0; a < L.D; a++) {
-    int n = L.n(a);
-    int ti = n % 8 == 0 ? 8 : (n % 4 == 0 ? 4 : (n % 2 == 0 ? 2 : 1));
-    int tasks = (L.interior() / n) * (n / ti);
-    best = std::max(best, tasks);
-  }
-  best = (best + 31) / 32 * 32;
-  return std::min(best, 256);
 }
 
 template <class T>

@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
     vc_restrict_fine_kernel(const int* __restrict__ fparent, const int* __restrict__ forth,
                             const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
                             const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                            const GCall* __restrict__ calls, const int* __restrict__ side_slab,
+                            const GCall* __restrict__ calls, const int* __restrict__ side_code,
                             const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse) {
   using S = RShape<DIM, NN>;
   constexpr int NB = DIM == 3 ? 8 : 4;  // fine cells per thread
@@ -61,9 +61,9 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
   const PlainAcc<T> acc{u, (long long)S::CS, 0};
   for (int e = t; e < 2 * DIM * S::NF; e += S::NT) {
     const int s = e / S::NF, r = e % S::NF;
-    if (nt[s] < 0) continue;
-    const GSlab sl = slabs[side_slab[p * 2 * DIM + s]];
-    gbuf[e] = gather_ghost<T, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, DIM, r % NN, r / NN, T(0));
+    const int code = side_code[p * 2 * DIM + s];
+    if (code == -1) continue;
+    gbuf[e] = side_ghost<T, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, r % NN, r / NN);
   }
   // 1. the padded patch (its ghosts are replaced below)
   if ((S::CS * sizeof(T)) % 16 == 0) {
@@ -161,7 +161,7 @@ static void launch_fine(const te_restrictor* r, const te_operator* op, const T* 
   const T* coeff = KIND ? (const T*)op->coeff_ptr(sizeof(T) == 8 ? TE_F64 : TE_F32) : nullptr;
   vc_restrict_fine_kernel<T, TF, KIND, SCHEME, DIM, NN><<<fd->lay.P, S::NT, 0, s>>>(
       r->fine_parent.p, r->fine_orth.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(), op->neumann, coeff, g->faces,
-      g->d_slabs.p, g->d_calls.p, g->d_side_slab.p, u, f, coarse);
+      g->d_slabs.p, g->d_calls.p, g->d_side_code.p, u, f, coarse);
   count_launch();
   TE_LAUNCH_CHECK();
 }

@@ -61,28 +61,50 @@ __device__ __forceinline__ int interior_offset(const Layout& L, int e) {
 }
 
 template <class T, int OP>
+__device__ __forceinline__ T vec_op(T xv, T av, T bv, double alpha, double beta, double gamma) {
+  if (OP == OP_SET) xv = (T)alpha;
+  if (OP == OP_SCALE) xv *= (T)alpha;
+  if (OP == OP_SHIFT) xv += (T)alpha;
+  if (OP == OP_COPY) xv = av;
+  if (OP == OP_ADD) xv += av;
+  // reference: view += b_view * alpha  (Vector.h:495)
+  if (OP == OP_ADD_SCALED) xv += av * (T)alpha;
+  // view += a * alpha + b * beta  (Vector.h:507-511)
+  if (OP == OP_ADD_SCALED2) xv += av * (T)alpha + bv * (T)beta;
+  // view = view * alpha + b  (Vector.h:523)
+  if (OP == OP_SCALE_THEN_ADD) xv = xv * (T)alpha + av;
+  if (OP == OP_SCALE_THEN_ADD_SCALED) xv = xv * (T)alpha + av * (T)beta;
+  if (OP == OP_SCALE_THEN_ADD_SCALED2) xv = xv * (T)alpha + av * (T)beta + bv * (T)gamma;
+  return xv;
+}
+
+// Each thread takes VEC_UNROLL cells of a patch-component per round and
+// loads all of their operands before it computes, so several loads per thread
+// are in flight; x is read only by the operations that use it.
+constexpr int VEC_UNROLL = 4;
+template <class T, int OP>
 __global__ void vec_kernel(Layout L, int npc, T* x, const T* a, const T* b, double alpha, double beta,
                            double gamma) {
+  constexpr bool RX = OP != OP_SET && OP != OP_COPY;
+  constexpr bool RA = OP != OP_SET && OP != OP_SCALE && OP != OP_SHIFT;
+  constexpr bool RB = OP == OP_ADD_SCALED2 || OP == OP_SCALE_THEN_ADD_SCALED2;
   const int N = L.interior();
   for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    long long base = (long long)pc * L.cs;
-    for (int e = threadIdx.x; e < N; e += blockDim.x) {
-      long long k = base + interior_offset(L, e);
-      T xv = x[k];
-      if (OP == OP_SET) xv = (T)alpha;
-      if (OP == OP_SCALE) xv *= (T)alpha;
-      if (OP == OP_SHIFT) xv += (T)alpha;
-      if (OP == OP_COPY) xv = a[k];
-      if (OP == OP_ADD) xv += a[k];
-      // reference: view += b_view * alpha  (Vector.h:495)
-      if (OP == OP_ADD_SCALED) xv += a[k] * (T)alpha;
-      // view += a * alpha + b * beta  (Vector.h:507-511)
-      if (OP == OP_ADD_SCALED2) xv += a[k] * (T)alpha + b[k] * (T)beta;
-      // view = view * alpha + b  (Vector.h:523)
-      if (OP == OP_SCALE_THEN_ADD) xv = xv * (T)alpha + a[k];
-      if (OP == OP_SCALE_THEN_ADD_SCALED) xv = xv * (T)alpha + a[k] * (T)beta;
-      if (OP == OP_SCALE_THEN_ADD_SCALED2) xv = xv * (T)alpha + a[k] * (T)beta + b[k] * (T)gamma;
-      x[k] = xv;
+    const long long base = (long long)pc * L.cs;
+    for (int e0 = threadIdx.x; e0 < N; e0 += VEC_UNROLL * blockDim.x) {
+      long long kk[VEC_UNROLL];
+      T xs[VEC_UNROLL], as[VEC_UNROLL], bs[VEC_UNROLL];
+#pragma unroll
+      for (int r = 0; r < VEC_UNROLL; r++) {
+        const int e = e0 + r * blockDim.x;
+        kk[r] = e < N ? base + interior_offset(L, e) : -1;
+        xs[r] = RX && kk[r] >= 0 ? x[kk[r]] : T(0);
+        as[r] = RA && kk[r] >= 0 ? a[kk[r]] : T(0);
+        bs[r] = RB && kk[r] >= 0 ? b[kk[r]] : T(0);
+      }
+#pragma unroll
+      for (int r = 0; r < VEC_UNROLL; r++)
+        if (kk[r] >= 0) x[kk[r]] = vec_op<T, OP>(xs[r], as[r], bs[r], alpha, beta, gamma);
     }
   }
 }
@@ -179,19 +201,36 @@ __device__ double block_reduce(double v) {
 template <class T, int MODE>
 __global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double* partials,
                               unsigned int* counter, double* out) {
-  double acc = 0.0;
+  // VEC_UNROLL independent partial sums per thread (loads of a round issued
+  // together), combined in a fixed order: the result depends only on the
+  // level's layout and the launch shape
+  double acc[VEC_UNROLL];
+#pragma unroll
+  for (int r = 0; r < VEC_UNROLL; r++) acc[r] = 0.0;
   const int N = L.interior();
   for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    long long base = (long long)pc * L.cs;
-    for (int e = threadIdx.x; e < N; e += blockDim.x) {
-      long long k = base + interior_offset(L, e);
-      if (MODE == 0)
-        acc += (double)x[k] * (double)y[k];
-      else
-        acc = fmax((double)x[k], acc);
+    const long long base = (long long)pc * L.cs;
+    for (int e0 = threadIdx.x; e0 < N; e0 += VEC_UNROLL * blockDim.x) {
+      T xs[VEC_UNROLL], ys[VEC_UNROLL];
+#pragma unroll
+      for (int r = 0; r < VEC_UNROLL; r++) {
+        const int e = e0 + r * blockDim.x;
+        const long long k = e < N ? base + interior_offset(L, e) : -1;
+        xs[r] = k >= 0 ? x[k] : T(0);
+        ys[r] = MODE == 0 && k >= 0 ? y[k] : T(0);
+      }
+#pragma unroll
+      for (int r = 0; r < VEC_UNROLL; r++) {
+        if (MODE == 0)
+          acc[r] += (double)xs[r] * (double)ys[r];
+        else
+          acc[r] = fmax((double)xs[r], acc[r]);
+      }
     }
   }
-  double b = block_reduce<MODE == 1>(acc);
+  static_assert(VEC_UNROLL == 4, "the partial sums are combined as four");
+  double t = MODE == 0 ? (acc[0] + acc[1]) + (acc[2] + acc[3]) : fmax(fmax(acc[0], acc[1]), fmax(acc[2], acc[3]));
+  double b = block_reduce<MODE == 1>(t);
   __shared__ bool last;
   if (threadIdx.x == 0) {
     partials[blockIdx.x] = b;
@@ -377,7 +416,7 @@ int te_domain_create(const te_level_desc* desc, te_domain** out) {
       inv_df[2 * i + 1] = (float)(inv[i] - (double)h);
     }
     d->d_inv_df.upload(inv_df, st);
-    d->red_blocks = 152 * 2;
+    d->red_blocks = 152 * 8;
     d->d_partials.alloc(d->red_blocks);
     d->d_counter.alloc(1);
     TE_CUDA(cudaMemsetAsync(d->d_counter.p, 0, sizeof(unsigned int), st));
