@@ -10,11 +10,14 @@
 // runs as 3xTF32 (A_hi B_hi + A_hi B_lo + A_lo B_hi, FP32 accumulation in
 // TMEM), which keeps about 22 significant bits, close to FP32.
 //
-// One CTA holds G patches: ROWS = 128 (2D) or 256 (3D, n = 16) threads, one
-// per line.  After each pass every thread reads its line back from TMEM
-// (tcgen05.ld), splits it into TF32 hi/lo parts and writes it into the operand
-// tile of the next pass; when the next pass runs along another axis the write
-// is a transpose (each thread writes one element into n different lines).  The
+// One CTA holds G patches: ROWS = 128 (2D) or 256 (3D, n = 16) lines, each
+// taken by SPLIT threads (SPLIT * ROWS threads; thread t has line t % ROWS and
+// the n / SPLIT columns of part t / ROWS, so the warps of a part cover the four
+// TMEM lane quarters).  After each pass every thread reads its columns back
+// from TMEM (tcgen05.ld), splits them into TF32 hi/lo parts and writes them
+// into the operand tile of the next pass; when the next pass runs along
+// another axis the write is a transpose (each thread writes one element into
+// n / SPLIT different lines).  The
 // forward passes run x, y(, z); the inverse passes z(, y), x, so the pass after
 // the eigenvalue divide needs no transpose.  CTAs loop over patch groups.
 //
@@ -53,9 +56,12 @@ struct DftTcArgs {
 
 template <int DIM, int NN>
 struct TcShape {
+  static constexpr int SPLIT = 2;                               // threads per line
   static constexpr int RPP = DIM == 2 ? NN : NN * NN;          // lines per patch
   static constexpr int NCELL = RPP * NN;                        // cells per patch
   static constexpr int ROWS = RPP > 128 ? RPP : 128;            // lines (threads) per CTA
+  static constexpr int THREADS = ROWS * SPLIT;                  // threads per CTA
+  static constexpr int JN = NN / SPLIT;                         // columns per thread
   static constexpr int G = ROWS / RPP;                          // patches per CTA
   static constexpr int R = ROWS / 128;                          // 128-row blocks
   static constexpr int PITCH = NN >= 32 ? 128 : 4 * NN;         // bytes per tile row within a K atom
@@ -63,6 +69,9 @@ struct TcShape {
   static constexpr int BTILE = NN * NN * 4;                     // bytes of one operand-B tile
   static constexpr int COLS_USED = R * NN;
   static constexpr int NCOLS = COLS_USED <= 32 ? 32 : (COLS_USED <= 64 ? 64 : (COLS_USED <= 128 ? 128 : 256));
+  // resident CTAs per SM the registers are sized for (shared memory allows four for 2D n <= 32;
+  // four lines per thread group and three CTAs measured slower than two and four)
+  static constexpr int MIN_CTAS = NN == 64 ? 1 : 512 / ROWS;
 };
 
 __device__ __forceinline__ void line_coords(int a, int line, int j, int n, int& cx, int& cy, int& cz) {
@@ -92,16 +101,20 @@ __device__ __forceinline__ int interior_offset(int c) {
 }
 
 template <class TI, class TO, int DIM, int NN>
-__global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / TcShape<DIM, NN>::ROWS)
+__global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::MIN_CTAS)
     dft_tc_kernel(DftTcArgs a, const TI* in, TO* out) {
   using S = TcShape<DIM, NN>;
   constexpr int SY = NN + 2;
   constexpr int CS = DIM == 3 ? SY * SY * SY : SY * SY;  // padded cells per patch
-  constexpr int PER = S::G * S::NCELL / S::ROWS;          // interior cells per thread per group
+  constexpr int NT = S::THREADS;
+  constexpr int JN = S::JN;
+  constexpr int PER = S::G * S::NCELL / NT;                // interior cells per thread per group
   constexpr int OP = NN + 1;                               // row pitch (floats) of the output staging
   constexpr int NF = S::RPP;                               // cells of one side face
-  constexpr int CPER = S::G * 2 * DIM * NF / S::ROWS;      // corrections per thread per group
-  static_assert(S::G * 2 * DIM * NF % S::ROWS == 0, "corrections must split evenly over the threads");
+  constexpr int CPER = S::G * 2 * DIM * NF / NT;           // corrections per thread per group
+  static_assert(S::G * S::NCELL % NT == 0, "cells must split evenly over the threads");
+  static_assert(S::G * 2 * DIM * NF % NT == 0, "corrections must split evenly over the threads");
+  static_assert(JN % 8 == 0, "TMEM is read in blocks of 8 columns");
   extern __shared__ uint8_t dsm[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base;
@@ -123,7 +136,7 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
     const int p0 = grp * S::G;
 #pragma unroll
     for (int k = 0; k < PER; k++) {
-      int e = t + k * S::ROWS;
+      int e = t + k * NT;
       int i = e / S::NCELL, c = e % S::NCELL;
       int p = p0 + i;
       pf[k] = p < P ? __ldg(in + (long long)p * CS + interior_offset<DIM, NN>(c)) : TI(0);
@@ -131,7 +144,7 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
     if (has_corr) {
 #pragma unroll
       for (int k = 0; k < CPER; k++) {
-        int e = t + k * S::ROWS;
+        int e = t + k * NT;
         int p = p0 + e / (2 * DIM * NF);
         cpf[k] = p < P ? __ldg(a.corr + (long long)p0 * 2 * DIM * NF + e) : 0.f;
       }
@@ -140,7 +153,7 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
   prefetch(blockIdx.x);
 
   // transform matrices into their swizzled tiles
-  for (int e = t; e < a.nmat * 2 * NN * NN; e += S::ROWS) {
+  for (int e = t; e < a.nmat * 2 * NN * NN; e += NT) {
     int m = e / (NN * NN), r = e % (NN * NN);
     *reinterpret_cast<float*>(Bm + m * S::BTILE + tc::tile_offset(r / NN, r % NN, NN, NN)) = a.bmat[e];
   }
@@ -151,11 +164,13 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = tmem_base;
-  // this thread's line: TMEM lane t % 128 (a warp reads the 32 lanes of its quarter), column block t / 128
-  const uint32_t my_row = tmem + ((uint32_t)((t & 127) & ~31) << 16) + (uint32_t)(t >> 7) * NN;
+  // this thread's line and columns: TMEM lane line % 128 (a warp reads the 32 lanes of its quarter),
+  // column block line / 128, columns j0 .. j0 + JN - 1 of the line
+  const int line = t % S::ROWS, j0 = (t / S::ROWS) * JN;
+  const uint32_t my_row = tmem + ((uint32_t)((line & 127) & ~31) << 16) + (uint32_t)(line >> 7) * NN + j0;
   constexpr uint32_t idesc = tc::idesc_tf32(128, NN);
   const uint32_t a_hi = tc::smem_addr(Ahi), a_lo = tc::smem_addr(Alo), b0 = tc::smem_addr(Bm);
-  const int my_i = t / S::RPP, my_line = t % S::RPP;
+  const int my_i = line / S::RPP, my_line = line % S::RPP;
   uint32_t phase = 0;
   bool abort = false;
 
@@ -163,13 +178,13 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
     const int p0 = grp * S::G;
     if (has_corr) {
 #pragma unroll
-      for (int k = 0; k < CPER; k++) cbuf[t + k * S::ROWS] = cpf[k];
+      for (int k = 0; k < CPER; k++) cbuf[t + k * NT] = cpf[k];
       __syncthreads();
     }
     // right-hand sides into the operand tiles of the x pass: line (i, y[, z]), k = x
 #pragma unroll
     for (int k = 0; k < PER; k++) {
-      int e = t + k * S::ROWS;
+      int e = t + k * NT;
       int i = e / S::NCELL, c = e % S::NCELL;
       float v = (float)pf[k];
       if (has_corr) {
@@ -227,33 +242,38 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
       }
       phase ^= 1;
       tc::fence_after_sync();
-      float v[NN];
+      float v[JN];  // columns j0 .. j0 + JN - 1 of this thread's line
+      if (JN % 16 == 0) {
 #pragma unroll
-      for (int c = 0; c < NN; c += 16) tc::tmem_ld16(my_row + c, *reinterpret_cast<float(*)[16]>(&v[c]));
+        for (int c = 0; c < JN; c += 16) tc::tmem_ld16(my_row + c, *reinterpret_cast<float(*)[16]>(&v[c]));
+      } else {
+#pragma unroll
+        for (int c = 0; c < JN; c += 8) tc::tmem_ld8(my_row + c, *reinterpret_cast<float(*)[8]>(&v[c]));
+      }
       tc::tmem_ld_wait();
       const int ax = q < DIM ? q : 2 * DIM - 1 - q;  // axis of this pass
       if (q == DIM - 1 && my_valid) {
         // eigenvalue divide; the cell of (line, j) on the last axis is line + RPP * j
         const float* ie = a.inv_eig + (long long)my_plan * S::NCELL + my_line;
 #pragma unroll
-        for (int j = 0; j < NN; j++) v[j] *= __ldg(ie + S::RPP * j);
-        if (my_zero && my_line == 0) v[0] = 0.f;
+        for (int j = 0; j < JN; j++) v[j] *= __ldg(ie + S::RPP * (j0 + j));
+        if (my_zero && my_line == 0 && j0 == 0) v[0] = 0.f;
       }
       if (q == 2 * DIM - 1) {
         // line (i, y[, z]) with x = j: into the staging rows, then whole padded patches out
 #pragma unroll
-        for (int j = 0; j < NN; j++) stage[t * OP + j] = v[j] * a.scale;
+        for (int j = 0; j < JN; j++) stage[line * OP + j0 + j] = v[j] * a.scale;
         __syncthreads();
         // interior rows, coalesced: thread t writes cells t, t + ROWS, ... of the group
 #pragma unroll
         for (int k = 0; k < PER; k++) {
-          const int e = t + k * S::ROWS;
+          const int e = t + k * NT;
           const int i = e / S::NCELL, c = e % S::NCELL;
           const int p = p0 + i;
           if (p < P) out[(long long)p * CS + interior_offset<DIM, NN>(c)] = (TO)stage[(i * S::RPP + c / NN) * OP + c % NN];
         }
         if (a.zero_ghosts) {
-          for (int e = t; e < S::G * CS; e += S::ROWS) {
+          for (int e = t; e < S::G * CS; e += NT) {
             const int i = e / CS, k = e % CS;
             const int p = p0 + i;
             if (p >= P) break;
@@ -269,7 +289,7 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
       if (nx == ax) {
         // own line, 16-byte chunks: the 8 lanes of a store phase hit 8 different chunk positions
 #pragma unroll
-        for (int j = 0; j < NN; j += 4) {
+        for (int j = 0; j < JN; j += 4) {
           float4 hi, lo;
           hi.x = tc::to_tf32(v[j]);
           hi.y = tc::to_tf32(v[j + 1]);
@@ -279,19 +299,19 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::ROWS, NN == 64 ? 1 : 512 / T
           lo.y = v[j + 1] - hi.y;
           lo.z = v[j + 2] - hi.z;
           lo.w = v[j + 3] - hi.w;
-          uint32_t off = tc::tile_offset(t, j, S::ROWS, NN);
+          uint32_t off = tc::tile_offset(line, j0 + j, S::ROWS, NN);
           *reinterpret_cast<float4*>(Ahi + off) = hi;
           *reinterpret_cast<float4*>(Alo + off) = lo;
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < NN; j++) {
+        for (int j = 0; j < JN; j++) {
           int cx, cy, cz;
-          line_coords(ax, my_line, j, NN, cx, cy, cz);
-          int line = nx == 0 ? cy + NN * cz : (nx == 1 ? cx + NN * cz : cx + NN * cy);
-          int k = nx == 0 ? cx : (nx == 1 ? cy : cz);
+          line_coords(ax, my_line, j0 + j, NN, cx, cy, cz);
+          const int nline = nx == 0 ? cy + NN * cz : (nx == 1 ? cx + NN * cz : cx + NN * cy);
+          const int k = nx == 0 ? cx : (nx == 1 ? cy : cz);
           float hi = tc::to_tf32(v[j]), lo = v[j] - hi;
-          uint32_t off = tc::tile_offset(my_i * S::RPP + line, k, S::ROWS, NN);
+          uint32_t off = tc::tile_offset(my_i * S::RPP + nline, k, S::ROWS, NN);
           *reinterpret_cast<float*>(Ahi + off) = hi;
           *reinterpret_cast<float*>(Alo + off) = lo;
         }
@@ -429,12 +449,12 @@ static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStrea
   cudaFuncAttributes fa;
   TE_CUDA(cudaFuncGetAttributes(&fa, (const void*)kern));
   int occ = (int)(smem_sm / (smem + fa.sharedSizeBytes + reserved));
-  occ = std::min(occ, threads_sm / S::ROWS);
-  occ = std::min(occ, regs_sm / std::max(1, fa.numRegs * S::ROWS));
+  occ = std::min(occ, threads_sm / S::THREADS);
+  occ = std::min(occ, regs_sm / std::max(1, fa.numRegs * S::THREADS));
   occ = std::min(occ, tmem_cap);
   require(occ >= 1, "tensor-core DFT: kernel does not fit on an SM", TE_ERR_UNSUPPORTED);
   int grid = std::min(a.ngroups, occ * sm_count);
-  kern<<<grid, S::ROWS, smem, s>>>(a, in, out);
+  kern<<<grid, S::THREADS, smem, s>>>(a, in, out);
   count_launch();
   TE_LAUNCH_CHECK();
 }
