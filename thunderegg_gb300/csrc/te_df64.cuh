@@ -75,6 +75,52 @@ __device__ __forceinline__ df64 operator*(df64 a, float b) {
   p.lo = __fmaf_rn(a.lo, b, p.lo);
   return fast_two_sum(p.hi, p.lo);
 }
+// a * x + b * y for FP32 x, y: both products' high parts summed exactly
+// (TwoProd, TwoSum), every low-order term collected in one FP32 sum, then
+// renormalised.  The error is about 2^-47 (|a x| + |b y|), the same order as
+// forming the two products and their float-float sum separately, at less
+// than half the operations.
+__device__ __forceinline__ df64 df_sum2(df64 a, float x, df64 b, float y) {
+  const df64 p = two_prod(a.hi, x), q = two_prod(b.hi, y);
+  const df64 t = two_sum(p.hi, q.hi);
+  float lo = __fadd_rn(t.lo, __fadd_rn(p.lo, q.lo));
+  lo = __fmaf_rn(a.lo, x, lo);
+  lo = __fmaf_rn(b.lo, y, lo);
+  return fast_two_sum(t.hi, lo);
+}
+// a * x + b * y for float-float x, y (the cross terms a.hi x.lo + a.lo x.hi
+// of each product join the low-order sum)
+__device__ __forceinline__ df64 df_sum2(df64 a, df64 x, df64 b, df64 y) {
+  const df64 p = two_prod(a.hi, x.hi), q = two_prod(b.hi, y.hi);
+  const df64 t = two_sum(p.hi, q.hi);
+  float lo = __fadd_rn(t.lo, __fadd_rn(p.lo, q.lo));
+  lo = __fmaf_rn(a.hi, x.lo, lo);
+  lo = __fmaf_rn(a.lo, x.hi, lo);
+  lo = __fmaf_rn(b.hi, y.lo, lo);
+  lo = __fmaf_rn(b.lo, y.hi, lo);
+  return fast_two_sum(t.hi, lo);
+}
+
+// Dot-product accumulator after Ogita, Rump and Oishi, "Accurate sum and dot
+// product" (SIAM J. Sci. Comput. 26(6), 2005), algorithm Dot2, with
+// float-float factors: the running FP32 sum s takes each product's high part
+// through TwoSum, and c collects the rounding errors of those additions, the
+// products' low parts (TwoProd) and the cross terms.  The value s + c is kept
+// as a float-float number (not rounded to FP32), so for n terms its error is
+// about n^2 2^-48 sum |a_i b_i|: far below what the 1e-10 stopping test
+// resolves, at half the operations of a float-float multiply and add per term.
+struct dot2 {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(df64 a, df64 b) {
+    const df64 p = two_prod(a.hi, b.hi);
+    const float cross = __fmaf_rn(a.hi, b.lo, __fmul_rn(a.lo, b.hi));
+    const df64 t = two_sum(s, p.hi);
+    s = t.hi;
+    c = __fadd_rn(c, __fadd_rn(t.lo, __fadd_rn(p.lo, cross)));
+  }
+  __device__ __forceinline__ df64 value() const { return two_sum(s, c); }
+};
+
 __device__ __forceinline__ df64& operator+=(df64& a, df64 b) { return a = a + b; }
 __device__ __forceinline__ df64& operator-=(df64& a, df64 b) { return a = a - b; }
 

@@ -63,25 +63,46 @@ struct Batch {
   const int* active;  // [B] 1 while the solve iterates
 };
 
-__device__ __forceinline__ int k_interior_offset(const Layout& L, int e) {
-  int x = e % L.n0;
-  int r = e / L.n0;
-  int y = r % L.n1;
-  int z = r / L.n1;
-  return L.at(x, y, z);
-}
+// Interior cells threadIdx.x, + blockDim.x, ... of a patch (x fastest) walked
+// without divisions: the start and the stride are decomposed once into cell
+// coordinates, and each step adds them with at most one carry per axis (the
+// stride's coordinate on each axis is below that axis' size).
+struct InteriorWalk {
+  int x0, y0, z0, dx, dy, dz;
+  __device__ __forceinline__ explicit InteriorWalk(const Layout& L) {
+    x0 = threadIdx.x % L.n0;
+    y0 = (threadIdx.x / L.n0) % L.n1;
+    z0 = threadIdx.x / (L.n0 * L.n1);
+    dx = blockDim.x % L.n0;
+    dy = (blockDim.x / L.n0) % L.n1;
+    dz = blockDim.x / (L.n0 * L.n1);
+  }
+};
 
 // iterate the interior cells of chunk `ch` of solve `b`
 #define TE_CHUNK_LOOP(BT, L, nc, b, ch, k, body)                                       \
   {                                                                                    \
     const int _N = (L).interior();                                                     \
     const long long _ps = (L).pstride(nc);                                             \
+    const InteriorWalk _w(L);                                                          \
     for (int _p = (BT).offs[b] + (ch); _p < (BT).offs[(b) + 1]; _p += (BT).nch[b])     \
       for (int _c = 0; _c < (nc); _c++) {                                              \
         const long long _base = _p * _ps + (long long)_c * (L).cs;                     \
+        int _x = _w.x0, _y = _w.y0, _z = _w.z0;                                        \
         _Pragma("unroll 4") for (int _e = threadIdx.x; _e < _N; _e += blockDim.x) {    \
-          const long long k = _base + k_interior_offset((L), _e);                      \
+          const long long k = _base + (L).at(_x, _y, _z);                              \
           body;                                                                        \
+          _x += _w.dx;                                                                 \
+          _y += _w.dy;                                                                 \
+          _z += _w.dz;                                                                 \
+          if (_x >= (L).n0) {                                                          \
+            _x -= (L).n0;                                                              \
+            _y++;                                                                      \
+          }                                                                            \
+          if (_y >= (L).n1) {                                                          \
+            _y -= (L).n1;                                                              \
+            _z++;                                                                      \
+          }                                                                            \
         }                                                                              \
       }                                                                                \
   }
@@ -298,6 +319,63 @@ __device__ __forceinline__ void stv(const DV& v, long long k, df64 x) {
   v.lo[k] = x.lo;
 }
 
+// The interior cells of chunk `ch` of solve `b` (the cells TE_CHUNK_LOOP
+// visits, in the same order per thread), U at a time: next() fills k[0..U-1]
+// with padded offsets (-1 past the end), so a kernel can load the operands of
+// U cells before it computes and stores any of them.
+template <int U>
+struct ChunkCells {
+  const Layout& L;
+  const int nc, N, pend, pstep;
+  const long long ps;
+  const InteriorWalk w;
+  int p, c, e, x, y, z;
+  long long base;
+  __device__ __forceinline__ ChunkCells(const Batch& bt, const Layout& L_, int nc_, int b, int ch)
+      : L(L_), nc(nc_), N(L_.interior()), pend(bt.offs[b + 1]), pstep(bt.nch[b]), ps(L_.pstride(nc_)), w(L_) {
+    p = bt.offs[b] + ch;
+    c = 0;
+    restart();
+  }
+  __device__ __forceinline__ void restart() {
+    e = threadIdx.x;
+    x = w.x0;
+    y = w.y0;
+    z = w.z0;
+    base = (long long)p * ps + (long long)c * L.cs;
+  }
+  __device__ __forceinline__ bool next(long long (&k)[U]) {
+#pragma unroll
+    for (int r = 0; r < U; r++) {
+      while (p < pend && e >= N) {  // this patch-component is done: the next one
+        if (++c == nc) {
+          c = 0;
+          p += pstep;
+        }
+        restart();
+      }
+      if (p >= pend) {
+        k[r] = -1;
+        continue;
+      }
+      k[r] = base + L.at(x, y, z);
+      e += blockDim.x;
+      x += w.dx;
+      y += w.dy;
+      z += w.dz;
+      if (x >= L.n0) {
+        x -= L.n0;
+        y++;
+      }
+      if (y >= L.n1) {
+        y -= L.n1;
+        z++;
+      }
+    }
+    return k[0] >= 0;
+  }
+};
+
 // block sums of float-float accumulators (the FP64 pipe stays idle until the last block)
 template <int NV>
 __device__ void kd_reduce(df64 (&v)[NV], const Batch& bt, int b, int ch, double* part, unsigned int* counter,
@@ -330,13 +408,14 @@ template <int NV>
 __global__ void __launch_bounds__(KT) kd_dots(Layout L, int nc, Batch bt, CV a0, CV b0, CV a1, CV b1, CV a2, CV b2,
                                               double* part, unsigned int* counter, double* S, int slot0, int fin) {
   TE_BLOCK_SOLVE(bt);
-  df64 v[NV];
-  for (int i = 0; i < NV; i++) v[i] = df64(0.f, 0.f);
+  dot2 d[NV];
   TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
-    v[0] += ldv(a0, k) * ldv(b0, k);
-    if (NV > 1) v[1] += ldv(a1, k) * ldv(b1, k);
-    if (NV > 2) v[2] += ldv(a2, k) * ldv(b2, k);
+    d[0].add(ldv(a0, k), ldv(b0, k));
+    if (NV > 1) d[1].add(ldv(a1, k), ldv(b1, k));
+    if (NV > 2) d[2].add(ldv(a2, k), ldv(b2, k));
   });
+  df64 v[NV];
+  for (int i = 0; i < NV; i++) v[i] = d[i].value();
   kd_reduce<NV>(v, bt, b, ch, part, counter, S, slot0, fin, 0);
 }
 
@@ -346,16 +425,30 @@ __global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double to
   __shared__ df64 sc[1];
   kd_scalars(S + (size_t)b * S_NSLOTS, sc, 1, S_ALPHA, S_ALPHA);
   const df64 nalpha = -sc[0];
-  df64 v[1] = {df64(0.f, 0.f)};
-  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
-    df64 sv = ldv(r, k) + ldv(ap, k) * nalpha;
-    stv(s, k, sv);
-    v[0] += sv * sv;
-  });
+  dot2 d;
+  ChunkCells<2> cells(bt, L, nc, b, ch);
+  long long k[2];
+  while (cells.next(k)) {
+    df64 rv[2], av[2];
+#pragma unroll
+    for (int u = 0; u < 2; u++)
+      if (k[u] >= 0) {
+        rv[u] = ldv(r, k[u]);
+        av[u] = ldv(ap, k[u]);
+      }
+#pragma unroll
+    for (int u = 0; u < 2; u++)
+      if (k[u] >= 0) {
+        const df64 sv = rv[u] + av[u] * nalpha;
+        stv(s, k[u], sv);
+        d.add(sv, sv);
+      }
+  }
+  df64 v[1] = {d.value()};
   kd_reduce<1>(v, bt, b, ch, part, counter, S, S_SS, 5, tol);
 }
 
-__global__ void __launch_bounds__(KT) kd_xr(Layout L, int nc, Batch bt, DV x, DV r, const float* mp, const float* ms,
+__global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV x, DV r, const float* mp, const float* ms,
                                             CV ap, CV as, CV rhat, CV dir, double* part, unsigned int* counter,
                                             double* S) {
   TE_BLOCK_SOLVE(bt);
@@ -365,19 +458,39 @@ __global__ void __launch_bounds__(KT) kd_xr(Layout L, int nc, Batch bt, DV x, DV
   const df64 alpha = sc[0], omega = sc[1];
   const df64 nalpha = -alpha, nomega = -omega;
   const bool done = Sb[S_DONE] != 0.0;
-  df64 v[2] = {df64(0.f, 0.f), df64(0.f, 0.f)};
+  dot2 d0, d1;
   const CV xc = as_cv(x), rc = as_cv(r);
-  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
-    if (done) {
-      stv(x, k, ldv(xc, k) + ldv(dir, k) * alpha);
-    } else {
-      stv(x, k, ldv(xc, k) + (alpha * mp[k] + omega * ms[k]));
-      df64 rv = ldv(rc, k) + (ldv(ap, k) * nalpha + ldv(as, k) * nomega);
-      stv(r, k, rv);
-      v[0] += rv * rv;
-      v[1] += rv * ldv(rhat, k);
+  if (done) {
+    TE_CHUNK_LOOP(bt, L, nc, b, ch, k, { stv(x, k, ldv(xc, k) + ldv(dir, k) * alpha); });
+  } else {
+    ChunkCells<2> cells(bt, L, nc, b, ch);
+    long long k[2];
+    while (cells.next(k)) {
+      df64 xv[2], rv[2], av[2], sv[2], hv[2];
+      float mv[2], nv[2];
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+        if (k[u] >= 0) {
+          xv[u] = ldv(xc, k[u]);
+          mv[u] = mp[k[u]];
+          nv[u] = ms[k[u]];
+          rv[u] = ldv(rc, k[u]);
+          av[u] = ldv(ap, k[u]);
+          sv[u] = ldv(as, k[u]);
+          hv[u] = ldv(rhat, k[u]);
+        }
+#pragma unroll
+      for (int u = 0; u < 2; u++)
+        if (k[u] >= 0) {
+          stv(x, k[u], xv[u] + df_sum2(alpha, mv[u], omega, nv[u]));
+          const df64 rn = rv[u] + df_sum2(av[u], nalpha, sv[u], nomega);
+          stv(r, k[u], rn);
+          d0.add(rn, rn);
+          d1.add(rn, hv[u]);
+        }
     }
-  });
+  }
+  df64 v[2] = {d0.value(), d1.value()};
   kd_reduce<2>(v, bt, b, ch, part, counter, S, S_RR, 3, 0);
 }
 
@@ -389,10 +502,21 @@ __global__ void __launch_bounds__(KT) kd_p(Layout L, int nc, Batch bt, DV p, CV 
   kd_scalars(Sb, sc, 2, S_OMEGA, S_BETA);
   const df64 nomega = -sc[0], beta = sc[1];
   const CV pc = as_cv(p);
-  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
-    df64 pv = ldv(pc, k) + ldv(ap, k) * nomega;
-    stv(p, k, pv * beta + ldv(r, k));
-  });
+  ChunkCells<2> cells(bt, L, nc, b, ch);
+  long long k[2];
+  while (cells.next(k)) {
+    df64 pv[2], av[2], rv[2];
+#pragma unroll
+    for (int u = 0; u < 2; u++)
+      if (k[u] >= 0) {
+        pv[u] = ldv(pc, k[u]);
+        av[u] = ldv(ap, k[u]);
+        rv[u] = ldv(r, k[u]);
+      }
+#pragma unroll
+    for (int u = 0; u < 2; u++)
+      if (k[u] >= 0) stv(p, k[u], (pv[u] + av[u] * nomega) * beta + rv[u]);
+  }
 }
 
 __global__ void kd_split(const double* src, DV dst, long long n) {
@@ -546,15 +670,14 @@ __global__ void __launch_bounds__(256)
   if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
   const float* up = u + (long long)p * CS;
   const long long base = (long long)p * CS;
-  df64 v[NV];
-  for (int i = 0; i < NV; i++) v[i] = df64(0.f, 0.f);
+  dot2 v[NV];
   auto emit = [&](int k, df64 res) {
     stv(f, base + k, res);
     if (NV == 1) {
-      v[0] += ldv(w, base + k) * res;
+      v[0].add(ldv(w, base + k), res);
     } else {
-      v[0] += res * ldv(w, base + k);
-      v[1] += res * res;
+      v[0].add(res, ldv(w, base + k));
+      v[1].add(res, res);
     }
   };
   // cells away from the boundary: every neighbour is an interior FP32 value
@@ -637,7 +760,7 @@ __global__ void __launch_bounds__(256)
   __shared__ df64 red[NV][256 / 32];
 #pragma unroll
   for (int i = 0; i < NV; i++) {
-    df64 x = v[i];
+    df64 x = v[i].value();
     for (int o = 16; o > 0; o >>= 1) x += df_shfl_down(x, o);
     if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = x;
   }
