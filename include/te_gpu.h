@@ -202,6 +202,14 @@ typedef struct te_cycle_opts {
  * cycle converts f to FP32, cycles in FP32 and writes FP64 u). */
 int te_vcycle_create(const te_cycle_level* levels, int num_levels, te_cycle_opts opts, int dtype,
                      te_cycle** out);
+/* CycleBuilder::getCycle (CycleBuilder.h:176-191): cycle_type TE_CYCLE_V
+ * ("V", VCycle.h), TE_CYCLE_W ("W", WCycle.h:50-84: a mid_sweeps smooth and
+ * a second coarse visit per level) or TE_CYCLE_FMG ("F", FMGCycle.h:43-104).
+ * te_vcycle_create(...) is te_cycle_create(..., TE_CYCLE_V, ...); other types
+ * give TE_ERR_UNSUPPORTED. */
+enum { TE_CYCLE_V = 0, TE_CYCLE_W = 1, TE_CYCLE_FMG = 2 };
+int te_cycle_create(const te_cycle_level* levels, int num_levels, te_cycle_opts opts, int cycle_type, int dtype,
+                    te_cycle** out);
 int te_cycle_destroy(te_cycle* c);
 /* u = M f  (u.setWithGhost(0); visit(finest, f, u)); f and u are FP64 */
 int te_cycle_apply(const te_cycle* c, int ncomp, const void* f, void* u);

@@ -27,6 +27,7 @@
 #pragma once
 
 #include <ThunderEgg/Domain.h>
+#include <ThunderEgg/GMG/CycleOpts.h>
 #include <ThunderEgg/GMG/Interpolator.h>
 #include <ThunderEgg/GMG/Restrictor.h>
 #include <ThunderEgg/GhostFiller.h>
@@ -386,7 +387,10 @@ class GpuDirectInterpolator : public ThunderEgg::GMG::Interpolator<D> {
 };
 
 // ---------------------------------------------------------------------------
-// The V-cycle as the right preconditioner Mr (Cycle::apply, GMG/Cycle.h:94-98)
+// The multigrid cycle as the right preconditioner Mr (Cycle::apply,
+// GMG/Cycle.h:94-98): a V-cycle by default, or the W / FMG cycle that
+// CycleBuilder::getCycle (GMG/CycleBuilder.h:176-191) makes for cycle_type
+// "W" / "F"
 // ---------------------------------------------------------------------------
 template <int D>
 class GpuVCycle : public ThunderEgg::Operator<D> {
@@ -399,7 +403,7 @@ class GpuVCycle : public ThunderEgg::Operator<D> {
   };
   // dtype TE_F32: the mixed-precision cycle (FP32 on every level, FP64 in and out)
   GpuVCycle(std::shared_ptr<GpuDomain<D>> finest, const std::vector<LevelParts>& parts, te_cycle_opts opts,
-            int dtype = TE_F32)
+            int dtype = TE_F32, int cycle_type = TE_CYCLE_V)
       : finest_(finest) {
     std::vector<te_cycle_level> lv(parts.size());
     for (size_t k = 0; k < parts.size(); k++) {
@@ -409,8 +413,19 @@ class GpuVCycle : public ThunderEgg::Operator<D> {
       lv[k].interpolator = parts[k].interpolator;
     }
     te_cycle* h = nullptr;
-    check(te_vcycle_create(lv.data(), (int)lv.size(), opts, dtype, &h));
+    check(te_cycle_create(lv.data(), (int)lv.size(), opts, cycle_type, dtype, &h));
     h_ = std::shared_ptr<te_cycle>(h, [](te_cycle* x) { te_cycle_destroy(x); });
+  }
+  // the reference's CycleOpts, cycle_type included
+  GpuVCycle(std::shared_ptr<GpuDomain<D>> finest, const std::vector<LevelParts>& parts,
+            const ThunderEgg::GMG::CycleOpts& o, int dtype = TE_F32)
+      : GpuVCycle(finest, parts, te_cycle_opts{o.pre_sweeps, o.post_sweeps, o.mid_sweeps, o.coarse_sweeps}, dtype,
+                  cycle_type_of(o.cycle_type)) {}
+  static int cycle_type_of(const std::string& t) {
+    if (t == "V") return TE_CYCLE_V;
+    if (t == "W") return TE_CYCLE_W;
+    if (t == "F") return TE_CYCLE_FMG;
+    throw ThunderEgg::RuntimeError("Unsupported Cycle type: " + t);
   }
   GpuVCycle* clone() const override { return new GpuVCycle(*this); }
   void apply(const ThunderEgg::Vector<D>& f, ThunderEgg::Vector<D>& u) const override {

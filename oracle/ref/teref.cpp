@@ -238,6 +238,8 @@ static int gmg(const te_level_desc* levels, int nlevels, const teo_gmg_config* c
   opts.pre_sweeps = cfg->pre_sweeps;
   opts.post_sweeps = cfg->post_sweeps;
   opts.coarse_sweeps = cfg->coarse_sweeps;
+  opts.mid_sweeps = cfg->mid_sweeps;
+  opts.cycle_type = cfg->cycle_type == 1 ? "W" : (cfg->cycle_type == 2 ? "F" : "V");
   GMG::CycleBuilder<D> b(opts);
   bool ex = cfg->extrapolate_boundary_ghosts != 0;
   for (int k = 0; k < nlevels; k++) {

@@ -1096,35 +1096,74 @@ void interpolate_vec(const Level& C, const Level& F, const double* coarse, doubl
 }
 
 // ---------------------------------------------------------------------------
-// GMG V-cycle (GMG/Cycle.h:57-98, GMG/VCycle.h:46-70) and the outer solve
+// GMG cycles (GMG/Cycle.h:57-98; VCycle.h:46-70, WCycle.h:50-84,
+// FMGCycle.h:43-104) and the outer solve
 // ---------------------------------------------------------------------------
 struct Hierarchy {
   std::vector<Level> levels;
   std::vector<Op*> ops;
   std::vector<Smoother*> smoothers;
-  int pre = 1, post = 1, coarse_sweeps = 1;
+  int pre = 1, post = 1, coarse_sweeps = 1, mid = 1;
+  int type = 0;  // 0 V, 1 W, 2 FMG
   bool extrapolate = false;
   ~Hierarchy() {
     for (auto* o : ops) delete o;
     for (auto* s : smoothers) delete s;
   }
-  void visit(int k, const double* f, double* u, int nc) const {
+  // Cycle::restrict (:57-65): the restriction of r = f - A u
+  std::vector<double> restrict_residual(int k, const double* f, double* u, int nc) const {
     const Level& L = levels[k];
-    if (k + 1 == (int)levels.size()) {
-      for (int i = 0; i < coarse_sweeps; i++) smoothers[k]->smooth(f, u, nc);
-      return;
-    }
-    for (int i = 0; i < pre; i++) smoothers[k]->smooth(f, u, nc);
-    // Cycle::restrict (:57-65): r = f - A u
     std::vector<double> r(L.size(nc), 0.0);
     ops[k]->apply(u, r.data(), nc);
     for_interior(L, L.P, nc, [&](long i) { r[i] = r[i] * -1 + f[i]; });
     const Level& C = levels[k + 1];
-    std::vector<double> cf(C.size(nc)), cu(C.size(nc), 0.0);
+    std::vector<double> cf(C.size(nc));
     restrict_vec(L, C, extrapolate, r.data(), cf.data(), nc);
+    return cf;
+  }
+  void sweeps(int k, const double* f, double* u, int nc, int n) const {
+    for (int i = 0; i < n; i++) smoothers[k]->smooth(f, u, nc);
+  }
+  // VCycle::visit, WCycle::visit, FMGCycle::visit.  W and FMG smooth mid_sweeps
+  // times after the first coarse correction and visit the coarser level a
+  // second time from that level's first result (the coarse vector is not
+  // zeroed again, as in the reference); FMG's second visit is its v_visit.
+  void visit(int k, const double* f, double* u, int nc) const {
+    if (k + 1 == (int)levels.size()) {
+      sweeps(k, f, u, nc, coarse_sweeps);
+      return;
+    }
+    sweeps(k, f, u, nc, pre);
+    std::vector<double> cf = restrict_residual(k, f, u, nc);
+    const Level& C = levels[k + 1];
+    const Level& L = levels[k];
+    std::vector<double> cu(C.size(nc), 0.0);
     visit(k + 1, cf.data(), cu.data(), nc);
     interpolate_vec(C, L, cu.data(), u, nc);
-    for (int i = 0; i < post; i++) smoothers[k]->smooth(f, u, nc);
+    if (type != 0) {
+      sweeps(k, f, u, nc, mid);
+      cf = restrict_residual(k, f, u, nc);
+      if (type == 1)
+        visit(k + 1, cf.data(), cu.data(), nc);
+      else
+        v_visit(k + 1, cf.data(), cu.data(), nc);
+      interpolate_vec(C, L, cu.data(), u, nc);
+    }
+    sweeps(k, f, u, nc, post);
+  }
+  // FMGCycle::v_visit (:43-66): one pre/post-smoothed pass whose coarser visit is visit()
+  void v_visit(int k, const double* f, double* u, int nc) const {
+    if (k + 1 == (int)levels.size()) {
+      sweeps(k, f, u, nc, coarse_sweeps);
+      return;
+    }
+    sweeps(k, f, u, nc, pre);
+    std::vector<double> cf = restrict_residual(k, f, u, nc);
+    const Level& C = levels[k + 1];
+    std::vector<double> cu(C.size(nc), 0.0);
+    visit(k + 1, cf.data(), cu.data(), nc);
+    interpolate_vec(C, levels[k], cu.data(), u, nc);
+    sweeps(k, f, u, nc, post);
   }
   void apply(const double* f, double* u, int nc) const {
     std::fill(u, u + levels[0].size(nc), 0.0);
@@ -1259,6 +1298,9 @@ static Hierarchy* make_hierarchy(const te_level_desc* levels, int nlevels, const
   H->pre = cfg->pre_sweeps;
   H->post = cfg->post_sweeps;
   H->coarse_sweeps = cfg->coarse_sweeps;
+  H->mid = cfg->mid_sweeps;
+  if (cfg->cycle_type < 0 || cfg->cycle_type > 2) throw std::runtime_error("unsupported cycle type");
+  H->type = cfg->cycle_type;
   H->extrapolate = cfg->extrapolate_boundary_ghosts != 0;
   return H;
 }

@@ -21,6 +21,8 @@ typedef struct teo_gmg_config {
   double tol;             /* outer BiCGStab                                 */
   int max_it;
   int use_precond;        /* 0: BiCGStab without the V-cycle                */
+  int mid_sweeps;         /* W and FMG cycles (CycleOpts.h:45)              */
+  int cycle_type;         /* 0 "V", 1 "W", 2 "F" (CycleBuilder.h:176-191)   */
 } teo_gmg_config;
 #ifdef __cplusplus
 }

@@ -116,6 +116,9 @@ def main():
             out["interp"] = R.interpolate(levels[1], levels[0], inp["tr_coarse"], inp["tr_fine"])
             cfg = orc.gmg_config(scheme=sc, smoother=0, tol=1e-10)
             out["vcycle"] = R.vcycle(levels, inp["gmg_f"], cfg)
+            for ct in ("W", "F"):  # WCycle / FMGCycle through CycleBuilder's cycle_type
+                cfg_t = orc.gmg_config(scheme=sc, smoother=0, tol=1e-10, cycle_type=ct)
+                out[f"cycle_{ct}"] = R.vcycle(levels, inp["gmg_f"], cfg_t)
             us, its, res, rc = R.solve(levels, inp["gmg_f"], cfg)
             out["solve_u"], out["solve_its"] = us, np.array(its)
         path = os.path.join(HERE, f"{name}.npz")

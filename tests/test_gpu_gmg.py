@@ -1,4 +1,4 @@
-"""GMG V-cycle and BiCGStab solves on the GPU against the CPU oracle.
+"""GMG cycles (V, W, FMG) and BiCGStab solves on the GPU against the CPU oracle.
 
 V-cycle applications agree with the oracle to 1e-11 (FP64).  Solves reach the
 same iteration count and the same solution to the solver tolerance; with the
@@ -193,3 +193,67 @@ def test_batched_solves_match_alone(te, n):
         u2 = te.Vector(one.finest)
         assert one.solve(f1, u2) == its[b]
         assert np.array_equal(u2.numpy()[inner], part[inner])
+
+
+@pytest.mark.parametrize("idx", range(3))
+@pytest.mark.parametrize("cycle_type", ("W", "F"))
+@pytest.mark.parametrize("smoother", (0, 1))
+def test_w_and_fmg_cycles(te, oracle, idx, cycle_type, smoother):
+    """WCycle (GMG/WCycle.h:50-84) and FMGCycle (GMG/FMGCycle.h:43-104) through
+    CycleBuilder's cycle_type, FP64 and FP32, against the oracle (pinned to the
+    reference's own cycles by tests/test_oracle_pin.py).  FP64 tolerance as the
+    V-cycle; FP32 5e-5; the second application replays the captured graph."""
+    from oracle import gmg_config
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    name, levels, scheme = meshes()[idx]
+    mid = 2 if smoother else 1
+    cfg = gmg_config(scheme=scheme, smoother=smoother, cycle_type=cycle_type, mid_sweeps=mid)
+    f = np.random.default_rng(50 + idx).standard_normal(levels[0].padded_shape(1))
+    want = oracle.vcycle(levels, f, cfg)
+    g = levels[0].num_ghost
+    inner = (Ellipsis,) + tuple(slice(g, -g) for _ in range(levels[0].dim))
+    tols = ((te.TE_F64, 1e-11 if smoother == 0 else 1e-7), (te.TE_F32, 5e-5))
+    for dt, tol in tols:
+        s = GmgSolver(levels, GmgOptions(scheme=scheme, smoother=smoother, cycle_type=cycle_type, mid_sweeps=mid,
+                                         cycle_dtype=dt))
+        fv = te.Vector.from_numpy(s.finest, f)
+        uv = te.Vector(s.finest)
+        for _ in range(2):
+            s.cycle.apply(fv, uv)
+            assert rel_err(uv.numpy()[inner], want[inner]) <= tol, (dt, cycle_type)
+
+
+@pytest.mark.parametrize("cycle_type", ("W", "F"))
+def test_solve_with_w_and_fmg_cycles(te, oracle, cycle_type):
+    """GMG-preconditioned BiCGStab with the W / FMG cycle: the same iteration
+    count and solution as the oracle (FP64 cycle), and the FP64 residual below
+    the tolerance with the mixed-precision cycle."""
+    from oracle import gmg_config
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    name, levels, scheme = meshes()[1]
+    f = np.random.default_rng(60).standard_normal(levels[0].padded_shape(1))
+    u_o, its_o, _, rc = oracle.solve(levels, f, gmg_config(scheme=scheme, smoother=0, cycle_type=cycle_type))
+    assert rc == 0
+    s = GmgSolver(levels, GmgOptions(scheme=scheme, smoother=0, cycle_type=cycle_type))
+    fv = te.Vector.from_numpy(s.finest, f)
+    uv = te.Vector(s.finest)
+    assert s.solve(fv, uv) == its_o
+    inner = (Ellipsis, slice(1, -1), slice(1, -1))
+    assert rel_err(uv.numpy()[inner], u_o[inner]) <= 1e-8
+    s32 = GmgSolver(levels, GmgOptions(scheme=scheme, smoother=0, cycle_type=cycle_type, cycle_dtype=te.TE_F32,
+                                       bicgstab_flags=1))
+    uv = te.Vector(s32.finest)
+    s32.solve(fv, uv)
+    assert s32.residual(fv, uv) <= 1e-10
+
+
+def test_unknown_cycle_type(te):
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300.capi import TE_ERR_UNSUPPORTED, TeError
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    with pytest.raises(TeError) as e:
+        GmgSolver(M.uniform_mesh(2, 2, 8), GmgOptions(cycle_type="X"))
+    assert e.value.code == TE_ERR_UNSUPPORTED

@@ -3,7 +3,7 @@
 1. Against the committed golden fixtures (tests/golden/*.npz, written by
    tests/golden/make_golden.py from the reference compiled from its own
    sources): ghost fills, call tables, operator applies, RHS modification,
-   both patch smoothers, restriction, interpolation, V-cycle and a full
+   both patch smoothers, restriction, interpolation, V-, W- and FMG cycles and a full
    GMG-BiCGStab solve.  The restatement reproduces them bit for bit.
 2. Against the reference library live, where its sources are present.
 """
@@ -63,6 +63,9 @@ def test_oracle_matches_reference_fixtures(oracle, path):
         assert np.array_equal(oracle.interpolate(levels[1], levels[0], inp["tr_coarse"], inp["tr_fine"]), z["interp"])
         cfg = gmg_config(scheme=sc, smoother=0, tol=1e-10)
         assert np.array_equal(oracle.vcycle(levels, inp["gmg_f"], cfg), z["vcycle"])
+        for ct in ("W", "F"):
+            cfg_t = gmg_config(scheme=sc, smoother=0, tol=1e-10, cycle_type=ct)
+            assert np.array_equal(oracle.vcycle(levels, inp["gmg_f"], cfg_t), z[f"cycle_{ct}"]), ct
         u, its, res, rc = oracle.solve(levels, inp["gmg_f"], cfg)
         g = lv.num_ghost
         inner = (Ellipsis,) + tuple(slice(g, -g) for _ in range(lv.dim))
@@ -83,8 +86,9 @@ def test_oracle_matches_reference_live(oracle, ref):
             assert np.array_equal(oracle.ghost_calls(lv, ft), ref.ghost_calls(lv, ft))
         f = rng.standard_normal(lv.padded_shape(1))
         for sm in (0, 1):
-            cfg = gmg_config(scheme=sc, smoother=sm)
-            assert np.array_equal(oracle.vcycle(levels, f, cfg), ref.vcycle(levels, f, cfg))
+            for ct in ("V", "W", "F"):
+                cfg = gmg_config(scheme=sc, smoother=sm, cycle_type=ct, mid_sweeps=1 + sm)
+                assert np.array_equal(oracle.vcycle(levels, f, cfg), ref.vcycle(levels, f, cfg)), (sm, ct)
 
 
 def test_reference_bicgstab_early_exit_quirk(oracle):

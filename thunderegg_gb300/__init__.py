@@ -353,10 +353,9 @@ class CycleOpts:
     """GMG::CycleOpts (GMG/CycleOpts.h:33-55)."""
 
     def __init__(self, pre_sweeps=1, post_sweeps=1, mid_sweeps=1, coarse_sweeps=1, cycle_type="V"):
-        if cycle_type != "V":
-            raise TeError(capi.TE_ERR_UNSUPPORTED, "only V cycles are built")
         self.pre_sweeps, self.post_sweeps = pre_sweeps, post_sweeps
         self.mid_sweeps, self.coarse_sweeps = mid_sweeps, coarse_sweeps
+        self.cycle_type = cycle_type  # "V", "W" or "F" (checked by CycleBuilder.getCycle)
 
 
 class Cycle(_Handle):
@@ -404,9 +403,13 @@ class CycleBuilder:
         self.levels.append((op, smoother, None, interpolator))
 
     def getCycle(self, dtype=TE_F64) -> Cycle:
-        """The V-cycle; dtype=TE_F32 runs it in FP32 (f and u stay FP64)."""
+        """The cycle of opts.cycle_type ("V", "W" or "F" for FMG, CycleBuilder.h:176-191);
+        dtype=TE_F32 runs it in FP32 (f and u stay FP64)."""
         if not self.has_coarsest:
             raise TeError(capi.TE_ERR_INVALID, "addCoarsestLevel has not been called")
+        types = {"V": capi.TE_CYCLE_V, "W": capi.TE_CYCLE_W, "F": capi.TE_CYCLE_FMG}
+        if self.opts.cycle_type not in types:
+            raise TeError(capi.TE_ERR_UNSUPPORTED, "Unsupported Cycle type: " + str(self.opts.cycle_type))
         arr = (capi.TeCycleLevel * len(self.levels))()
         for k, (op, sm, r, i) in enumerate(self.levels):
             arr[k].op = op.h.value
@@ -417,7 +420,8 @@ class CycleBuilder:
         opts = capi.TeCycleOpts(o.pre_sweeps, o.post_sweeps, o.mid_sweeps, o.coarse_sweeps)
         c = Cycle()
         _bind_stream()
-        check(lib().te_vcycle_create(arr, len(self.levels), opts, dtype, ctypes.byref(c.h)))
+        check(lib().te_cycle_create(arr, len(self.levels), opts, types[self.opts.cycle_type], dtype,
+                                    ctypes.byref(c.h)))
         c._keep = list(self.levels)
         return c
 

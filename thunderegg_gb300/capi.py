@@ -18,6 +18,7 @@ TE_F64, TE_F32 = 0, 1
 TE_GHOST_BILINEAR, TE_GHOST_BIQUADRATIC, TE_GHOST_TRILINEAR = 0, 1, 2
 TE_FILL_FACES, TE_FILL_EDGES, TE_FILL_CORNERS = 0, 1, 2
 TE_NOALLOC_MAX_PARTIALS = 65536
+TE_CYCLE_V, TE_CYCLE_W, TE_CYCLE_FMG = 0, 1, 2
 
 _ip = ctypes.POINTER(ctypes.c_int)
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -107,6 +108,7 @@ _SIGS = {
     "te_interpolator_destroy": (_I, [_V]),
     "te_interpolate": (_I, [_V, _I, _I, _V, _V]),
     "te_vcycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, ctypes.POINTER(_V)]),
+    "te_cycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, _I, ctypes.POINTER(_V)]),
     "te_cycle_destroy": (_I, [_V]),
     "te_cycle_apply": (_I, [_V, _I, _V, _V]),
     "te_cycle_timings": (_I, [_V, _I, _V, _V, _I, ctypes.c_char_p, _dp, _ip]),

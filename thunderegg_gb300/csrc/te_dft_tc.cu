@@ -59,7 +59,7 @@ struct TcShape {
   static constexpr int SPLIT = 2;                               // threads per line
   static constexpr int RPP = DIM == 2 ? NN : NN * NN;          // lines per patch
   static constexpr int NCELL = RPP * NN;                        // cells per patch
-  static constexpr int ROWS = RPP > 128 ? RPP : 128;            // lines (threads) per CTA
+  static constexpr int ROWS = RPP > 128 ? RPP : 128;            // lines per CTA
   static constexpr int THREADS = ROWS * SPLIT;                  // threads per CTA
   static constexpr int JN = NN / SPLIT;                         // columns per thread
   static constexpr int G = ROWS / RPP;                          // patches per CTA

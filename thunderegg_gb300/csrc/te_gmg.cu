@@ -716,12 +716,22 @@ int te_interpolate(const te_interpolator* i, int nc, int dtype, const void* coar
 }
 
 int te_vcycle_create(const te_cycle_level* levels, int num_levels, te_cycle_opts opts, int dtype, te_cycle** out) {
+  return te_cycle_create(levels, num_levels, opts, TE_CYCLE_V, dtype, out);
+}
+
+int te_cycle_create(const te_cycle_level* levels, int num_levels, te_cycle_opts opts, int cycle_type, int dtype,
+                    te_cycle** out) {
   return guard([&] {
     require(levels && out && num_levels >= 1, "bad arguments");
     require(dtype == TE_F64 || dtype == TE_F32, "bad dtype");
+    require(cycle_type == TE_CYCLE_V || cycle_type == TE_CYCLE_W || cycle_type == TE_CYCLE_FMG,
+            "Unsupported Cycle type", TE_ERR_UNSUPPORTED);
+    require(opts.pre_sweeps >= 0 && opts.post_sweeps >= 0 && opts.mid_sweeps >= 0 && opts.coarse_sweeps >= 0,
+            "sweep counts must be >= 0");
     auto c = std::make_unique<te_cycle>();
     c->levels.assign(levels, levels + num_levels);
     c->opts = opts;
+    c->type = cycle_type;
     c->dtype = dtype;
     for (int k = 0; k < num_levels; k++) {
       require(levels[k].op && levels[k].smoother, "every level needs an operator and a smoother");

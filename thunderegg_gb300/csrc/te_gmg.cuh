@@ -69,6 +69,7 @@ bool vc_restrict_fine(const te_restrictor* r, const te_operator* op, const T* u,
 struct te_cycle {
   std::vector<te_cycle_level> levels;
   te_cycle_opts opts{1, 1, 1, 1};
+  int type = TE_CYCLE_V;  // CycleOpts::cycle_type "V", "W" or "F"
   int dtype = TE_F64;
   int nc = 1;
   cudaStream_t stream = nullptr;  // caller's stream (that of the level handles)
@@ -102,7 +103,7 @@ struct te_cycle {
   // fused path: every level smooths with the DFT solver, one pre/post sweep,
   // even patch sizes, no ghost extrapolation, one component
   bool fusable = false;
-  bool fused() const { return fusable && nc == 1; }
+  bool fused() const { return fusable && nc == 1 && type == TE_CYCLE_V; }
   // the FP32 fused cycle runs the DFT solves of level k on the tensor cores
   bool tc_enabled = true;
   bool use_tc(int k) const { return tc_enabled && dtype == TE_F32 && levels[k].smoother->tc_ok; }
@@ -181,19 +182,12 @@ struct te_cycle {
   void smooth(int k, const void* fk, void* uk, int times, bool fresh, cudaStream_t s) const {
     for (int i = 0; i < times; i++) te::patch_smooth(levels[k].smoother, nc, dtype, fk, uk, fresh && i == 0, s);
   }
-  // VCycle::visit (GMG/VCycle.h:46-70); u enters as zero at every level
-  void visit(int k, const void* fk, void* uk, cudaStream_t s) const {
-    int last = (int)levels.size() - 1;
-    if (k == last) {
-      smooth(k, fk, uk, opts.coarse_sweeps, true, s);
-      return;
-    }
-    smooth(k, fk, uk, opts.pre_sweeps, true, s);
+  // Cycle::restrict (GMG/Cycle.h:57-65) into f[k + 1]; `fresh`: u is still zero
+  void restrict_residual(int k, const void* fk, void* uk, bool fresh, cudaStream_t s) const {
     void* fc = f[k + 1].p;
-    void* uc = u[k + 1].p;
     const te_restrictor* R = levels[k].restrictor;
-    if (!R->extrapolate && opts.pre_sweeps > 0) {
-      // Cycle::restrict (GMG/Cycle.h:57-65) fused: fill ghosts, then r = f - A u restricted
+    if (!R->extrapolate && !fresh) {
+      // fused: fill ghosts, then r = f - A u restricted
       te::ghost_fill(levels[k].op->gf, nc, dtype, uk, s);
       te::residual_restrict(R, levels[k].op, nc, dtype, fk, uk, fc, s);
     } else {
@@ -202,13 +196,61 @@ struct te_cycle {
       te::residual(dom(k), nc, dtype, fk, rk, s);
       te::restrict_level(R, nc, dtype, rk, fc, s);
     }
-    // the coarse iterate starts at zero: its first sweep writes every cell
-    if (opts.pre_sweeps == 0 && (int)k + 1 != last) TE_CUDA(cudaMemsetAsync(uc, 0, bytes(k + 1), s));
-    if ((int)k + 1 == last && opts.coarse_sweeps == 0) TE_CUDA(cudaMemsetAsync(uc, 0, bytes(k + 1), s));
-    visit(k + 1, fc, uc, s);
+  }
+  // the coarse iterate u[k + 1] starts at zero (getZeroClone); a first sweep
+  // from a fresh iterate writes every cell, otherwise it is cleared here
+  void zero_coarse(int k, cudaStream_t s) const {
+    const int last = (int)levels.size() - 1;
+    const int first = k + 1 == last ? opts.coarse_sweeps : opts.pre_sweeps;
+    if (first == 0) TE_CUDA(cudaMemsetAsync(u[k + 1].p, 0, bytes(k + 1), s));
+  }
+  // VCycle::visit (GMG/VCycle.h:46-70), WCycle::visit (GMG/WCycle.h:50-84),
+  // FMGCycle::visit (GMG/FMGCycle.h:68-104).  `fresh`: u is zero on entry.
+  // The W and FMG cycles smooth mid_sweeps times after the first coarse
+  // correction, restrict the new residual and visit the coarser level again
+  // from its first result (u[k + 1] is not cleared in between, as in the
+  // reference); the FMG cycle's second visit is its v_visit.
+  void visit(int k, const void* fk, void* uk, bool fresh, cudaStream_t s) const {
+    const int last = (int)levels.size() - 1;
+    if (k == last) {
+      smooth(k, fk, uk, opts.coarse_sweeps, fresh, s);
+      return;
+    }
+    smooth(k, fk, uk, opts.pre_sweeps, fresh, s);
+    restrict_residual(k, fk, uk, fresh && opts.pre_sweeps == 0, s);
+    void* fc = f[k + 1].p;
+    void* uc = u[k + 1].p;
+    zero_coarse(k, s);
+    visit(k + 1, fc, uc, true, s);
     te::interpolate_level(levels[k + 1].interpolator, nc, dtype, uc, uk, s);
+    if (type != TE_CYCLE_V) {
+      smooth(k, fk, uk, opts.mid_sweeps, false, s);
+      restrict_residual(k, fk, uk, false, s);
+      if (type == TE_CYCLE_W)
+        visit(k + 1, fc, uc, false, s);
+      else
+        v_visit(k + 1, fc, uc, s);
+      te::interpolate_level(levels[k + 1].interpolator, nc, dtype, uc, uk, s);
+    }
     smooth(k, fk, uk, opts.post_sweeps, false, s);
   }
+  // FMGCycle::v_visit (GMG/FMGCycle.h:43-66): u enters with the level's previous
+  // result; one pre/post-smoothed pass whose coarser visit is visit()
+  void v_visit(int k, const void* fk, void* uk, cudaStream_t s) const {
+    const int last = (int)levels.size() - 1;
+    if (k == last) {
+      smooth(k, fk, uk, opts.coarse_sweeps, false, s);
+      return;
+    }
+    smooth(k, fk, uk, opts.pre_sweeps, false, s);
+    restrict_residual(k, fk, uk, false, s);
+    zero_coarse(k, s);
+    visit(k + 1, f[k + 1].p, u[k + 1].p, true, s);
+    te::interpolate_level(levels[k + 1].interpolator, nc, dtype, u[k + 1].p, uk, s);
+    smooth(k, fk, uk, opts.post_sweeps, false, s);
+  }
+  // sweeps of the finest level's first smooth; a single-level cycle clears u first
+  int first_sweeps() const { return levels.size() == 1 ? 0 : opts.pre_sweeps; }
   void body(const void* f64, void* u64, cudaStream_t s) const {
     // Cycle::apply (GMG/Cycle.h:94-98): u.setWithGhost(0); visit(finest, f, u)
     if (fused()) {
@@ -219,12 +261,12 @@ struct te_cycle {
       return;
     }
     if (dtype == TE_F64) {
-      if (opts.pre_sweeps == 0 || levels.size() == 1) TE_CUDA(cudaMemsetAsync(u64, 0, bytes(0), s));
-      visit(0, f64, u64, s);
+      if (first_sweeps() == 0) TE_CUDA(cudaMemsetAsync(u64, 0, bytes(0), s));
+      visit(0, f64, u64, true, s);
     } else {
       te::convert_level(dom(0), nc, dtype, f[0].p, TE_F64, f64, s);
-      if (opts.pre_sweeps == 0 || levels.size() == 1) TE_CUDA(cudaMemsetAsync(u[0].p, 0, bytes(0), s));
-      visit(0, f[0].p, u[0].p, s);
+      if (first_sweeps() == 0) TE_CUDA(cudaMemsetAsync(u[0].p, 0, bytes(0), s));
+      visit(0, f[0].p, u[0].p, true, s);
       te::convert_level(dom(0), nc, TE_F64, u64, dtype, u[0].p, s);
     }
   }
@@ -235,8 +277,8 @@ struct te_cycle {
       vfused<float, float, float>(0, f32, u32, s);
       return;
     }
-    if (opts.pre_sweeps == 0 || levels.size() == 1) TE_CUDA(cudaMemsetAsync(u32, 0, bytes(0), s));
-    visit(0, f32, u32, s);
+    if (first_sweeps() == 0) TE_CUDA(cudaMemsetAsync(u32, 0, bytes(0), s));
+    visit(0, f32, u32, true, s);
   }
   // run on stream s (which may itself be capturing)
   void apply_on(const void* f64, void* u64, cudaStream_t s) {

@@ -30,6 +30,8 @@ class GmgOptions:
     pre_sweeps: int = 1
     post_sweeps: int = 1
     coarse_sweeps: int = 1
+    mid_sweeps: int = 1             # W and FMG cycles
+    cycle_type: str = "V"           # "V", "W" or "F" (FMG)
     extrapolate_boundary_ghosts: bool = False
     tol: float = 1e-10
     max_it: int = 1000
@@ -63,7 +65,8 @@ class GmgSolver:
                             for k in range(n - 1)]
         self.interpolators = [None] + [DirectInterpolator(self.domains[k], self.domains[k - 1])
                                        for k in range(1, n)]
-        b = CycleBuilder(CycleOpts(opts.pre_sweeps, opts.post_sweeps, 1, opts.coarse_sweeps))
+        b = CycleBuilder(CycleOpts(opts.pre_sweeps, opts.post_sweeps, opts.mid_sweeps, opts.coarse_sweeps,
+                                   opts.cycle_type))
         for k in range(n):
             if k == 0 and n > 1:
                 b.addFinestLevel(self.ops[0], self.smoothers[0], self.restrictors[0])
