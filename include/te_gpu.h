@@ -246,6 +246,16 @@ int te_bicgstab_solve(const te_operator* A, int ncomp, void* x, const void* b, c
                       double tol, int max_iterations, int flags, int* iterations,
                       double* final_residual);
 
+/* ---- Iterative::CG (Iterative/CG.h:126-194) ------------------------------- */
+/* CG on FP64 device vectors of A's domain in the reference's form: the
+ * iteration runs on a correction started at zero, applies M to each search
+ * direction before A, and ends with x = M y + x0.  M may be NULL (any cycle
+ * type and precision).  Stops when ||r||/||b|| <= tol; *final_residual is
+ * that recursive residual.  TE_ERR_BREAKDOWN when rho == 0 (the reference
+ * throws BreakdownError).  A zero b returns at once with x's interior zero. */
+int te_cg_solve(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M, double tol,
+                int max_iterations, int* iterations, double* final_residual);
+
 /* Batched form: num_solves independent systems whose finest-level patches
  * are the contiguous ranges [patch_offsets[i], patch_offsets[i+1]) of A's
  * domain (a union of meshes of equal depth; M a V-cycle on the union).  Each

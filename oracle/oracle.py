@@ -37,7 +37,7 @@ class GmgConfig(ctypes.Structure):
                 ("pre_sweeps", ctypes.c_int), ("post_sweeps", ctypes.c_int),
                 ("coarse_sweeps", ctypes.c_int), ("extrapolate_boundary_ghosts", ctypes.c_int),
                 ("tol", ctypes.c_double), ("max_it", ctypes.c_int), ("use_precond", ctypes.c_int),
-                ("mid_sweeps", ctypes.c_int), ("cycle_type", ctypes.c_int)]
+                ("mid_sweeps", ctypes.c_int), ("cycle_type", ctypes.c_int), ("krylov", ctypes.c_int)]
 
 
 CYCLE_TYPES = {"V": 0, "W": 1, "F": 2}  # CycleOpts::cycle_type strings (CycleBuilder.h:176-191)
@@ -46,11 +46,11 @@ CYCLE_TYPES = {"V": 0, "W": 1, "F": 2}  # CycleOpts::cycle_type strings (CycleBu
 def gmg_config(scheme=0, fill_type=0, op_kind=0, neumann=0, smoother=0, dft_neumann_mask=0,
                inner_tol=1e-12, inner_max_it=1000, inner_continue_on_breakdown=1, pre_sweeps=1,
                post_sweeps=1, coarse_sweeps=1, extrapolate_boundary_ghosts=0, tol=1e-10,
-               max_it=1000, use_precond=1, mid_sweeps=1, cycle_type="V"):
+               max_it=1000, use_precond=1, mid_sweeps=1, cycle_type="V", krylov="bicgstab"):
     return GmgConfig(scheme, fill_type, op_kind, neumann, smoother, dft_neumann_mask, inner_tol,
                      inner_max_it, inner_continue_on_breakdown, pre_sweeps, post_sweeps,
                      coarse_sweeps, extrapolate_boundary_ghosts, tol, max_it, use_precond,
-                     mid_sweeps, CYCLE_TYPES[cycle_type])
+                     mid_sweeps, CYCLE_TYPES[cycle_type], {"bicgstab": 0, "cg": 1}[krylov])
 
 
 def build(ref: bool = False):
@@ -177,7 +177,8 @@ class Oracle:
         return u
 
     def solve(self, levels, f, cfg, u0=None, coeffs=None, ncomp=1):
-        """BiCGStab(A, u, f, VCycle) -> (u, iterations, final relative residual, status)."""
+        """BiCGStab(A, u, f, cycle), or CG with cfg.krylov = 1 -> (u, iterations, final relative
+        residual, status)."""
         arr, keep = self._levels(levels)
         carr, ckeep = self._coeffs(coeffs, len(levels))
         f = np.ascontiguousarray(f, dtype=np.float64)

@@ -17,6 +17,7 @@
 #include <ThunderEgg/GMG/DirectInterpolator.h>
 #include <ThunderEgg/GMG/LinearRestrictor.h>
 #include <ThunderEgg/Iterative/BiCGStab.h>
+#include <ThunderEgg/Iterative/CG.h>
 #include <ThunderEgg/Iterative/PatchSolver.h>
 #include <ThunderEgg/Poisson/DFTPatchSolver.h>
 #include <ThunderEgg/Poisson/StarPatchOperator.h>
@@ -258,11 +259,18 @@ static int gmg(const te_level_desc* levels, int nlevels, const teo_gmg_config* c
     M->apply(fv, uv);
     return TE_OK;
   }
-  Iterative::BiCGStab<D> outer;
-  outer.setTolerance(cfg->tol);
-  outer.setMaxIterations(cfg->max_it);
   try {
-    *iterations = outer.solve(*ops[0], uv, fv, cfg->use_precond ? M.get() : nullptr);
+    if (cfg->krylov == 1) {
+      Iterative::CG<D> outer;
+      outer.setTolerance(cfg->tol);
+      outer.setMaxIterations(cfg->max_it);
+      *iterations = outer.solve(*ops[0], uv, fv, cfg->use_precond ? M.get() : nullptr);
+    } else {
+      Iterative::BiCGStab<D> outer;
+      outer.setTolerance(cfg->tol);
+      outer.setMaxIterations(cfg->max_it);
+      *iterations = outer.solve(*ops[0], uv, fv, cfg->use_precond ? M.get() : nullptr);
+    }
   } catch (const Iterative::BreakdownError&) {
     return TE_ERR_BREAKDOWN;
   }

@@ -1319,7 +1319,61 @@ int teo_vcycle_apply(const te_level_desc* levels, int nlevels, const teo_gmg_con
   });
 }
 
-// BiCGStab(A = finest operator, M = V-cycle) solve; returns TE_ERR_BREAKDOWN on rho == 0
+// Iterative::CG::solve (Iterative/CG.h:126-194): right-preconditioned in the
+// reference's form -- the iteration runs on a correction started at zero
+// (x.set(0) after the initial residual), the preconditioner is applied to the
+// search direction before A, and at the end the correction is mapped through
+// Mr and the initial guess added back.  A zero right-hand side returns at once
+// with x = 0 (the initial guess is not restored there, as in the reference).
+int cg(const Space& V, const ApplyFn& A, double* x, const double* b, const ApplyFn* Mr, double tol, int max_it,
+       double* final_res, bool* breakdown) {
+  *breakdown = false;
+  std::vector<double> resid = V.zero();
+  A(x, resid.data());
+  V.each([&](long i) { resid[i] = resid[i] * -1 + b[i]; });  // scaleThenAdd(-1, b)
+  std::vector<double> initial_guess(x, x + V.size());
+  V.each([&](long i) { x[i] = 0.0; });  // x.set(0)
+  double r0 = V.norm(b);
+  std::vector<double> p = resid, ap = V.zero(), tmp;
+  if (Mr) tmp = V.zero();
+  double rho = V.dot(resid.data(), resid.data());
+  int its = 0;
+  if (final_res) *final_res = 0.0;
+  if (r0 == 0) return its;
+  double residual = V.norm(resid.data()) / r0;
+  if (final_res) *final_res = residual;
+  while (residual > tol && its < max_it) {
+    if (rho == 0) {
+      *breakdown = true;
+      return its;
+    }
+    if (Mr) {
+      std::fill(tmp.begin(), tmp.end(), 0.0);
+      (*Mr)(p.data(), tmp.data());
+      A(tmp.data(), ap.data());
+    } else {
+      A(p.data(), ap.data());
+    }
+    double alpha = rho / V.dot(p.data(), ap.data());
+    V.each([&](long i) { x[i] += p[i] * alpha; });           // x.addScaled(alpha, p)
+    V.each([&](long i) { resid[i] += ap[i] * -alpha; });     // resid.addScaled(-alpha, ap)
+    double rho_new = V.dot(resid.data(), resid.data());
+    double beta = rho_new / rho;
+    V.each([&](long i) { p[i] = p[i] * beta + resid[i]; });  // p.scaleThenAdd(beta, resid)
+    its++;
+    rho = rho_new;
+    residual = V.norm(resid.data()) / r0;
+    if (final_res) *final_res = residual;
+  }
+  if (Mr) {
+    (*Mr)(x, resid.data());
+    V.each([&](long i) { x[i] = resid[i]; });  // x.copy(resid)
+  }
+  V.each([&](long i) { x[i] += initial_guess[i]; });  // x.add(initial_guess)
+  return its;
+}
+
+// BiCGStab (or CG) with A = finest operator, M = the cycle; returns TE_ERR_BREAKDOWN on rho == 0
 int teo_gmg_solve(const te_level_desc* levels, int nlevels, const teo_gmg_config* cfg,
                   const double* const* coeffs, int nc, double* u, const double* f, int* iterations,
                   double* final_residual) {
@@ -1332,8 +1386,11 @@ int teo_gmg_solve(const te_level_desc* levels, int nlevels, const teo_gmg_config
     ApplyFn M = [&](double* x, double* b) { H->apply(x, b, nc); };
     bool bd = false;
     try {
-      *iterations = bicgstab(V, A, u, f, cfg->use_precond ? &M : nullptr, cfg->tol, cfg->max_it,
-                             final_residual, &bd);
+      if (cfg->krylov == 1)
+        *iterations = cg(V, A, u, f, cfg->use_precond ? &M : nullptr, cfg->tol, cfg->max_it, final_residual, &bd);
+      else
+        *iterations = bicgstab(V, A, u, f, cfg->use_precond ? &M : nullptr, cfg->tol, cfg->max_it,
+                               final_residual, &bd);
     } catch (...) {
       delete H;
       throw;

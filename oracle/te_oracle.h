@@ -23,6 +23,7 @@ typedef struct teo_gmg_config {
   int use_precond;        /* 0: BiCGStab without the V-cycle                */
   int mid_sweeps;         /* W and FMG cycles (CycleOpts.h:45)              */
   int cycle_type;         /* 0 "V", 1 "W", 2 "F" (CycleBuilder.h:176-191)   */
+  int krylov;             /* outer solver: 0 Iterative::BiCGStab, 1 Iterative::CG */
 } teo_gmg_config;
 #ifdef __cplusplus
 }

@@ -257,3 +257,54 @@ def test_unknown_cycle_type(te):
     with pytest.raises(TeError) as e:
         GmgSolver(M.uniform_mesh(2, 2, 8), GmgOptions(cycle_type="X"))
     assert e.value.code == TE_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("idx", range(3))
+@pytest.mark.parametrize("cycle_type", ("V", "W"))
+def test_cg_matches_oracle(te, oracle, idx, cycle_type):
+    """Iterative::CG (Iterative/CG.h:126-194) preconditioned by the FP64 cycle:
+    the oracle's iteration count (pinned to the reference's CG by
+    tests/test_oracle_pin.py) and its solution to the solver tolerance, from a
+    nonzero initial guess."""
+    from oracle import gmg_config
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    name, levels, scheme = meshes()[idx]
+    rng = np.random.default_rng(70 + idx)
+    f = rng.standard_normal(levels[0].padded_shape(1))
+    u0 = rng.standard_normal(levels[0].padded_shape(1))
+    u_o, its_o, _, rc = oracle.solve(levels, f, gmg_config(scheme=scheme, smoother=0, cycle_type=cycle_type,
+                                                           krylov="cg"), u0=u0)
+    assert rc == 0
+    s = GmgSolver(levels, GmgOptions(scheme=scheme, smoother=0, cycle_type=cycle_type, krylov="cg"))
+    fv = te.Vector.from_numpy(s.finest, f)
+    uv = te.Vector.from_numpy(s.finest, u0)
+    assert s.solve(fv, uv) == its_o
+    g = levels[0].num_ghost
+    inner = (Ellipsis,) + tuple(slice(g, -g) for _ in range(levels[0].dim))
+    assert rel_err(uv.numpy()[inner], u_o[inner]) <= 1e-8
+    assert s.residual(fv, uv) <= 1e-9
+
+
+def test_cg_unpreconditioned_and_zero_rhs(te, oracle):
+    """CG without a preconditioner runs the oracle's iterations; a zero
+    right-hand side returns at once with the interior zeroed."""
+    from oracle import gmg_config
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels = M.uniform_mesh(2, 2, 8)
+    rng = np.random.default_rng(80)
+    f = rng.standard_normal(levels[0].padded_shape(1))
+    u_o, its_o, _, rc = oracle.solve(levels, f, gmg_config(scheme=0, krylov="cg", use_precond=0, tol=1e-9))
+    s = GmgSolver(levels, GmgOptions(scheme=0, krylov="cg", tol=1e-9))
+    fv = te.Vector.from_numpy(s.finest, f)
+    uv = te.Vector(s.finest)
+    its = s.solve(fv, uv, precondition=False)
+    assert abs(its - its_o) <= 1  # unpreconditioned CG: reduction order may move the last iteration
+    inner = (Ellipsis, slice(1, -1), slice(1, -1))
+    assert rel_err(uv.numpy()[inner], u_o[inner]) <= 1e-7
+    zv = te.Vector(s.finest)
+    uv = te.Vector.from_numpy(s.finest, rng.standard_normal(levels[0].padded_shape(1)))
+    assert s.solve(zv, uv) == 0
+    assert np.all(uv.numpy()[inner] == 0.0)

@@ -106,3 +106,28 @@ def test_reference_bicgstab_early_exit_quirk(oracle):
     inner = (Ellipsis, slice(1, -1), slice(1, -1))
     true_res = np.linalg.norm((f - Au)[inner]) / np.linalg.norm(f[inner])
     assert rc == 0 and its < 20 and true_res > 1e-8
+
+
+def test_oracle_cg_matches_reference_live(oracle, ref):
+    """The oracle's CG (te_oracle.cpp cg) against Iterative::CG itself, with and
+    without the V/W/FMG cycle as preconditioner, from a nonzero initial guess,
+    and the zero right-hand-side early return."""
+    from oracle import gmg_config
+    from thunderegg_gb300 import mesh as M
+
+    rng = np.random.default_rng(7)
+    for levels, sc in ((M.circle_mesh(n=6, lo=1, hi=4), 1), (M.random_mesh(11, n=4, dim=3, lo=1, hi=3), 2)):
+        lv = levels[0]
+        g = lv.num_ghost
+        inner = (Ellipsis,) + tuple(slice(g, -g) for _ in range(lv.dim))
+        f = rng.standard_normal(lv.padded_shape(1))
+        u0 = rng.standard_normal(lv.padded_shape(1))
+        for pre, ct in ((1, "V"), (1, "W"), (1, "F"), (0, "V")):
+            cfg = gmg_config(scheme=sc, smoother=0, cycle_type=ct, tol=1e-10, krylov="cg", use_precond=pre,
+                             max_it=200)
+            a, b = oracle.solve(levels, f, cfg, u0=u0), ref.solve(levels, f, cfg, u0=u0)
+            assert a[1] == b[1] and a[3] == b[3] and np.array_equal(a[0][inner], b[0][inner]), (pre, ct)
+        z = np.zeros_like(f)
+        a, b = oracle.solve(levels, z, gmg_config(scheme=sc, krylov="cg"), u0=u0), \
+            ref.solve(levels, z, gmg_config(scheme=sc, krylov="cg"), u0=u0)
+        assert a[1] == b[1] == 0 and np.array_equal(a[0][inner], b[0][inner])

@@ -457,3 +457,33 @@ class BiCGStab:
                                       ctypes.byref(its), ctypes.byref(res)))
         self.final_residual = res.value
         return its.value
+
+
+class CG:
+    """Iterative::CG (Iterative/CG.h:40-194) on the GPU, FP64 vectors; Mr is
+    applied to each search direction before A, as in the reference."""
+
+    def __init__(self, tolerance=1e-12, max_iterations=1000):
+        self.tolerance, self.max_iterations = tolerance, max_iterations
+        self.final_residual = None
+
+    def setTolerance(self, tol):
+        self.tolerance = tol
+
+    def setMaxIterations(self, n):
+        self.max_iterations = n
+
+    def getTolerance(self):
+        return self.tolerance
+
+    def getMaxIterations(self):
+        return self.max_iterations
+
+    def solve(self, A, x: Vector, b: Vector, Mr=None):
+        its = ctypes.c_int(0)
+        res = ctypes.c_double(0)
+        check(lib().te_cg_solve(A.h, x.ncomp, x.ptr, b.ptr, Mr.h if Mr is not None else None,
+                                float(self.tolerance), int(self.max_iterations), ctypes.byref(its),
+                                ctypes.byref(res)))
+        self.final_residual = res.value
+        return its.value

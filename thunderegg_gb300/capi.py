@@ -109,6 +109,7 @@ _SIGS = {
     "te_interpolate": (_I, [_V, _I, _I, _V, _V]),
     "te_vcycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, ctypes.POINTER(_V)]),
     "te_cycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, _I, ctypes.POINTER(_V)]),
+    "te_cg_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
     "te_cycle_destroy": (_I, [_V]),
     "te_cycle_apply": (_I, [_V, _I, _V, _V]),
     "te_cycle_timings": (_I, [_V, _I, _V, _V, _I, ctypes.c_char_p, _dp, _ip]),

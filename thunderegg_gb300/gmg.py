@@ -11,7 +11,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from . import (BiCGStab, BiCGStabPatchSolver, BiLinearGhostFiller, BiQuadraticGhostFiller, CycleBuilder,
+from . import (CG, BiCGStab, BiCGStabPatchSolver, BiLinearGhostFiller, BiQuadraticGhostFiller, CycleBuilder,
                CycleOpts, DFTPatchSolver, DirectInterpolator, Domain, LinearRestrictor,
                PoissonStarPatchOperator, TriLinearGhostFiller, VarPoissonStarPatchOperator, Vector)
 from .capi import TE_F32, TE_F64
@@ -37,6 +37,7 @@ class GmgOptions:
     max_it: int = 1000
     cycle_dtype: int = TE_F64       # TE_F32: mixed-precision V-cycle
     bicgstab_flags: int = 0         # 1: preconditioned early-exit update
+    krylov: str = "bicgstab"        # outer solver: "bicgstab" or "cg"
 
 
 class GmgSolver:
@@ -75,7 +76,10 @@ class GmgSolver:
             else:
                 b.addCoarsestLevel(self.ops[k], self.smoothers[k], self.interpolators[k])
         self.cycle = b.getCycle(opts.cycle_dtype)
-        self.krylov = BiCGStab(opts.tol, opts.max_it, opts.bicgstab_flags)
+        if opts.krylov == "cg":
+            self.krylov = CG(opts.tol, opts.max_it)
+        else:
+            self.krylov = BiCGStab(opts.tol, opts.max_it, opts.bicgstab_flags)
 
     @property
     def finest(self):
