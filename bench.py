@@ -272,6 +272,56 @@ def level_kernel_rooflines(te, solver, hbm, reps=15, warm=3):
             "peak_gbs": hbm, "l2": "flushed before every call", "kernels": out}
 
 
+def solver_variants_measure(te, reps=3):
+    """One solve at a time with the other cycles and Krylov solvers of the API,
+    device time per solve (CUDA events, median of `reps` after one warm-up),
+    outer iterations and the true FP64 residual.  W and FMG cycles run the
+    config-2 problem.  CG runs unpreconditioned on a uniform 2D mesh (32 x 32
+    patches of 32^2: no coarse-fine faces, a symmetric operator) with a
+    sine-mode RHS: the reference's CG applies Mr on the right (A Mr p), which
+    is not symmetric, and with the multigrid cycle as Mr it diverges on these
+    problems in the reference itself (the oracle reproduces it bit for bit)."""
+    import numpy as np
+    import torch
+
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels, f_np, _ = PB.config2()
+    uni = M.uniform_mesh(2, 5, 32)
+    f_uni = PB.sine_modes_rhs(uni[0], np.random.default_rng(3))
+    stream = torch.cuda.current_stream()
+    out = {}
+    c2 = (levels, f_np, "config 2 (circle L3-7, 1444 patches of 32^2)")
+    u2 = (uni, f_uni, "2D uniform L5, 1024 patches of 32^2")
+    variants = [("bicgstab_W_cycle_mixed", c2, dict(cycle_type="W", cycle_dtype=te.TE_F32, bicgstab_flags=1)),
+                ("bicgstab_FMG_cycle_mixed", c2, dict(cycle_type="F", cycle_dtype=te.TE_F32, bicgstab_flags=1)),
+                ("bicgstab_W_cycle_fp64", c2, dict(cycle_type="W", cycle_dtype=te.TE_F64, bicgstab_flags=1)),
+                ("bicgstab_V_cycle_mixed_uniform", u2, dict(cycle_dtype=te.TE_F32, bicgstab_flags=1)),
+                ("cg_unpreconditioned_fp64_uniform", u2, dict(krylov="cg", max_it=5000))]
+    for name, (lv, f_np, what), kw in variants:
+        pre = not name.startswith("cg_unpreconditioned")
+        s = GmgSolver(lv, GmgOptions(scheme=1, smoother=0, tol=1e-10, **kw))
+        fv = te.Vector.from_numpy(s.finest, f_np)
+        uv = te.Vector(s.finest)
+        times, its = [], 0
+        for i in range(reps + 1):
+            uv.t.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            its = s.solve(fv, uv, precondition=pre)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i:
+                times.append(e0.elapsed_time(e1) / 1000.0)
+        t = statistics.median(times)
+        out[name] = {"problem": what, "solves_per_s": 1.0 / t, "ms": 1000 * t, "outer_iterations": its,
+                     "true_rel_residual_fp64": s.residual(fv, uv)}
+    return out
+
+
 def replica_throughput(local_seconds, local_solves, device="cuda"):
     """Whole-job throughput of independent replicas (one process per GPU, no data
     exchange): every rank's solves summed, divided by the slowest rank's time.
@@ -579,6 +629,7 @@ def run_gpu(args):
     c3 = config3_measure(te) if extra else None
     c4 = config4_measure(te) if extra else None
     lk = level_kernel_rooflines(te, served, hbm) if extra else None
+    sv = solver_variants_measure(te) if extra else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -623,6 +674,7 @@ def run_gpu(args):
         "config3": c3,
         "config4": c4,
         "level_kernels": lk,
+        "solver_variants": sv,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
