@@ -445,7 +445,8 @@ def serving_stream(args, te):
     for i in range(len(kinds)):
         srv.submit(Request(meshes[i], PB.sine_modes_rhs(meshes[i][0], rng), kinds[i][2]))
     srv.run()
-    srv = Server(budget_bytes=150e9, steps_per_round=2)
+    srv.results = {}
+    builds0, hits0, reforms0 = srv.stats["union_builds"], srv.stats["union_hits"], srv.stats["reforms"]
     t0 = time.perf_counter()
     ids, nxt = {}, 0
     while nxt < len(reqs) or not srv.idle():
@@ -469,7 +470,8 @@ def serving_stream(args, te):
     return {"requests": len(reqs), "arrival_rate_per_s": args.stream_rate, "solves_per_s": len(reqs) / wall,
             "latency_ms_p50": 1000 * pick(0.5), "latency_ms_p99": 1000 * pick(0.99),
             "max_rel_residual": res_max, "mean_iterations": float(np.mean(its)),
-            "max_batch": srv.stats["max_batch"], "reforms": srv.stats["reforms"],
+            "max_batch": srv.stats["max_batch"], "reforms": srv.stats["reforms"] - reforms0,
+            "union_builds": srv.stats["union_builds"] - builds0, "union_cache_hits": srv.stats["union_hits"] - hits0,
             "mix": "0.7 x 2D (circle L3-6 32^2, uniform L4 32^2, uniform L5 16^2), "
                    "0.3 x 3D (uniform L3 16^3, uniform L3 8^3); 150 GB budget",
             "latency_from": "scheduled arrival"}

@@ -97,3 +97,40 @@ def test_serving_rejects_oversize(te):
     with pytest.raises(TeError) as e:
         srv.submit(req)
     assert e.value.code == TE_ERR_BUDGET
+
+
+def test_serving_union_cache(te):
+    """A second wave of requests on the same meshes reuses the cached union
+    hierarchies (and their captured graphs); results are unchanged."""
+    from thunderegg_gb300.serve import Server
+
+    reqs = _requests(te, 4)
+    srv = Server(budget_bytes=64 << 30, steps_per_round=2)
+    for r in reqs:
+        srv.submit(r)
+    first = srv.run()
+    builds = srv.stats["union_builds"]
+    assert builds >= 1
+    for r in reqs:
+        srv.submit(r)
+    results = srv.run()
+    assert srv.stats["union_hits"] >= 1
+    assert srv.stats["union_builds"] - builds < builds  # most unions of the second wave were cached
+    _check(te, reqs, {rid: first[rid] for rid in range(len(reqs))})
+    _check(te, reqs, {rid - len(reqs): results[rid] for rid in range(len(reqs), 2 * len(reqs))})
+
+
+def test_serving_cache_respects_budget(te):
+    """Idle cached unions count against the budget and are evicted to admit new work."""
+    from thunderegg_gb300.serve import Server, request_bytes
+
+    reqs = _requests(te, 4)
+    per = max(request_bytes(r.levels, r.opts) for r in reqs)
+    srv = Server(budget_bytes=2 * per, steps_per_round=3)
+    for r in reqs:
+        srv.submit(r)
+    results = srv.run()
+    assert srv.stats["max_active_bytes"] <= 2 * per
+    assert srv.active_bytes + srv._idle_cache_bytes() <= 2 * per
+    assert srv.stats["union_evictions"] >= 1
+    _check(te, reqs, results)

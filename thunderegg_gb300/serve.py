@@ -17,6 +17,14 @@ iterations at a time (te_bicgstab_batch_step).  Between steps it
     right-hand side are copied into it, and its BiCGStab restarts from that
     iterate (its residual keeps decreasing; only the Krylov space is rebuilt).
 
+A union hierarchy depends only on its members' meshes (and coefficients), not
+on their right-hand sides, so the device objects of every union built are kept
+in a per-server cache keyed by the members' mesh sequence, together with the
+batch's x and b buffers (so the cycle's and the iteration's captured CUDA
+graphs are replayed, not captured again).  Idle cache entries count against
+the memory budget and are evicted least recently used when an admission needs
+the room.
+
 Each request stops on its own residual test; its arithmetic never mixes with
 other requests' (per-patch kernels, per-solve reductions), so its result
 matches a solve of the same request alone within the solver tolerance.  The
@@ -87,13 +95,12 @@ class _Active:
         self.x = None  # current iterate on the host between batches (numpy), None on the device
 
 
-class _Batch:
-    """One union-hierarchy batch of a class and its stepping BiCGStab run."""
+class _Union:
+    """The device objects of one union hierarchy and its batch buffers (a cache entry)."""
 
-    def __init__(self, members, x_parts, opts):
+    def __init__(self, members, opts):
         import torch
 
-        self.members = list(members)  # this batch's members, in patch order
         levels, offsets = M.union_hierarchy([m.req.levels for m in members])
         coeffs = None
         if members[0].req.coeffs is not None:
@@ -101,9 +108,30 @@ class _Batch:
         self.solver = GmgSolver(levels, opts, coeffs)
         self.offsets = offsets[0]
         shape = self.solver.finest.padded_shape(1)
-        # every patch range is written below, so the buffers need no zero fill
+        # every patch range is written before a batch runs, so the buffers need no zero fill
         self.x = Vector(self.solver.finest, data=torch.empty(shape, dtype=torch.float64, device="cuda"))
         self.b = Vector(self.solver.finest, data=torch.empty(shape, dtype=torch.float64, device="cuda"))
+        self.keep = [(m.req.levels, m.req.coeffs) for m in members]  # keeps the key's ids valid
+        self.bytes = sum(request_bytes(m.req.levels, m.req.opts) for m in members)
+        self.busy = False
+
+
+def _union_key(members):
+    return tuple((id(m.req.levels), id(m.req.coeffs)) for m in members)
+
+
+class _Batch:
+    """One union-hierarchy batch of a class and its stepping BiCGStab run."""
+
+    def __init__(self, members, x_parts, un):
+        import torch
+
+        self.members = list(members)  # this batch's members, in patch order
+        self.un = un
+        un.busy = True
+        self.solver = un.solver
+        self.offsets = un.offsets
+        self.x, self.b = un.x, un.b
         for i, m in enumerate(members):
             lo, hi = self.offsets[i], self.offsets[i + 1]
             self.b.t[lo:hi].copy_(torch.as_tensor(m.req.f.reshape(self.b.t[lo:hi].shape)), non_blocking=False)
@@ -144,6 +172,7 @@ class _Batch:
         if self.h:
             lib().te_bicgstab_batch_destroy(self.h)
             self.h = ctypes.c_void_p()
+            self.un.busy = False
 
 
 class Server:
@@ -154,7 +183,7 @@ class Server:
     steps_per_round: BiCGStab iterations a batch runs between scheduling
     decisions; max_batch: most requests per class batch."""
 
-    def __init__(self, budget_bytes=150e9, steps_per_round=2, max_batch=64):
+    def __init__(self, budget_bytes=150e9, steps_per_round=2, max_batch=64, cache=True):
         self.budget = int(budget_bytes)
         self.k = int(steps_per_round)
         self.max_batch = int(max_batch)
@@ -163,7 +192,35 @@ class Server:
         self.classes = {}         # key -> {"active": [_Active], "batch": _Batch or None, "dirty": bool}
         self.results = {}
         self.active_bytes = 0
-        self.stats = {"rounds": 0, "reforms": 0, "max_batch": 0, "max_active_bytes": 0, "admitted": 0}
+        self.use_cache = bool(cache)
+        self.unions = {}          # union key -> _Union, least recently used first
+        self.stats = {"rounds": 0, "reforms": 0, "max_batch": 0, "max_active_bytes": 0, "admitted": 0,
+                      "union_builds": 0, "union_hits": 0, "union_evictions": 0}
+
+    # ---- union cache
+    def _idle_cache_bytes(self):
+        return sum(u.bytes for u in self.unions.values() if not u.busy)
+
+    def _evict(self, need):
+        """Drop idle cached unions, least recently used first, until `need` more bytes fit."""
+        for key in list(self.unions):
+            if self.active_bytes + need + self._idle_cache_bytes() <= self.budget:
+                return
+            if not self.unions[key].busy:
+                del self.unions[key]
+                self.stats["union_evictions"] += 1
+
+    def _union(self, members, opts):
+        key = _union_key(members)
+        un = self.unions.pop(key, None)
+        if un is None:
+            un = _Union(members, opts)
+            self.stats["union_builds"] += 1
+        else:
+            self.stats["union_hits"] += 1
+        if self.use_cache:
+            self.unions[key] = un  # most recently used last
+        return un
 
     # ---- requests
     def submit(self, req: Request) -> int:
@@ -184,6 +241,8 @@ class Server:
         for rid, req, t0, nb in self.queue:
             key = _class_key(req)
             cls = self.classes.setdefault(key, {"active": [], "batch": None, "dirty": False, "bytes": {}})
+            if self.active_bytes + nb > self.budget:
+                self._evict(nb)
             if self.active_bytes + nb <= self.budget and len(cls["active"]) < self.max_batch:
                 a = _Active(rid, req, t0)
                 a.x = req.u0
@@ -198,6 +257,7 @@ class Server:
                 keep.append((rid, req, t0, nb))
         self.queue = keep
         self.stats["max_active_bytes"] = max(self.stats["max_active_bytes"], self.active_bytes)
+        self._evict(0)
 
     def _retire(self, cls, a, u, its, res, st):
         self.results[a.rid] = Result(u=u, iterations=its, residual=res, status=st,
@@ -224,7 +284,7 @@ class Server:
         cls["wait_rounds"] = 0
         while cls["active"]:
             members = cls["active"]
-            b = _Batch(members, [m.x for m in members], members[0].req.opts)
+            b = _Batch(members, [m.x for m in members], self._union(members, members[0].req.opts))
             self.stats["reforms"] += 1
             self.stats["max_batch"] = max(self.stats["max_batch"], len(members))
             its, res, st, run = b.state()
