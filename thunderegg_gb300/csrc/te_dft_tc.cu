@@ -115,6 +115,7 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
   static_assert(S::G * S::NCELL % NT == 0, "cells must split evenly over the threads");
   static_assert(S::G * 2 * DIM * NF % NT == 0, "corrections must split evenly over the threads");
   static_assert(JN % 8 == 0, "TMEM is read in blocks of 8 columns");
+  static_assert(NT % NN == 0, "every thread's cells share one x");
   extern __shared__ uint8_t dsm[];
   __shared__ uint64_t bar;
   __shared__ uint32_t tmem_base;
@@ -157,6 +158,11 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
     int m = e / (NN * NN), r = e % (NN * NN);
     *reinterpret_cast<float*>(Bm + m * S::BTILE + tc::tile_offset(r / NN, r % NN, NN, NN)) = a.bmat[e];
   }
+  // the first group's corrections; later groups' are written before the barrier that ends the previous group
+  if (has_corr) {
+#pragma unroll
+    for (int k = 0; k < CPER; k++) cbuf[t + k * NT] = cpf[k];
+  }
   if (t == 0) tc::mbar_init(&bar, 1);
   if (warp == 0) tc::tmem_alloc(&tmem_base, S::NCOLS);
   tc::fence_async_smem();
@@ -176,10 +182,34 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
 
   for (int grp = blockIdx.x; grp < a.ngroups && !abort; grp += gridDim.x) {
     const int p0 = grp * S::G;
+    // f_copy = f - corrections of the cell's sides, in side order (x, then y, then z
+    // sides): each thread's cells share one x (NT is a multiple of n), so the x
+    // sides concern two threads in n and the y and z sides whole rows (an FP64
+    // right-hand side takes its corrections in FP64)
     if (has_corr) {
+      const int xt = t % NN;
+      if (xt == 0 || xt == NN - 1) {
+        const int side = xt == 0 ? 0 : 1;
 #pragma unroll
-      for (int k = 0; k < CPER; k++) cbuf[t + k * NT] = cpf[k];
-      __syncthreads();
+        for (int k = 0; k < PER; k++) {
+          const int e = t + k * NT, i = e / S::NCELL, c = e % S::NCELL;
+          pf[k] -= (TI)cbuf[i * 2 * DIM * NF + side * NF + c / NN];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < PER; k++) {
+        const int e = t + k * NT, i = e / S::NCELL, c = e % S::NCELL;
+        const int y = (c / NN) % NN, z = DIM == 3 ? c / (NN * NN) : 0;
+        if (y == 0 || y == NN - 1) pf[k] -= (TI)cbuf[i * 2 * DIM * NF + (y == 0 ? 2 : 3) * NF + xt + NN * z];
+      }
+      if (DIM == 3) {
+#pragma unroll
+        for (int k = 0; k < PER; k++) {
+          const int e = t + k * NT, i = e / S::NCELL, c = e % S::NCELL;
+          const int y = (c / NN) % NN, z = c / (NN * NN);
+          if (z == 0 || z == NN - 1) pf[k] -= (TI)cbuf[i * 2 * DIM * NF + (z == 0 ? 4 : 5) * NF + xt + NN * y];
+        }
+      }
     }
     // right-hand sides into the operand tiles of the x pass: line (i, y[, z]), k = x
 #pragma unroll
@@ -187,17 +217,6 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
       int e = t + k * NT;
       int i = e / S::NCELL, c = e % S::NCELL;
       float v = (float)pf[k];
-      if (has_corr) {
-        // f_copy = f - corrections of the cell's sides, in side order
-        const float* cb = cbuf + i * 2 * DIM * NF;
-        const int x = c % NN, y = (c / NN) % NN, z = DIM == 3 ? c / (NN * NN) : 0;
-        if (x == 0) v -= cb[0 * NF + y + NN * z];
-        if (x == NN - 1) v -= cb[1 * NF + y + NN * z];
-        if (y == 0) v -= cb[2 * NF + x + NN * z];
-        if (y == NN - 1) v -= cb[3 * NF + x + NN * z];
-        if (DIM == 3 && z == 0) v -= cb[4 * NF + x + NN * y];
-        if (DIM == 3 && z == NN - 1) v -= cb[5 * NF + x + NN * y];
-      }
       float hi = tc::to_tf32(v), lo = v - hi;
       uint32_t off = tc::tile_offset(i * S::RPP + c / NN, c % NN, S::ROWS, NN);
       *reinterpret_cast<float*>(Ahi + off) = hi;
@@ -316,6 +335,11 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
           *reinterpret_cast<float*>(Alo + off) = lo;
         }
       }
+    }
+    // the next group's corrections (prefetched above; this group no longer reads cbuf)
+    if (has_corr) {
+#pragma unroll
+      for (int k = 0; k < CPER; k++) cbuf[t + k * NT] = cpf[k];
     }
     // the staging rows overlap the operand tiles the next group writes
     __syncthreads();

@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(256)
 // ghosts, the boundary shell after it.  f's ghost cells are not written (the
 // outer loop never reads them).
 template <int KIND, int SCHEME, int DIM, int NN, int NV>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 6)
     apply_dots_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const float2* __restrict__ inv_df,
                       int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
                       const GCall* __restrict__ calls, const int* __restrict__ side_code, int gs,
@@ -661,39 +661,77 @@ __global__ void __launch_bounds__(256)
     inv[a] = df64(v.x, v.y);
   }
   const F32Acc acc{u, (long long)CS};
-  for (int e = threadIdx.x; e < 2 * DIM * NF; e += blockDim.x) {
-    const int s = e / NF, r = e % NF;
-    const int code = side_code[p * 2 * DIM + s];
-    if (code == -1) continue;
-    G[s * gs + r] = side_ghost<df64, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, r % NN, r / NN);
+  // side ghosts gathered into registers first; they are written to shared
+  // memory after the interior cells, so the gather's dependent loads overlap
+  // the interior work instead of delaying the barrier
+  constexpr int NG = 2 * DIM * NF;
+  constexpr int GPT = (NG + 255) / 256;
+  df64 gv[GPT];
+#pragma unroll
+  for (int i = 0; i < GPT; i++) {
+    const int e = threadIdx.x + i * 256;
+    gv[i] = df64(0.f, 0.f);
+    if (NG % 256 == 0 || e < NG) {
+      const int s = e / NF, r = e % NF;
+      const int code = side_code[p * 2 * DIM + s];
+      if (code != -1) gv[i] = side_ghost<df64, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, r % NN, r / NN);
+    }
   }
   if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
   const float* up = u + (long long)p * CS;
   const long long base = (long long)p * CS;
   dot2 v[NV];
-  auto emit = [&](int k, df64 res) {
+  auto emitw = [&](int k, df64 res, df64 wv) {
     stv(f, base + k, res);
     if (NV == 1) {
-      v[0].add(ldv(w, base + k), res);
+      v[0].add(wv, res);
     } else {
-      v[0].add(res, ldv(w, base + k));
+      v[0].add(res, wv);
       v[1].add(res, res);
     }
   };
-  // cells away from the boundary: every neighbour is an interior FP32 value
-  for (int e = threadIdx.x; e < NIN; e += blockDim.x) {
+  auto emit = [&](int k, df64 res) { emitw(k, res, ldv(w, base + k)); };
+  auto interior_k = [&](int e) {
     const int x = e % (NN - 2) + 1, r = e / (NN - 2);
     const int y = r % (NN - 2) + 1, z = DIM == 3 ? r / (NN - 2) + 1 : 0;
-    const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
-    df64 res;
-    if (KIND == 0) {
-      const float mid = up[k];
-      res = df_second_difference(up[k + 1], mid, up[k - 1]) * inv[0];
-      res += df_second_difference(up[k + SY], mid, up[k - SY]) * inv[1];
-      if (DIM == 3) res += df_second_difference(up[k + SZ], mid, up[k - SZ]) * inv[2];
-    } else {
+    return (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
+  };
+  // cells away from the boundary: every neighbour is an interior FP32 value
+  if (KIND == 0) {
+    // two cells per round, all their loads issued before either is computed
+    for (int e0 = threadIdx.x; e0 < NIN; e0 += 512) {
+      int kk[2];
+      bool ok[2];
+      float m[2], xp[2], xm[2], yp[2], ym[2], zp[2], zm[2];
+      df64 wv[2];
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        ok[q] = e0 + q * 256 < NIN;
+        const int k = interior_k(ok[q] ? e0 + q * 256 : e0);
+        kk[q] = k;
+        m[q] = up[k];
+        xp[q] = up[k + 1];
+        xm[q] = up[k - 1];
+        yp[q] = up[k + SY];
+        ym[q] = up[k - SY];
+        zp[q] = DIM == 3 ? up[k + SZ] : 0.f;
+        zm[q] = DIM == 3 ? up[k - SZ] : 0.f;
+        wv[q] = ldv(w, base + k);
+      }
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        if (!ok[q]) continue;
+        df64 res = df_second_difference(xp[q], m[q], xm[q]) * inv[0];
+        res += df_second_difference(yp[q], m[q], ym[q]) * inv[1];
+        if (DIM == 3) res += df_second_difference(zp[q], m[q], zm[q]) * inv[2];
+        emitw(kk[q], res, wv[q]);
+      }
+    }
+  } else {
+    for (int e = threadIdx.x; e < NIN; e += blockDim.x) {
+      const int k = interior_k(e);
       const df64 mid(up[k], 0.f);
-      res = df64(0.f, 0.f);
+      df64 res(0.f, 0.f);
 #pragma unroll
       for (int a = 0; a < DIM; a++) {
         const int st = a == 0 ? 1 : (a == 1 ? SY : SZ);
@@ -701,8 +739,13 @@ __global__ void __launch_bounds__(256)
         const df64 cl = ldv(coeff, base + k - st), cm = ldv(coeff, base + k), cu = ldv(coeff, base + k + st);
         res += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
       }
+      emit(k, res);
     }
-    emit(k, res);
+  }
+#pragma unroll
+  for (int i = 0; i < GPT; i++) {
+    const int e = threadIdx.x + i * 256;
+    if (NG % 256 == 0 || e < NG) G[(e / NF) * gs + e % NF] = gv[i];
   }
   __syncthreads();
   // the boundary shell: 2D: the ring; 3D: the z = 0 and z = NN-1 planes, then the ring of every inner slice
