@@ -34,7 +34,7 @@ struct RShape {
 };
 
 template <class T, class TF, int KIND, int SCHEME, int DIM, int NN>
-__global__ void __launch_bounds__(RShape<DIM, NN>::NT)
+__global__ void __launch_bounds__(RShape<DIM, NN>::NT, 2048 / RShape<DIM, NN>::NT)
     vc_restrict_fine_kernel(const int* __restrict__ fparent, const int* __restrict__ forth,
                             const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
                             const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
@@ -57,23 +57,53 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT)
     fv[q] = __ldg(ff + (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0));
   }
   const int8_t* nt = fntype + (size_t)p * FS + side0;
-  // neighbour-side ghosts (gathered from the neighbours' values, not this tile)
-  const PlainAcc<T> acc{u, (long long)S::CS, 0};
-  for (int e = t; e < 2 * DIM * S::NF; e += S::NT) {
-    const int s = e / S::NF, r = e % S::NF;
-    const int code = side_code[p * 2 * DIM + s];
-    if (code == -1) continue;
-    gbuf[e] = side_ghost<T, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, r % NN, r / NN);
+  // every load is issued before the first shared-memory store: this thread's
+  // side codes, its 16-byte pieces of the padded patch, then the neighbour-side
+  // ghosts (gathered from the neighbours' values, not this tile)
+  constexpr int NG = 2 * DIM * S::NF;
+  constexpr int GPT = (NG + S::NT - 1) / S::NT;
+  int code[GPT];
+#pragma unroll
+  for (int i = 0; i < GPT; i++) {
+    const int e = t + i * S::NT;
+    code[i] = (NG % S::NT == 0 || e < NG) ? side_code[p * 2 * DIM + e / S::NF] : -1;
   }
-  // 1. the padded patch (its ghosts are replaced below)
-  if ((S::CS * sizeof(T)) % 16 == 0) {
-    constexpr int V = 16 / sizeof(T);
+  constexpr bool VEC = (S::CS * sizeof(T)) % 16 == 0;
+  constexpr int V = 16 / sizeof(T);
+  constexpr int TPT = VEC ? (S::CS / V + S::NT - 1) / S::NT : 1;
+  float4 tv[TPT];
+  if (VEC) {
     const float4* src = reinterpret_cast<const float4*>(up);
+#pragma unroll
+    for (int i = 0; i < TPT; i++) {
+      const int e = t + i * S::NT;
+      if ((S::CS / V) % S::NT == 0 || e < S::CS / V) tv[i] = __ldg(src + e);
+    }
+  }
+  const PlainAcc<T> acc{u, (long long)S::CS, 0};
+  T gv[GPT];
+#pragma unroll
+  for (int i = 0; i < GPT; i++) {
+    const int e = t + i * S::NT;
+    if (code[i] != -1) {
+      const int s = e / S::NF, r = e % S::NF;
+      gv[i] = side_ghost<T, SCHEME>(acc, p, s, code[i], slabs, calls, ft, DIM, r % NN, r / NN);
+    }
+  }
+  // 1. the padded patch (its ghosts are replaced below) and the gathered ghosts
+  if (VEC) {
     float4* dst = reinterpret_cast<float4*>(tile);
-    for (int e = t; e < S::CS / V; e += S::NT) dst[e] = __ldg(src + e);
+#pragma unroll
+    for (int i = 0; i < TPT; i++) {
+      const int e = t + i * S::NT;
+      if ((S::CS / V) % S::NT == 0 || e < S::CS / V) dst[e] = tv[i];
+    }
   } else {
     for (int e = t; e < S::CS; e += S::NT) tile[e] = up[e];
   }
+#pragma unroll
+  for (int i = 0; i < GPT; i++)
+    if (code[i] != -1) gbuf[t + i * S::NT] = gv[i];
   const T i0 = finv[(size_t)p * 6 + (KIND ? 3 : 0)], i1 = finv[(size_t)p * 6 + (KIND ? 3 : 0) + 1];
   const T i2 = DIM == 3 ? finv[(size_t)p * 6 + (KIND ? 3 : 0) + 2] : T(0);
   __syncthreads();
