@@ -70,8 +70,7 @@ extern "C" int te_cg_solve(const te_operator* A, int nc, void* xv, const void* b
     cudaStream_t st = d->stream;
     double* x = (double*)xv;
     // resid = b - A x
-    operator_apply(A, nc, TE_F64, x, W.resid.p, st);
-    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.resid.p, bv, nullptr, -1.0, 0.0, 0.0);
+    operator_residual(A, nc, x, bv, W.resid.p, st);
     // initial_guess = x (a copy with ghosts); x.set(0)
     TE_CUDA(cudaMemcpyAsync(W.init.p, x, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
     vec_dispatch(d, nc, TE_F64, OP_SET, x, nullptr, nullptr, 0.0, 0.0, 0.0);

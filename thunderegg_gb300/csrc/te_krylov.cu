@@ -1152,9 +1152,9 @@ struct BatchRun {
     if (df) {
       // resid = b - A x in FP64, then split into float-float; rhat = p = resid (BiCGStab.h:113-131)
       if (!W.xdf.p) W.xdf.alloc(W.n);
-      operator_apply(A, nc, TE_F64, x, W.ap.p, st);
-      vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.ap.p, b, nullptr, -1, 0, 0);
-      launch_dots(W, 3, b, b, W.ap.p, W.ap.p, W.ap.p, W.ap.p, S_BB, 0, st);
+      operator_residual(A, nc, x, b, W.ap.p, st);
+      // rhat = resid here, so rhat . resid and resid . resid are one sum (the same bits)
+      launch_dots(W, 2, b, b, W.ap.p, W.ap.p, nullptr, nullptr, S_BB, 0, st);
       kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
       kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
       count_launch(2);
@@ -1163,17 +1163,16 @@ struct BatchRun {
       TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
     } else {
       // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
-      operator_apply(A, nc, TE_F64, x, W.resid.p, st);
-      vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.resid.p, b, nullptr, -1, 0, 0);
+      operator_residual(A, nc, x, b, W.resid.p, st);
       TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
       TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-      launch_dots(W, 3, b, b, W.rhat.p, W.resid.p, W.resid.p, W.resid.p, S_BB, 0, st);
+      launch_dots(W, 2, b, b, W.resid.p, W.resid.p, nullptr, nullptr, S_BB, 0, st);
     }
     W.read_scalars(st);
     nactive = 0;
     for (int i = 0; i < B; i++) {
       double* h = W.h + (size_t)i * S_NSLOTS;
-      double bb = h[S_BB], rh = h[S_BB + 1], rr = h[S_BB + 2];
+      double bb = h[S_BB], rr = h[S_BB + 1], rh = rr;
       r0[i] = std::sqrt(bb);
       rho[i] = rh;
       residual[i] = r0[i] != 0 ? std::sqrt(rr) / r0[i] : 0.0;
@@ -1196,6 +1195,7 @@ struct BatchRun {
 
   void iterate_once() {
     KrylovWork& W = *Wp;
+    joined = false;
     if (use_graph) {
       auto it = W.graphs.find(gkey);
       if (it == W.graphs.end()) {
@@ -1261,12 +1261,14 @@ struct BatchRun {
     }
   }
 
-  // float-float x into the FP64 x
+  // float-float x into the FP64 x (once after the last iteration)
+  bool joined = false;
   void join_x() {
-    if (!df) return;
+    if (!df || joined) return;
     kd_join<<<1216, 256, 0, st>>>(Wp->cv(Wp->xdf), x, nvals);
     count_launch();
     TE_LAUNCH_CHECK();
+    joined = true;
   }
 
   // Residual replacement: the float-float recurrence keeps ~1e-14 of the
@@ -1277,8 +1279,7 @@ struct BatchRun {
     join_x();
     for (int i = 0; i < B; i++) W.h_active[i] = statuses[i] == TE_OK ? 1 : 0;
     W.push_active(st);
-    operator_apply(A, nc, TE_F64, x, W.ap.p, st);
-    vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, W.ap.p, b, nullptr, -1, 0, 0);
+    operator_residual(A, nc, x, b, W.ap.p, st);
     launch_dots(W, 1, W.ap.p, W.ap.p, nullptr, nullptr, nullptr, nullptr, S_TRUE, 0, st);
     W.read_scalars(st);
     nactive = 0;

@@ -169,7 +169,8 @@ __device__ __forceinline__ T stencil_n(const T* u, const T* c, int k, const T* i
 template <class T, int KIND, int DIM, int NN>
 __global__ void __launch_bounds__(256)
     apply_n_kernel(Layout L, int nc, const int8_t* __restrict__ ntype, int F, const T* __restrict__ sp,
-                   int neumann, const T* __restrict__ coeff, T* u, T* __restrict__ f) {
+                   int neumann, const T* __restrict__ coeff, T* u, T* __restrict__ f,
+                   const T* __restrict__ rhs) {
   constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
   constexpr int PER = (CS + 255) / 256;
   const int p = blockIdx.x;
@@ -190,8 +191,11 @@ __global__ void __launch_bounds__(256)
       v[r] = T(0);
       if (k < CS) {
         const int x = k % SY, y = (k / SY) % SY, z = DIM == 3 ? k / SZ : 1;
-        if (x >= 1 && x <= NN && y >= 1 && y <= NN && z >= 1 && z <= NN)
+        if (x >= 1 && x <= NN && y >= 1 && y <= NN && z >= 1 && z <= NN) {
           v[r] = stencil_n<T, KIND, DIM, SY, SZ>(uc, cp, k, inv);
+          // residual form: rhs - A u, the value of (A u) * -1 + rhs (Vector::scaleThenAdd)
+          if (rhs) v[r] = rhs[(long long)p * CS * nc + (long long)c * CS + k] - v[r];
+        }
       }
     }
 #pragma unroll
@@ -201,18 +205,42 @@ __global__ void __launch_bounds__(256)
     }
   }
 }
+// rhs != nullptr: f = rhs - A u on interior cells (constant-size kernels only;
+// returns false when the level has none and nothing ran)
 template <class T, int KIND>
-static void launch_apply(const te_operator* op, int nc, const T* inv, const T* coeff, int neumann, T* u, T* f,
-                         cudaStream_t s) {
+static bool launch_apply(const te_operator* op, int nc, const T* inv, const T* coeff, int neumann, T* u, T* f,
+                         cudaStream_t s, const T* rhs = nullptr) {
   const te_domain* d = op->dom;
   const Layout& L = d->lay;
   const bool fixed = with_cubic_size(L, [&](auto dim, auto nn) {
     apply_n_kernel<T, KIND, decltype(dim)::value, decltype(nn)::value>
-        <<<L.P, 256, 0, s>>>(L, nc, d->d_nbr_type.p, d->F, inv, neumann, coeff, u, f);
+        <<<L.P, 256, 0, s>>>(L, nc, d->d_nbr_type.p, d->F, inv, neumann, coeff, u, f, rhs);
   });
-  if (!fixed) apply_kernel<T, KIND><<<L.P, 256, 0, s>>>(L, nc, d->d_nbr_type.p, d->F, inv, neumann, coeff, u, f);
+  if (!fixed) {
+    if (rhs) return false;
+    apply_kernel<T, KIND><<<L.P, 256, 0, s>>>(L, nc, d->d_nbr_type.p, d->F, inv, neumann, coeff, u, f);
+  }
   count_launch();
   TE_LAUNCH_CHECK();
+  return true;
+}
+
+void operator_residual(const te_operator* op, int nc, void* u, const void* b, void* r, cudaStream_t s) {
+  const te_domain* d = op->dom;
+  ghost_fill(op->gf, nc, TE_F64, u, s);
+  const bool fused =
+      op->kind == 0
+          ? launch_apply<double, 0>(op, nc, d->d_inv.p, nullptr, op->neumann, (double*)u, (double*)r, s,
+                                    (const double*)b)
+          : launch_apply<double, 1>(op, nc, d->d_inv.p, op->coeffs.p, 0, (double*)u, (double*)r, s,
+                                    (const double*)b);
+  if (fused) return;
+  // Cycle::restrict's form (GMG/Cycle.h:59-61): r = A u, then r = r * -1 + b
+  if (op->kind == 0)
+    launch_apply<double, 0>(op, nc, d->d_inv.p, nullptr, op->neumann, (double*)u, (double*)r, s);
+  else
+    launch_apply<double, 1>(op, nc, d->d_inv.p, op->coeffs.p, 0, (double*)u, (double*)r, s);
+  vec_dispatch(d, nc, TE_F64, OP_SCALE_THEN_ADD, r, b, nullptr, -1.0, 0.0, 0.0);
 }
 
 void operator_apply(const te_operator* op, int nc, int dtype, void* u, void* f, cudaStream_t s) {

@@ -55,6 +55,8 @@ struct te_patch_solver {
 
 namespace te {
 void operator_apply(const te_operator* op, int nc, int dtype, void* u, void* f, cudaStream_t s);
+// r = b - A u (FP64; u's ghosts are filled as by operator_apply); one pass on cubic levels
+void operator_residual(const te_operator* op, int nc, void* u, const void* b, void* r, cudaStream_t s);
 void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, void* u, bool zero_first,
                   cudaStream_t s);
 // tensor-core DFT solve of every patch: out = DFT-solve(in) (in == out allowed)
