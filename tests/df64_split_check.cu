@@ -1,0 +1,56 @@
+// Host check of df_split_bits (thunderegg_gb300/csrc/te_df64.cuh): the integer
+// split of a double into float-float must equal the FP64 formula
+// hi = RN(d), lo = RN(d - hi) bit for bit.  Built and run by
+// tests/test_df64_split.py (host code only, no GPU).
+#include <cstdio>
+#include <cstdint>
+#include <cstring>
+#include <random>
+
+#include "te_df64.cuh"
+
+static uint32_t fbits(float f) {
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return u;
+}
+
+int main() {
+  std::mt19937_64 g(12345);
+  long long bad = 0, n = 0;
+  auto check = [&](double d) {
+    const te::df64 a = te::df_split_bits(d);
+    const float hi = (float)d;
+    const float lo = (float)(d - (double)hi);
+    n++;
+    if (fbits(a.hi) != fbits(hi) || fbits(a.lo) != fbits(lo)) {
+      if (bad < 10) std::printf("mismatch d=%a: got (%a, %a) want (%a, %a)\n", d, a.hi, a.lo, hi, lo);
+      bad++;
+    }
+  };
+  // random bit patterns over every exponent, random values in the solver's range
+  for (int i = 0; i < 2000000; i++) {
+    uint64_t b = g();
+    double d;
+    std::memcpy(&d, &b, 8);
+    if (d == d) check(d);
+  }
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  std::uniform_int_distribution<int> ex(-80, 130);
+  for (int i = 0; i < 2000000; i++) check(std::ldexp(u(g), ex(g)));
+  // ties and carries: significands whose low 29 bits are exactly half, all ones or zero
+  for (int i = 0; i < 200000; i++) {
+    uint64_t b = g();
+    const uint64_t low[4] = {1ull << 28, (1ull << 29) - 1, 0, (1ull << 28) + 1};
+    b = (b & ~((1ull << 29) - 1)) | low[i & 3];
+    if (i & 4) b |= ((1ull << 52) - 1) & ~((1ull << 29) - 1);  // all-ones high part: rounding carries
+    double d;
+    std::memcpy(&d, &b, 8);
+    if (d == d) check(d);
+  }
+  const double special[] = {0.0, -0.0, 1.0, -1.0, 3.4028234663852886e38, 1.1754943508222875e-38, 5e-324, 1e300,
+                            -1e-300, 2.0e-23, 1.5, 0.1, 1.0 / 3.0};
+  for (double d : special) check(d);
+  std::printf("%lld of %lld splits differ\n", bad, n);
+  return bad == 0 ? 0 : 1;
+}

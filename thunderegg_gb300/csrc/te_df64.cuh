@@ -31,6 +31,54 @@ struct df64 {
 };
 
 __host__ __device__ __forceinline__ df64 df_from_double(double d) { return df64(d); }
+
+// The split df64(d) -- hi = RN(d), lo = RN(d - hi) in FP32 -- by integer
+// operations, for the bulk conversions of FP64 vectors: on GB300 every
+// FP64<->FP32 conversion runs on the FP64 pipe.  With d = (-1)^s M 2^(E-52),
+// M the 53-bit significand: hi keeps M's top 24 bits rounded to nearest even
+// (a carry moves it to the next binade), the remainder d - hi is the integer
+// r = (M mod 2^29) - [rounded up] 2^29 times 2^(E-52), and RN(r) as an FP32
+// integer conversion scaled by the exact power 2^(E-52) is RN(d - hi).  Used
+// when E is in [-74, 126], so hi and a nonzero lo are normal FP32 numbers;
+// other values (zeros, subnormals, huge, Inf, NaN) take the FP64 formula.
+__host__ __device__ __forceinline__ df64 df_split_bits(double d) {
+  unsigned long long b;
+#ifdef __CUDA_ARCH__
+  b = (unsigned long long)__double_as_longlong(d);
+#else
+  __builtin_memcpy(&b, &d, 8);
+#endif
+  const int E = (int)((b >> 52) & 0x7ff) - 1023;
+  if (E < -74 || E > 126) return df64(d);
+  const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);
+  const unsigned long long rem = M & ((1ull << 29) - 1);
+  unsigned long long q = M >> 29;  // 24 bits
+  const unsigned long long half = 1ull << 28;
+  const int up = (rem > half || (rem == half && (q & 1))) ? 1 : 0;
+  q += up;
+  int eh = E;
+  if (q == (1ull << 24)) {
+    q >>= 1;
+    eh += 1;
+  }
+  const unsigned int sign = (unsigned int)(b >> 63) << 31;
+  const unsigned int hb = sign | ((unsigned int)(eh + 127) << 23) | (unsigned int)(q & 0x7fffff);
+  // the remainder with d's sign (an exact zero stays +0, as RN(d - hi) gives)
+  const long long r0 = (long long)rem - (up ? (1ll << 29) : 0ll);
+  const int r = (int)(sign ? -r0 : r0);
+  const unsigned int pb = (unsigned int)(E - 52 + 127) << 23;  // 2^(E-52), a normal FP32 power of two
+  float hi, lo, pw;
+#ifdef __CUDA_ARCH__
+  hi = __uint_as_float(hb);
+  pw = __uint_as_float(pb);
+  lo = __int2float_rn(r) * pw;
+#else
+  __builtin_memcpy(&hi, &hb, 4);
+  __builtin_memcpy(&pw, &pb, 4);
+  lo = (float)r * pw;
+#endif
+  return df64(hi, lo);
+}
 __host__ __device__ __forceinline__ double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
 
 // s + e == a + b exactly

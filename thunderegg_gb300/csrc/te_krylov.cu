@@ -521,7 +521,17 @@ __global__ void __launch_bounds__(KT) kd_p(Layout L, int nc, Batch bt, DV p, CV 
 
 __global__ void kd_split(const double* src, DV dst, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    stv(dst, i, df64(src[i]));
+    stv(dst, i, df_split_bits(src[i]));
+}
+// one split into three vectors (resid, rhat and p start equal)
+__global__ void kd_split3(const double* src, DV d0, DV d1, DV d2, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const df64 v = df_split_bits(src[i]);
+    stv(d0, i, v);
+    stv(d1, i, v);
+    stv(d2, i, v);
+  }
 }
 __global__ void kd_join(CV src, double* dst, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -1155,12 +1165,10 @@ struct BatchRun {
       operator_residual(A, nc, x, b, W.ap.p, st);
       // rhat = resid here, so rhat . resid and resid . resid are one sum (the same bits)
       launch_dots(W, 2, b, b, W.ap.p, W.ap.p, nullptr, nullptr, S_BB, 0, st);
-      kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
+      kd_split3<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), W.dv(W.rhat), W.dv(W.p), nvals);
       kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
       count_launch(2);
       TE_LAUNCH_CHECK();
-      TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-      TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
     } else {
       // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
       operator_residual(A, nc, x, b, W.resid.p, st);
@@ -1298,12 +1306,10 @@ struct BatchRun {
     }
     W.push_active(st);
     if (nactive == 0) return false;
-    kd_split<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), nvals);
+    kd_split3<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), W.dv(W.rhat), W.dv(W.p), nvals);
     kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
     count_launch(2);
     TE_LAUNCH_CHECK();
-    TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
-    TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
     TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
     return true;
   }
