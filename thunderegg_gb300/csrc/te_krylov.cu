@@ -519,23 +519,48 @@ __global__ void __launch_bounds__(KT) kd_p(Layout L, int nc, Batch bt, DV p, CV 
   }
 }
 
-__global__ void kd_split(const double* src, DV dst, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    stv(dst, i, df_split_bits(src[i]));
-}
-// one split into three vectors (resid, rhat and p start equal)
-__global__ void kd_split3(const double* src, DV d0, DV d1, DV d2, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const df64 v = df_split_bits(src[i]);
-    stv(d0, i, v);
-    stv(d1, i, v);
-    stv(d2, i, v);
+// Whole-vector conversions: each thread takes CONV_U elements per round and
+// loads them all before converting and storing any.
+constexpr int CONV_U = 4;
+__global__ void kd_split(const double* __restrict__ src, DV dst, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += CONV_U * stride) {
+    double v[CONV_U];
+#pragma unroll
+    for (int u = 0; u < CONV_U; u++) v[u] = i0 + u * stride < n ? src[i0 + u * stride] : 0.0;
+#pragma unroll
+    for (int u = 0; u < CONV_U; u++)
+      if (i0 + u * stride < n) stv(dst, i0 + u * stride, df_split_bits(v[u]));
   }
 }
-__global__ void kd_join(CV src, double* dst, long long n) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    dst[i] = df_to_double(ldv(src, i));
+// one split into three vectors (resid, rhat and p start equal)
+__global__ void kd_split3(const double* __restrict__ src, DV d0, DV d1, DV d2, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += CONV_U * stride) {
+    double v[CONV_U];
+#pragma unroll
+    for (int u = 0; u < CONV_U; u++) v[u] = i0 + u * stride < n ? src[i0 + u * stride] : 0.0;
+#pragma unroll
+    for (int u = 0; u < CONV_U; u++) {
+      const long long i = i0 + u * stride;
+      if (i >= n) continue;
+      const df64 s = df_split_bits(v[u]);
+      stv(d0, i, s);
+      stv(d1, i, s);
+      stv(d2, i, s);
+    }
+  }
+}
+__global__ void kd_join(CV src, double* __restrict__ dst, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += CONV_U * stride) {
+    df64 v[CONV_U];
+#pragma unroll
+    for (int u = 0; u < CONV_U; u++) v[u] = i0 + u * stride < n ? ldv(src, i0 + u * stride) : df64(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < CONV_U; u++)
+      if (i0 + u * stride < n) dst[i0 + u * stride] = df_to_double(v[u]);
+  }
 }
 
 // FP32 values of a level buffer, read as float-float numbers
