@@ -146,43 +146,57 @@ __global__ void interpolate_kernel(Layout F, Layout C, int nc, const int* __rest
 
 // interpolate_kernel for cubic patches of NN cells with one ghost layer:
 // fine += the parent's coarse cell (DirectInterpolator, GMG/DirectInterpolator.h:
-// 40-91) with constant index arithmetic.  A thread loads all of its cells
-// (fine and coarse) before it stores.
-template <class T, int DIM, int NN>
+// 40-91) with constant index arithmetic.  A CTA takes PPC fine patches (two
+// for FP32, so each thread keeps as many bytes in flight as for FP64) and a
+// thread loads all of its cells (fine and coarse) before it stores.
+template <class T, int DIM, int NN, int PPC>
 __global__ void __launch_bounds__(256)
-    interpolate_n_kernel(int nc, const int* __restrict__ parent, const int* __restrict__ orth,
+    interpolate_n_kernel(int P, int nc, const int* __restrict__ parent, const int* __restrict__ orth,
                          const T* __restrict__ coarse, T* __restrict__ fine) {
   constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
   constexpr int NI = DIM == 3 ? NN * NN * NN : NN * NN;
   constexpr int PER = (NI + 255) / 256;
-  const int fp = blockIdx.x;
-  const int o = orth[fp];
-  const T* cv = coarse + (long long)parent[fp] * CS * nc;
-  T* fv = fine + (long long)fp * CS * nc;
-  const int ox = (o >= 0 && (o & 1)) ? NN : 0, oy = (o >= 0 && (o & 2)) ? NN : 0,
-            oz = (o >= 0 && (o & 4)) ? NN : 0;
-  for (int c = 0; c < nc; c++) {
-    T a[PER], b[PER];
+  int fp[PPC], o[PPC];
+  const T* cv[PPC];
+  T* fv[PPC];
 #pragma unroll
-    for (int r = 0; r < PER; r++) {
-      const int e = threadIdx.x + r * 256;
-      if (NI % 256 == 0 || e < NI) {
-        const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
-        const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
-        const int kc = o < 0 ? k
-                             : ((x + ox) >> 1) + 1 + (((y + oy) >> 1) + 1) * SY +
-                                   (DIM == 3 ? (((z + oz) >> 1) + 1) * SZ : 0);
-        a[r] = fv[(long long)c * CS + k];
-        b[r] = cv[(long long)c * CS + kc];
+  for (int q = 0; q < PPC; q++) {
+    fp[q] = blockIdx.x * PPC + q;
+    const int pp = fp[q] < P ? fp[q] : blockIdx.x * PPC;  // a valid patch for the table loads
+    o[q] = orth[pp];
+    cv[q] = coarse + (long long)parent[pp] * CS * nc;
+    fv[q] = fine + (long long)pp * CS * nc;
+  }
+  for (int c = 0; c < nc; c++) {
+    T a[PPC][PER], b[PPC][PER];
+#pragma unroll
+    for (int q = 0; q < PPC; q++) {
+      const int ox = (o[q] >= 0 && (o[q] & 1)) ? NN : 0, oy = (o[q] >= 0 && (o[q] & 2)) ? NN : 0,
+                oz = (o[q] >= 0 && (o[q] & 4)) ? NN : 0;
+#pragma unroll
+      for (int r = 0; r < PER; r++) {
+        const int e = threadIdx.x + r * 256;
+        if ((NI % 256 == 0 || e < NI) && fp[q] < P) {
+          const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
+          const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
+          const int kc = o[q] < 0 ? k
+                                  : ((x + ox) >> 1) + 1 + (((y + oy) >> 1) + 1) * SY +
+                                        (DIM == 3 ? (((z + oz) >> 1) + 1) * SZ : 0);
+          a[q][r] = fv[q][(long long)c * CS + k];
+          b[q][r] = cv[q][(long long)c * CS + kc];
+        }
       }
     }
 #pragma unroll
-    for (int r = 0; r < PER; r++) {
-      const int e = threadIdx.x + r * 256;
-      if (NI % 256 == 0 || e < NI) {
-        const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
-        const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
-        fv[(long long)c * CS + k] = a[r] + b[r];
+    for (int q = 0; q < PPC; q++) {
+#pragma unroll
+      for (int r = 0; r < PER; r++) {
+        const int e = threadIdx.x + r * 256;
+        if ((NI % 256 == 0 || e < NI) && fp[q] < P) {
+          const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
+          const int k = (x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0);
+          fv[q][(long long)c * CS + k] = a[q][r] + b[q][r];
+        }
       }
     }
   }
@@ -555,11 +569,11 @@ void interpolate_level(const te_interpolator* in, int nc, int dtype, const void*
     const bool fixed = with_cubic_size(F, [&](auto dim, auto nn) {
       constexpr int DIM = decltype(dim)::value, NN = decltype(nn)::value;
       if (dtype == TE_F64)
-        interpolate_n_kernel<double, DIM, NN><<<F.P, 256, 0, s>>>(nc, in->parent.p, in->orth.p,
-                                                                 (const double*)coarse, (double*)fine);
+        interpolate_n_kernel<double, DIM, NN, 1><<<F.P, 256, 0, s>>>(F.P, nc, in->parent.p, in->orth.p,
+                                                                    (const double*)coarse, (double*)fine);
       else
-        interpolate_n_kernel<float, DIM, NN><<<F.P, 256, 0, s>>>(nc, in->parent.p, in->orth.p,
-                                                                (const float*)coarse, (float*)fine);
+        interpolate_n_kernel<float, DIM, NN, 2><<<(F.P + 1) / 2, 256, 0, s>>>(
+            F.P, nc, in->parent.p, in->orth.p, (const float*)coarse, (float*)fine);
     });
     if (fixed) {
       count_launch();
