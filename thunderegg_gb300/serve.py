@@ -98,32 +98,46 @@ class _Active:
 class _Union:
     """The device objects of one union hierarchy and its batch buffers (a cache entry)."""
 
-    def __init__(self, members, opts):
+    def __init__(self, reqs, opts):
         import torch
 
-        levels, offsets = M.union_hierarchy([m.req.levels for m in members])
+        levels, offsets = M.union_hierarchy([r.levels for r in reqs])
         coeffs = None
-        if members[0].req.coeffs is not None:
-            coeffs = [np.concatenate([m.req.coeffs[k] for m in members], axis=0) for k in range(len(levels))]
+        if reqs[0].coeffs is not None:
+            coeffs = [np.concatenate([r.coeffs[k] for r in reqs], axis=0) for k in range(len(levels))]
         self.solver = GmgSolver(levels, opts, coeffs)
         self.offsets = offsets[0]
         shape = self.solver.finest.padded_shape(1)
         # every patch range is written before a batch runs, so the buffers need no zero fill
         self.x = Vector(self.solver.finest, data=torch.empty(shape, dtype=torch.float64, device="cuda"))
         self.b = Vector(self.solver.finest, data=torch.empty(shape, dtype=torch.float64, device="cuda"))
-        self.keep = [(m.req.levels, m.req.coeffs) for m in members]  # keeps the key's ids valid
-        self.bytes = sum(request_bytes(m.req.levels, m.req.opts) for m in members)
+        self.keep = [(r.levels, r.coeffs) for r in reqs]  # keeps the key's ids valid
+        self.bytes = sum(request_bytes(r.levels, r.opts) for r in reqs)
         self.busy = False
 
 
-def _union_key(members):
-    return tuple((id(m.req.levels), id(m.req.coeffs)) for m in members)
+def _union_key(reqs):
+    return tuple((id(r.levels), id(r.coeffs)) for r in reqs)
+
+
+# batch sizes a class's union is rounded up to (ratio <= 1.5), so that the
+# unions of a busy class repeat and come from the cache
+_BUCKETS = (1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256)
+
+
+def _bucket(n, cap):
+    for s in _BUCKETS:
+        if s >= n:
+            return s if s <= cap else n
+    return n
 
 
 class _Batch:
-    """One union-hierarchy batch of a class and its stepping BiCGStab run."""
+    """One union-hierarchy batch of a class and its stepping BiCGStab run.  The
+    union may hold phantom slots after the members (zero right-hand side: their
+    solves are finished at the start and the Krylov kernels skip them)."""
 
-    def __init__(self, members, x_parts, un):
+    def __init__(self, members, x_parts, un, phantom_bytes=0):
         import torch
 
         self.members = list(members)  # this batch's members, in patch order
@@ -132,6 +146,7 @@ class _Batch:
         self.solver = un.solver
         self.offsets = un.offsets
         self.x, self.b = un.x, un.b
+        self.phantom_bytes = phantom_bytes
         for i, m in enumerate(members):
             lo, hi = self.offsets[i], self.offsets[i + 1]
             self.b.t[lo:hi].copy_(torch.as_tensor(m.req.f.reshape(self.b.t[lo:hi].shape)), non_blocking=False)
@@ -142,8 +157,12 @@ class _Batch:
                 self.x.t[lo:hi].copy_(torch.as_tensor(src.reshape(self.x.t[lo:hi].shape)))
             else:
                 self.x.t[lo:hi].zero_()
+        B = len(self.offsets) - 1  # members, then phantom slots
+        if B > len(members):
+            tail = slice(self.offsets[len(members)], self.offsets[B])
+            self.b.t[tail].zero_()
+            self.x.t[tail].zero_()
         torch.cuda.synchronize()
-        B = len(members)
         offs = (ctypes.c_int * (B + 1))(*self.offsets)
         self.h = ctypes.c_void_p()
         o = self.solver.opts
@@ -158,11 +177,13 @@ class _Batch:
         return n.value
 
     def state(self):
-        B = len(self.members)
+        """Iterations, residuals, statuses and running flags of the members (phantoms left out)."""
+        B = len(self.offsets) - 1
         its, res = (ctypes.c_int * B)(), (ctypes.c_double * B)()
         st, run = (ctypes.c_int * B)(), (ctypes.c_int * B)()
         check(lib().te_bicgstab_batch_state(self.h, its, res, st, run))
-        return list(its), list(res), list(st), list(run)
+        n = len(self.members)
+        return list(its)[:n], list(res)[:n], list(st)[:n], list(run)[:n]
 
     def slice_x(self, i):
         lo, hi = self.offsets[i], self.offsets[i + 1]
@@ -210,11 +231,11 @@ class Server:
                 del self.unions[key]
                 self.stats["union_evictions"] += 1
 
-    def _union(self, members, opts):
-        key = _union_key(members)
+    def _union(self, reqs, opts):
+        key = _union_key(reqs)
         un = self.unions.pop(key, None)
         if un is None:
-            un = _Union(members, opts)
+            un = _Union(reqs, opts)
             self.stats["union_builds"] += 1
         else:
             self.stats["union_hits"] += 1
@@ -259,6 +280,11 @@ class Server:
         self.stats["max_active_bytes"] = max(self.stats["max_active_bytes"], self.active_bytes)
         self._evict(0)
 
+    def _close(self, b):
+        b.close()
+        self.active_bytes -= b.phantom_bytes
+        b.phantom_bytes = 0
+
     def _retire(self, cls, a, u, its, res, st):
         self.results[a.rid] = Result(u=u, iterations=its, residual=res, status=st,
                                      latency_s=time.perf_counter() - a.submitted, restarts=a.restarts)
@@ -277,14 +303,25 @@ class Server:
                     m.x = old.slice_x(i)
                     m.iterations = old.base_its[i] + its[i]
                     m.restarts += 1
-            old.close()
+            self._close(old)
             cls["batch"] = None
         cls["dirty"] = False
         cls["waiting"] = 0
         cls["wait_rounds"] = 0
         while cls["active"]:
             members = cls["active"]
-            b = _Batch(members, [m.x for m in members], self._union(members, members[0].req.opts))
+            reqs = [m.req for m in members]
+            # phantom slots round the batch up to a bucket size, when the budget has room for them
+            last = members[-1].req
+            extra = _bucket(len(members), self.max_batch) - len(members)
+            pbytes = extra * request_bytes(last.levels, last.opts)
+            if extra and self.active_bytes + self._idle_cache_bytes() + pbytes > self.budget:
+                self._evict(pbytes)
+            if extra and self.active_bytes + self._idle_cache_bytes() + pbytes > self.budget:
+                extra, pbytes = 0, 0
+            reqs += [Request(last.levels, None, last.opts, last.coeffs)] * extra
+            self.active_bytes += pbytes
+            b = _Batch(members, [m.x for m in members], self._union(reqs, members[0].req.opts), pbytes)
             self.stats["reforms"] += 1
             self.stats["max_batch"] = max(self.stats["max_batch"], len(members))
             its, res, st, run = b.state()
@@ -302,7 +339,7 @@ class Server:
             cls["active"] = [m for m in members if m.rid not in gone]
             for m in cls["active"]:
                 m.x = b.slice_x(members.index(m))
-            b.close()
+            self._close(b)
 
     def _collect(self, cls):
         """Retire every request of the class's batch once the whole batch has finished."""
@@ -314,7 +351,7 @@ class Server:
             self._retire(cls, m, b.slice_x(i).cpu().numpy(), b.base_its[i] + its[i], res[i], st[i])
         gone = {m.rid for m in b.members}
         cls["active"] = [m for m in cls["active"] if m.rid not in gone]
-        b.close()
+        self._close(b)
         cls["batch"] = None
         if cls["active"]:
             cls["dirty"] = True
