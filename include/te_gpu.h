@@ -160,6 +160,10 @@ int te_operator_modify_rhs(const te_operator* op, int ncomp, int dtype, const vo
 /* Poisson::DFTPatchSolver (Poisson/DFTPatchSolver.h:385-450); neumann_mask
  * bit i = Side index i is Neumann (when it has no neighbour). */
 int te_dft_patch_solver_create(const te_operator* op, int neumann_mask, te_patch_solver** out);
+/* Poisson::FFTWPatchSolver (Poisson/FFTWPatchSolver.h:189-308) computes the
+ * same solve (FFTW's RODFT/REDFT kinds are the same DST/DCT families, the
+ * eigenvalues and the prod 1/(2n) scale match): a caller of that class binds
+ * te_dft_patch_solver_create. */
 /* Iterative::PatchSolver with an inner BiCGStab (Iterative/PatchSolver.h:121-175) */
 int te_bicgstab_patch_solver_create(const te_operator* op, double tol, int max_iterations,
                                     int continue_on_breakdown, te_patch_solver** out);

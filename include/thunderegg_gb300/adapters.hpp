@@ -335,6 +335,13 @@ class GpuDFTPatchSolver : public ThunderEgg::PatchSolver<D> {
   std::shared_ptr<te_patch_solver> h_;
 };
 
+// Poisson::FFTWPatchSolver<D> (Poisson/FFTWPatchSolver.h:189-308) computes the
+// same solve as DFTPatchSolver (the same transform families, eigenvalues, zero
+// mode and normalisation, with the transforms as FFTs); the GPU runs both as
+// dense contractions.
+template <int D>
+using GpuFFTWPatchSolver = GpuDFTPatchSolver<D>;
+
 // ---------------------------------------------------------------------------
 // GMG::Restrictor<D> and GMG::Interpolator<D>
 // ---------------------------------------------------------------------------

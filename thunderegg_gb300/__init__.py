@@ -304,6 +304,17 @@ class DFTPatchSolver(_PatchSolver):
         return bool(v.value)
 
 
+class FFTWPatchSolver(DFTPatchSolver):
+    """Poisson::FFTWPatchSolver (Poisson/FFTWPatchSolver.h:189-308): the same
+    solve as DFTPatchSolver -- per axis the FFTW r2r kinds RODFT10/01, REDFT10/01
+    and REDFT11/RODFT11 are DST-II/III, DCT-II/III and DCT-IV/DST-IV, the
+    eigenvalues are -sum 4/h^2 sin^2, the all-Neumann patch without neighbours
+    drops its zero mode and the result is scaled by prod 1/(2n) (FFTW's
+    unnormalised transforms carry the factor 2 that the DFT solver's matrices
+    move into prod 2/n).  On the GPU the transforms run as dense contractions
+    (tensor cores in FP32 for n <= 64), which beat an FFT at these sizes."""
+
+
 class BiCGStabPatchSolver(_PatchSolver):
     """Iterative::PatchSolver with an inner Iterative::BiCGStab (Iterative/PatchSolver.h:121-175)."""
 
