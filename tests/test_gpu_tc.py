@@ -190,3 +190,40 @@ def test_fine_restrict_matches_coarse_centric(tmp_path, mesh, scheme):
         subprocess.run([sys.executable, "-c", code], check=True, env=env, timeout=300)
         outs.append(np.load(out))
     assert rel_err(outs[0], outs[1]) <= 1e-6
+
+
+@pytest.mark.parametrize("name", ["2d_circle_n16", "3d_uniform_n16"])
+@pytest.mark.parametrize("cycle_type", ("W", "F"))
+def test_tc_w_and_fmg_cycles(te, oracle, name, cycle_type):
+    """The FP32 W and FMG cycles on the tensor-core path (mid smooth, second coarse visit
+    from the first visit's result) against the FP64 oracle cycles (pinned to the
+    reference's own), against the same cycles on the general kernels, and a mixed
+    precision solve with them reaching 1e-10."""
+    from oracle import gmg_config
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels, sc = meshes()[name]
+    f = np.random.default_rng(15).standard_normal(levels[0].padded_shape(1))
+    want = oracle.vcycle(levels, f, gmg_config(scheme=sc, smoother=0, cycle_type=cycle_type))
+    inner = _inner(levels[0])
+    opts = dict(scheme=sc, smoother=0, cycle_type=cycle_type, cycle_dtype=te.TE_F32)
+    s = GmgSolver(levels, GmgOptions(**opts))
+    assert all(ps.uses_tensor_cores for ps in s.smoothers)
+    fv = te.Vector.from_numpy(s.finest, f)
+    uv = te.Vector(s.finest)
+    for _ in range(2):
+        s.cycle.apply(fv, uv)
+        got = uv.numpy()
+        assert rel_err(got[inner], want[inner]) <= 5e-5
+    os.environ["TE_NO_TC"] = "1"
+    try:
+        s2 = GmgSolver(levels, GmgOptions(**opts))
+    finally:
+        del os.environ["TE_NO_TC"]
+    uv2 = te.Vector(s2.finest)
+    s2.cycle.apply(te.Vector.from_numpy(s2.finest, f), uv2)
+    assert rel_err(got[inner], uv2.numpy()[inner]) <= 2e-5
+    s3 = GmgSolver(levels, GmgOptions(bicgstab_flags=1, **opts))
+    uv3 = te.Vector(s3.finest)
+    s3.solve(fv, uv3)
+    assert s3.residual(fv, uv3) <= 1e-10

@@ -28,7 +28,8 @@
 
 namespace te {
 
-// u + interpolated coarse correction, evaluated on the fly (DirectInterpolator.h:60-91)
+// u + interpolated coarse correction, evaluated on the fly (DirectInterpolator.h:60-91);
+// uc == nullptr: u alone
 template <class T>
 struct InterpAcc {
   const T* A;
@@ -37,6 +38,7 @@ struct InterpAcc {
   const int* orth;
   Layout F, C;
   __device__ __forceinline__ T operator()(int q, int idx) const {
+    if (!uc) return A[(long long)q * F.cs + idx];
     int x = idx % F.sy - F.g;
     int r = idx / F.sy;
     const int py = F.n1 + 2 * F.g;
@@ -66,6 +68,7 @@ struct InterpAccN {
   const int* orth;
   static constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
   __device__ __forceinline__ T operator()(int q, int idx) const {
+    if (!uc) return A[(long long)q * CS + idx];
     const int x = idx % SY - 1, r = idx / SY;
     const int y = r % SY - 1, z = DIM == 3 ? r / SY - 1 : 0;
     const int o = __ldg(orth + q);
@@ -542,7 +545,11 @@ static void vc_corr_t(const te_patch_solver* ps, const te_interpolator* in, cons
                       float* corr, cudaStream_t s) {
   const te_operator* op = ps->op;
   const te_domain* d = op->dom;
-  const Layout &F = d->lay, &C = in->coarse->lay;
+  // in == nullptr (with uc == nullptr): the corrections of A alone, e.g. on the coarsest level
+  const Layout &F = d->lay, &C = in ? in->coarse->lay : d->lay;
+  const int* parent = in ? in->parent.p : nullptr;
+  const int* orth = in ? in->orth.p : nullptr;
+  require(in || !uc, "vc_corr: a coarse correction needs its interpolator");
   const te_ghost_filler* g = op->gf;
   const int gs = gstride_of(F);
   const long long total = (long long)F.P * 2 * F.D * gs;
@@ -550,7 +557,7 @@ static void vc_corr_t(const te_patch_solver* ps, const te_interpolator* in, cons
   const unsigned blocks = (unsigned)((total + threads - 1) / threads);
   const bool cube = F.g == 1 && F.n1 == F.n0 && (F.D == 2 || F.n2 == F.n0);
   auto fixed = [&](auto kn) {
-    kn<<<blocks, threads, 0, s>>>(F.P, in->parent.p, in->orth.p, d->template inv<float>(), op->coeffs_f.p, g->faces,
+    kn<<<blocks, threads, 0, s>>>(F.P, parent, orth, d->template inv<float>(), op->coeffs_f.p, g->faces,
                                   g->d_slabs.p, g->d_calls.p, g->d_side_code.p, A, uc, corr);
   };
   bool done = false;
@@ -568,7 +575,7 @@ static void vc_corr_t(const te_patch_solver* ps, const te_interpolator* in, cons
   }
   if (!done) {
     auto kern = F.D == 2 ? vc_corr_kernel<KIND, SCHEME, 2> : vc_corr_kernel<KIND, SCHEME, 3>;
-    kern<<<blocks, threads, 0, s>>>(F, C, in->parent.p, in->orth.p, d->template inv<float>(), op->coeffs_f.p,
+    kern<<<blocks, threads, 0, s>>>(F, C, parent, orth, d->template inv<float>(), op->coeffs_f.p,
                                     g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_code.p, gs, A, uc, corr);
   }
   count_launch();

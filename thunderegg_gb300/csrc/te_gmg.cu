@@ -757,7 +757,8 @@ int te_cycle_create(const te_cycle_level* levels, int num_levels, te_cycle_opts 
     c->serial = serials.fetch_add(1);
     const char* ng = getenv("TE_NO_GRAPH");
     c->use_graph = !(ng && ng[0] == '1');
-    bool fz = num_levels >= 2 && opts.pre_sweeps == 1 && opts.post_sweeps == 1 && opts.coarse_sweeps == 1;
+    bool fz = num_levels >= 2 && opts.pre_sweeps == 1 && opts.post_sweeps == 1 && opts.coarse_sweeps == 1 &&
+              (cycle_type == TE_CYCLE_V || opts.mid_sweeps == 1);
     const char* nf = getenv("TE_NO_FUSION");
     if (nf && nf[0] == '1') fz = false;
     for (int k = 0; k < num_levels && fz; k++) {

@@ -104,6 +104,13 @@ struct te_cycle {
   // even patch sizes, no ghost extrapolation, one component
   bool fusable = false;
   bool fused() const { return fusable && nc == 1 && type == TE_CYCLE_V; }
+  // the W and FMG cycles run fused when every level takes the tensor-core path
+  bool fused_wf() const {
+    if (!fusable || nc != 1 || type == TE_CYCLE_V || dtype != TE_F32) return false;
+    for (size_t k = 0; k < levels.size(); k++)
+      if (!use_tc((int)k)) return false;
+    return true;
+  }
   // the FP32 fused cycle runs the DFT solves of level k on the tensor cores
   bool tc_enabled = true;
   bool use_tc(int k) const { return tc_enabled && dtype == TE_F32 && levels[k].smoother->tc_ok; }
@@ -178,6 +185,65 @@ struct te_cycle {
     }
     return (const T*)out;
   }
+  // ---- the W and FMG cycles on the tensor-core path (FP32 in and out, one sweep each)
+  // PatchSolver::smooth of level k from the iterate uin (nullptr: zero) into out: the
+  // tensor-core solve of f minus the boundary corrections of uin
+  void smooth_tc(int k, const float* fk, const float* uin, float* out, cudaStream_t s) const {
+    const te_patch_solver* ps = levels[k].smoother;
+    if (!uin) {
+      te::dft_tc<float, float>(ps, fk, out, s);
+      return;
+    }
+    float* cr = (float*)corr[k].p;
+    te::vc_corr(ps, nullptr, uin, nullptr, cr, s);
+    te::dft_tc<float, float>(ps, fk, out, s, cr);
+  }
+  // interpolate the coarse correction uc into A and smooth, into out: the corrections of
+  // A + P uc (never stored), then the solve (out may be A: A is read only by the corrections)
+  void corr_smooth_tc(int k, const float* fk, const float* A, const float* uc, float* out, cudaStream_t s) const {
+    float* cr = (float*)corr[k].p;
+    te::vc_corr(levels[k].smoother, levels[k + 1].interpolator, A, uc, cr, s);
+    te::dft_tc<float, float>(levels[k].smoother, fk, out, s, cr);
+  }
+  // WCycle::visit (GMG/WCycle.h:50-84) and FMGCycle::visit (GMG/FMGCycle.h:68-104); uin: the
+  // level's iterate on entry (nullptr: zero).  u[k] holds the pre- and mid-smoothed iterate,
+  // r[k + 1] the coarse result, which the second coarse visit starts from (as in the reference)
+  void wf_visit(int k, const float* fk, float* out, const float* uin, cudaStream_t s) const {
+    const int last = (int)levels.size() - 1;
+    if (k == last) {
+      smooth_tc(k, fk, uin, out, s);
+      return;
+    }
+    float* A = (float*)u[k].p;
+    float* fc = (float*)f[k + 1].p;
+    float* uc = (float*)r[k + 1].p;
+    smooth_tc(k, fk, uin, A, s);
+    te::vc_restrict<float, float>(levels[k].restrictor, levels[k].op, A, fk, fc, s);
+    wf_visit(k + 1, fc, uc, nullptr, s);
+    corr_smooth_tc(k, fk, A, uc, A, s);  // mid smooth
+    te::vc_restrict<float, float>(levels[k].restrictor, levels[k].op, A, fk, fc, s);
+    if (type == TE_CYCLE_W)
+      wf_visit(k + 1, fc, uc, uc, s);
+    else
+      fmg_v_visit(k + 1, fc, uc, uc, s);
+    corr_smooth_tc(k, fk, A, uc, out, s);
+  }
+  // FMGCycle::v_visit (GMG/FMGCycle.h:43-66) from the iterate uin; its coarser visit is wf_visit
+  void fmg_v_visit(int k, const float* fk, float* out, const float* uin, cudaStream_t s) const {
+    const int last = (int)levels.size() - 1;
+    if (k == last) {
+      smooth_tc(k, fk, uin, out, s);
+      return;
+    }
+    float* A = (float*)u[k].p;
+    float* fc = (float*)f[k + 1].p;
+    float* uc = (float*)r[k + 1].p;
+    smooth_tc(k, fk, uin, A, s);
+    te::vc_restrict<float, float>(levels[k].restrictor, levels[k].op, A, fk, fc, s);
+    wf_visit(k + 1, fc, uc, nullptr, s);
+    corr_smooth_tc(k, fk, A, uc, out, s);
+  }
+
   // `fresh`: u is known to be zero (ghosts included) before the first sweep
   void smooth(int k, const void* fk, void* uk, int times, bool fresh, cudaStream_t s) const {
     for (int i = 0; i < times; i++) te::patch_smooth(levels[k].smoother, nc, dtype, fk, uk, fresh && i == 0, s);
@@ -263,6 +329,10 @@ struct te_cycle {
     if (dtype == TE_F64) {
       if (first_sweeps() == 0) TE_CUDA(cudaMemsetAsync(u64, 0, bytes(0), s));
       visit(0, f64, u64, true, s);
+    } else if (fused_wf()) {
+      te::convert_level(dom(0), nc, dtype, f[0].p, TE_F64, f64, s);
+      wf_visit(0, (const float*)f[0].p, (float*)r[0].p, nullptr, s);
+      te::convert_level(dom(0), nc, TE_F64, u64, dtype, r[0].p, s);
     } else {
       te::convert_level(dom(0), nc, dtype, f[0].p, TE_F64, f64, s);
       if (first_sweeps() == 0) TE_CUDA(cudaMemsetAsync(u[0].p, 0, bytes(0), s));
@@ -275,6 +345,10 @@ struct te_cycle {
   void body_f32(const float* f32, float* u32, cudaStream_t s) const {
     if (fused()) {
       vfused<float, float, float>(0, f32, u32, s);
+      return;
+    }
+    if (fused_wf()) {
+      wf_visit(0, f32, u32, nullptr, s);
       return;
     }
     if (first_sweeps() == 0) TE_CUDA(cudaMemsetAsync(u32, 0, bytes(0), s));
