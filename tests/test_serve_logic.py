@@ -1,0 +1,183 @@
+"""The serving loop's scheduling on the CPU (thunderegg_gb300.serve.Server).
+
+The device objects (_Union: a union hierarchy's solver and buffers; _Batch: its
+resumable BiCGStab run) are replaced by fakes in which request i needs a given
+number of iterations, so admission against the memory budget, the union cache
+and its LRU eviction, the bucketed batch sizes with phantom slots and the
+re-forms are checked without a GPU.  The GPU tests (test_gpu_serve.py) check
+the same loop's numerical results.
+"""
+import numpy as np
+import pytest
+
+import thunderegg_gb300.serve as S
+from thunderegg_gb300 import mesh as M
+from thunderegg_gb300.gmg import GmgOptions
+
+MESH = None
+
+
+def mesh():
+    global MESH
+    if MESH is None:
+        MESH = (M.uniform_mesh(2, 2, 8), M.uniform_mesh(2, 3, 8))
+    return MESH
+
+
+class _X:
+    def __init__(self, v):
+        self.v = v
+
+    def cpu(self):
+        return self
+
+    def numpy(self):
+        return self.v
+
+    def clone(self):
+        return _X(self.v)
+
+
+class FakeUnion:
+    built = []
+
+    def __init__(self, reqs, opts):
+        self.reqs = list(reqs)
+        self.bytes = sum(S.request_bytes(r.levels, r.opts) for r in reqs)
+        self.busy = False
+        FakeUnion.built.append(len(reqs))
+
+
+class FakeBatch:
+    """Request m needs int(m.req.f[0]) iterations in total; a re-formed member keeps its count."""
+
+    def __init__(self, members, x_parts, un, phantom_bytes=0):
+        self.members = list(members)
+        self.un = un
+        un.busy = True
+        self.phantom_bytes = phantom_bytes
+        self.h = object()
+        self.base_its = [m.iterations for m in members]
+        self.done = [0] * len(members)
+        assert len(un.reqs) >= len(members)
+
+    def _left(self, i):
+        return int(self.members[i].req.f[0]) - self.base_its[i] - self.done[i]
+
+    def step(self, k):
+        for i in range(len(self.members)):
+            self.done[i] += max(0, min(k, self._left(i)))
+        return sum(1 for i in range(len(self.members)) if self._left(i) > 0)
+
+    def state(self):
+        run = [1 if self._left(i) > 0 else 0 for i in range(len(self.members))]
+        return list(self.done), [1e-11] * len(self.members), [0] * len(self.members), run
+
+    def slice_x(self, i):
+        return _X(np.full(3, float(self.members[i].rid)))
+
+    def close(self):
+        self.un.busy = False
+        self.h = None
+
+
+@pytest.fixture
+def fake(monkeypatch):
+    FakeUnion.built = []
+    monkeypatch.setattr(S, "_Union", FakeUnion)
+    monkeypatch.setattr(S, "_Batch", FakeBatch)
+
+    class Lib:
+        def te_bicgstab_batch_sync_x(self, h):
+            return 0
+
+    monkeypatch.setattr(S, "lib", lambda: Lib())
+    monkeypatch.setattr(S, "check", lambda rc: rc)
+    return FakeUnion
+
+
+def req(iters, which=0):
+    return S.Request(mesh()[which], np.array([float(iters)]), GmgOptions())
+
+
+def run_checked(srv, max_rounds=10000):
+    """Run to the end, checking the memory invariant after every round."""
+    r = 0
+    while not srv.idle() and r < max_rounds:
+        srv.step()
+        assert srv.active_bytes + srv._idle_cache_bytes() <= srv.budget
+        r += 1
+    assert srv.idle()
+    return srv.results
+
+
+def test_budget_bounds_active_requests(fake):
+    per = S.request_bytes(mesh()[0], GmgOptions())
+    srv = S.Server(budget_bytes=2 * per, steps_per_round=2)
+    ids = [srv.submit(req(5 + i)) for i in range(5)]
+    res = run_checked(srv)
+    assert sorted(res) == ids
+    assert srv.stats["max_active_bytes"] <= 2 * per
+    assert srv.active_bytes == 0
+    # each request ran exactly the iterations it needed, through any re-forms
+    for i, rid in enumerate(ids):
+        assert res[rid].iterations == 5 + i
+
+
+def test_oversize_request_rejected(fake):
+    from thunderegg_gb300.capi import TE_ERR_BUDGET, TeError
+
+    srv = S.Server(budget_bytes=1000)
+    with pytest.raises(TeError) as e:
+        srv.submit(req(3))
+    assert e.value.code == TE_ERR_BUDGET
+
+
+def test_union_cache_reuses_member_sequences(fake):
+    srv = S.Server(budget_bytes=1 << 40, steps_per_round=4)
+    for _ in range(3):
+        srv.submit(req(4))
+    run_checked(srv)
+    builds = srv.stats["union_builds"]
+    for _ in range(3):
+        srv.submit(req(4))
+    run_checked(srv)
+    assert srv.stats["union_builds"] == builds  # the same sequence of meshes: all from the cache
+    assert srv.stats["union_hits"] >= 1
+
+
+def test_batches_round_up_to_buckets_with_phantom_slots(fake):
+    per = S.request_bytes(mesh()[0], GmgOptions())
+    srv = S.Server(budget_bytes=1 << 40, steps_per_round=2)
+    for _ in range(5):
+        srv.submit(req(6))
+    srv.step()  # admit and form the first batch
+    assert FakeUnion.built[-1] == 6  # five members, rounded up to the bucket of six
+    cls = next(iter(srv.classes.values()))
+    assert cls["batch"].phantom_bytes == per
+    assert srv.active_bytes == 6 * per
+    run_checked(srv)
+    assert srv.active_bytes == 0
+
+
+def test_no_phantoms_without_budget_room(fake):
+    per = S.request_bytes(mesh()[0], GmgOptions())
+    srv = S.Server(budget_bytes=5 * per, steps_per_round=2)
+    for _ in range(5):
+        srv.submit(req(6))
+    srv.step()
+    assert FakeUnion.built[-1] == 5
+    run_checked(srv)
+
+
+def test_idle_unions_evicted_lru_to_admit(fake):
+    per0 = S.request_bytes(mesh()[0], GmgOptions())
+    per1 = S.request_bytes(mesh()[1], GmgOptions())
+    srv = S.Server(budget_bytes=per0 + per1 - 1, steps_per_round=8)
+    srv.submit(req(3, 0))
+    run_checked(srv)  # one idle cached union of mesh 0
+    assert srv._idle_cache_bytes() == per0
+    srv.submit(req(3, 1))  # needs the room the idle union holds
+    run_checked(srv)
+    assert srv.stats["union_evictions"] >= 1
+    assert len(srv.results) == 2
