@@ -181,3 +181,14 @@ def test_idle_unions_evicted_lru_to_admit(fake):
     run_checked(srv)
     assert srv.stats["union_evictions"] >= 1
     assert len(srv.results) == 2
+
+
+def test_union_cache_key_includes_solver_options(fake):
+    """Requests on the same mesh with different solver options never share a union."""
+    srv = S.Server(budget_bytes=1 << 40, steps_per_round=4)
+    srv.submit(req(3))
+    run_checked(srv)
+    builds = srv.stats["union_builds"]
+    srv.submit(S.Request(mesh()[0], np.array([3.0]), GmgOptions(cycle_type="W")))
+    run_checked(srv)
+    assert srv.stats["union_builds"] == builds + 1

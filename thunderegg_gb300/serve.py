@@ -27,14 +27,23 @@ the room.
 
 Each request stops on its own residual test; its arithmetic never mixes with
 other requests' (per-patch kernels, per-solve reductions), so its result
-matches a solve of the same request alone within the solver tolerance.  The
-server is single-threaded: all handles live on the thread that created it.
+matches a solve of the same request alone within the solver tolerance.
+
+Every class has its own CUDA stream (its handles bind to it when its unions
+are built), and the batches of different classes are stepped concurrently
+from worker threads (the step entry point releases the interpreter lock), so
+one class's kernels fill the GPU while another waits on its host-side
+convergence test.  Everything else -- admission, building unions, copying
+iterates, retiring -- runs on the thread that owns the server.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
+import dataclasses
 import itertools
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -81,10 +90,10 @@ def request_bytes(levels, opts: GmgOptions) -> int:
 
 
 def _class_key(r: Request):
+    """Requests batch together when their patch shape, depth, coefficient use and every
+    solver option agree."""
     lv = r.levels[0]
-    o = r.opts
-    return (lv.dim, tuple(lv.ns), lv.num_ghost, len(r.levels), o.scheme, o.fill_type, o.smoother, o.cycle_dtype,
-            o.tol, o.max_it, o.bicgstab_flags, o.pre_sweeps, o.post_sweeps, o.coarse_sweeps, r.coeffs is not None)
+    return (lv.dim, tuple(lv.ns), lv.num_ghost, len(r.levels), r.coeffs is not None) + dataclasses.astuple(r.opts)
 
 
 class _Active:
@@ -117,7 +126,8 @@ class _Union:
 
 
 def _union_key(reqs):
-    return tuple((id(r.levels), id(r.coeffs)) for r in reqs)
+    # the class (patch shape, depth, solver options) and the members' meshes and coefficients
+    return (_class_key(reqs[0]),) + tuple((id(r.levels), id(r.coeffs)) for r in reqs)
 
 
 # batch sizes a class's union is rounded up to (ratio <= 1.5), so that the
@@ -204,7 +214,7 @@ class Server:
     steps_per_round: BiCGStab iterations a batch runs between scheduling
     decisions; max_batch: most requests per class batch."""
 
-    def __init__(self, budget_bytes=150e9, steps_per_round=2, max_batch=64, cache=True):
+    def __init__(self, budget_bytes=150e9, steps_per_round=2, max_batch=64, cache=True, parallel=True):
         self.budget = int(budget_bytes)
         self.k = int(steps_per_round)
         self.max_batch = int(max_batch)
@@ -214,9 +224,24 @@ class Server:
         self.results = {}
         self.active_bytes = 0
         self.use_cache = bool(cache)
+        self.parallel = bool(parallel)
+        self.streams = {}         # class key -> its CUDA stream
+        self.pool = None
         self.unions = {}          # union key -> _Union, least recently used first
         self.stats = {"rounds": 0, "reforms": 0, "max_batch": 0, "max_active_bytes": 0, "admitted": 0,
                       "union_builds": 0, "union_hits": 0, "union_evictions": 0}
+
+    def _on_class_stream(self, key):
+        """Context that makes the class's stream current (its handles bind to it)."""
+        try:
+            import torch
+        except ImportError:
+            return contextlib.nullcontext()
+        if not self.parallel or not torch.cuda.is_available():
+            return contextlib.nullcontext()
+        if key not in self.streams:
+            self.streams[key] = torch.cuda.Stream()
+        return torch.cuda.stream(self.streams[key])
 
     # ---- union cache
     def _idle_cache_bytes(self):
@@ -363,19 +388,28 @@ class Server:
         self._admit()
         for key, cls in self.classes.items():
             if cls["dirty"]:
-                self._reform(key, cls)
+                with self._on_class_stream(key):
+                    self._reform(key, cls)
+        running = [cls["batch"] for cls in self.classes.values() if cls["batch"] is not None]
+        if self.parallel and len(running) > 1:
+            if self.pool is None:
+                self.pool = ThreadPoolExecutor(max_workers=8)
+            list(self.pool.map(lambda b: b.step(self.k), running))
+        else:
+            for b in running:
+                b.step(self.k)
         for key, cls in self.classes.items():
             b = cls["batch"]
             if b is None:
                 continue
-            b.step(self.k)
             its, res, st, run = b.state()
             stopped = len(run) - sum(run)
             waiting = cls.get("waiting", 0)
             if waiting:
                 cls["wait_rounds"] = cls.get("wait_rounds", 0) + 1
             if stopped == len(run):
-                self._collect(cls)
+                with self._on_class_stream(key):
+                    self._collect(cls)
             elif (stopped and (self.queue or waiting or 4 * stopped >= len(run))) or \
                     (waiting and (2 * waiting >= len(run) or cls.get("wait_rounds", 0) >= 3)):
                 # retire stopped requests and let admitted ones join: re-form at the next round.
