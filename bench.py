@@ -272,6 +272,46 @@ def level_kernel_rooflines(te, solver, hbm, reps=15, warm=3):
             "peak_gbs": hbm, "l2": "flushed before every call", "kernels": out}
 
 
+def batch_scaling_measure(te, sizes=(1, 4, 16, 32, 64), reps=3):
+    """Served config-2 batches of B solves (union hierarchies, the benchmark RHS plus
+    seeded sine modes): solves/s and batch latency per B, CUDA events around each
+    solve_batched call (median of `reps` after one warm-up), L2 flushed between."""
+    import numpy as np
+    import torch
+
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels, f_np, _ = PB.config2()
+    rng = np.random.default_rng(77)
+    opts = GmgOptions(scheme=1, smoother=0, tol=1e-10, cycle_dtype=te.TE_F32, bicgstab_flags=1)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    out = {}
+    for B in sizes:
+        blevels, offsets = M.union_hierarchy([levels] * B)
+        s = GmgSolver(blevels, opts)
+        fs = np.concatenate([f_np + 0.1 * PB.sine_modes_rhs(levels[0], rng) for _ in range(B)], axis=0)
+        fv, uv = te.Vector.from_numpy(s.finest, fs), te.Vector(s.finest)
+        times = []
+        for i in range(reps + 1):
+            flush.fill_(i & 0xFF)
+            uv.t.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.solve_batched(fv, uv, offsets[0])
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i:
+                times.append(e0.elapsed_time(e1) / 1000.0)
+        t = statistics.median(times)
+        out[str(B)] = {"solves_per_s": B / t, "batch_ms": 1000 * t}
+        del s, fv, uv
+    return out
+
+
 def solver_variants_measure(te, reps=3):
     """One solve at a time with the other cycles and Krylov solvers of the API,
     device time per solve (CUDA events, median of `reps` after one warm-up),
@@ -632,6 +672,7 @@ def run_gpu(args):
     c4 = config4_measure(te) if extra else None
     lk = level_kernel_rooflines(te, served, hbm) if extra else None
     sv = solver_variants_measure(te) if extra else None
+    bs = batch_scaling_measure(te) if extra else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -677,6 +718,7 @@ def run_gpu(args):
         "config4": c4,
         "level_kernels": lk,
         "solver_variants": sv,
+        "batch_scaling": bs,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
