@@ -487,6 +487,7 @@ def serving_stream(args, te):
     srv.run()
     srv.results = {}
     builds0, hits0, reforms0 = srv.stats["union_builds"], srv.stats["union_hits"], srv.stats["reforms"]
+    fills0 = srv.stats["slot_fills"]
     t0 = time.perf_counter()
     ids, nxt = {}, 0
     while nxt < len(reqs) or not srv.idle():
@@ -511,6 +512,7 @@ def serving_stream(args, te):
             "latency_ms_p50": 1000 * pick(0.5), "latency_ms_p99": 1000 * pick(0.99),
             "max_rel_residual": res_max, "mean_iterations": float(np.mean(its)),
             "max_batch": srv.stats["max_batch"], "reforms": srv.stats["reforms"] - reforms0,
+            "slot_fills": srv.stats["slot_fills"] - fills0,
             "union_builds": srv.stats["union_builds"] - builds0, "union_cache_hits": srv.stats["union_hits"] - hits0,
             "mix": "0.7 x 2D (circle L3-6 32^2, uniform L4 32^2, uniform L5 16^2), "
                    "0.3 x 3D (uniform L3 16^3, uniform L3 8^3); 150 GB budget",

@@ -245,7 +245,7 @@ int te_cycle_timings(const te_cycle* c, int ncomp, const void* f, void* u, int m
  * residual of a preconditioned solve well above tol); TE_BICGSTAB_FP64_OUTER
  * = run the iteration in FP64 even with an FP32 cycle (no counterpart in the
  * reference). */
-enum { TE_BICGSTAB_PRECONDITIONED_EXIT = 1, TE_BICGSTAB_FP64_OUTER = 2 };
+enum { TE_BICGSTAB_PRECONDITIONED_EXIT = 1, TE_BICGSTAB_FP64_OUTER = 2, TE_BICGSTAB_SLOTS = 4 };
 int te_bicgstab_solve(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M,
                       double tol, int max_iterations, int flags, int* iterations,
                       double* final_residual);
@@ -280,8 +280,9 @@ int te_bicgstab_solve_batched(const te_operator* A, int ncomp, void* x, const vo
  * of the solves still iterating and sets *num_running (0: every solve has
  * finished, x holds the results); state reports per solve the iterations,
  * the last residual (the FP64 true residual once finished in the float-float
- * loop), the status and whether it is still iterating; sync_x writes the
- * current iterate of every solve into x and synchronises. */
+ * loop), the status and whether it is still iterating; sync_x waits for the
+ * batch's work to finish (x holds every solve's current iterate between
+ * steps). */
 typedef struct te_bicgstab_batch te_bicgstab_batch;
 int te_bicgstab_batch_create(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M, double tol,
                              int max_iterations, int flags, int num_solves, const int* patch_offsets,
@@ -290,6 +291,17 @@ int te_bicgstab_batch_step(te_bicgstab_batch* batch, int max_iterations, int* nu
 int te_bicgstab_batch_state(const te_bicgstab_batch* batch, int* iterations, double* residuals, int* statuses,
                             int* running);
 int te_bicgstab_batch_sync_x(te_bicgstab_batch* batch);
+/* Slot mode (a batch created with flags | TE_BICGSTAB_SLOTS; no reference
+ * counterpart): continuous batching of the solves.  _step only iterates; a
+ * solve that stopped on its recurrence is finished by _finish_slot, which
+ * computes its true FP64 residual and either reports it finished (*finished
+ * = 1; x holds its result in its patch range) or restarts it from that
+ * residual (at most 8 times per solve).  _reset puts a new system into a solve
+ * that is not iterating: the caller has written its right-hand side and
+ * initial iterate into the solve's patch range of b and x; it starts at
+ * iteration 0 while the other solves keep their state. */
+int te_bicgstab_batch_finish_slot(te_bicgstab_batch* batch, int slot, int* finished);
+int te_bicgstab_batch_reset(te_bicgstab_batch* batch, int slot);
 int te_bicgstab_batch_destroy(te_bicgstab_batch* batch);
 
 /* ---- dot product without allocation ---------------------------------------

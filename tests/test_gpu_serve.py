@@ -134,3 +134,31 @@ def test_serving_cache_respects_budget(te):
     assert srv.active_bytes + srv._idle_cache_bytes() <= 2 * per
     assert srv.stats["union_evictions"] >= 1
     _check(te, reqs, results)
+
+
+def test_serving_slot_fill(te):
+    """A request on the mesh of a free slot starts in it while the batch keeps
+    iterating (te_bicgstab_batch_reset); the running solves are not restarted
+    and every result still matches its solo solve."""
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions
+    from thunderegg_gb300.serve import Request, Server
+
+    rng = np.random.default_rng(41)
+    circ = M.circle_mesh(n=16, lo=2, hi=4)
+    opts = GmgOptions(scheme=1, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1)
+    reqs = [Request(circ, PB.sine_modes_rhs(circ[0], rng), opts) for _ in range(7)]
+    srv = Server(budget_bytes=64 << 30, steps_per_round=2)
+    for r in reqs[:5]:
+        srv.submit(r)  # five members in a batch of six: one free slot
+    srv.step()
+    srv.step()
+    srv.submit(reqs[5])  # takes the free slot
+    srv.step()
+    srv.submit(reqs[6])  # waits for a slot freed by a finished request, or a re-form
+    results = srv.run()
+    assert srv.stats["slot_fills"] >= 1
+    assert results[5].restarts == 0
+    assert all(results[i].restarts == 0 for i in range(5)) or srv.stats["reforms"] > 1
+    _check(te, reqs, results)

@@ -20,7 +20,8 @@ MESH = None
 def mesh():
     global MESH
     if MESH is None:
-        MESH = (M.uniform_mesh(2, 2, 8), M.uniform_mesh(2, 3, 8))
+        # 0 and 2: two meshes of one class (same shape and depth); 1: another class
+        MESH = (M.uniform_mesh(2, 2, 8), M.uniform_mesh(2, 3, 8), M.uniform_mesh(2, 2, 8))
     return MESH
 
 
@@ -43,38 +44,65 @@ class FakeUnion:
 
     def __init__(self, reqs, opts):
         self.reqs = list(reqs)
+        self.keep = [(r.levels, r.coeffs) for r in reqs]
         self.bytes = sum(S.request_bytes(r.levels, r.opts) for r in reqs)
         self.busy = False
         FakeUnion.built.append(len(reqs))
 
 
 class FakeBatch:
-    """Request m needs int(m.req.f[0]) iterations in total; a re-formed member keeps its count."""
+    """Slot batch: the request in slot i needs int(req.f[0]) iterations in total; a
+    re-formed member keeps its count; slots beyond the members start free."""
 
-    def __init__(self, members, x_parts, un, phantom_bytes=0):
-        self.members = list(members)
+    def __init__(self, members, x_parts, un):
         self.un = un
         un.busy = True
-        self.phantom_bytes = phantom_bytes
         self.h = object()
-        self.base_its = [m.iterations for m in members]
-        self.done = [0] * len(members)
-        assert len(un.reqs) >= len(members)
+        self.B = len(un.keep)
+        assert self.B >= len(members)
+        self.slot_key = [(id(lv), id(c)) for lv, c in un.keep]
+        self.slots = list(members) + [None] * (self.B - len(members))
+        self.base_its = [m.iterations for m in members] + [0] * (self.B - len(members))
+        self.done = [0] * self.B
+        self.puts = 0
+
+    @property
+    def members(self):
+        return [m for m in self.slots if m is not None]
+
+    def free_slot(self, req):
+        key = (id(req.levels), id(req.coeffs))
+        for i, m in enumerate(self.slots):
+            if m is None and self.slot_key[i] == key:
+                return i
+        return -1
+
+    def put(self, i, member):
+        assert self.slots[i] is None and self.slot_key[i] == (id(member.req.levels), id(member.req.coeffs))
+        self.slots[i] = member
+        self.base_its[i] = member.iterations
+        self.done[i] = 0
+        self.puts += 1
 
     def _left(self, i):
-        return int(self.members[i].req.f[0]) - self.base_its[i] - self.done[i]
+        m = self.slots[i]
+        return 0 if m is None else int(m.req.f[0]) - self.base_its[i] - self.done[i]
 
     def step(self, k):
-        for i in range(len(self.members)):
+        for i in range(self.B):
             self.done[i] += max(0, min(k, self._left(i)))
-        return sum(1 for i in range(len(self.members)) if self._left(i) > 0)
+        return sum(1 for i in range(self.B) if self._left(i) > 0)
 
     def state(self):
-        run = [1 if self._left(i) > 0 else 0 for i in range(len(self.members))]
-        return list(self.done), [1e-11] * len(self.members), [0] * len(self.members), run
+        run = [1 if self._left(i) > 0 else 0 for i in range(self.B)]
+        return list(self.done), [1e-11] * self.B, [0] * self.B, run
+
+    def finish(self, i):
+        assert self.slots[i] is not None and self._left(i) == 0
+        return True
 
     def slice_x(self, i):
-        return _X(np.full(3, float(self.members[i].rid)))
+        return _X(np.full(3, float(self.slots[i].rid)))
 
     def close(self):
         self.un.busy = False
@@ -146,7 +174,7 @@ def test_union_cache_reuses_member_sequences(fake):
     assert srv.stats["union_hits"] >= 1
 
 
-def test_batches_round_up_to_buckets_with_phantom_slots(fake):
+def test_batches_round_up_to_buckets_with_free_slots(fake):
     per = S.request_bytes(mesh()[0], GmgOptions())
     srv = S.Server(budget_bytes=1 << 40, steps_per_round=2)
     for _ in range(5):
@@ -154,7 +182,7 @@ def test_batches_round_up_to_buckets_with_phantom_slots(fake):
     srv.step()  # admit and form the first batch
     assert FakeUnion.built[-1] == 6  # five members, rounded up to the bucket of six
     cls = next(iter(srv.classes.values()))
-    assert cls["batch"].phantom_bytes == per
+    assert cls["batch"].B == 6 and len(cls["batch"].members) == 5
     assert srv.active_bytes == 6 * per
     run_checked(srv)
     assert srv.active_bytes == 0
@@ -192,3 +220,59 @@ def test_union_cache_key_includes_solver_options(fake):
     srv.submit(S.Request(mesh()[0], np.array([3.0]), GmgOptions(cycle_type="W")))
     run_checked(srv)
     assert srv.stats["union_builds"] == builds + 1
+
+
+def test_new_requests_fill_free_slots_without_reform(fake):
+    """A request on the mesh of a free slot starts in it while the others keep iterating:
+    no new union, no re-form, no restart of the running solves."""
+    srv = S.Server(budget_bytes=1 << 40, steps_per_round=2)
+    first = [srv.submit(req(20)) for _ in range(3)]  # bucket of 3: no free slot
+    short = srv.submit(req(2))  # waits a round, then the batch re-forms to 4 slots
+    srv.step()
+    srv.step()
+    builds, reforms = srv.stats["union_builds"], srv.stats["reforms"]
+    while short not in srv.results:
+        srv.step()
+    late = [srv.submit(req(4)) for _ in range(1)]  # the freed slot takes it
+    res = run_checked(srv)
+    assert srv.stats["slot_fills"] >= 1
+    assert srv.stats["union_builds"] == builds and srv.stats["reforms"] == reforms
+    for rid in first:
+        assert res[rid].iterations == 20
+    assert res[late[0]].iterations == 4 and res[late[0]].restarts == 0
+
+
+def test_other_mesh_reforms_and_carries_iterations(fake):
+    """A waiting request of another mesh finds no slot: the batch re-forms with it and the
+    running requests carry their iteration counts (one restart each)."""
+    srv = S.Server(budget_bytes=1 << 40, steps_per_round=2)
+    a = [srv.submit(req(12, 0)) for _ in range(2)]
+    srv.step()
+    srv.step()
+    b = srv.submit(req(5, 2))
+    res = run_checked(srv)
+    for rid in a:
+        assert res[rid].iterations == 12 and res[rid].restarts == 1
+    assert res[b].iterations == 5
+    assert srv.stats["reforms"] >= 2
+
+
+def test_slot_reservation_counts_waiting_requests(fake):
+    """Two arrivals for one free slot: only the first is admitted without memory."""
+    per = S.request_bytes(mesh()[0], GmgOptions())
+    srv = S.Server(budget_bytes=1 << 40, steps_per_round=1)
+    [srv.submit(req(30)) for _ in range(2)]
+    srv.submit(req(1))
+    srv.step()
+    cls = next(iter(srv.classes.values()))
+    assert cls["batch"].B == 3
+    while any(m is not None and int(m.req.f[0]) == 1 for m in cls["batch"].slots):
+        srv.step()
+    cls["batch"].step(0)
+    srv.queue = []
+    srv.submit(req(3))
+    srv.submit(req(3))
+    srv._admit()
+    assert sorted(cls["bytes"].values()) == [0, per]
+    run_checked(srv)
+    assert srv.active_bytes == 0

@@ -19,6 +19,7 @@ TE_GHOST_BILINEAR, TE_GHOST_BIQUADRATIC, TE_GHOST_TRILINEAR = 0, 1, 2
 TE_FILL_FACES, TE_FILL_EDGES, TE_FILL_CORNERS = 0, 1, 2
 TE_NOALLOC_MAX_PARTIALS = 65536
 TE_CYCLE_V, TE_CYCLE_W, TE_CYCLE_FMG = 0, 1, 2
+TE_BICGSTAB_PRECONDITIONED_EXIT, TE_BICGSTAB_FP64_OUTER, TE_BICGSTAB_SLOTS = 1, 2, 4
 
 _ip = ctypes.POINTER(ctypes.c_int)
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -110,6 +111,8 @@ _SIGS = {
     "te_vcycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, ctypes.POINTER(_V)]),
     "te_cycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, _I, ctypes.POINTER(_V)]),
     "te_cg_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
+    "te_bicgstab_batch_finish_slot": (_I, [_V, _I, ctypes.POINTER(_I)]),
+    "te_bicgstab_batch_reset": (_I, [_V, _I]),
     "te_cycle_destroy": (_I, [_V]),
     "te_cycle_apply": (_I, [_V, _I, _V, _V]),
     "te_cycle_timings": (_I, [_V, _I, _V, _V, _I, ctypes.c_char_p, _dp, _ip]),

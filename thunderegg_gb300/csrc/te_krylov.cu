@@ -302,7 +302,11 @@ __global__ void __launch_bounds__(KT) k_p(Layout L, int nc, Batch bt, double* p,
 // Float-float outer loop (mixed precision: FP32 V-cycle preconditioner).
 // The same recurrences and operation order as the FP64 kernels above, with
 // every Krylov vector a float-float pair stored as hi and lo FP32 arrays and
-// the preconditioner results mp, ms plain FP32 (they are FP32 values).
+// the preconditioner results mp, ms plain FP32 (they are FP32 values).  The
+// iterate x stays FP64: a float-float x (48-bit significand) rounds the
+// solution finely enough for the recurrence but not for the true residual,
+// which then stalls near 1e-10 on meshes of 2048^2 cells; an FP64 x costs the
+// same 8 bytes per cell.
 // ---------------------------------------------------------------------------
 struct DV {
   float* hi;
@@ -448,7 +452,8 @@ __global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double to
   kd_reduce<1>(v, bt, b, ch, part, counter, S, S_SS, 5, tol);
 }
 
-__global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV x, DV r, const float* mp, const float* ms,
+__global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, double* __restrict__ x, DV r,
+                                            const float* mp, const float* ms,
                                             CV ap, CV as, CV rhat, CV dir, double* part, unsigned int* counter,
                                             double* S) {
   TE_BLOCK_SOLVE(bt);
@@ -459,19 +464,20 @@ __global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV x,
   const df64 nalpha = -alpha, nomega = -omega;
   const bool done = Sb[S_DONE] != 0.0;
   dot2 d0, d1;
-  const CV xc = as_cv(x), rc = as_cv(r);
+  const CV rc = as_cv(r);
   if (done) {
-    TE_CHUNK_LOOP(bt, L, nc, b, ch, k, { stv(x, k, ldv(xc, k) + ldv(dir, k) * alpha); });
+    TE_CHUNK_LOOP(bt, L, nc, b, ch, k, { x[k] += df_to_double(ldv(dir, k) * alpha); });
   } else {
     ChunkCells<2> cells(bt, L, nc, b, ch);
     long long k[2];
     while (cells.next(k)) {
-      df64 xv[2], rv[2], av[2], sv[2], hv[2];
+      double xv[2];
+      df64 rv[2], av[2], sv[2], hv[2];
       float mv[2], nv[2];
 #pragma unroll
       for (int u = 0; u < 2; u++)
         if (k[u] >= 0) {
-          xv[u] = ldv(xc, k[u]);
+          xv[u] = x[k[u]];
           mv[u] = mp[k[u]];
           nv[u] = ms[k[u]];
           rv[u] = ldv(rc, k[u]);
@@ -482,7 +488,7 @@ __global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV x,
 #pragma unroll
       for (int u = 0; u < 2; u++)
         if (k[u] >= 0) {
-          stv(x, k[u], xv[u] + df_sum2(alpha, mv[u], omega, nv[u]));
+          x[k[u]] = xv[u] + df_to_double(df_sum2(alpha, mv[u], omega, nv[u]));
           const df64 rn = rv[u] + df_sum2(av[u], nalpha, sv[u], nomega);
           stv(r, k[u], rn);
           d0.add(rn, rn);
@@ -522,17 +528,6 @@ __global__ void __launch_bounds__(KT) kd_p(Layout L, int nc, Batch bt, DV p, CV 
 // Whole-vector conversions: each thread takes CONV_U elements per round and
 // loads them all before converting and storing any.
 constexpr int CONV_U = 4;
-__global__ void kd_split(const double* __restrict__ src, DV dst, long long n) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += CONV_U * stride) {
-    double v[CONV_U];
-#pragma unroll
-    for (int u = 0; u < CONV_U; u++) v[u] = i0 + u * stride < n ? src[i0 + u * stride] : 0.0;
-#pragma unroll
-    for (int u = 0; u < CONV_U; u++)
-      if (i0 + u * stride < n) stv(dst, i0 + u * stride, df_split_bits(v[u]));
-  }
-}
 // one split into three vectors (resid, rhat and p start equal)
 __global__ void kd_split3(const double* __restrict__ src, DV d0, DV d1, DV d2, long long n) {
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -549,17 +544,6 @@ __global__ void kd_split3(const double* __restrict__ src, DV d0, DV d1, DV d2, l
       stv(d1, i, s);
       stv(d2, i, s);
     }
-  }
-}
-__global__ void kd_join(CV src, double* __restrict__ dst, long long n) {
-  const long long stride = (long long)gridDim.x * blockDim.x;
-  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += CONV_U * stride) {
-    df64 v[CONV_U];
-#pragma unroll
-    for (int u = 0; u < CONV_U; u++) v[u] = i0 + u * stride < n ? ldv(src, i0 + u * stride) : df64(0.f, 0.f);
-#pragma unroll
-    for (int u = 0; u < CONV_U; u++)
-      if (i0 + u * stride < n) dst[i0 + u * stride] = df_to_double(v[u]);
   }
 }
 
@@ -903,7 +887,6 @@ struct KrylovWork {
   size_t n;
   std::vector<int> h_offs, h_nch;
   DevBuf<double> resid, rhat, p, ap, as, s, ms, mp, S, part;
-  DevBuf<double> xdf;  // float-float outer loop: the iterate (allocated on first use)
   DevBuf<unsigned int> counter;
   DevBuf<int> offs, nch, active;
   DevBuf<int> patch_solve;  // [P] solve of each finest patch
@@ -1084,7 +1067,8 @@ static bool apply_dots(const te_operator* A, KrylovWork& W, const float* u, DV f
 }
 
 // one float-float iteration; M is an FP32 cycle
-static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, double tol, int flags, cudaStream_t st) {
+static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, double* x, double tol, int flags,
+                         cudaStream_t st) {
   const Layout& L = W.d->lay;
   const int nc = W.nc;
   Batch bt = W.batch();
@@ -1110,7 +1094,7 @@ static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, doubl
     TE_LAUNCH_CHECK();
   }
   const CV dir = (flags & TE_BICGSTAB_PRECONDITIONED_EXIT) ? CV{W.f32(W.mp), nullptr} : W.cv(W.p);
-  kd_xr<<<W.grid(), KT, 0, st>>>(L, nc, bt, W.dv(W.xdf), W.dv(W.resid), W.f32(W.mp), W.f32(W.ms), W.cv(W.ap),
+  kd_xr<<<W.grid(), KT, 0, st>>>(L, nc, bt, x, W.dv(W.resid), W.f32(W.mp), W.f32(W.ms), W.cv(W.ap),
                                  W.cv(W.as), W.cv(W.rhat), dir, W.part.p, W.counter.p, W.S.p);
   count_launch();
   TE_LAUNCH_CHECK();
@@ -1152,12 +1136,19 @@ struct BatchRun {
   std::vector<int> its, statuses;
   int nactive = 0, restart = 0;
   bool done = false, use_graph = true;
+  // slot mode (TE_BICGSTAB_SLOTS): solves are reset and finished one at a time while the
+  // others iterate; step() only iterates
+  bool slot_mode = false;
+  std::vector<int> offs, restarts;
   std::tuple<void*, const void*, unsigned long long, unsigned long long, double, int> gkey;
 
   BatchRun(const te_operator* A_, int nc_, void* xv, const void* bv, const te_cycle* Mc, double tol_, int max_it,
            int flags_, const std::vector<int>& offsets)
       : A(A_), nc(nc_), d(A_->dom), st(A_->dom->stream), B((int)offsets.size() - 1), x((double*)xv),
         b((const double*)bv), tol(tol_), max_iterations(max_it), flags(flags_) {
+    offs = offsets;
+    restarts.assign(B, 0);
+    slot_mode = (flags & TE_BICGSTAB_SLOTS) != 0;
     // the solver's work vectors live with the operator (freed with it), per component count and batch layout
     auto& slot = A->krylov[std::make_pair(nc, offsets)];
     if (!slot) slot = std::make_shared<KrylovWork>(d, nc, offsets);
@@ -1186,13 +1177,11 @@ struct BatchRun {
     W.push_active(st);
     if (df) {
       // resid = b - A x in FP64, then split into float-float; rhat = p = resid (BiCGStab.h:113-131)
-      if (!W.xdf.p) W.xdf.alloc(W.n);
       operator_residual(A, nc, x, b, W.ap.p, st);
       // rhat = resid here, so rhat . resid and resid . resid are one sum (the same bits)
       launch_dots(W, 2, b, b, W.ap.p, W.ap.p, nullptr, nullptr, S_BB, 0, st);
       kd_split3<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), W.dv(W.rhat), W.dv(W.p), nvals);
-      kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
-      count_launch(2);
+      count_launch();
       TE_LAUNCH_CHECK();
     } else {
       // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
@@ -1228,7 +1217,6 @@ struct BatchRun {
 
   void iterate_once() {
     KrylovWork& W = *Wp;
-    joined = false;
     if (use_graph) {
       auto it = W.graphs.find(gkey);
       if (it == W.graphs.end()) {
@@ -1237,7 +1225,7 @@ struct BatchRun {
         TE_CUDA(cudaStreamBeginCapture(W.cap, cudaStreamCaptureModeThreadLocal));
         try {
           if (df)
-            iteration_df(W, A, M, tol, flags, W.cap);
+            iteration_df(W, A, M, x, tol, flags, W.cap);
           else
             iteration(W, A, M, x, tol, flags, W.cap);
         } catch (...) {
@@ -1259,7 +1247,7 @@ struct BatchRun {
       TE_CUDA(cudaEventRecord(W.ev_out, W.cap));
       TE_CUDA(cudaStreamWaitEvent(st, W.ev_out, 0));
     } else if (df) {
-      iteration_df(W, A, M, tol, flags, st);
+      iteration_df(W, A, M, x, tol, flags, st);
     } else {
       iteration(W, A, M, x, tol, flags, st);
     }
@@ -1294,22 +1282,12 @@ struct BatchRun {
     }
   }
 
-  // float-float x into the FP64 x (once after the last iteration)
-  bool joined = false;
-  void join_x() {
-    if (!df || joined) return;
-    kd_join<<<1216, 256, 0, st>>>(Wp->cv(Wp->xdf), x, nvals);
-    count_launch();
-    TE_LAUNCH_CHECK();
-    joined = true;
-  }
-
   // Residual replacement: the float-float recurrence keeps ~1e-14 of the
   // initial residual, so check every solve's true residual b - A x in FP64
-  // and restart the ones above tol from it.  True when some solve restarted.
-  bool replacement_check() {
+  // (the residual each solve reports) and, while restarts are allowed,
+  // restart the ones above tol from it.  True when some solve restarted.
+  bool replacement_check(bool allow_restart) {
     KrylovWork& W = *Wp;
-    join_x();
     for (int i = 0; i < B; i++) W.h_active[i] = statuses[i] == TE_OK ? 1 : 0;
     W.push_active(st);
     operator_residual(A, nc, x, b, W.ap.p, st);
@@ -1321,7 +1299,7 @@ struct BatchRun {
       const bool ok = statuses[i] == TE_OK && r0[i] != 0;
       const double tr = ok ? std::sqrt(h[S_TRUE]) / r0[i] : 0.0;
       if (ok) finals[i] = tr;
-      W.h_active[i] = (ok && tr > tol && its[i] < max_iterations) ? 1 : 0;
+      W.h_active[i] = (allow_restart && ok && tr > tol && its[i] < max_iterations) ? 1 : 0;
       const double rr = h[S_TRUE];
       for (int k = 0; k < S_NSLOTS; k++) h[k] = 0.0;
       h[S_RHO] = rr;  // rhat = r
@@ -1332,17 +1310,20 @@ struct BatchRun {
     W.push_active(st);
     if (nactive == 0) return false;
     kd_split3<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), W.dv(W.rhat), W.dv(W.p), nvals);
-    kd_split<<<1216, 256, 0, st>>>(x, W.dv(W.xdf), nvals);
-    count_launch(2);
+    count_launch();
     TE_LAUNCH_CHECK();
     TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
     return true;
   }
 
   void finish() {
-    join_x();
     TE_CUDA(cudaStreamSynchronize(st));
     done = true;
+    check_tc();
+  }
+
+  // a tensor-core DFT smoother whose MMA completion wait timed out flags it; the results are invalid
+  void check_tc() {
     if (M)
       for (const te_cycle_level& lv : M->levels)
         if (lv.smoother && dft_tc_error(lv.smoother, st)) {
@@ -1351,8 +1332,116 @@ struct BatchRun {
         }
   }
 
+  // ---- slot mode: one solve reset or finished while the others keep their state
+  long long slot_begin(int i) const { return (long long)offs[i] * d->lay.pstride(nc); }
+  long long slot_len(int i) const { return (long long)(offs[i + 1] - offs[i]) * d->lay.pstride(nc); }
+  // only solve i active on the device (for its reductions); returns the flags to restore
+  std::vector<int> only(int i) {
+    KrylovWork& W = *Wp;
+    std::vector<int> saved(W.h_active, W.h_active + B);
+    for (int j = 0; j < B; j++) W.h_active[j] = j == i ? 1 : 0;
+    W.push_active(st);
+    return saved;
+  }
+  void restore(const std::vector<int>& saved) {
+    KrylovWork& W = *Wp;
+    nactive = 0;
+    for (int j = 0; j < B; j++) {
+      W.h_active[j] = saved[j];
+      nactive += saved[j];
+    }
+    W.push_active(st);
+  }
+  // solve i's Krylov vectors from the FP64 residual in ap: resid = rhat = p = ap on its
+  // patch range only
+  void split_slot(int i) {
+    KrylovWork& W = *Wp;
+    const long long o = slot_begin(i), n = slot_len(i);
+    if (df) {
+      auto at = [&](DevBuf<double>& v) {
+        DV w = W.dv(v);
+        return DV{w.hi + o, w.lo + o};
+      };
+      kd_split3<<<1216, 256, 0, st>>>(W.ap.p + o, at(W.resid), at(W.rhat), at(W.p), n);
+      count_launch();
+      TE_LAUNCH_CHECK();
+    } else {
+      for (DevBuf<double>* v : {&W.resid, &W.rhat, &W.p})
+        TE_CUDA(cudaMemcpyAsync(v->p + o, W.ap.p + o, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+    }
+  }
+  // solve i's scalars restart with rho = rr (rhat = r) and its reference norm r0
+  void restart_row(int i, double rr) {
+    KrylovWork& W = *Wp;
+    double* h = W.h + (size_t)i * S_NSLOTS;
+    for (int k = 0; k < S_NSLOTS; k++) h[k] = 0.0;
+    h[S_RHO] = rr;
+    h[S_R0] = r0[i];
+    rho[i] = rr;
+    TE_CUDA(cudaMemcpyAsync(W.S.p + (size_t)i * S_NSLOTS, h, S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
+  }
+  // a new system in solve i: its b and x have been written into its patch range
+  void reset_slot(int i) {
+    KrylovWork& W = *Wp;
+    std::vector<int> saved = only(i);
+    operator_residual(A, nc, x, b, W.ap.p, st);
+    launch_dots(W, 2, b, b, W.ap.p, W.ap.p, nullptr, nullptr, S_BB, 0, st);
+    W.read_scalars(st);
+    const double* h = W.h + (size_t)i * S_NSLOTS;
+    const double bb = h[S_BB], rr = h[S_BB + 1];
+    r0[i] = std::sqrt(bb);
+    residual[i] = r0[i] != 0 ? std::sqrt(rr) / r0[i] : 0.0;
+    finals[i] = residual[i];
+    its[i] = 0;
+    restarts[i] = 0;
+    statuses[i] = TE_OK;
+    restart_row(i, rr);
+    split_slot(i);
+    bool run = r0[i] != 0 && residual[i] > tol && max_iterations > 0;  // BiCGStab.h:140-144
+    if (run && rr == 0) {
+      statuses[i] = TE_ERR_BREAKDOWN;
+      run = false;
+    }
+    saved[i] = run ? 1 : 0;
+    restore(saved);
+    done = false;
+  }
+  // solve i stopped on its recurrence: its true FP64 residual decides between finished
+  // (x holds its result) and a restart from that residual (at most 8 per solve)
+  bool finish_slot(int i) {
+    KrylovWork& W = *Wp;
+    require(!W.h_active[i], "solve is still iterating");
+    std::vector<int> saved = only(i);
+    operator_residual(A, nc, x, b, W.ap.p, st);
+    launch_dots(W, 1, W.ap.p, W.ap.p, nullptr, nullptr, nullptr, nullptr, S_TRUE, 0, st);
+    W.read_scalars(st);
+    const double rr = W.h[(size_t)i * S_NSLOTS + S_TRUE];
+    const bool ok = statuses[i] == TE_OK && r0[i] != 0;
+    const double tr = ok ? std::sqrt(rr) / r0[i] : 0.0;
+    if (ok) finals[i] = tr;
+    const bool again = ok && tr > tol && its[i] < max_iterations && restarts[i] < 8;
+    if (again) {
+      restarts[i]++;
+      restart_row(i, rr);
+      split_slot(i);
+    }
+    saved[i] = again ? 1 : 0;
+    restore(saved);
+    TE_CUDA(cudaStreamSynchronize(st));
+    check_tc();
+    return !again;
+  }
+
   // up to k iterations; returns the number of solves still iterating (0: finished, x holds the results)
   int step(long long k) {
+    if (slot_mode) {  // only iterate: resets and finishes are per solve
+      long long n = 0;
+      while (nactive > 0 && n < k) {
+        iterate_once();
+        n++;
+      }
+      return nactive;
+    }
     long long n = 0;
     while (!done) {
       if (nactive > 0) {
@@ -1361,7 +1450,7 @@ struct BatchRun {
         n++;
         continue;
       }
-      if (df && restart < 8 && replacement_check()) {
+      if (df && replacement_check(restart < 8)) {
         restart++;
         continue;
       }
@@ -1466,11 +1555,31 @@ int te_bicgstab_batch_state(const te_bicgstab_batch* h, int* iterations, double*
   });
 }
 
+int te_bicgstab_batch_reset(te_bicgstab_batch* h, int slot) {
+  return guard([&] {
+    require(h, "null argument");
+    BatchRun* r = reinterpret_cast<BatchRun*>(h);
+    require(r->slot_mode, "the batch was not created with TE_BICGSTAB_SLOTS");
+    require(slot >= 0 && slot < r->B, "slot out of range");
+    require(!r->Wp->h_active[slot], "slot is still iterating");
+    r->reset_slot(slot);
+  });
+}
+
+int te_bicgstab_batch_finish_slot(te_bicgstab_batch* h, int slot, int* finished) {
+  return guard([&] {
+    require(h && finished, "null argument");
+    BatchRun* r = reinterpret_cast<BatchRun*>(h);
+    require(r->slot_mode, "the batch was not created with TE_BICGSTAB_SLOTS");
+    require(slot >= 0 && slot < r->B, "slot out of range");
+    *finished = r->finish_slot(slot) ? 1 : 0;
+  });
+}
+
 int te_bicgstab_batch_sync_x(te_bicgstab_batch* h) {
   return guard([&] {
     require(h, "null argument");
     BatchRun* r = reinterpret_cast<BatchRun*>(h);
-    r->join_x();
     TE_CUDA(cudaStreamSynchronize(r->st));
   });
 }

@@ -5,15 +5,23 @@ hierarchy.  Requests whose hierarchies share patch shape, depth and solver
 options form a class; the active requests of a class are packed into one
 union hierarchy (mesh.union_hierarchy), so every per-level kernel of the
 V-cycle and every Krylov kernel runs over all of them in one launch (one CUDA
-graph replay per iteration).  The server steps each class's batch a few
-iterations at a time (te_bicgstab_batch_step).  Between steps it
+graph replay per iteration).  A batch is a fixed set of slots, one solve each
+(TE_BICGSTAB_SLOTS): the server steps each class's batch a few iterations at a
+time (te_bicgstab_batch_step), and between steps it
 
-  * admits queued requests while the estimated device memory of all active
-    requests stays within the budget,
-  * retires requests that have finished (their result is copied out and
-    their memory is released),
-  * re-forms a class's batch when its membership changes: the new union
-    hierarchy is built, every continuing request's current iterate and
+  * admits queued requests while the estimated device memory of the live
+    batches, the requests waiting for a slot and the idle cached unions stays
+    within the budget,
+  * puts a waiting request into a free slot built on its mesh
+    (te_bicgstab_batch_reset): its right-hand side and initial iterate are
+    copied into the slot and its solve starts while the other slots keep
+    iterating,
+  * finishes every slot whose solve stopped (te_bicgstab_batch_finish_slot:
+    its true FP64 residual either confirms it, and the result is copied out
+    and the slot freed, or restarts it),
+  * re-forms a class's batch when requests have waited without a slot of
+    their mesh: the new union hierarchy is built (rounded up to a bucket size,
+    the extra slots free), every continuing request's current iterate and
     right-hand side are copied into it, and its BiCGStab restarts from that
     iterate (its residual keeps decreasing; only the Krylov space is rebuilt).
 
@@ -50,7 +58,7 @@ import numpy as np
 
 from . import Vector
 from . import mesh as M
-from .capi import check, lib
+from .capi import TE_BICGSTAB_SLOTS, check, lib
 from .gmg import GmgOptions, GmgSolver
 
 
@@ -143,43 +151,70 @@ def _bucket(n, cap):
 
 
 class _Batch:
-    """One union-hierarchy batch of a class and its stepping BiCGStab run.  The
-    union may hold phantom slots after the members (zero right-hand side: their
-    solves are finished at the start and the Krylov kernels skip them)."""
+    """One union-hierarchy batch of a class in slot mode (TE_BICGSTAB_SLOTS): slot i
+    is solve i of the union.  A slot holds a request or is free (zero right-hand
+    side, not iterating); a free slot takes a new request of the same mesh while
+    the other slots keep iterating, and a stopped slot is finished on its own."""
 
-    def __init__(self, members, x_parts, un, phantom_bytes=0):
+    def __init__(self, members, x_parts, un):
         import torch
 
-        self.members = list(members)  # this batch's members, in patch order
         self.un = un
         un.busy = True
         self.solver = un.solver
         self.offsets = un.offsets
         self.x, self.b = un.x, un.b
-        self.phantom_bytes = phantom_bytes
+        self.B = len(self.offsets) - 1
+        self.slot_key = [(id(lv), id(c)) for lv, c in un.keep]
+        self.slots = list(members) + [None] * (self.B - len(members))
+        self.base_its = [m.iterations for m in members] + [0] * (self.B - len(members))
         for i, m in enumerate(members):
-            lo, hi = self.offsets[i], self.offsets[i + 1]
-            self.b.t[lo:hi].copy_(torch.as_tensor(m.req.f.reshape(self.b.t[lo:hi].shape)), non_blocking=False)
-            src = x_parts[i]
-            if isinstance(src, torch.Tensor):
-                self.x.t[lo:hi].copy_(src)
-            elif src is not None:
-                self.x.t[lo:hi].copy_(torch.as_tensor(src.reshape(self.x.t[lo:hi].shape)))
-            else:
-                self.x.t[lo:hi].zero_()
-        B = len(self.offsets) - 1  # members, then phantom slots
-        if B > len(members):
-            tail = slice(self.offsets[len(members)], self.offsets[B])
+            self._write(i, m.req.f, x_parts[i])
+        if self.B > len(members):
+            tail = slice(self.offsets[len(members)], self.offsets[self.B])
             self.b.t[tail].zero_()
             self.x.t[tail].zero_()
         torch.cuda.synchronize()
-        offs = (ctypes.c_int * (B + 1))(*self.offsets)
+        offs = (ctypes.c_int * (self.B + 1))(*self.offsets)
         self.h = ctypes.c_void_p()
         o = self.solver.opts
         check(lib().te_bicgstab_batch_create(self.solver.ops[0].h, 1, self.x.ptr, self.b.ptr, self.solver.cycle.h,
-                                             float(o.tol), int(o.max_it), int(o.bicgstab_flags), B, offs,
-                                             ctypes.byref(self.h)))
-        self.base_its = [m.iterations for m in members]
+                                             float(o.tol), int(o.max_it), int(o.bicgstab_flags) | TE_BICGSTAB_SLOTS,
+                                             self.B, offs, ctypes.byref(self.h)))
+
+    def _write(self, i, f, x0):
+        import torch
+
+        lo, hi = self.offsets[i], self.offsets[i + 1]
+        self.b.t[lo:hi].copy_(torch.as_tensor(f.reshape(self.b.t[lo:hi].shape)))
+        if isinstance(x0, torch.Tensor):
+            self.x.t[lo:hi].copy_(x0)
+        elif x0 is not None:
+            self.x.t[lo:hi].copy_(torch.as_tensor(x0.reshape(self.x.t[lo:hi].shape)))
+        else:
+            self.x.t[lo:hi].zero_()
+
+    @property
+    def members(self):
+        return [m for m in self.slots if m is not None]
+
+    def free_slot(self, req):
+        """A free slot built on req's mesh and coefficients, or -1."""
+        key = (id(req.levels), id(req.coeffs))
+        for i, m in enumerate(self.slots):
+            if m is None and self.slot_key[i] == key:
+                return i
+        return -1
+
+    def put(self, i, member):
+        """Start member in free slot i; the other slots keep iterating."""
+        import torch
+
+        self._write(i, member.req.f, member.x)
+        torch.cuda.current_stream().synchronize()
+        check(lib().te_bicgstab_batch_reset(self.h, int(i)))
+        self.slots[i] = member
+        self.base_its[i] = member.iterations
 
     def step(self, k):
         n = ctypes.c_int(0)
@@ -187,13 +222,19 @@ class _Batch:
         return n.value
 
     def state(self):
-        """Iterations, residuals, statuses and running flags of the members (phantoms left out)."""
-        B = len(self.offsets) - 1
+        """Iterations, residuals, statuses and running flags of every slot."""
+        B = self.B
         its, res = (ctypes.c_int * B)(), (ctypes.c_double * B)()
         st, run = (ctypes.c_int * B)(), (ctypes.c_int * B)()
         check(lib().te_bicgstab_batch_state(self.h, its, res, st, run))
-        n = len(self.members)
-        return list(its)[:n], list(res)[:n], list(st)[:n], list(run)[:n]
+        return list(its), list(res), list(st), list(run)
+
+    def finish(self, i):
+        """Slot i stopped: True when its FP64 residual confirms it (x holds its result),
+        False when it was restarted from that residual."""
+        done = ctypes.c_int(0)
+        check(lib().te_bicgstab_batch_finish_slot(self.h, int(i), ctypes.byref(done)))
+        return bool(done.value)
 
     def slice_x(self, i):
         lo, hi = self.offsets[i], self.offsets[i + 1]
@@ -209,10 +250,11 @@ class _Batch:
 class Server:
     """Admits, batches, steps and retires requests.
 
-    budget_bytes: device memory the active requests may hold (request_bytes);
-    a request larger than the budget alone is rejected (TE_ERR_BUDGET).
+    budget_bytes: device memory the live unions, the requests waiting for a slot
+    and the idle cached unions may hold together (request_bytes per slot); a
+    request larger than the budget alone is rejected (TE_ERR_BUDGET).
     steps_per_round: BiCGStab iterations a batch runs between scheduling
-    decisions; max_batch: most requests per class batch."""
+    decisions; max_batch: most slots per class batch."""
 
     def __init__(self, budget_bytes=150e9, steps_per_round=2, max_batch=64, cache=True, parallel=True):
         self.budget = int(budget_bytes)
@@ -220,16 +262,16 @@ class Server:
         self.max_batch = int(max_batch)
         self._ids = itertools.count()
         self.queue = []           # (rid, request, submit time, bytes)
-        self.classes = {}         # key -> {"active": [_Active], "batch": _Batch or None, "dirty": bool}
+        self.classes = {}         # key -> {"active": [_Active] in a slot, "waiting": [_Active], "batch": _Batch}
         self.results = {}
-        self.active_bytes = 0
+        self.active_bytes = 0     # live unions (every slot) + admitted requests waiting for a slot
         self.use_cache = bool(cache)
         self.parallel = bool(parallel)
         self.streams = {}         # class key -> its CUDA stream
         self.pool = None
         self.unions = {}          # union key -> _Union, least recently used first
         self.stats = {"rounds": 0, "reforms": 0, "max_batch": 0, "max_active_bytes": 0, "admitted": 0,
-                      "union_builds": 0, "union_hits": 0, "union_evictions": 0}
+                      "union_builds": 0, "union_hits": 0, "union_evictions": 0, "slot_fills": 0}
 
     def _on_class_stream(self, key):
         """Context that makes the class's stream current (its handles bind to it)."""
@@ -256,18 +298,6 @@ class Server:
                 del self.unions[key]
                 self.stats["union_evictions"] += 1
 
-    def _union(self, reqs, opts):
-        key = _union_key(reqs)
-        un = self.unions.pop(key, None)
-        if un is None:
-            un = _Union(reqs, opts)
-            self.stats["union_builds"] += 1
-        else:
-            self.stats["union_hits"] += 1
-        if self.use_cache:
-            self.unions[key] = un  # most recently used last
-        return un
-
     # ---- requests
     def submit(self, req: Request) -> int:
         nb = request_bytes(req.levels, req.opts)
@@ -279,117 +309,158 @@ class Server:
         return rid
 
     def idle(self):
-        return not self.queue and all(not c["active"] for c in self.classes.values())
+        return not self.queue and all(not c["active"] and not c["waiting"] for c in self.classes.values())
 
     # ---- scheduling
+    def _free_slots(self, cls, req):
+        """Free slots of req's mesh in the class's batch that no earlier waiting request claims."""
+        b = cls["batch"]
+        if b is None:
+            return 0
+        key = (id(req.levels), id(req.coeffs))
+        free = sum(1 for i, m in enumerate(b.slots) if m is None and b.slot_key[i] == key)
+        return free - sum(1 for a in cls["waiting"] if (id(a.req.levels), id(a.req.coeffs)) == key)
+
     def _admit(self):
+        """Queue -> the class's waiting list while the budget has room.  A request that will
+        take a free slot of its mesh needs no new memory; any other reserves its own bytes
+        until a batch holds it."""
         keep = []
         for rid, req, t0, nb in self.queue:
             key = _class_key(req)
-            cls = self.classes.setdefault(key, {"active": [], "batch": None, "dirty": False, "bytes": {}})
-            if self.active_bytes + nb > self.budget:
-                self._evict(nb)
-            if self.active_bytes + nb <= self.budget and len(cls["active"]) < self.max_batch:
+            cls = self.classes.setdefault(key, {"active": [], "waiting": [], "batch": None, "bytes": {},
+                                                "wait_rounds": 0})
+            need = 0 if self._free_slots(cls, req) > 0 else nb
+            if need and self.active_bytes + need + self._idle_cache_bytes() > self.budget:
+                self._evict(need)
+            if self.active_bytes + need + self._idle_cache_bytes() <= self.budget and \
+                    len(cls["active"]) + len(cls["waiting"]) < self.max_batch:
                 a = _Active(rid, req, t0)
                 a.x = req.u0
-                cls["active"].append(a)
-                cls["bytes"][rid] = nb
-                cls["waiting"] = cls.get("waiting", 0) + 1
-                if cls["batch"] is None:
-                    cls["dirty"] = True
-                self.active_bytes += nb
+                cls["waiting"].append(a)
+                cls["bytes"][rid] = need
+                self.active_bytes += need
                 self.stats["admitted"] += 1
             else:
                 keep.append((rid, req, t0, nb))
         self.queue = keep
         self.stats["max_active_bytes"] = max(self.stats["max_active_bytes"], self.active_bytes)
-        self._evict(0)
 
-    def _close(self, b):
-        b.close()
-        self.active_bytes -= b.phantom_bytes
-        b.phantom_bytes = 0
-
-    def _retire(self, cls, a, u, its, res, st):
+    def _retire(self, a, u, its, res, st):
         self.results[a.rid] = Result(u=u, iterations=its, residual=res, status=st,
                                      latency_s=time.perf_counter() - a.submitted, restarts=a.restarts)
-        self.active_bytes -= cls["bytes"].pop(a.rid)
 
-    def _reform(self, key, cls):
-        old = cls["batch"]
-        if old is not None:
-            # carry every continuing request's iterate (device copy) into the new batch
-            check(lib().te_bicgstab_batch_sync_x(old.h))
-            its, _, _, _ = old.state()
-            pos = {m.rid: i for i, m in enumerate(old.members)}
-            for m in cls["active"]:
-                if m.rid in pos:
-                    i = pos[m.rid]
-                    m.x = old.slice_x(i)
-                    m.iterations = old.base_its[i] + its[i]
-                    m.restarts += 1
-            self._close(old)
-            cls["batch"] = None
-        cls["dirty"] = False
-        cls["waiting"] = 0
-        cls["wait_rounds"] = 0
-        while cls["active"]:
-            members = cls["active"]
-            reqs = [m.req for m in members]
-            # phantom slots round the batch up to a bucket size, when the budget has room for them
-            last = members[-1].req
-            extra = _bucket(len(members), self.max_batch) - len(members)
-            pbytes = extra * request_bytes(last.levels, last.opts)
-            if extra and self.active_bytes + self._idle_cache_bytes() + pbytes > self.budget:
-                self._evict(pbytes)
-            if extra and self.active_bytes + self._idle_cache_bytes() + pbytes > self.budget:
-                extra, pbytes = 0, 0
-            reqs += [Request(last.levels, None, last.opts, last.coeffs)] * extra
-            self.active_bytes += pbytes
-            b = _Batch(members, [m.x for m in members], self._union(reqs, members[0].req.opts), pbytes)
-            self.stats["reforms"] += 1
-            self.stats["max_batch"] = max(self.stats["max_batch"], len(members))
-            its, res, st, run = b.state()
-            # requests already finished when the batch starts (their FP64 residual is within tolerance,
-            # or they broke down or ran out of iterations) leave now; the rest run without them
-            fin = [i for i in range(len(members)) if not run[i]]
-            if not fin or len(fin) == len(members):
-                cls["batch"] = b
-                if len(fin) == len(members):
-                    self._collect(cls)
-                return
-            for i in fin:
-                self._retire(cls, members[i], b.slice_x(i).cpu().numpy(), b.base_its[i] + its[i], res[i], st[i])
-            gone = {members[i].rid for i in fin}
-            cls["active"] = [m for m in members if m.rid not in gone]
-            for m in cls["active"]:
-                m.x = b.slice_x(members.index(m))
-            self._close(b)
+    def _form(self, cls):
+        """A new batch of the class's waiting requests (continuing ones carry their iterate),
+        rounded up to a bucket size with free slots of the last request's mesh when the
+        budget has room.  The union's bytes replace the requests' reservations."""
+        members = cls["waiting"]
+        self.active_bytes -= sum(cls["bytes"].pop(m.rid, 0) for m in members)
+        last = members[-1].req
+        extra = _bucket(len(members), self.max_batch) - len(members)
+        for pad in ((extra, 0) if extra else (0,)):
+            reqs = [m.req for m in members] + [Request(last.levels, None, last.opts, last.coeffs)] * pad
+            key = _union_key(reqs)
+            un = self.unions.pop(key, None)  # out of the idle cache while it is weighed
+            need = un.bytes if un is not None else sum(request_bytes(r.levels, r.opts) for r in reqs)
+            if self.active_bytes + need + self._idle_cache_bytes() > self.budget:
+                self._evict(need)
+            if pad == 0 or self.active_bytes + need + self._idle_cache_bytes() <= self.budget:
+                break
+            if un is not None:
+                self.unions[key] = un
+        if un is None:
+            un = _Union(reqs, members[0].req.opts)
+            self.stats["union_builds"] += 1
+        else:
+            self.stats["union_hits"] += 1
+        if self.use_cache:
+            self.unions[key] = un  # most recently used last
+        b = _Batch(members, [m.x for m in members], un)
+        self.active_bytes += un.bytes
+        self._evict(0)  # the idle cache shrinks to what the budget leaves
+        cls["batch"], cls["active"], cls["waiting"], cls["wait_rounds"] = b, list(members), [], 0
+        self.stats["reforms"] += 1
+        self.stats["max_batch"] = max(self.stats["max_batch"], b.B)
+        self.stats["max_active_bytes"] = max(self.stats["max_active_bytes"], self.active_bytes)
 
-    def _collect(self, cls):
-        """Retire every request of the class's batch once the whole batch has finished."""
+    def _close(self, cls):
+        """Release the class's batch: its union becomes an idle cache entry."""
         b = cls["batch"]
-        if b.step(0) != 0:
-            return
-        its, res, st, run = b.state()
-        for i, m in enumerate(b.members):
-            self._retire(cls, m, b.slice_x(i).cpu().numpy(), b.base_its[i] + its[i], res[i], st[i])
-        gone = {m.rid for m in b.members}
-        cls["active"] = [m for m in cls["active"] if m.rid not in gone]
-        self._close(b)
+        b.close()
+        self.active_bytes -= b.un.bytes
         cls["batch"] = None
-        if cls["active"]:
-            cls["dirty"] = True
+
+    def _place(self, cls):
+        """Waiting requests into free slots of their mesh; a new batch when the class has
+        none, or when requests have waited without a slot (the batch then grows)."""
+        b = cls["batch"]
+        if b is None:
+            if cls["waiting"]:
+                self._form(cls)
+            return
+        still = []
+        for a in cls["waiting"]:
+            i = b.free_slot(a.req)
+            if i < 0:
+                still.append(a)
+                continue
+            b.put(i, a)
+            self.active_bytes -= cls["bytes"].pop(a.rid, 0)
+            cls["active"].append(a)
+            self.stats["slot_fills"] += 1
+        cls["waiting"] = still
+        if not still:
+            cls["wait_rounds"] = 0
+            return
+        cls["wait_rounds"] += 1
+        if cls["active"] and 2 * len(still) < b.B and cls["wait_rounds"] < 2:
+            return  # let a few more arrivals gather before the batch is re-formed
+        # re-form: continuing requests carry their iterates (their Krylov spaces restart)
+        check(lib().te_bicgstab_batch_sync_x(b.h))
+        its, _, _, _ = b.state()
+        carried = []
+        for i, m in enumerate(b.slots):
+            if m is not None:
+                m.x = b.slice_x(i)
+                m.iterations = b.base_its[i] + its[i]
+                m.restarts += 1
+                carried.append(m)
+        self._close(cls)
+        for m in carried:  # reserved again until the new union holds them
+            cls["bytes"][m.rid] = request_bytes(m.req.levels, m.req.opts)
+            self.active_bytes += cls["bytes"][m.rid]
+        cls["waiting"] = carried + still
+        self._form(cls)
+
+    def _harvest(self, cls):
+        """Finish the stopped slots: retire confirmed requests and free their slots; a batch
+        with no requests left is closed."""
+        b = cls["batch"]
+        if b is None:
+            return
+        _, _, _, run = b.state()
+        for i, m in enumerate(b.slots):
+            if m is None or run[i]:
+                continue
+            if not b.finish(i):
+                continue  # restarted from its true residual
+            its, res, st, _ = b.state()
+            self._retire(m, b.slice_x(i).cpu().numpy(), b.base_its[i] + its[i], res[i], st[i])
+            b.slots[i] = None
+            cls["active"].remove(m)
+        if not cls["active"] and not cls["waiting"]:
+            self._close(cls)
 
     def step(self):
-        """One scheduling round: admit, re-form changed batches, advance every batch
-        by up to steps_per_round iterations, retire finished requests."""
+        """One scheduling round: admit, place waiting requests into free slots (or
+        re-form), advance every batch by up to steps_per_round iterations, finish
+        stopped slots and retire their requests."""
         self.stats["rounds"] += 1
         self._admit()
         for key, cls in self.classes.items():
-            if cls["dirty"]:
-                with self._on_class_stream(key):
-                    self._reform(key, cls)
+            with self._on_class_stream(key):
+                self._place(cls)
         running = [cls["batch"] for cls in self.classes.values() if cls["batch"] is not None]
         if self.parallel and len(running) > 1:
             if self.pool is None:
@@ -399,23 +470,8 @@ class Server:
             for b in running:
                 b.step(self.k)
         for key, cls in self.classes.items():
-            b = cls["batch"]
-            if b is None:
-                continue
-            its, res, st, run = b.state()
-            stopped = len(run) - sum(run)
-            waiting = cls.get("waiting", 0)
-            if waiting:
-                cls["wait_rounds"] = cls.get("wait_rounds", 0) + 1
-            if stopped == len(run):
-                with self._on_class_stream(key):
-                    self._collect(cls)
-            elif (stopped and (self.queue or waiting or 4 * stopped >= len(run))) or \
-                    (waiting and (2 * waiting >= len(run) or cls.get("wait_rounds", 0) >= 3)):
-                # retire stopped requests and let admitted ones join: re-form at the next round.
-                # Admitted requests join a running batch once they are half its size or have
-                # waited three rounds, so that arrivals do not rebuild the batch one by one.
-                cls["dirty"] = True
+            with self._on_class_stream(key):
+                self._harvest(cls)
         return not self.idle()
 
     def run(self, max_rounds=10**9):
