@@ -292,15 +292,16 @@ int te_bicgstab_batch_state(const te_bicgstab_batch* batch, int* iterations, dou
                             int* running);
 int te_bicgstab_batch_sync_x(te_bicgstab_batch* batch);
 /* Slot mode (a batch created with flags | TE_BICGSTAB_SLOTS; no reference
- * counterpart): continuous batching of the solves.  _step only iterates; a
- * solve that stopped on its recurrence is finished by _finish_slot, which
- * computes its true FP64 residual and either reports it finished (*finished
- * = 1; x holds its result in its patch range) or restarts it from that
- * residual (at most 8 times per solve).  _reset puts a new system into a solve
- * that is not iterating: the caller has written its right-hand side and
- * initial iterate into the solve's patch range of b and x; it starts at
- * iteration 0 while the other solves keep their state. */
-int te_bicgstab_batch_finish_slot(te_bicgstab_batch* batch, int slot, int* finished);
+ * counterpart): continuous batching of the solves.  _step only iterates.
+ * Solves that stopped on their recurrences are finished together by
+ * _finish_slots: one FP64 residual pass gives each listed solve's true
+ * residual, and per solve either reports it finished (finished[k] = 1; x holds
+ * its result in its patch range) or restarts it from that residual (at most 8
+ * times per solve).  _reset puts a new system into a solve that is not
+ * iterating: the caller has written its right-hand side and initial iterate
+ * into the solve's patch range of b and x; it starts at iteration 0 while the
+ * other solves keep their state. */
+int te_bicgstab_batch_finish_slots(te_bicgstab_batch* batch, int num_slots, const int* slots, int* finished);
 int te_bicgstab_batch_reset(te_bicgstab_batch* batch, int slot);
 int te_bicgstab_batch_destroy(te_bicgstab_batch* batch);
 

@@ -97,9 +97,10 @@ class FakeBatch:
         run = [1 if self._left(i) > 0 else 0 for i in range(self.B)]
         return list(self.done), [1e-11] * self.B, [0] * self.B, run
 
-    def finish(self, i):
-        assert self.slots[i] is not None and self._left(i) == 0
-        return True
+    def finish(self, slots):
+        for i in slots:
+            assert self.slots[i] is not None and self._left(i) == 0
+        return [True] * len(slots)
 
     def slice_x(self, i):
         return _X(np.full(3, float(self.slots[i].rid)))

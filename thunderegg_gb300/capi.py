@@ -111,7 +111,7 @@ _SIGS = {
     "te_vcycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, ctypes.POINTER(_V)]),
     "te_cycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, _I, ctypes.POINTER(_V)]),
     "te_cg_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
-    "te_bicgstab_batch_finish_slot": (_I, [_V, _I, ctypes.POINTER(_I)]),
+    "te_bicgstab_batch_finish_slots": (_I, [_V, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "te_bicgstab_batch_reset": (_I, [_V, _I]),
     "te_cycle_destroy": (_I, [_V]),
     "te_cycle_apply": (_I, [_V, _I, _V, _V]),

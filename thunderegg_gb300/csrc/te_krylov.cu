@@ -1406,30 +1406,42 @@ struct BatchRun {
     restore(saved);
     done = false;
   }
-  // solve i stopped on its recurrence: its true FP64 residual decides between finished
+  // the listed solves stopped on their recurrences: one FP64 residual b - A x and one
+  // masked reduction give their true residuals, which decide per solve between finished
   // (x holds its result) and a restart from that residual (at most 8 per solve)
-  bool finish_slot(int i) {
+  void finish_slots(const std::vector<int>& sl, int* finished) {
     KrylovWork& W = *Wp;
-    require(!W.h_active[i], "solve is still iterating");
-    std::vector<int> saved = only(i);
+    std::vector<char> seen(B, 0);
+    for (int i : sl) {
+      require(i >= 0 && i < B, "slot out of range");
+      require(!seen[i], "slot listed twice");
+      require(!W.h_active[i], "solve is still iterating");
+      seen[i] = 1;
+    }
+    std::vector<int> saved(W.h_active, W.h_active + B);
+    for (int j = 0; j < B; j++) W.h_active[j] = seen[j];
+    W.push_active(st);
     operator_residual(A, nc, x, b, W.ap.p, st);
     launch_dots(W, 1, W.ap.p, W.ap.p, nullptr, nullptr, nullptr, nullptr, S_TRUE, 0, st);
     W.read_scalars(st);
-    const double rr = W.h[(size_t)i * S_NSLOTS + S_TRUE];
-    const bool ok = statuses[i] == TE_OK && r0[i] != 0;
-    const double tr = ok ? std::sqrt(rr) / r0[i] : 0.0;
-    if (ok) finals[i] = tr;
-    const bool again = ok && tr > tol && its[i] < max_iterations && restarts[i] < 8;
-    if (again) {
-      restarts[i]++;
-      restart_row(i, rr);
-      split_slot(i);
+    for (size_t k = 0; k < sl.size(); k++) {
+      const int i = sl[k];
+      const double rr = W.h[(size_t)i * S_NSLOTS + S_TRUE];
+      const bool ok = statuses[i] == TE_OK && r0[i] != 0;
+      const double tr = ok ? std::sqrt(rr) / r0[i] : 0.0;
+      if (ok) finals[i] = tr;
+      const bool again = ok && tr > tol && its[i] < max_iterations && restarts[i] < 8;
+      if (again) {
+        restarts[i]++;
+        restart_row(i, rr);
+        split_slot(i);
+      }
+      saved[i] = again ? 1 : 0;
+      finished[k] = again ? 0 : 1;
     }
-    saved[i] = again ? 1 : 0;
     restore(saved);
     TE_CUDA(cudaStreamSynchronize(st));
     check_tc();
-    return !again;
   }
 
   // up to k iterations; returns the number of solves still iterating (0: finished, x holds the results)
@@ -1566,13 +1578,14 @@ int te_bicgstab_batch_reset(te_bicgstab_batch* h, int slot) {
   });
 }
 
-int te_bicgstab_batch_finish_slot(te_bicgstab_batch* h, int slot, int* finished) {
+int te_bicgstab_batch_finish_slots(te_bicgstab_batch* h, int num_slots, const int* slots, int* finished) {
   return guard([&] {
-    require(h && finished, "null argument");
+    require(h && (num_slots == 0 || (slots && finished)), "null argument");
+    require(num_slots >= 0, "num_slots must be >= 0");
     BatchRun* r = reinterpret_cast<BatchRun*>(h);
     require(r->slot_mode, "the batch was not created with TE_BICGSTAB_SLOTS");
-    require(slot >= 0 && slot < r->B, "slot out of range");
-    *finished = r->finish_slot(slot) ? 1 : 0;
+    if (num_slots == 0) return;
+    r->finish_slots(std::vector<int>(slots, slots + num_slots), finished);
   });
 }
 

@@ -16,9 +16,10 @@ time (te_bicgstab_batch_step), and between steps it
     (te_bicgstab_batch_reset): its right-hand side and initial iterate are
     copied into the slot and its solve starts while the other slots keep
     iterating,
-  * finishes every slot whose solve stopped (te_bicgstab_batch_finish_slot:
-    its true FP64 residual either confirms it, and the result is copied out
-    and the slot freed, or restarts it),
+  * finishes the slots whose solves stopped, together
+    (te_bicgstab_batch_finish_slots: one FP64 residual pass; each true
+    residual either confirms its solve, whose result is copied out and whose
+    slot is freed, or restarts it),
   * re-forms a class's batch when requests have waited without a slot of
     their mesh: the new union hierarchy is built (rounded up to a bucket size,
     the extra slots free), every continuing request's current iterate and
@@ -229,12 +230,13 @@ class _Batch:
         check(lib().te_bicgstab_batch_state(self.h, its, res, st, run))
         return list(its), list(res), list(st), list(run)
 
-    def finish(self, i):
-        """Slot i stopped: True when its FP64 residual confirms it (x holds its result),
-        False when it was restarted from that residual."""
-        done = ctypes.c_int(0)
-        check(lib().te_bicgstab_batch_finish_slot(self.h, int(i), ctypes.byref(done)))
-        return bool(done.value)
+    def finish(self, slots):
+        """The listed slots stopped: per slot True when its FP64 residual confirms it (x holds
+        its result), False when it was restarted from that residual."""
+        n = len(slots)
+        arr, done = (ctypes.c_int * n)(*slots), (ctypes.c_int * n)()
+        check(lib().te_bicgstab_batch_finish_slots(self.h, n, arr, done))
+        return [bool(d) for d in done]
 
     def slice_x(self, i):
         lo, hi = self.offsets[i], self.offsets[i + 1]
@@ -440,15 +442,17 @@ class Server:
         if b is None:
             return
         _, _, _, run = b.state()
-        for i, m in enumerate(b.slots):
-            if m is None or run[i]:
-                continue
-            if not b.finish(i):
-                continue  # restarted from its true residual
+        stopped = [i for i, m in enumerate(b.slots) if m is not None and not run[i]]
+        if stopped:
+            done = b.finish(stopped)
             its, res, st, _ = b.state()
-            self._retire(m, b.slice_x(i).cpu().numpy(), b.base_its[i] + its[i], res[i], st[i])
-            b.slots[i] = None
-            cls["active"].remove(m)
+            for i, ok in zip(stopped, done):
+                if not ok:
+                    continue  # restarted from its true residual
+                m = b.slots[i]
+                self._retire(m, b.slice_x(i).cpu().numpy(), b.base_its[i] + its[i], res[i], st[i])
+                b.slots[i] = None
+                cls["active"].remove(m)
         if not cls["active"] and not cls["waiting"]:
             self._close(cls)
 
