@@ -303,10 +303,12 @@ __global__ void __launch_bounds__(KT) k_p(Layout L, int nc, Batch bt, double* p,
 // The same recurrences and operation order as the FP64 kernels above, with
 // every Krylov vector a float-float pair stored as hi and lo FP32 arrays and
 // the preconditioner results mp, ms plain FP32 (they are FP32 values).  The
-// iterate x stays FP64: a float-float x (48-bit significand) rounds the
-// solution finely enough for the recurrence but not for the true residual,
-// which then stalls near 1e-10 on meshes of 2048^2 cells; an FP64 x costs the
-// same 8 bytes per cell.
+// iterate is split: x stays FP64 and the loop accumulates a float-float
+// correction dx, folded into x (x += dx, dx = 0, in FP64) at every true-
+// residual check.  A float-float x re-rounded to 48 bits at each restart
+// stalls the true residual near 1e-10 on meshes of 2048^2 cells; after the
+// first check dx only carries the small correction, so 48 bits suffice, and
+// the loop itself needs no FP64 arithmetic.
 // ---------------------------------------------------------------------------
 struct DV {
   float* hi;
@@ -452,8 +454,8 @@ __global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double to
   kd_reduce<1>(v, bt, b, ch, part, counter, S, S_SS, 5, tol);
 }
 
-__global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, double* __restrict__ x, DV r,
-                                            const float* mp, const float* ms,
+__global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV dx, DV r, const float* mp,
+                                            const float* ms,
                                             CV ap, CV as, CV rhat, CV dir, double* part, unsigned int* counter,
                                             double* S) {
   TE_BLOCK_SOLVE(bt);
@@ -464,20 +466,19 @@ __global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, doubl
   const df64 nalpha = -alpha, nomega = -omega;
   const bool done = Sb[S_DONE] != 0.0;
   dot2 d0, d1;
-  const CV rc = as_cv(r);
+  const CV xc = as_cv(dx), rc = as_cv(r);
   if (done) {
-    TE_CHUNK_LOOP(bt, L, nc, b, ch, k, { x[k] += df_to_double(ldv(dir, k) * alpha); });
+    TE_CHUNK_LOOP(bt, L, nc, b, ch, k, { stv(dx, k, ldv(xc, k) + ldv(dir, k) * alpha); });
   } else {
     ChunkCells<2> cells(bt, L, nc, b, ch);
     long long k[2];
     while (cells.next(k)) {
-      double xv[2];
-      df64 rv[2], av[2], sv[2], hv[2];
+      df64 xv[2], rv[2], av[2], sv[2], hv[2];
       float mv[2], nv[2];
 #pragma unroll
       for (int u = 0; u < 2; u++)
         if (k[u] >= 0) {
-          xv[u] = x[k[u]];
+          xv[u] = ldv(xc, k[u]);
           mv[u] = mp[k[u]];
           nv[u] = ms[k[u]];
           rv[u] = ldv(rc, k[u]);
@@ -488,7 +489,7 @@ __global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, doubl
 #pragma unroll
       for (int u = 0; u < 2; u++)
         if (k[u] >= 0) {
-          x[k[u]] = xv[u] + df_to_double(df_sum2(alpha, mv[u], omega, nv[u]));
+          stv(dx, k[u], xv[u] + df_sum2(alpha, mv[u], omega, nv[u]));
           const df64 rn = rv[u] + df_sum2(av[u], nalpha, sv[u], nomega);
           stv(r, k[u], rn);
           d0.add(rn, rn);
@@ -543,6 +544,28 @@ __global__ void kd_split3(const double* __restrict__ src, DV d0, DV d1, DV d2, l
       stv(d0, i, s);
       stv(d1, i, s);
       stv(d2, i, s);
+    }
+  }
+}
+
+// x += dx in FP64, then dx = 0: the loop's float-float correction folded into the FP64 iterate
+__global__ void kd_fold(DV dx, double* __restrict__ x, long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += CONV_U * stride) {
+    df64 d[CONV_U];
+    double v[CONV_U];
+#pragma unroll
+    for (int u = 0; u < CONV_U; u++) {
+      const long long i = i0 + u * stride;
+      d[u] = i < n ? ldv(as_cv(dx), i) : df64(0.f, 0.f);
+      v[u] = i < n ? x[i] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < CONV_U; u++) {
+      const long long i = i0 + u * stride;
+      if (i >= n) continue;
+      x[i] = v[u] + df_to_double(d[u]);
+      stv(dx, i, df64(0.f, 0.f));
     }
   }
 }
@@ -891,6 +914,7 @@ struct KrylovWork {
   DevBuf<int> offs, nch, active;
   DevBuf<int> patch_solve;  // [P] solve of each finest patch
   DevBuf<double> part_p;    // [2][P] per-patch dot partials of the fused apply
+  DevBuf<double> dx;        // float-float loop: correction to x since the last fold (allocated on first use)
   double* h = nullptr;
   int* h_active = nullptr;
   cudaStream_t cap = nullptr;
@@ -1067,8 +1091,7 @@ static bool apply_dots(const te_operator* A, KrylovWork& W, const float* u, DV f
 }
 
 // one float-float iteration; M is an FP32 cycle
-static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, double* x, double tol, int flags,
-                         cudaStream_t st) {
+static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, double tol, int flags, cudaStream_t st) {
   const Layout& L = W.d->lay;
   const int nc = W.nc;
   Batch bt = W.batch();
@@ -1094,7 +1117,7 @@ static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, doubl
     TE_LAUNCH_CHECK();
   }
   const CV dir = (flags & TE_BICGSTAB_PRECONDITIONED_EXIT) ? CV{W.f32(W.mp), nullptr} : W.cv(W.p);
-  kd_xr<<<W.grid(), KT, 0, st>>>(L, nc, bt, x, W.dv(W.resid), W.f32(W.mp), W.f32(W.ms), W.cv(W.ap),
+  kd_xr<<<W.grid(), KT, 0, st>>>(L, nc, bt, W.dv(W.dx), W.dv(W.resid), W.f32(W.mp), W.f32(W.ms), W.cv(W.ap),
                                  W.cv(W.as), W.cv(W.rhat), dir, W.part.p, W.counter.p, W.S.p);
   count_launch();
   TE_LAUNCH_CHECK();
@@ -1176,7 +1199,11 @@ struct BatchRun {
     for (int i = 0; i < B; i++) W.h_active[i] = 1;
     W.push_active(st);
     if (df) {
-      // resid = b - A x in FP64, then split into float-float; rhat = p = resid (BiCGStab.h:113-131)
+      // resid = b - A x in FP64, then split into float-float; rhat = p = resid (BiCGStab.h:113-131);
+      // the correction dx starts at 0
+      if (!W.dx.p) W.dx.alloc(W.n);
+      TE_CUDA(cudaMemsetAsync(W.dx.p, 0, (size_t)W.n * sizeof(double), st));
+      folded = true;
       operator_residual(A, nc, x, b, W.ap.p, st);
       // rhat = resid here, so rhat . resid and resid . resid are one sum (the same bits)
       launch_dots(W, 2, b, b, W.ap.p, W.ap.p, nullptr, nullptr, S_BB, 0, st);
@@ -1217,6 +1244,7 @@ struct BatchRun {
 
   void iterate_once() {
     KrylovWork& W = *Wp;
+    folded = false;
     if (use_graph) {
       auto it = W.graphs.find(gkey);
       if (it == W.graphs.end()) {
@@ -1225,7 +1253,7 @@ struct BatchRun {
         TE_CUDA(cudaStreamBeginCapture(W.cap, cudaStreamCaptureModeThreadLocal));
         try {
           if (df)
-            iteration_df(W, A, M, x, tol, flags, W.cap);
+            iteration_df(W, A, M, tol, flags, W.cap);
           else
             iteration(W, A, M, x, tol, flags, W.cap);
         } catch (...) {
@@ -1247,7 +1275,7 @@ struct BatchRun {
       TE_CUDA(cudaEventRecord(W.ev_out, W.cap));
       TE_CUDA(cudaStreamWaitEvent(st, W.ev_out, 0));
     } else if (df) {
-      iteration_df(W, A, M, x, tol, flags, st);
+      iteration_df(W, A, M, tol, flags, st);
     } else {
       iteration(W, A, M, x, tol, flags, st);
     }
@@ -1282,12 +1310,23 @@ struct BatchRun {
     }
   }
 
+  // x += dx, dx = 0 over every solve (a solve still iterating keeps x + dx)
+  bool folded = true;
+  void fold() {
+    if (!df || folded) return;
+    kd_fold<<<1216, 256, 0, st>>>(Wp->dv(Wp->dx), x, nvals);
+    count_launch();
+    TE_LAUNCH_CHECK();
+    folded = true;
+  }
+
   // Residual replacement: the float-float recurrence keeps ~1e-14 of the
   // initial residual, so check every solve's true residual b - A x in FP64
   // (the residual each solve reports) and, while restarts are allowed,
   // restart the ones above tol from it.  True when some solve restarted.
   bool replacement_check(bool allow_restart) {
     KrylovWork& W = *Wp;
+    fold();
     for (int i = 0; i < B; i++) W.h_active[i] = statuses[i] == TE_OK ? 1 : 0;
     W.push_active(st);
     operator_residual(A, nc, x, b, W.ap.p, st);
@@ -1317,6 +1356,7 @@ struct BatchRun {
   }
 
   void finish() {
+    fold();
     TE_CUDA(cudaStreamSynchronize(st));
     done = true;
     check_tc();
@@ -1384,6 +1424,12 @@ struct BatchRun {
   void reset_slot(int i) {
     KrylovWork& W = *Wp;
     std::vector<int> saved = only(i);
+    if (df) {  // the new system's correction starts at 0
+      const long long o = slot_begin(i), n = slot_len(i);
+      DV w = W.dv(W.dx);
+      TE_CUDA(cudaMemsetAsync(w.hi + o, 0, (size_t)n * sizeof(float), st));
+      TE_CUDA(cudaMemsetAsync(w.lo + o, 0, (size_t)n * sizeof(float), st));
+    }
     operator_residual(A, nc, x, b, W.ap.p, st);
     launch_dots(W, 2, b, b, W.ap.p, W.ap.p, nullptr, nullptr, S_BB, 0, st);
     W.read_scalars(st);
@@ -1418,6 +1464,7 @@ struct BatchRun {
       require(!W.h_active[i], "solve is still iterating");
       seen[i] = 1;
     }
+    fold();
     std::vector<int> saved(W.h_active, W.h_active + B);
     for (int j = 0; j < B; j++) W.h_active[j] = seen[j];
     W.push_active(st);
@@ -1593,6 +1640,7 @@ int te_bicgstab_batch_sync_x(te_bicgstab_batch* h) {
   return guard([&] {
     require(h, "null argument");
     BatchRun* r = reinterpret_cast<BatchRun*>(h);
+    r->fold();
     TE_CUDA(cudaStreamSynchronize(r->st));
   });
 }
