@@ -1,11 +1,12 @@
 """The serving loop's scheduling on the CPU (thunderegg_gb300.serve.Server).
 
 The device objects (_Union: a union hierarchy's solver and buffers; _Batch: its
-resumable BiCGStab run) are replaced by fakes in which request i needs a given
-number of iterations, so admission against the memory budget, the union cache
-and its LRU eviction, the bucketed batch sizes with phantom slots and the
-re-forms are checked without a GPU.  The GPU tests (test_gpu_serve.py) check
-the same loop's numerical results.
+resumable slot-mode BiCGStab run) are replaced by fakes in which request i
+needs a given number of iterations, so admission against the memory budget,
+the union cache and its LRU eviction, the bucketed batch sizes with free
+slots, slot fills, restarts from the true residual and re-forms are checked
+without a GPU.  The GPU tests (test_gpu_serve.py) check the same loop's
+numerical results.
 """
 import numpy as np
 import pytest
@@ -52,7 +53,9 @@ class FakeUnion:
 
 class FakeBatch:
     """Slot batch: the request in slot i needs int(req.f[0]) iterations in total; a
-    re-formed member keeps its count; slots beyond the members start free."""
+    re-formed member keeps its count; slots beyond the members start free.  A
+    request with f[1] = k fails its true-residual check k times: each failed
+    finish restarts it for one more iteration."""
 
     def __init__(self, members, x_parts, un):
         self.un = un
@@ -64,7 +67,13 @@ class FakeBatch:
         self.slots = list(members) + [None] * (self.B - len(members))
         self.base_its = [m.iterations for m in members] + [0] * (self.B - len(members))
         self.done = [0] * self.B
+        self.extra = [0] * self.B  # iterations added by restarts
+        self.fails = [self._fails(m) for m in members] + [0] * (self.B - len(members))
         self.puts = 0
+
+    @staticmethod
+    def _fails(m):
+        return int(m.req.f[1]) if len(m.req.f) > 1 else 0
 
     @property
     def members(self):
@@ -82,11 +91,13 @@ class FakeBatch:
         self.slots[i] = member
         self.base_its[i] = member.iterations
         self.done[i] = 0
+        self.extra[i] = 0
+        self.fails[i] = self._fails(member)
         self.puts += 1
 
     def _left(self, i):
         m = self.slots[i]
-        return 0 if m is None else int(m.req.f[0]) - self.base_its[i] - self.done[i]
+        return 0 if m is None else int(m.req.f[0]) + self.extra[i] - self.base_its[i] - self.done[i]
 
     def step(self, k):
         for i in range(self.B):
@@ -98,9 +109,16 @@ class FakeBatch:
         return list(self.done), [1e-11] * self.B, [0] * self.B, run
 
     def finish(self, slots):
+        out = []
         for i in slots:
             assert self.slots[i] is not None and self._left(i) == 0
-        return [True] * len(slots)
+            if self.fails[i] > 0:  # restarted from its true residual
+                self.fails[i] -= 1
+                self.extra[i] += 1
+                out.append(False)
+            else:
+                out.append(True)
+        return out
 
     def slice_x(self, i):
         return _X(np.full(3, float(self.slots[i].rid)))
@@ -189,7 +207,7 @@ def test_batches_round_up_to_buckets_with_free_slots(fake):
     assert srv.active_bytes == 0
 
 
-def test_no_phantoms_without_budget_room(fake):
+def test_no_free_slots_without_budget_room(fake):
     per = S.request_bytes(mesh()[0], GmgOptions())
     srv = S.Server(budget_bytes=5 * per, steps_per_round=2)
     for _ in range(5):
@@ -277,3 +295,15 @@ def test_slot_reservation_counts_waiting_requests(fake):
     assert sorted(cls["bytes"].values()) == [0, per]
     run_checked(srv)
     assert srv.active_bytes == 0
+
+
+def test_restarted_slots_stay_until_confirmed(fake):
+    """A slot whose true residual fails the check restarts in place: its request keeps the
+    slot, iterates again and retires only once confirmed."""
+    srv = S.Server(budget_bytes=1 << 40, steps_per_round=2)
+    plain = srv.submit(req(4))
+    retried = srv.submit(S.Request(mesh()[0], np.array([4.0, 2.0]), GmgOptions()))
+    res = run_checked(srv)
+    assert res[plain].iterations == 4
+    assert res[retried].iterations == 6  # two restarts of one iteration each
+    assert srv.stats["reforms"] == 1 and srv.active_bytes == 0
