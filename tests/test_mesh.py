@@ -116,3 +116,26 @@ def test_builder_reproduces_reference_meshes(path):
                 assert [m[int(x)] for x in a.nbr_ids[i, s, :nn]] == list(b.nbr_ids[j2, s, :nn])
                 if t == M.NBR_COARSE:
                     assert a.nbr_orth[i, s] == b.nbr_orth[j2, s]
+
+
+def test_union_hierarchy_shifts_each_solve():
+    """Every level of a union lists each solve's patches in order, every id of solve b
+    shifted by the id ranges of the solves before it, and absent links left at -1."""
+    hs = [M.circle_mesh(n=8, lo=2, hi=4), M.uniform_mesh(2, 2, 8), M.circle_mesh(n=8, lo=2, hi=4)]
+    hs = [h[:3] for h in hs]
+    union, offs = M.union_hierarchy(hs)
+    shift = np.cumsum([0] + [max(int(lv.id.max()) for lv in h) + 1 for h in hs])[:-1]
+    for k, lv in enumerate(union):
+        assert offs[k][-1] == lv.num_patches
+        for b, h in enumerate(hs):
+            part, sl, s = h[k], slice(offs[k][b], offs[k][b + 1]), int(shift[b])
+            assert np.array_equal(lv.id[sl], part.id + s)
+            assert np.array_equal(lv.parent_id[sl], np.where(part.parent_id >= 0, part.parent_id + s, -1))
+            assert np.array_equal(lv.child_ids[sl], np.where(part.child_ids >= 0, part.child_ids + s, -1))
+            has = (part.nbr_type >= 0)[:, :, None] & (part.nbr_ids >= 0)
+            assert np.array_equal(lv.nbr_ids[sl], np.where(has, part.nbr_ids + s, part.nbr_ids))
+            for name in ("refine_level", "orth_on_parent", "starts", "spacings", "nbr_type", "nbr_orth"):
+                assert np.array_equal(getattr(lv, name)[sl], getattr(part, name))
+        assert lv.id.dtype == np.int32 and lv.nbr_ids.dtype == np.int32
+        # ids stay unique across the solves
+        assert len(np.unique(lv.id)) == lv.num_patches

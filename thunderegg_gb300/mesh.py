@@ -659,12 +659,9 @@ def union_hierarchy(hierarchies):
     for h in hierarchies:
         shifts.append(acc)
         acc += int(max(int(lv.id.max()) for lv in h)) + 1
-
-    def shift(a, s, valid=None):
-        a = np.array(a, copy=True)
-        mask = a >= 0 if valid is None else valid
-        a[mask] += s
-        return a
+    if acc > np.iinfo(np.int32).max:
+        raise ValueError("the union's patch ids exceed the int32 range")
+    shifts = np.asarray(shifts, dtype=np.int32)
 
     levels, offsets = [], []
     for k in range(depth):
@@ -673,27 +670,26 @@ def union_hierarchy(hierarchies):
         for p in parts:
             if p.dim != d0.dim or tuple(p.ns) != tuple(d0.ns) or p.num_ghost != d0.num_ghost:
                 raise ValueError("hierarchies in one batch must share patch shape")
-        F = num_face_slots(d0.dim)
-        lv = _empty_level(d0.dim, sum(p.num_patches for p in parts), d0.ns, d0.num_ghost)
-        fields = {n: [] for n in ("id", "refine_level", "parent_id", "orth_on_parent", "child_ids", "starts",
-                                  "spacings", "nbr_type", "nbr_ids", "nbr_orth")}
-        off = [0]
-        for p, s in zip(parts, shifts):
-            fields["id"].append(p.id + s)
-            fields["refine_level"].append(p.refine_level)
-            fields["parent_id"].append(shift(p.parent_id, s))
-            fields["orth_on_parent"].append(p.orth_on_parent)
-            fields["child_ids"].append(shift(p.child_ids, s))
-            fields["starts"].append(p.starts)
-            fields["spacings"].append(p.spacings)
-            fields["nbr_type"].append(p.nbr_type)
-            valid = np.repeat((p.nbr_type >= 0)[:, :, None], 4, axis=2) & (p.nbr_ids >= 0)
-            fields["nbr_ids"].append(shift(p.nbr_ids, s, valid))
-            fields["nbr_orth"].append(p.nbr_orth)
-            off.append(off[-1] + p.num_patches)
-        for n, v in fields.items():
-            setattr(lv, n, np.concatenate(v, axis=0))
-        assert lv.nbr_type.shape[1] == F
+        counts = np.array([p.num_patches for p in parts])
+        s = np.repeat(shifts, counts)  # the id shift of every union patch
+
+        def cat(name):
+            return np.concatenate([getattr(p, name) for p in parts], axis=0)
+
+        # every id moves by its solve's shift; absent links (-1, or a missing neighbour) stay
+        parent, child = cat("parent_id"), cat("child_ids")
+        nbr_type, nbr_ids = cat("nbr_type"), cat("nbr_ids")
+        valid = (nbr_type >= 0)[:, :, None] & (nbr_ids >= 0)
+        lv = MeshLevel(
+            dim=d0.dim, ns=tuple(d0.ns), num_ghost=d0.num_ghost,
+            id=(cat("id") + s).astype(np.int32), refine_level=cat("refine_level"),
+            parent_id=np.where(parent >= 0, parent + s, parent).astype(np.int32),
+            orth_on_parent=cat("orth_on_parent"),
+            child_ids=np.where(child >= 0, child + s[:, None], child).astype(np.int32),
+            starts=cat("starts"), spacings=cat("spacings"), nbr_type=nbr_type,
+            nbr_ids=np.where(valid, nbr_ids + s[:, None, None], nbr_ids).astype(np.int32),
+            nbr_orth=cat("nbr_orth"))
+        assert lv.nbr_type.shape[1] == num_face_slots(d0.dim)
         levels.append(lv)
-        offsets.append(off)
+        offsets.append([0] + np.cumsum(counts).tolist())
     return levels, offsets
