@@ -37,7 +37,8 @@ from .capi import (TE_F32, TE_F64, TE_FILL_CORNERS, TE_FILL_EDGES, TE_FILL_FACES
 __all__ = ["Domain", "Vector", "BiLinearGhostFiller", "BiQuadraticGhostFiller", "TriLinearGhostFiller",
            "PoissonStarPatchOperator", "VarPoissonStarPatchOperator", "DFTPatchSolver",
            "BiCGStabPatchSolver", "LinearRestrictor", "DirectInterpolator", "CycleOpts", "CycleBuilder",
-           "BiCGStab", "BreakdownError", "TeError", "mesh", "capi", "GhostFillingType"]
+           "BiCGStab", "CG", "Cycle", "FFTWPatchSolver", "BreakdownError", "TeError", "mesh", "capi",
+           "GhostFillingType", "TE_F32", "TE_F64", "TE_FILL_FACES", "TE_FILL_EDGES", "TE_FILL_CORNERS"]
 
 
 class GhostFillingType:

@@ -9,12 +9,10 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 
-import numpy as np
-
 from . import (CG, BiCGStab, BiCGStabPatchSolver, BiLinearGhostFiller, BiQuadraticGhostFiller, CycleBuilder,
                CycleOpts, DFTPatchSolver, DirectInterpolator, Domain, LinearRestrictor,
                PoissonStarPatchOperator, TriLinearGhostFiller, VarPoissonStarPatchOperator, Vector)
-from .capi import TE_F32, TE_F64
+from .capi import TE_F64
 
 SMOOTHER_DFT, SMOOTHER_BICGSTAB = 0, 1
 
