@@ -38,3 +38,18 @@ def test_library_loads_without_gpu(te):
     from thunderegg_gb300 import capi
 
     assert capi.lib().te_kernel_launch_count() >= 0
+
+
+def test_slot_entry_points_reject_bad_arguments_without_gpu(te):
+    """The slot-mode batch entry points check their arguments before any device work, so
+    a null handle is an error status and a message, not a crash."""
+    import ctypes
+
+    from thunderegg_gb300 import capi
+
+    L = capi.lib()
+    fin, sl = (ctypes.c_int * 1)(), (ctypes.c_int * 1)(0)
+    assert L.te_bicgstab_batch_reset(None, 0) == capi.TE_ERR_INVALID
+    assert b"null" in L.te_last_error_message()
+    assert L.te_bicgstab_batch_finish_slots(None, 1, sl, fin) == capi.TE_ERR_INVALID
+    assert L.te_bicgstab_batch_step(None, 1, ctypes.byref(ctypes.c_int())) == capi.TE_ERR_INVALID
