@@ -151,13 +151,27 @@ class _LeafIndex:
         """Leaf containing cell c of ``level`` (level <= that of the cell), or
         None when the cell is subdivided / outside the domain."""
         m = 1 << level
-        if any(x < 0 or x >= m for x in c):
+        leaves = self.set
+        if len(c) == 2:
+            x, y = c
+            if x < 0 or y < 0 or x >= m or y >= m:
+                return None
+            for L in range(level, -1, -1):
+                key = (L, (x, y))
+                if key in leaves:
+                    return key
+                x >>= 1
+                y >>= 1
             return None
+        for x in c:
+            if x < 0 or x >= m:
+                return None
+        cc = tuple(c)
         for L in range(level, -1, -1):
-            s = level - L
-            key = (L, tuple(x >> s for x in c))
-            if key in self.set:
+            key = (L, cc)
+            if key in leaves:
                 return key
+            cc = tuple(x >> 1 for x in cc)
         return None
 
     def leaf_at_point(self, p):
@@ -307,6 +321,13 @@ def _link_level(lvl: MeshLevel, quads, connect: str):
     idx = _LeafIndex(quads, dim)
     maxl = idx.maxl
     qid = {q: int(lvl.id[k]) for k, q in enumerate(quads)}
+    boxes = {}
+
+    def bbox(q):
+        b = boxes.get(q)
+        if b is None:
+            b = boxes[q] = _quad_bbox(q, maxl)
+        return b
     for p, (l, c) in enumerate(quads):
         # ---- sides
         for axis in range(dim):
@@ -342,7 +363,7 @@ def _link_level(lvl: MeshLevel, quads, connect: str):
                         lvl.nbr_ids[p, slot, o] = qid[f]
         if connect != "full":
             continue
-        lo, hi = _quad_bbox((l, c), maxl)
+        lo, hi = bbox((l, c))
         # ---- corners: every leaf around the vertex has it as a corner
         for corner in range(1 << dim):
             v = tuple(hi[a] if (corner >> a) & 1 else lo[a] for a in range(dim))
@@ -354,7 +375,7 @@ def _link_level(lvl: MeshLevel, quads, connect: str):
                 if q is None:
                     ok = False
                     break
-                qlo, qhi = _quad_bbox(q, maxl)
+                qlo, qhi = bbox(q)
                 for a in range(dim):
                     if (d[a] == 1 and qlo[a] != v[a]) or (d[a] == 0 and qhi[a] != v[a]):
                         ok = False
@@ -401,7 +422,7 @@ def _link_level(lvl: MeshLevel, quads, connect: str):
                             if q is None:
                                 ok = False
                                 break
-                            qlo, qhi = _quad_bbox(q, maxl)
+                            qlo, qhi = bbox(q)
                             if q not in leaves_here:
                                 leaves_here.append(q)
                             a = qhi[axis]
@@ -416,7 +437,7 @@ def _link_level(lvl: MeshLevel, quads, connect: str):
                 nlo, nhi = seg_lo, seg_hi
                 for qs in regions.values():
                     for q in qs:
-                        qlo, qhi = _quad_bbox(q, maxl)
+                        qlo, qhi = bbox(q)
                         nlo, nhi = min(nlo, qlo[axis]), max(nhi, qhi[axis])
                 if (nlo, nhi) == (seg_lo, seg_hi):
                     break
@@ -425,7 +446,7 @@ def _link_level(lvl: MeshLevel, quads, connect: str):
                 continue
             for (d0, d1), qs in regions.items():
                 for q in qs:
-                    qlo, qhi = _quad_bbox(q, maxl)
+                    qlo, qhi = bbox(q)
                     if (d0 == 1 and qlo[t0] != v0) or (d0 == 0 and qhi[t0] != v0):
                         ok = False
                     if (d1 == 1 and qlo[t1] != v1) or (d1 == 0 and qhi[t1] != v1):
@@ -435,8 +456,8 @@ def _link_level(lvl: MeshLevel, quads, connect: str):
             slot = edge_slot(edge)
             # the diagonal region restricted to this patch's extent along the axis
             diag = [q for q in regions[(u0, u1)]
-                    if _quad_bbox(q, maxl)[0][axis] < hi[axis]
-                    and _quad_bbox(q, maxl)[1][axis] > lo[axis]]
+                    if bbox(q)[0][axis] < hi[axis]
+                    and bbox(q)[1][axis] > lo[axis]]
             if len(diag) == 1 and diag[0][0] == l:
                 lvl.nbr_type[p, slot] = NBR_NORMAL
                 lvl.nbr_ids[p, slot, 0] = qid[diag[0]]
@@ -446,7 +467,7 @@ def _link_level(lvl: MeshLevel, quads, connect: str):
                 lvl.nbr_orth[p, slot] = c[axis] & 1
             else:
                 lvl.nbr_type[p, slot] = NBR_FINE
-                diag.sort(key=lambda q: _quad_bbox(q, maxl)[0][axis])
+                diag.sort(key=lambda q: bbox(q)[0][axis])
                 for o, q in enumerate(diag[:2]):
                     lvl.nbr_ids[p, slot, o] = qid[q]
 
