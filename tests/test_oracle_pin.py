@@ -131,3 +131,48 @@ def test_oracle_cg_matches_reference_live(oracle, ref):
         a, b = oracle.solve(levels, z, gmg_config(scheme=sc, krylov="cg"), u0=u0), \
             ref.solve(levels, z, gmg_config(scheme=sc, krylov="cg"), u0=u0)
         assert a[1] == b[1] == 0 and np.array_equal(a[0][inner], b[0][inner])
+
+
+def test_oracle_matches_reference_live_operators_and_transfers(oracle, ref):
+    """The rows the cycle test does not reach directly, against the compiled reference:
+    BiLinear fills, Poisson with Dirichlet and Neumann boundaries, VarPoisson, modifyRHS,
+    both patch solvers (smooth and apply), restriction with and without boundary
+    extrapolation, interpolation, and a VarPoisson BiCGStab solve."""
+    from oracle import gmg_config
+    from thunderegg_gb300 import mesh as M
+
+    rng = np.random.default_rng(123)
+    cases = ((M.random_mesh(3, n=6, dim=2, lo=1, hi=4), 0), (M.circle_mesh(n=6, lo=1, hi=4), 1),
+             (M.random_mesh(11, n=4, dim=3, lo=1, hi=3), 2))
+    for levels, sc in cases:
+        lv = levels[0]
+        shape = lv.padded_shape(1)
+        u, f = rng.standard_normal(shape), rng.standard_normal(shape)
+        coeffs = [1.0 + rng.random(l.padded_shape(1)) for l in levels]
+        for ft in ((0, 2) if lv.dim == 2 else (0, 1, 2)):
+            assert np.array_equal(oracle.ghost_fill(lv, u.copy(), sc, ft), ref.ghost_fill(lv, u.copy(), sc, ft))
+        for kind, neumann in ((0, 0), (0, 1), (1, 0)):
+            c = coeffs[0] if kind else None
+            a, b = oracle.apply(lv, u.copy(), sc, kind=kind, neumann=neumann, coeffs=c), \
+                ref.apply(lv, u.copy(), sc, kind=kind, neumann=neumann, coeffs=c)
+            assert np.array_equal(a[1], b[1]), (sc, kind, neumann)
+            if neumann == 0:
+                assert np.array_equal(oracle.modify_rhs(lv, u, f, sc, kind=kind, coeffs=c),
+                                      ref.modify_rhs(lv, u, f, sc, kind=kind, coeffs=c)), (sc, kind)
+        for kind, smoother in ((0, 0), (0, 1), (1, 1)):
+            c = coeffs[0] if kind else None
+            for mode in (0, 1):
+                a = oracle.patch_solver(lv, f, u, sc, kind=kind, coeffs=c, smoother=smoother, mode=mode)
+                b = ref.patch_solver(lv, f, u, sc, kind=kind, coeffs=c, smoother=smoother, mode=mode)
+                # the reference's PatchSolver does not report inner iterations (the wrapper gives -1)
+                assert np.array_equal(a[0], b[0]), (sc, kind, smoother, mode)
+        for extrap in (0, 1):
+            assert np.array_equal(oracle.restrict(lv, levels[1], u, extrap), ref.restrict(lv, levels[1], u, extrap))
+        vc = rng.standard_normal(levels[1].padded_shape(1))
+        assert np.array_equal(oracle.interpolate(levels[1], lv, vc, u), ref.interpolate(levels[1], lv, vc, u))
+        # the solution's interior (its ghost cells hold whatever the last ghost fill left)
+        g = lv.num_ghost
+        inner = (Ellipsis,) + tuple(slice(g, -g) for _ in range(lv.dim))
+        cfg = gmg_config(scheme=sc, op_kind=1, smoother=1, tol=1e-9, max_it=100)
+        a, b = oracle.solve(levels, f, cfg, coeffs=coeffs), ref.solve(levels, f, cfg, coeffs=coeffs)
+        assert a[1] == b[1] and a[3] == b[3] and np.array_equal(a[0][inner], b[0][inner]), sc
