@@ -1230,8 +1230,12 @@ struct BatchRun {
       h[S_RHO] = rho[i];
       h[S_R0] = r0[i];
       finals[i] = residual[i];
-      // zero right-hand side or already converged: no iterations (BiCGStab.h:140-144)
-      W.h_active[i] = (r0[i] != 0 && residual[i] > tol && max_iterations > 0) ? 1 : 0;
+      // zero right-hand side or already converged: no iterations (BiCGStab.h:140-144); a
+      // non-finite right-hand side or initial residual is a breakdown (the reference would
+      // return at once, its comparisons with NaN being false)
+      const bool finite = std::isfinite(bb) && std::isfinite(rr);
+      if (!finite) statuses[i] = TE_ERR_BREAKDOWN;
+      W.h_active[i] = (finite && r0[i] != 0 && residual[i] > tol && max_iterations > 0) ? 1 : 0;
       if (W.h_active[i] && rho[i] == 0) {  // BiCGStab.h:149-151
         statuses[i] = TE_ERR_BREAKDOWN;
         W.h_active[i] = 0;
@@ -1294,7 +1298,13 @@ struct BatchRun {
       rho[i] = h[S_RHO];
       residual[i] = std::sqrt(h[S_RR]) / r0[i];
       finals[i] = residual[i];
-      if (residual[i] <= tol || its[i] >= max_iterations) {
+      if (!std::isfinite(residual[i]) || !std::isfinite(rho[i])) {
+        // non-finite scalars (a singular operator or preconditioner): stop this solve
+        // instead of iterating to the limit on NaN
+        statuses[i] = TE_ERR_BREAKDOWN;
+        W.h_active[i] = 0;
+        changed = true;
+      } else if (residual[i] <= tol || its[i] >= max_iterations) {
         W.h_active[i] = 0;
         changed = true;
       } else if (rho[i] == 0) {  // BiCGStab.h:149-151
@@ -1443,7 +1453,9 @@ struct BatchRun {
     statuses[i] = TE_OK;
     restart_row(i, rr);
     split_slot(i);
-    bool run = r0[i] != 0 && residual[i] > tol && max_iterations > 0;  // BiCGStab.h:140-144
+    const bool finite = std::isfinite(bb) && std::isfinite(rr);
+    if (!finite) statuses[i] = TE_ERR_BREAKDOWN;
+    bool run = finite && r0[i] != 0 && residual[i] > tol && max_iterations > 0;  // BiCGStab.h:140-144
     if (run && rr == 0) {
       statuses[i] = TE_ERR_BREAKDOWN;
       run = false;
@@ -1556,7 +1568,8 @@ int te_bicgstab_solve(const te_operator* A, int nc, void* xv, const void* bv, co
     int st = TE_OK;
     status = solve_batched(A, nc, xv, bv, Mc, tol, max_iterations, flags, offs, iterations, final_residual, &st);
     if (status == TE_ERR_BREAKDOWN)
-      set_error("BiCGStab broke down, rho was 0 on iteration " + std::to_string(*iterations));
+      set_error("BiCGStab broke down on iteration " + std::to_string(*iterations) +
+                " (rho was 0, or a residual or scalar was not finite)");
   });
   return rc != TE_OK ? rc : status;
 }
@@ -1572,7 +1585,9 @@ int te_bicgstab_solve_batched(const te_operator* A, int nc, void* xv, const void
     require(offs[0] == 0 && offs[num_solves] == A->dom->lay.P, "patch_offsets must span the finest level");
     for (int i = 0; i < num_solves; i++) require(offs[i + 1] > offs[i], "every solve needs at least one patch");
     status = solve_batched(A, nc, xv, bv, Mc, tol, max_iterations, flags, offs, iterations, final_residuals, statuses);
-    if (status == TE_ERR_BREAKDOWN) set_error("BiCGStab broke down in at least one solve of the batch");
+    if (status == TE_ERR_BREAKDOWN)
+      set_error("BiCGStab broke down in at least one solve of the batch (rho was 0, or a residual or scalar was "
+                "not finite)");
   });
   return rc != TE_OK ? rc : status;
 }
