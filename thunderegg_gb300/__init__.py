@@ -27,6 +27,7 @@ or a GPU, constructing any of these objects raises.
 from __future__ import annotations
 
 import ctypes
+import sys
 
 import numpy as np
 
@@ -461,7 +462,12 @@ class BiCGStab:
     def getMaxIterations(self):
         return self.max_iterations
 
-    def solve(self, A, x: Vector, b: Vector, Mr=None):
+    def solve(self, A, x: Vector, b: Vector, Mr=None, output=False, os=None):
+        """Returns the iteration count.  With output=True, prints the reference's progress
+        line "%5d %16.8e" (iteration, relative residual) to os (default stdout) before the
+        first iteration and after each one (BiCGStab.h:134-139,193-197)."""
+        if output:
+            return self._solve_printing(A, x, b, Mr, os if os is not None else sys.stdout)
         its = ctypes.c_int(0)
         res = ctypes.c_double(0)
         check(lib().te_bicgstab_solve(A.h, x.ncomp, x.ptr, b.ptr, Mr.h if Mr is not None else None,
@@ -469,6 +475,35 @@ class BiCGStab:
                                       ctypes.byref(its), ctypes.byref(res)))
         self.final_residual = res.value
         return its.value
+
+    def _solve_printing(self, A, x, b, Mr, os):
+        """The same solve advanced one iteration at a time through the resumable batch
+        (a batch of one), reading the residual after each iteration."""
+        P = x.domain.getNumLocalPatches()
+        offs = (ctypes.c_int * 2)(0, P)
+        h = ctypes.c_void_p()
+        check(lib().te_bicgstab_batch_create(A.h, x.ncomp, x.ptr, b.ptr, Mr.h if Mr is not None else None,
+                                             float(self.tolerance), int(self.max_iterations), int(self.flags),
+                                             1, offs, ctypes.byref(h)))
+        try:
+            its, res, st, run = (ctypes.c_int * 1)(), (ctypes.c_double * 1)(), (ctypes.c_int * 1)(), (ctypes.c_int * 1)()
+            check(lib().te_bicgstab_batch_state(h, its, res, st, run))
+            os.write("%5d %16.8e\n" % (its[0], res[0]))
+            shown = its[0]
+            n = ctypes.c_int(1)
+            while n.value:
+                check(lib().te_bicgstab_batch_step(h, 1, ctypes.byref(n)))
+                check(lib().te_bicgstab_batch_state(h, its, res, st, run))
+                if its[0] != shown:
+                    os.write("%5d %16.8e\n" % (its[0], res[0]))
+                    shown = its[0]
+            self.final_residual = res[0]
+            if st[0] == capi.TE_ERR_BREAKDOWN:
+                raise BreakdownError(st[0], f"BiCGStab broke down on iteration {its[0]}")
+            check(st[0])
+            return its[0]
+        finally:
+            lib().te_bicgstab_batch_destroy(h)
 
 
 class CG:
