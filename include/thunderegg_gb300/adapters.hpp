@@ -13,6 +13,7 @@
 //   GpuDirectInterpolator<D>   GMG::Interpolator<D>           (GMG/Interpolator.h:47-54)
 //   GpuVCycle<D>               Operator<D> applying a whole V-cycle (the Mr of BiCGStab)
 //   GpuBiCGStab<D>             Iterative::Solver<D>           (Iterative/Solver.h:47-69)
+//   GpuCG<D>                   Iterative::Solver<D>, Iterative::CG's right-preconditioned form (CG.h:126-194)
 //
 // Vectors: ThunderEgg's Vector<D> is concrete; a device-backed one is made
 // with its unmanaged constructor (Vector.h:199-215) over a GpuDomain's level
@@ -42,6 +43,7 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <cstdio>
 #include <memory>
 #include <string>
 #include <vector>
@@ -462,12 +464,80 @@ class GpuBiCGStab : public ThunderEgg::Iterative::Solver<D> {
     if (!op) throw ThunderEgg::RuntimeError("GpuBiCGStab needs a GpuStarPatchOperator");
     const auto* cyc = Mr ? dynamic_cast<const GpuVCycle<D>*>(Mr) : nullptr;
     if (Mr && !cyc) throw ThunderEgg::RuntimeError("GpuBiCGStab needs a GpuVCycle (or no) preconditioner");
+    if (output) return solvePrinting(*op, x, b, cyc, os);
     int its = 0;
     double res = 0;
     check(te_bicgstab_solve(op->handle(), x.getNumComponents(), levelPointer(x, *op->gpuDomain()),
                             levelPointer(b, *op->gpuDomain()), cyc ? cyc->handle() : nullptr, tolerance,
                             max_iterations, flags, &its, &res));
-    if (output) os << "GpuBiCGStab: " << its << " iterations, relative residual " << res << "\n";
+    return its;
+  }
+
+ private:
+  // output = true: the reference's progress lines ("%5d %16.8e", BiCGStab.h:134-139,193-197),
+  // before the first iteration and after each, from a resumable batch of one solve
+  // advanced one iteration at a time
+  int solvePrinting(const GpuStarPatchOperator<D>& op, ThunderEgg::Vector<D>& x, const ThunderEgg::Vector<D>& b,
+                    const GpuVCycle<D>* cyc, std::ostream& os) const {
+    const int offs[2] = {0, op.gpuDomain()->domain().getNumLocalPatches()};
+    te_bicgstab_batch* h = nullptr;
+    check(te_bicgstab_batch_create(op.handle(), x.getNumComponents(), levelPointer(x, *op.gpuDomain()),
+                                   levelPointer(b, *op.gpuDomain()), cyc ? cyc->handle() : nullptr, tolerance,
+                                   max_iterations, flags, 1, offs, &h));
+    std::unique_ptr<te_bicgstab_batch, int (*)(te_bicgstab_batch*)> guard(h, te_bicgstab_batch_destroy);
+    int its = 0, status = TE_OK, running = 0, n = 1;
+    double res = 0;
+    auto line = [&] {
+      char buf[64];
+      std::snprintf(buf, sizeof buf, "%5d %16.8e\n", its, res);
+      os << buf;
+    };
+    check(te_bicgstab_batch_state(h, &its, &res, &status, &running));
+    line();
+    int shown = its;
+    while (n) {
+      check(te_bicgstab_batch_step(h, 1, &n));
+      check(te_bicgstab_batch_state(h, &its, &res, &status, &running));
+      if (its != shown) {
+        line();
+        shown = its;
+      }
+    }
+    if (status == TE_ERR_BREAKDOWN)
+      throw ThunderEgg::Iterative::BreakdownError("te_gpu: BiCGStab broke down on iteration " + std::to_string(its));
+    check(status);
+    return its;
+  }
+};
+
+// Iterative::CG on the GPU (te_cg_solve): the reference's right-preconditioned
+// form, FP64 vectors, any GpuVCycle (or none) as Mr.  With output = true it
+// prints one "%5d %16.8e" line, for the final iteration count and residual
+// (the per-iteration lines of CG.h:151-156,179-183 need a per-iteration hook
+// that the ABI does not have).
+template <int D>
+class GpuCG : public ThunderEgg::Iterative::Solver<D> {
+ public:
+  double tolerance = 1e-12;
+  int max_iterations = 1000;
+  GpuCG* clone() const override { return new GpuCG(*this); }
+  int solve(const ThunderEgg::Operator<D>& A, ThunderEgg::Vector<D>& x, const ThunderEgg::Vector<D>& b,
+            const ThunderEgg::Operator<D>* Mr = nullptr, bool output = false,
+            std::ostream& os = std::cout) const override {
+    const auto* op = dynamic_cast<const GpuStarPatchOperator<D>*>(&A);
+    if (!op) throw ThunderEgg::RuntimeError("GpuCG needs a GpuStarPatchOperator");
+    const auto* cyc = Mr ? dynamic_cast<const GpuVCycle<D>*>(Mr) : nullptr;
+    if (Mr && !cyc) throw ThunderEgg::RuntimeError("GpuCG needs a GpuVCycle (or no) preconditioner");
+    int its = 0;
+    double res = 0;
+    check(te_cg_solve(op->handle(), x.getNumComponents(), levelPointer(x, *op->gpuDomain()),
+                      levelPointer(b, *op->gpuDomain()), cyc ? cyc->handle() : nullptr, tolerance, max_iterations,
+                      &its, &res));
+    if (output) {
+      char buf[64];
+      std::snprintf(buf, sizeof buf, "%5d %16.8e\n", its, res);
+      os << buf;
+    }
     return its;
   }
 };

@@ -19,5 +19,7 @@ template class thunderegg_gb300::GpuVCycle<2>;
 template class thunderegg_gb300::GpuVCycle<3>;
 template class thunderegg_gb300::GpuBiCGStab<2>;
 template class thunderegg_gb300::GpuBiCGStab<3>;
+template class thunderegg_gb300::GpuCG<2>;
+template class thunderegg_gb300::GpuCG<3>;
 template thunderegg_gb300::LevelTables<2> thunderegg_gb300::flatten<2>(const ThunderEgg::Domain<2>&);
 template thunderegg_gb300::LevelTables<3> thunderegg_gb300::flatten<3>(const ThunderEgg::Domain<3>&);
