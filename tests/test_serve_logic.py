@@ -307,3 +307,16 @@ def test_restarted_slots_stay_until_confirmed(fake):
     assert res[plain].iterations == 4
     assert res[retried].iterations == 6  # two restarts of one iteration each
     assert srv.stats["reforms"] == 1 and srv.active_bytes == 0
+
+
+def test_close_releases_everything(fake):
+    srv = S.Server(budget_bytes=1 << 40, steps_per_round=1)
+    with srv:
+        for _ in range(3):
+            srv.submit(req(10))
+        srv.submit(req(10, 1))
+        srv.step()
+        batches = [c["batch"] for c in srv.classes.values()]
+        assert all(b is not None for b in batches)
+    assert all(b.h is None and not b.un.busy for b in batches)  # destroyed, unions released
+    assert srv.unions == {} and srv.active_bytes == 0 and srv.idle() and srv.pool is None

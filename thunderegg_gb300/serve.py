@@ -484,3 +484,26 @@ class Server:
             self.step()
             r += 1
         return self.results
+
+    def close(self):
+        """Destroy the running batches, drop the cached unions (their device memory goes
+        with them) and stop the stepping threads.  Requests still queued or running are
+        dropped without a result."""
+        for cls in self.classes.values():
+            if cls["batch"] is not None:
+                self._close(cls)
+            cls["active"], cls["waiting"] = [], []
+            cls["bytes"].clear()
+        self.unions.clear()
+        self.queue = []
+        self.active_bytes = 0
+        if self.pool is not None:
+            self.pool.shutdown(wait=True)
+            self.pool = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False
