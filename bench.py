@@ -668,13 +668,24 @@ def run_gpu(args):
     achieved = alg / (top_ms / 1000.0) / 1e9
     cyc_total = sum(t for _, t in phases)
 
-    stream = serving_stream(args, te) if (args.stream > 0 and not args.only_mixed and rank == 0) else None
+    # measurements beside the headline, after its timed region: a failure in one is
+    # recorded in its key (the traceback goes to stderr) and the line still prints
+    def optional(fn, *a):
+        try:
+            return fn(*a)
+        except Exception as e:  # noqa: BLE001
+            import traceback
+
+            traceback.print_exc()
+            return {"error": f"{type(e).__name__}: {e}"}
+
+    stream = optional(serving_stream, args, te) if (args.stream > 0 and not args.only_mixed and rank == 0) else None
     extra = not args.no_extra and not args.only_mixed and rank == 0
-    c3 = config3_measure(te) if extra else None
-    c4 = config4_measure(te) if extra else None
-    lk = level_kernel_rooflines(te, served, hbm) if extra else None
-    sv = solver_variants_measure(te) if extra else None
-    bs = batch_scaling_measure(te) if extra else None
+    c3 = optional(config3_measure, te) if extra else None
+    c4 = optional(config4_measure, te) if extra else None
+    lk = optional(level_kernel_rooflines, te, served, hbm) if extra else None
+    sv = optional(solver_variants_measure, te) if extra else None
+    bs = optional(batch_scaling_measure, te) if extra else None
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
