@@ -264,7 +264,9 @@ class Server:
         self.max_batch = int(max_batch)
         self._ids = itertools.count()
         self.queue = []           # (rid, request, submit time, bytes)
-        self.classes = {}         # key -> {"active": [_Active] in a slot, "waiting": [_Active], "batch": _Batch}
+        # class key -> {"active": [_Active] in a slot, "waiting": [_Active] without one, "batch": _Batch
+        # or None, "bytes": rid -> bytes reserved while waiting, "wait_rounds": rounds a request waited}
+        self.classes = {}
         self.results = {}
         self.active_bytes = 0     # live unions (every slot) + admitted requests waiting for a slot
         self.use_cache = bool(cache)
