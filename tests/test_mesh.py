@@ -139,3 +139,39 @@ def test_union_hierarchy_shifts_each_solve():
         assert lv.id.dtype == np.int32 and lv.nbr_ids.dtype == np.int32
         # ids stay unique across the solves
         assert len(np.unique(lv.id)) == lv.num_patches
+
+
+def _same_tables(a, b, exact_geometry=True):
+    for la, lb in zip(a, b):
+        for f in ("id", "refine_level", "parent_id", "orth_on_parent", "child_ids", "nbr_type", "nbr_ids",
+                  "nbr_orth"):
+            assert np.array_equal(getattr(la, f), getattr(lb, f)), f
+        for f in ("starts", "spacings"):
+            x, y = getattr(la, f), getattr(lb, f)
+            assert np.array_equal(x, y) if exact_geometry else np.allclose(x, y, rtol=1e-15, atol=0), f
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_MESHES), reason="reference mesh fixtures not present")
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(REF_MESHES, "*.json"))))
+def test_json_round_trip_of_reference_meshes(path, tmp_path):
+    """The reference's mesh inputs read, written back in the same format and read again
+    give the same tables (ranks are not kept: everything is rank 0 here)."""
+    j = json.load(open(path))
+    dim = len(j["levels"][0][0]["starts"])
+    ns = (4,) * dim
+    ref = M.load_json_hierarchy(path, ns)
+    out = tmp_path / "mesh.json"
+    M.save_json_hierarchy(ref, out)
+    _same_tables(ref, M.load_json_hierarchy(out, ns))
+    # the written patches carry the reference's keys
+    w = json.load(open(out))["levels"][0][0]
+    assert set(j["levels"][0][0]) <= set(w) | {"forest"}
+
+
+@pytest.mark.parametrize("make", [lambda: M.circle_mesh(n=8, lo=2, hi=5), lambda: M.random_mesh(11, n=4, dim=3, lo=1, hi=3),
+                                  lambda: M.uniform_mesh(3, 2, 8)])
+def test_json_round_trip_of_built_meshes(make, tmp_path):
+    levels = make()
+    out = tmp_path / "mesh.json"
+    M.save_json_hierarchy(levels, out)
+    _same_tables(levels, M.load_json_hierarchy(out, levels[0].ns))

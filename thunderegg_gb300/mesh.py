@@ -613,6 +613,62 @@ def load_json_hierarchy(path, ns, num_ghost=1):
     return [_level_from_json(lv, dim, ns, num_ghost) for lv in j["levels"]]
 
 
+_ORTH_NAMES = {1: ["LOWER", "UPPER"], 2: ["SW", "SE", "NW", "NE"],
+               3: ["BSW", "BSE", "BNW", "BNE", "TSW", "TSE", "TNW", "TNE"]}
+_TYPE_NAME = {NBR_NORMAL: "NORMAL", NBR_COARSE: "COARSE", NBR_FINE: "FINE"}
+
+
+def _orth_to_json(v, m):
+    # Orthant<0> and the null orthant are written as null (Orthant.cpp to_json)
+    return None if m == 0 or v < 0 else _ORTH_NAMES[m][int(v)]
+
+
+def _nbr_to_json(lvl, k, slot, m, key, name):
+    """One neighbour entry (json.cpp to_json of Normal/Coarse/FineNbrInfo<m>): type, ids,
+    ranks (one rank here), the coarse neighbour's orthant, and the face's name."""
+    t = int(lvl.nbr_type[k, slot])
+    n = (1 << m) if t == NBR_FINE else 1
+    ids = [int(x) for x in lvl.nbr_ids[k, slot, :n]]
+    nb = {"type": _TYPE_NAME[t], "ids": ids, "ranks": [0] * n}
+    if t == NBR_COARSE:
+        nb["orth_on_coarse"] = _orth_to_json(lvl.nbr_orth[k, slot], m)
+    nb[key] = name
+    return nb
+
+
+def _level_to_json(lvl: MeshLevel):
+    """The level's PatchInfos in the reference's JSON form (json.cpp:160-240), all on rank 0."""
+    D = lvl.dim
+    out = []
+    for k in range(lvl.num_patches):
+        pid = int(lvl.parent_id[k])
+        pj = {"id": int(lvl.id[k]), "parent_id": pid, "parent_rank": 0 if pid >= 0 else -1,
+              "orth_on_parent": _orth_to_json(lvl.orth_on_parent[k], D), "rank": 0,
+              "starts": [float(x) for x in lvl.starts[k]],
+              "lengths": [float(lvl.spacings[k, a] * lvl.ns[a]) for a in range(D)],
+              "refine_level": int(lvl.refine_level[k])}
+        pj["nbrs"] = [_nbr_to_json(lvl, k, side_slot(D, s), D - 1, "side", _SIDE_NAMES[D][s])
+                      for s in range(2 * D) if lvl.nbr_type[k, side_slot(D, s)] != NBR_NONE]
+        pj["edge_nbrs"] = [_nbr_to_json(lvl, k, edge_slot(e), 1, "edge", _EDGE_NAMES[e])
+                           for e in range(12 if D == 3 else 0) if lvl.nbr_type[k, edge_slot(e)] != NBR_NONE]
+        pj["corner_nbrs"] = [_nbr_to_json(lvl, k, corner_slot(D, c), 0, "corner", _CORNER_NAMES[D][c])
+                             for c in range(1 << D) if lvl.nbr_type[k, corner_slot(D, c)] != NBR_NONE]
+        # always written, -1 without children, as in test/mesh_inputs (json.cpp's to_json
+        # omits them then; its from_json reads either)
+        pj["child_ids"] = [int(x) for x in lvl.child_ids[k]]
+        pj["child_ranks"] = [0 if x >= 0 else -1 for x in pj["child_ids"]]
+        out.append(pj)
+    return out
+
+
+def save_json_hierarchy(levels, path):
+    """Write a hierarchy (finest first) in the reference's mesh JSON format
+    ({"levels": [[PatchInfo, ...], ...]}, as test/mesh_inputs), readable by
+    load_json_hierarchy and by ThunderEgg's from_json (json.cpp:240-300)."""
+    with open(path, "w") as fh:
+        json.dump({"levels": [_level_to_json(lv) for lv in levels]}, fh)
+
+
 def leaves_of_level(lvl: MeshLevel):
     """Recover (level, coords) of each patch from starts/spacings (unit cube)."""
     out = []
