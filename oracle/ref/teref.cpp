@@ -23,9 +23,13 @@
 #include <ThunderEgg/Poisson/StarPatchOperator.h>
 #include <ThunderEgg/TriLinearGhostFiller.h>
 #include <ThunderEgg/VarPoisson/StarPatchOperator.h>
+#include <ThunderEgg/tpl/json.hpp>
 
+#include <array>
 #include <cstring>
 #include <memory>
+#include <stdexcept>
+#include <type_traits>
 #include <string>
 #include <vector>
 
@@ -481,6 +485,47 @@ int teref_flatten_roundtrip(const te_level_desc* in, int* id, int* refine_level,
       out(thunderegg_gb300::flatten<2>(make_domain<2>(in)));
     else
       out(thunderegg_gb300::flatten<3>(make_domain<3>(in)));
+  });
+}
+
+// One level of a mesh JSON file (a PatchInfo array, json.cpp:240-300) read by
+// ThunderEgg's own from_json into a Domain<D>, then flattened like
+// teref_flatten_roundtrip: checks that files written by this repository's
+// mesh.save_json_hierarchy are read by the reference as intended.
+int teref_json_level(const char* text, int dim, int n, int num_ghost, int num_patches, int* id, int* refine_level,
+                     int* parent_id, int* orth_on_parent, int* child_ids, double* starts, double* spacings,
+                     int* nbr_type, int* nbr_ids, int* nbr_orth) {
+  return guard([&] {
+    auto out = [&](auto t) {
+      if ((int)t.id.size() != num_patches) throw std::runtime_error("patch count differs");
+      std::copy(t.id.begin(), t.id.end(), id);
+      std::copy(t.refine_level.begin(), t.refine_level.end(), refine_level);
+      std::copy(t.parent_id.begin(), t.parent_id.end(), parent_id);
+      std::copy(t.orth_on_parent.begin(), t.orth_on_parent.end(), orth_on_parent);
+      std::copy(t.child_ids.begin(), t.child_ids.end(), child_ids);
+      std::copy(t.starts.begin(), t.starts.end(), starts);
+      std::copy(t.spacings.begin(), t.spacings.end(), spacings);
+      std::copy(t.nbr_type.begin(), t.nbr_type.end(), nbr_type);
+      std::copy(t.nbr_ids.begin(), t.nbr_ids.end(), nbr_ids);
+      std::copy(t.nbr_orth.begin(), t.nbr_orth.end(), nbr_orth);
+    };
+    auto read = [&](auto dimc) {
+      constexpr int D = decltype(dimc)::value;
+      std::vector<PatchInfo<D>> pinfos = tpl::nlohmann::json::parse(text).get<std::vector<PatchInfo<D>>>();
+      std::array<int, D> ns;
+      ns.fill(n);
+      for (PatchInfo<D>& pi : pinfos) {
+        pi.ns = ns;
+        pi.num_ghost_cells = num_ghost;
+        for (int a = 0; a < D; a++) pi.spacings[a] /= n;  // the file holds lengths
+      }
+      out(thunderegg_gb300::flatten<D>(
+          Domain<D>(Communicator(MPI_COMM_WORLD), 0, ns, num_ghost, pinfos.begin(), pinfos.end())));
+    };
+    if (dim == 2)
+      read(std::integral_constant<int, 2>());
+    else
+      read(std::integral_constant<int, 3>());
   });
 }
 
