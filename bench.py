@@ -710,6 +710,9 @@ def run_gpu(args):
                        "single_solve_p50": 1000 * pct(lat, 0.5), "single_solve_p99": 1000 * pct(lat, 0.99)},
         "single_solve_mixed": {"value": len(lat) / sum(lat), "unit": "solves/s", "outer_iterations": its1},
         "outer_iterations": max(its), "max_true_rel_residual_fp64": max(true_res), "max_err_vs_exact": err,
+        # finest-level cells x outer BiCGStab iterations per second (each iteration: two V-cycles,
+        # two operator applications)
+        "cell_updates_per_s": value * levels[0].num_cells * max(its),
         "fp64_dropin": {"value": len(d_times) / sum(d_times), "unit": "solves/s",
                         "latency_ms_p50": 1000 * pct(d_times, 0.5), "outer_iterations": d_its,
                         "final_rel_residual_fp64": d_res},
