@@ -136,8 +136,9 @@ def test_oracle_cg_matches_reference_live(oracle, ref):
 def test_oracle_matches_reference_live_operators_and_transfers(oracle, ref):
     """The rows the cycle test does not reach directly, against the compiled reference:
     BiLinear fills, Poisson with Dirichlet and Neumann boundaries, VarPoisson, modifyRHS,
-    both patch solvers (smooth and apply), restriction with and without boundary
-    extrapolation, interpolation, and a VarPoisson BiCGStab solve."""
+    both patch solvers (smooth and apply), the DFT solver with Neumann sides,
+    restriction with and without boundary extrapolation, interpolation, and a
+    VarPoisson BiCGStab solve."""
     from oracle import gmg_config
     from thunderegg_gb300 import mesh as M
 
@@ -166,6 +167,12 @@ def test_oracle_matches_reference_live_operators_and_transfers(oracle, ref):
                 b = ref.patch_solver(lv, f, u, sc, kind=kind, coeffs=c, smoother=smoother, mode=mode)
                 # the reference's PatchSolver does not report inner iterations (the wrapper gives -1)
                 assert np.array_equal(a[0], b[0]), (sc, kind, smoother, mode)
+        # the DFT solver with Neumann sides (DCT plans at the domain boundary, DFTPatchSolver.h:141-191)
+        for mask in (1, (1 << (2 * lv.dim)) - 1):
+            for mode in (0, 1):
+                a = oracle.patch_solver(lv, f, u, sc, smoother=0, dft_neumann_mask=mask, mode=mode)
+                b = ref.patch_solver(lv, f, u, sc, smoother=0, dft_neumann_mask=mask, mode=mode)
+                assert np.array_equal(a[0], b[0]), (sc, mask, mode)
         for extrap in (0, 1):
             assert np.array_equal(oracle.restrict(lv, levels[1], u, extrap), ref.restrict(lv, levels[1], u, extrap))
         vc = rng.standard_normal(levels[1].padded_shape(1))
