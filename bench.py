@@ -107,8 +107,8 @@ def run_reference(args):
     cores = os.cpu_count() or 1
     steps, warm = max(1, args.steps), max(0, args.warmup)
     # bounded: each step is one round of `cores` parallel solves; cap total rounds
-    rounds = min(steps, 3)
-    for _ in range(min(warm, 1)):
+    rounds, warm = min(steps, 3), min(warm, 3)
+    for _ in range(warm):
         cpu_solves(cores)
     walls, its = [], None
     for _ in range(rounds):
@@ -119,7 +119,7 @@ def run_reference(args):
     value = rounds * cores / total
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus,
-        "steps": rounds, "warmup": min(warm, 1), "ms_per_step": 1000 * total / rounds,
+        "steps": rounds, "warmup": warm, "ms_per_step": 1000 * total / rounds,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic", "config": {"workload": WORKLOAD, "outer_iterations": its},
         "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
