@@ -35,7 +35,8 @@ enum {
   TE_OK = 0,
   TE_ERR_INVALID = 1,     /* bad argument (null handle, size mismatch, ...) */
   TE_ERR_CUDA = 2,        /* a CUDA runtime call failed                     */
-  TE_ERR_BREAKDOWN = 3,   /* Krylov breakdown: rho == 0 (BreakdownError.h)  */
+  TE_ERR_BREAKDOWN = 3,   /* Krylov breakdown: rho == 0, or (BiCGStab) a non-
+                             finite residual or rho (BreakdownError.h)      */
   TE_ERR_UNSUPPORTED = 4, /* combination not supported (e.g. odd n trilinear) */
   TE_ERR_BUDGET = 5,      /* serving admission: request over memory budget  */
   TE_ERR_TIMEOUT = 6,     /* bounded device-side wait ran out               */
@@ -231,7 +232,9 @@ int te_cycle_timings(const te_cycle* c, int ncomp, const void* f, void* u, int m
 /* ---- Iterative::BiCGStab (Iterative/BiCGStab.h:111-203) ------------------- */
 /* Right-preconditioned BiCGStab on FP64 device vectors of A's domain.
  * M may be NULL.  Stops when ||r||/||b|| <= tol.  Returns TE_ERR_BREAKDOWN
- * when rho == 0 (the reference throws BreakdownError).
+ * when rho == 0 (the reference throws BreakdownError), and when the right-hand
+ * side, a residual or rho is not finite (no reference counterpart: its NaN
+ * comparisons are false, so it returns at once or runs to max_iterations).
  * With an FP32 cycle as M (mixed precision) the iteration runs in float-float
  * arithmetic (pairs of FP32 numbers, ~48 significant bits) on the FP32 pipes;
  * the initial residual and x in and out stay FP64.  When the float-float
