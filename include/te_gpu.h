@@ -310,10 +310,10 @@ int te_bicgstab_batch_destroy(te_bicgstab_batch* batch);
 
 /* ---- dot product without allocation ---------------------------------------
  * No counterpart in the reference (ThunderEgg reduces on the host).
- * For callers that cannot call cudaMalloc when they need a reduction: code
- * running while a stream is captured into a CUDA graph, hosts whose device
- * memory belongs to another allocator, or callers that must not trigger the
- * device-wide synchronisation an allocation can cause.  Computes the
+ * For callers that cannot call cudaMalloc when they need a reduction: hosts
+ * whose device memory belongs to another allocator (a pool that reserved the
+ * GPU at start-up), or callers that must not trigger the device-wide
+ * synchronisation an allocation can cause.  Computes the
  * interior dot product of two level buffers of the given layout (the same
  * result as te_vec_dot) and allocates nothing: its scratch is a fixed device
  * array of TE_NOALLOC_MAX_PARTIALS + 1 doubles that every GPU using this

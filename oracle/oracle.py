@@ -23,6 +23,12 @@ if ROOT not in sys.path:
 
 from thunderegg_gb300.capi import TeLevelDesc  # noqa: E402
 
+# The ThunderEgg source tree that the reference build (target "ref") compiles
+# and the mesh-input tests read; THUNDEREGG_REF overrides the default location.
+REF_ROOT = os.environ.get("THUNDEREGG_REF", "/root/reference")
+REF_SRC = os.path.join(REF_ROOT, "src", "ThunderEgg")
+REF_MESH_INPUTS = os.path.join(REF_ROOT, "test", "mesh_inputs")
+
 ORACLE_LIB = os.path.join(HERE, "_build", "libte_oracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libteref.so")
 
@@ -56,7 +62,13 @@ def gmg_config(scheme=0, fill_type=0, op_kind=0, neumann=0, smoother=0, dft_neum
 def build(ref: bool = False):
     """Compile the oracle (and, if asked and the sources exist, the reference)."""
     targets = ["oracle"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}"] + targets, check=True)
+    subprocess.run(["make", "-s", "-C", HERE, f"-j{os.cpu_count() or 4}", f"REF_ROOT={REF_ROOT}"] + targets,
+                   check=True)
+
+
+def ref_sources_present():
+    """True where the ThunderEgg source tree exists (the CPU machine, not the GPU machine)."""
+    return os.path.isdir(REF_SRC)
 
 
 def ref_available():

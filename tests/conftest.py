@@ -14,9 +14,6 @@ for p in (ROOT, os.path.join(ROOT, "oracle")):
     if p not in sys.path:
         sys.path.insert(0, p)
 
-REFERENCE_SRC = "/root/reference/src/ThunderEgg"
-
-
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
 
@@ -34,7 +31,7 @@ def ref():
     """ThunderEgg itself, compiled from its sources (only where they exist)."""
     import oracle as orc
 
-    if not os.path.isdir(REFERENCE_SRC):
+    if not orc.ref_sources_present():
         pytest.skip("reference sources not present")
     orc.build(ref=True)
     return orc.Oracle("teref")

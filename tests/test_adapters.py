@@ -12,26 +12,24 @@ import subprocess
 import numpy as np
 import pytest
 
-from conftest import REFERENCE_SRC
+import oracle as orc
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _need_reference():
-    if not os.path.isdir(REFERENCE_SRC):
+    if not orc.ref_sources_present():
         pytest.skip("reference sources not present")
 
 
 def test_adapters_compile_against_reference_headers():
     _need_reference()
-    import oracle as orc
-
     orc.build(ref=True)
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("no C++ compiler")
     inc = [os.path.join(ROOT, "oracle", "_ref", "gen"), os.path.join(ROOT, "oracle", "ref", "mpishim"),
-           os.path.dirname(REFERENCE_SRC), os.path.join(ROOT, "include"), "/usr/local/cuda/include"]
+           os.path.dirname(orc.REF_SRC), os.path.join(ROOT, "include"), "/usr/local/cuda/include"]
     cmd = [cxx, "-std=c++17", "-fsyntax-only"] + [f"-I{p}" for p in inc] + [os.path.join(ROOT, "tests",
                                                                                       "adapters_check.cpp")]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600)
@@ -48,8 +46,6 @@ def _meshes():
 @pytest.mark.parametrize("idx", range(5))
 def test_flatten_roundtrip(idx):
     _need_reference()
-    import oracle as orc
-
     orc.build(ref=True)
     lib = ctypes.CDLL(orc.REF_LIB)
     for lv in _meshes()[idx]:

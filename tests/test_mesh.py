@@ -17,7 +17,9 @@ import pytest
 
 from thunderegg_gb300 import mesh as M
 
-REF_MESHES = "/root/reference/test/mesh_inputs"
+import oracle as _orc  # noqa: E402  (only for the location of the reference tree)
+
+REF_MESHES = _orc.REF_MESH_INPUTS
 
 
 def check_symmetric(lv):
@@ -183,11 +185,10 @@ def test_reference_reads_written_json(make, tmp_path):
     a file written by save_json_hierarchy into a Domain whose tables are this builder's."""
     import ctypes
 
-    from conftest import REFERENCE_SRC
-
-    if not os.path.isdir(REFERENCE_SRC):
-        pytest.skip("reference sources not present")
     import oracle as orc
+
+    if not orc.ref_sources_present():
+        pytest.skip("reference sources not present")
 
     orc.build(ref=True)
     lib = ctypes.CDLL(orc.REF_LIB)

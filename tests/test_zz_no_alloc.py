@@ -1,8 +1,8 @@
 """te_level_dot_noalloc: the dot product for callers that cannot allocate.
 
-Such callers (code running during CUDA graph capture, hosts whose device
-memory is owned by another allocator) get a reduction whose scratch is a
-fixed device array instead of a cudaMalloc.  Its result must equal the
+Such callers (hosts whose device memory is owned by another allocator, or
+code that must not cause the device-wide synchronisation an allocation can)
+get a reduction whose scratch is a fixed device array instead of a cudaMalloc.  Its result must equal the
 existing te_vec_dot (same interior dot product) within FP64 reduction-order
 tolerance, on consecutive calls (the shared scratch keeps the previous
 call's contents), and oversized levels must be rejected before any GPU work.

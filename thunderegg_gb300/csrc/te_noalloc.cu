@@ -1,12 +1,12 @@
 // te_noalloc.cu -- a dot product of two level buffers that allocates nothing.
 //
 // Some callers cannot call cudaMalloc at the point where they need a
-// reduction: code running while a CUDA stream is being captured into a graph
-// (allocation is not allowed there), hosts whose device memory is owned by
-// another allocator that forbids raw cudaMalloc after start-up, or callers
-// that must not synchronise the device the way cudaMalloc/cudaFree can.  For
-// them, te_level_dot_noalloc takes only the level layout and two device
-// buffers and keeps its scratch in a fixed, file-scope device array.
+// reduction: hosts whose device memory is owned by another allocator (a pool
+// that reserved the GPU's memory at start-up and forbids raw cudaMalloc after
+// it), or callers that must not pay the device-wide synchronisation that
+// cudaMalloc/cudaFree can cause while other streams are running.  For them,
+// te_level_dot_noalloc takes only the level layout and two device buffers and
+// keeps its scratch in a fixed, file-scope device array.
 //
 // The scratch is TE_NOALLOC_MAX_PARTIALS + 1 doubles (512 KiB + 8 bytes): one
 // partial sum per (patch, component) plus the result.  Every GPU that loads
@@ -15,7 +15,8 @@
 // serialise them.  Nothing in it has to start at zero: each call writes every
 // slot it later reads.  The device address of the array is looked up once per
 // device, on the first call made with that device current; make that first
-// call before starting any stream capture.
+// call before starting any stream capture.  The call ends by copying the
+// result to the host and synchronising the caller's stream.
 
 #include <cuda_runtime.h>
 
