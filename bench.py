@@ -80,6 +80,86 @@ def _cpu_solve_worker(q):
     q.put((time.perf_counter() - t, its, rc))
 
 
+# FP64 oracle solutions of the benchmark problems, for the error of every GPU result
+# against an FP64 oracle solve.  Each job runs in its own spawned process, started
+# before the GPU work and collected after it; the solution goes through a temporary
+# .npy file (config 3's is 191 MB).
+ORACLE_JOBS = ("config1", "config2", "config3", "config4_0", "config4_1", "config4_2", "config4_3")
+CONFIG4_CHECKED = 4  # config-4 solves compared with the oracle (the first ones of the 32)
+
+
+def _oracle_ref_worker(name, outdir):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+
+    import oracle as orc
+    from thunderegg_gb300 import problems as PB
+
+    O = orc.Oracle("teo")
+    coeffs = None
+    if name == "config1":
+        # the plain method: BiCGStab patch smoother (inner 1e-12 / 1000 / continue on breakdown),
+        # the reference's BiCGStab update rule; the GPU config-1 drop-in runs the same rule
+        levels, f, _ = PB.config1()
+        cfg = orc.gmg_config(scheme=0, smoother=1, inner_tol=1e-12, inner_max_it=1000, tol=1e-10)
+    elif name == "config2":
+        levels, f, _ = PB.config2()
+        cfg = orc.gmg_config(scheme=1, smoother=0, tol=1e-10, precond_exit=1)
+    elif name == "config3":
+        levels, f, _ = PB.config3()
+        cfg = orc.gmg_config(scheme=2, smoother=0, tol=1e-10, precond_exit=1)
+    else:
+        k = int(name.split("_")[1])
+        levels, f, coeffs = PB.config4(num_solves=k + 1)[k]
+        cfg = orc.gmg_config(scheme=1, smoother=1, op_kind=1, inner_tol=1e-12, tol=1e-10, precond_exit=1)
+    t = time.perf_counter()
+    u, its, res, rc = O.solve(levels, f, cfg, coeffs=coeffs)
+    sec = time.perf_counter() - t
+    path = os.path.join(outdir, f"{name}.npy")
+    np.save(path, u)
+    return name, path, its, res, rc, sec
+
+
+class OracleRefs:
+    """The oracle's FP64 solutions, computed in spawned processes beside the GPU work."""
+
+    def __init__(self, names=ORACLE_JOBS):
+        import multiprocessing as mp
+
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+
+        orc.build()
+        self.dir = tempfile.mkdtemp(prefix="te_oracle_refs_")
+        self.pool = mp.get_context("spawn").Pool(min(len(names), max(1, (os.cpu_count() or 2) // 2)))
+        self.jobs = {n: self.pool.apply_async(_oracle_ref_worker, (n, self.dir)) for n in names}
+        self.info = {}
+
+    def get(self, name, timeout=900):
+        import numpy as np
+
+        n, path, its, res, rc, sec = self.jobs[name].get(timeout=timeout)
+        self.info[name] = {"outer_iterations": its, "final_rel_residual": res, "status": rc, "cpu_seconds": sec}
+        return np.load(path)
+
+    def close(self):
+        import shutil
+
+        self.pool.terminate()
+        shutil.rmtree(self.dir, ignore_errors=True)
+
+
+def err_vs(u, ref, lv):
+    """max |u - ref| / max |ref| over the interior cells of the finest level."""
+    import numpy as np
+
+    from thunderegg_gb300 import problems as PB
+
+    a = PB.interior_view(lv, np.asarray(u))
+    b = PB.interior_view(lv, np.asarray(ref))
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
 def cpu_solves(nproc):
     """Run nproc independent solves in parallel processes; returns (wall, [times])."""
     import multiprocessing as mp
@@ -379,6 +459,45 @@ def replica_throughput(local_seconds, local_solves, device="cuda"):
     return float(n.item()) / float(t.item()), float(t.item()), float(n.item())
 
 
+def config1_measure(te, reps=3):
+    """Config 1, the plain method as the FP64 GPU drop-in: 2D uniform L2 (16 patches of
+    32^2), f = -2 pi^2 sin(pi x) sin(pi y), u = 0 Dirichlet, BiLinear, BiCGStab patch
+    smoother (inner BiCGStab tol 1e-12, 1000 iterations, continue on breakdown), V(1,1)
+    to 1 patch, BiCGStab to 1e-10 with the reference's update rule; one solve at a time,
+    device time per solve (CUDA events, median of `reps` after one warm-up).  Returns
+    (record, solution)."""
+    import numpy as np
+    import torch
+
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    levels, f, exact = PB.config1()
+    s = GmgSolver(levels, GmgOptions(scheme=0, smoother=1, inner_tol=1e-12, inner_max_it=1000,
+                                     inner_continue_on_breakdown=True, tol=1e-10, bicgstab_flags=0))
+    fv, uv = te.Vector.from_numpy(s.finest, f), te.Vector(s.finest)
+    stream = torch.cuda.current_stream()
+    times, its = [], 0
+    for r in range(reps + 1):
+        uv.t.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its = s.solve(fv, uv)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if r:
+            times.append(e0.elapsed_time(e1) / 1000.0)
+    u = uv.numpy()
+    t = float(np.median(times))
+    rec = {"workload": "2D uniform L2, 16 patches of 32^2, BiLinear, BiCGStab patch smoother (inner 1e-12/1000/"
+                       "continue), V(1,1), BiCGStab (reference update rule) to 1e-10, FP64",
+           "seconds_per_solve": t, "solves_per_s": 1.0 / t, "outer_iterations": its,
+           "true_rel_residual_fp64": s.residual(fv, uv),
+           "max_err_vs_exact": float(np.abs(PB.interior_view(levels[0], u) - PB.interior_view(levels[0], exact)).max())}
+    return rec, u
+
+
 def config3_measure(te, reps=3):
     """Config 3: 3D uniform octree L4 (4096 patches of 16^3, 16.8M cells), TriLinear,
     DFT smoother, u = 0, RHS i.i.d. N(0,1) (seed 0); mixed precision (FP32 V-cycle
@@ -416,7 +535,7 @@ def config3_measure(te, reps=3):
     out["cells"] = int(levels[0].num_cells)
     out["cell_updates_per_s_mixed"] = levels[0].num_cells * out["mixed"]["outer_iterations"] / \
         out["mixed"]["seconds_per_solve"]
-    return out
+    return out, sols
 
 
 def config4_measure(te):
@@ -441,15 +560,15 @@ def config4_measure(te):
     warm.run()
     srv = Server(budget_bytes=150e9, steps_per_round=4)
     t = time.perf_counter()
-    for r in reqs:
-        srv.submit(r)
+    ids = [srv.submit(r) for r in reqs]
     res = srv.run()
     wall = time.perf_counter() - t
+    sols = [res[i].u for i in ids[:CONFIG4_CHECKED]]
     return {"solves": len(reqs), "solves_per_s": len(reqs) / wall, "seconds": wall,
             "max_rel_residual": max(r.residual for r in res.values()),
             "mean_iterations": float(np.mean([r.iterations for r in res.values()])),
             "depth_classes": len(srv.classes), "max_batch": srv.stats["max_batch"], "inner_tol": 1e-5,
-            "patches_total": int(sum(lv[0].num_patches for lv, _, _ in probs))}
+            "patches_total": int(sum(lv[0].num_patches for lv, _, _ in probs))}, sols, [lv for lv, _, _ in probs]
 
 
 def serving_stream(args, te):
@@ -538,6 +657,12 @@ def run_gpu(args):
     tb.build()
     L = te.capi.lib()
     B = args.batch
+    extra = not args.no_extra and not args.only_mixed and rank == 0
+    # FP64 oracle solutions, computed on host cores while the GPU legs run
+    refs = None
+    if rank == 0 and not args.kernels and not args.only_mixed:
+        names = [n for n in ORACLE_JOBS if extra or n in ("config2",)]
+        refs = OracleRefs(names)
     levels, f_np, exact = PB.config2()
     rng = np.random.default_rng(2024)
     # B independent right-hand sides on the same mesh: the benchmark problem plus
@@ -629,8 +754,10 @@ def run_gpu(args):
         return run
 
     lat, its1 = timed(single_step(single, f1, u1), args.steps, 2)
+    u_single = u1.numpy()
     d_times, d_its = timed(single_step(fp64, f1, u1), args.fp64_steps, 1)
     d_res = fp64.residual(f1, u1)
+    u_fp64 = u1.numpy()
 
     # ---- e2e: the served step through the C ABI from pinned host memory
     hf = torch.from_numpy(fB_np).pin_memory()
@@ -680,12 +807,51 @@ def run_gpu(args):
             return {"error": f"{type(e).__name__}: {e}"}
 
     stream = optional(serving_stream, args, te) if (args.stream > 0 and not args.only_mixed and rank == 0) else None
-    extra = not args.no_extra and not args.only_mixed and rank == 0
+    c1 = optional(config1_measure, te) if extra else None
     c3 = optional(config3_measure, te) if extra else None
     c4 = optional(config4_measure, te) if extra else None
     lk = optional(level_kernel_rooflines, te, served, hbm) if extra else None
     sv = optional(solver_variants_measure, te) if extra else None
     bs = optional(batch_scaling_measure, te) if extra else None
+
+    # error of every result against the oracle's FP64 solve of the same problem
+    oracle_err = None
+    if refs is not None:
+        def compare():
+            P0 = levels[0].num_patches
+            lv0 = levels[0]
+            r2 = refs.get("config2")
+            out = {"config2_served_batch_solve0": err_vs(uB_np[:P0], r2, lv0),
+                   "config2_e2e_solve0": err_vs(hu.numpy()[:P0], r2, lv0),
+                   "config2_single_mixed": err_vs(u_single, r2, lv0),
+                   "config2_fp64_dropin": err_vs(u_fp64, r2, lv0)}
+            if isinstance(c1, tuple):
+                from thunderegg_gb300 import problems as PB
+
+                out["config1_fp64_dropin"] = err_vs(c1[1], refs.get("config1"), PB.config1()[0][0])
+            if isinstance(c3, tuple):
+                from thunderegg_gb300 import problems as PB
+
+                r3 = refs.get("config3")
+                lv3 = PB.config3()[0][0]
+                out["config3_mixed"] = err_vs(c3[1]["mixed"], r3, lv3)
+                out["config3_fp64_dropin"] = err_vs(c3[1]["fp64"], r3, lv3)
+                del r3
+            if isinstance(c4, tuple):
+                out["config4_mixed_served"] = [err_vs(u, refs.get(f"config4_{k}"), c4[2][k][0])
+                                               for k, u in enumerate(c4[1])]
+            out["oracle"] = {"kind": "port (CPU restatement of the reference, FP64)",
+                             "solves": refs.info,
+                             "bicgstab_update": "config1: the reference's rule; others: alpha*M p on the early "
+                                                "exit, as the GPU solves they are compared with",
+                             "measure": "max |u - u_oracle| / max |u_oracle| over finest interior cells"}
+            return out
+
+        oracle_err = optional(compare)
+        refs.close()
+    c1 = c1[0] if isinstance(c1, tuple) else c1
+    c3 = c3[0] if isinstance(c3, tuple) else c3
+    c4 = c4[0] if isinstance(c4, tuple) else c4
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -726,10 +892,12 @@ def run_gpu(args):
                      "launch_ms": top_ms, "algorithmic_bytes": alg,
                      "share_of_vcycle": top_ms / cyc_total if cyc_total else None},
         "vcycle_phases_ms": [[n, round(t, 4)] for n, t in phases[:6]],
+        "err_vs_oracle": oracle_err,
         "cpu_baseline": cpu,
         "clocks": clocks,
         "wall_s_timed": t_wall,
         "serving_stream": stream,
+        "config1": c1,
         "config3": c3,
         "config4": c4,
         "level_kernels": lk,

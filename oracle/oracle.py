@@ -43,7 +43,8 @@ class GmgConfig(ctypes.Structure):
                 ("pre_sweeps", ctypes.c_int), ("post_sweeps", ctypes.c_int),
                 ("coarse_sweeps", ctypes.c_int), ("extrapolate_boundary_ghosts", ctypes.c_int),
                 ("tol", ctypes.c_double), ("max_it", ctypes.c_int), ("use_precond", ctypes.c_int),
-                ("mid_sweeps", ctypes.c_int), ("cycle_type", ctypes.c_int), ("krylov", ctypes.c_int)]
+                ("mid_sweeps", ctypes.c_int), ("cycle_type", ctypes.c_int), ("krylov", ctypes.c_int),
+                ("precond_exit", ctypes.c_int)]
 
 
 CYCLE_TYPES = {"V": 0, "W": 1, "F": 2}  # CycleOpts::cycle_type strings (CycleBuilder.h:176-191)
@@ -52,11 +53,15 @@ CYCLE_TYPES = {"V": 0, "W": 1, "F": 2}  # CycleOpts::cycle_type strings (CycleBu
 def gmg_config(scheme=0, fill_type=0, op_kind=0, neumann=0, smoother=0, dft_neumann_mask=0,
                inner_tol=1e-12, inner_max_it=1000, inner_continue_on_breakdown=1, pre_sweeps=1,
                post_sweeps=1, coarse_sweeps=1, extrapolate_boundary_ghosts=0, tol=1e-10,
-               max_it=1000, use_precond=1, mid_sweeps=1, cycle_type="V", krylov="bicgstab"):
+               max_it=1000, use_precond=1, mid_sweeps=1, cycle_type="V", krylov="bicgstab",
+               precond_exit=0):
+    """precond_exit=1: the BiCGStab early exit adds alpha * M p (the GPU's
+    TE_BICGSTAB_PRECONDITIONED_EXIT, flags=1); 0 is the reference's update.  Only the
+    restatement ("teo") honours it; the compiled reference always runs its own rule."""
     return GmgConfig(scheme, fill_type, op_kind, neumann, smoother, dft_neumann_mask, inner_tol,
                      inner_max_it, inner_continue_on_breakdown, pre_sweeps, post_sweeps,
                      coarse_sweeps, extrapolate_boundary_ghosts, tol, max_it, use_precond,
-                     mid_sweeps, CYCLE_TYPES[cycle_type], {"bicgstab": 0, "cg": 1}[krylov])
+                     mid_sweeps, CYCLE_TYPES[cycle_type], {"bicgstab": 0, "cg": 1}[krylov], precond_exit)
 
 
 def build(ref: bool = False):

@@ -712,7 +712,7 @@ struct Space {
 using ApplyFn = std::function<void(double* x, double* b)>;
 
 int bicgstab(const Space& V, const ApplyFn& A, double* x, const double* b, const ApplyFn* Mr,
-             double tol, int max_it, double* final_res, bool* breakdown) {
+             double tol, int max_it, double* final_res, bool* breakdown, bool precond_exit = false) {
   *breakdown = false;
   std::vector<double> resid = V.zero(), ms, mp;
   if (Mr) {
@@ -743,7 +743,12 @@ int bicgstab(const Space& V, const ApplyFn& A, double* x, const double* b, const
     V.each([&](long i) { s[i] = resid[i]; });
     V.each([&](long i) { s[i] += ap[i] * -alpha; });
     if (V.norm(s.data()) / r0 <= tol) {
-      V.each([&](long i) { x[i] += p[i] * alpha; });
+      // BiCGStab.h:162-168 adds alpha * p; with precond_exit the right-preconditioned
+      // update alpha * M p (the GPU's TE_BICGSTAB_PRECONDITIONED_EXIT)
+      if (Mr && precond_exit)
+        V.each([&](long i) { x[i] += mp[i] * alpha; });
+      else
+        V.each([&](long i) { x[i] += p[i] * alpha; });
       break;
     }
     if (Mr) {
@@ -1390,7 +1395,7 @@ int teo_gmg_solve(const te_level_desc* levels, int nlevels, const teo_gmg_config
         *iterations = cg(V, A, u, f, cfg->use_precond ? &M : nullptr, cfg->tol, cfg->max_it, final_residual, &bd);
       else
         *iterations = bicgstab(V, A, u, f, cfg->use_precond ? &M : nullptr, cfg->tol, cfg->max_it,
-                               final_residual, &bd);
+                               final_residual, &bd, cfg->precond_exit != 0);
     } catch (...) {
       delete H;
       throw;

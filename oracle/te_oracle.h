@@ -24,6 +24,9 @@ typedef struct teo_gmg_config {
   int mid_sweeps;         /* W and FMG cycles (CycleOpts.h:45)              */
   int cycle_type;         /* 0 "V", 1 "W", 2 "F" (CycleBuilder.h:176-191)   */
   int krylov;             /* outer solver: 0 Iterative::BiCGStab, 1 Iterative::CG */
+  int precond_exit;       /* BiCGStab early exit adds alpha*M p instead of the
+                             reference's alpha*p (te_gpu.h flag
+                             TE_BICGSTAB_PRECONDITIONED_EXIT); 0 = reference */
 } teo_gmg_config;
 #ifdef __cplusplus
 }

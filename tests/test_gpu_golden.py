@@ -46,11 +46,11 @@ def test_gpu_matches_reference_fixtures(te, path):
         u = te.Vector.from_numpy(dom, inp[f"apply_k{kind}_in"])
         f = te.Vector(dom)
         op.apply(u, f)
-        assert rel_err(f.numpy(), z[f"apply_k{kind}_f"]) <= 4e-13
+        assert rel_err(f.numpy(), z[f"apply_k{kind}_f"]) <= 1e-13
         assert rel_err(u.numpy(), z[f"apply_k{kind}_u"]) <= 1e-13
         fm = te.Vector.from_numpy(dom, inp[f"modrhs_k{kind}_f"])
         op.modifyRHSForInternalBoundaryConditions(te.Vector.from_numpy(dom, z[f"apply_k{kind}_u"]), fm)
-        assert rel_err(fm.numpy(), z[f"modrhs_k{kind}_out"]) <= 4e-13
+        assert rel_err(fm.numpy(), z[f"modrhs_k{kind}_out"]) <= 1e-13
     op = te.PoissonStarPatchOperator(dom, gf)
     for sm, tol in ((0, 1e-12), (1, 1e-8)):
         ps = te.DFTPatchSolver(op) if sm == 0 else te.BiCGStabPatchSolver(op, 1e-12, 1000, True)

@@ -80,14 +80,14 @@ def test_operator_apply_fixed_size(te, oracle, name, kind):
         op = te.VarPoissonStarPatchOperator(te.Vector.from_numpy(dom, coeffs), dom, gf)
     else:
         op = te.PoissonStarPatchOperator(dom, gf)
-    for dt, tol in ((te.TE_F64, 1e-13), (te.TE_F32, 2e-6)):
+    for dt, tol, tol_f in ((te.TE_F64, 1e-13, 1e-13), (te.TE_F32, 2e-6, 8e-6)):
         u = rng.standard_normal(lv.padded_shape(1))
         uo, fo = oracle.apply(lv, u.copy(), sc, 0, kind, 0, coeffs)
         uv = te.Vector.from_numpy(dom, u, dtype=dt)
         fv = te.Vector(dom, 1, dt)
         fv.t.fill_(7.0)  # every cell of f is written (ghosts zero)
         op.apply(uv, fv)
-        assert rel_err(fv.numpy(), fo) <= tol * 4, dt
+        assert rel_err(fv.numpy(), fo) <= tol_f, dt
         assert rel_err(uv.numpy(), uo) <= tol, dt
 
 

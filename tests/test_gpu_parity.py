@@ -87,21 +87,23 @@ def test_operator_apply(te, oracle, name, kind):
             op = te.VarPoissonStarPatchOperator(te.Vector.from_numpy(dom, coeffs), dom, gf)
         else:
             op = te.PoissonStarPatchOperator(dom, gf)
-        for dt, tol in ((te.TE_F64, 1e-13), (te.TE_F32, 2e-6)):
+        # FP64: measured at most 2.3e-16 on these meshes (many cells bit-identical); FP32: rounding of
+        # the single-precision stencil relative to the oracle's FP64 result
+        for dt, tol, tol_f in ((te.TE_F64, 1e-13, 1e-13), (te.TE_F32, 2e-6, 8e-6)):
             u = rng.standard_normal(lv.padded_shape(1))
             uo, fo = oracle.apply(lv, u.copy(), sc, 0, kind, 0, coeffs)
             uv = te.Vector.from_numpy(dom, u, dtype=dt)
             fv = te.Vector(dom, 1, dt)
             fv.t.fill_(7.0)  # apply must overwrite f everywhere (setWithGhost(0))
             op.apply(uv, fv)
-            assert rel_err(fv.numpy(), fo) <= tol * 4, (sc, dt)
+            assert rel_err(fv.numpy(), fo) <= tol_f, (sc, dt)
             assert rel_err(uv.numpy(), uo) <= tol, (sc, dt)  # ghosts of u are filled/mutated
             # modifyRHSForInternalBoundaryConditions
             f = rng.standard_normal(lv.padded_shape(1))
             want = oracle.modify_rhs(lv, uo, f, sc, 0, kind, coeffs)
             fv = te.Vector.from_numpy(dom, f, dtype=dt)
             op.modifyRHSForInternalBoundaryConditions(te.Vector.from_numpy(dom, uo, dtype=dt), fv)
-            assert rel_err(fv.numpy(), want) <= tol * 4
+            assert rel_err(fv.numpy(), want) <= tol_f
 
 
 def test_poisson_neumann(te, oracle):
@@ -116,7 +118,7 @@ def test_poisson_neumann(te, oracle):
     uo, fo = oracle.apply(lv, u.copy(), 0, 0, 0, 1)
     uv, fv = te.Vector.from_numpy(dom, u), te.Vector(dom)
     op.apply(uv, fv)
-    assert rel_err(fv.numpy(), fo) <= 4e-13
+    assert rel_err(fv.numpy(), fo) <= 1e-13
 
 
 @pytest.mark.parametrize("name", CASE_NAMES)
