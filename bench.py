@@ -49,6 +49,8 @@ def parse():
     ap.add_argument("--stream", type=int, default=40,
                     help="requests in the serving-stream measurement (0: skip)")
     ap.add_argument("--stream-rate", type=float, default=50.0, help="Poisson arrival rate, requests/s")
+    ap.add_argument("--c5-rates", default="10,40,160", help="config-5 stream: arrival rates swept, requests/s")
+    ap.add_argument("--c5-requests", type=int, default=60, help="config-5 stream: requests per rate (0: skip)")
     ap.add_argument("--no-extra", action="store_true", help="skip the config-3 and config-4 measurements")
     ap.add_argument("--kernels", action="store_true",
                     help="only time the drop-in level kernels against HBM (one JSON line)")
@@ -442,6 +444,28 @@ def solver_variants_measure(te, reps=3):
     return out
 
 
+def tuner_report(te):
+    """The autotuner's choices so far: per kernel and shape, the chosen candidate, the default
+    (candidate 0) and the default's time over the chosen one's."""
+    import ctypes
+
+    lib = te.capi.lib()
+    need = ctypes.c_int(0)
+    te.capi.check(lib.te_tune_report(None, 0, ctypes.byref(need)))
+    buf = ctypes.create_string_buffer(max(1, need.value))
+    te.capi.check(lib.te_tune_report(buf, need.value, ctypes.byref(need)))
+    out = []
+    for r in json.loads(buf.value.decode() or "[]"):
+        ms = r["ms"]
+        default = next(iter(ms)) if ms else None
+        gain = None
+        if ms and ms.get(default) and ms.get(r["choice"]):
+            gain = ms[default] / ms[r["choice"]]
+        out.append({"kernel_shape": r["key"].split("|", 1)[1], "choice": r["choice"], "default": default,
+                    "gain_over_default": gain, "candidates_ms": ms})
+    return out
+
+
 def replica_throughput(local_seconds, local_solves, device="cuda"):
     """Whole-job throughput of independent replicas (one process per GPU, no data
     exchange): every rank's solves summed, divided by the slowest rank's time.
@@ -512,7 +536,11 @@ def config3_measure(te, reps=3):
     levels, f, _ = PB.config3()
     out = {}
     sols = {}
-    for name, opts in (("mixed", GmgOptions(scheme=2, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1)),
+    # bf16_ir: the form the configuration names -- FP32 V-cycle whose DFT transforms run as per-patch-
+    # scaled BF16 tensor-core contractions (FP32 accumulation), inside FP64 iterative refinement
+    for name, opts in (("bf16_ir", GmgOptions(scheme=2, smoother=0, cycle_dtype=te.TE_F32, krylov="ir",
+                                              tc_precision=te.capi.TE_TC_BF16, max_it=200)),
+                       ("mixed", GmgOptions(scheme=2, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1)),
                        ("fp64", GmgOptions(scheme=2, smoother=0, cycle_dtype=te.TE_F64, bicgstab_flags=1))):
         s = GmgSolver(levels, opts)
         fv, uv = te.Vector.from_numpy(s.finest, f), te.Vector(s.finest)
@@ -532,6 +560,12 @@ def config3_measure(te, reps=3):
     d = sols["mixed"][inner] - sols["fp64"][inner]
     out["mixed_vs_fp64_rel_err"] = float(np.abs(d).max() / np.abs(sols["fp64"][inner]).max())
     out["speedup_mixed_vs_fp64"] = out["fp64"]["seconds_per_solve"] / out["mixed"]["seconds_per_solve"]
+    out["speedup_bf16_ir_vs_fp64"] = out["fp64"]["seconds_per_solve"] / out["bf16_ir"]["seconds_per_solve"]
+    out["forms"] = {"bf16_ir": "FP32 V-cycle, BF16 tensor-core transforms (per-patch power-of-two scaling, FP32 "
+                               "accumulation), FP64 iterative refinement",
+                    "mixed": "FP32 V-cycle, 3xTF32 tensor-core transforms, float-float BiCGStab with FP64 residual "
+                             "checks",
+                    "fp64": "FP64 V-cycle and BiCGStab (the plain drop-in)"}
     out["cells"] = int(levels[0].num_cells)
     out["cell_updates_per_s_mixed"] = levels[0].num_cells * out["mixed"]["outer_iterations"] / \
         out["mixed"]["seconds_per_solve"]
@@ -636,6 +670,113 @@ def serving_stream(args, te):
             "mix": "0.7 x 2D (circle L3-6 32^2, uniform L4 32^2, uniform L5 16^2), "
                    "0.3 x 3D (uniform L3 16^3, uniform L3 8^3); 150 GB budget",
             "latency_from": "scheduled arrival"}
+
+
+def config5_stream(args, te):
+    """Config 5's serving stream: requests with Poisson arrivals at several rates.  Each request is,
+    with probability 0.7, a 2D quadtree -- uniform at a level drawn from 2..6, or circle-adaptive
+    L3-7 -- with n x n patches, n drawn from {16, 32, 64}; otherwise a 3D uniform octree at a level
+    drawn from 2..4 with 8^3 or 16^3 patches.  Right-hand side: a seeded sum of 8 sine modes,
+    u = 0 Dirichlet; mixed precision (FP32 V-cycle, tensor-core transforms where the patch shape
+    allows) to a 1e-10 FP64 residual; 150 GB budget; solves of one patch size share launches
+    whatever their depth.  Latency is measured from each request's scheduled arrival.  Beside it:
+    the plain FP64 drop-in's time for the same request list, one solve at a time (each distinct
+    mesh timed once, CUDA events)."""
+    import numpy as np
+    import torch
+
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+    from thunderegg_gb300.serve import Request, Server
+
+    rng = np.random.default_rng(5)
+    meshes = {}
+
+    def mesh(kind):
+        if kind not in meshes:
+            d, shape, lvl, n = kind
+            if shape == "circle":
+                meshes[kind] = M.circle_mesh(n=n, lo=3, hi=7)
+            else:
+                meshes[kind] = M.uniform_mesh(d, lvl, n, connect="full" if d == 2 else "face")
+        return meshes[kind]
+
+    def draw():
+        if rng.random() < 0.7:
+            n = int(rng.choice([16, 32, 64]))
+            if rng.random() < 0.5:
+                return (2, "uniform", int(rng.integers(2, 7)), n)
+            return (2, "circle", 7, n)
+        return (3, "uniform", int(rng.integers(2, 5)), int(rng.choice([8, 16])))
+
+    def opts(kind, dtype):
+        return GmgOptions(scheme=1 if kind[0] == 2 else 2, smoother=0, cycle_dtype=dtype, bicgstab_flags=1)
+
+    rates = [float(x) for x in args.c5_rates.split(",")]
+    per_rate = args.c5_requests
+    streams = []
+    for rate in rates:
+        kinds = [draw() for _ in range(per_rate)]
+        reqs = [Request(mesh(k), PB.sine_modes_rhs(mesh(k)[0], rng), opts(k, te.TE_F32)) for k in kinds]
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, size=per_rate))
+        streams.append((rate, kinds, reqs, arrivals))
+    srv = Server(budget_bytes=150e9, steps_per_round=2)
+    # warm-up: one request of every distinct mesh (tuning, graph captures) before the clocks start
+    for k in sorted({k for _, kinds, _, _ in streams for k in kinds}):
+        srv.submit(Request(mesh(k), PB.sine_modes_rhs(mesh(k)[0], rng), opts(k, te.TE_F32)))
+    srv.run()
+    out = []
+    for rate, kinds, reqs, arrivals in streams:
+        srv.results = {}
+        builds0, hits0 = srv.stats["union_builds"], srv.stats["union_hits"]
+        t0 = time.perf_counter()
+        ids, nxt = {}, 0
+        while nxt < len(reqs) or not srv.idle():
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and arrivals[nxt] <= now:
+                ids[srv.submit(reqs[nxt])] = nxt
+                nxt += 1
+            if srv.idle():
+                time.sleep(max(0.0, min(arrivals[nxt] - now, 0.01)))
+                continue
+            srv.step()
+        wall = time.perf_counter() - t0
+        lat = sorted(r.latency_s for r in srv.results.values())
+        pick = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]  # noqa: E731
+        out.append({"arrival_rate_per_s": rate, "requests": len(reqs), "solves_per_s": len(reqs) / wall,
+                    "latency_ms_p50": 1000 * pick(0.5), "latency_ms_p99": 1000 * pick(0.99),
+                    "max_rel_residual": max(r.residual for r in srv.results.values()),
+                    "union_builds": srv.stats["union_builds"] - builds0,
+                    "union_cache_hits": srv.stats["union_hits"] - hits0})
+    srv.close()
+    # the plain FP64 drop-in, one solve at a time, over the same request lists
+    stream = torch.cuda.current_stream()
+    fp64_s = {}
+    for k in sorted({k for _, kinds, _, _ in streams for k in kinds}):
+        s = GmgSolver(mesh(k), opts(k, te.TE_F64))
+        fv = te.Vector.from_numpy(s.finest, PB.sine_modes_rhs(mesh(k)[0], rng))
+        uv = te.Vector(s.finest)
+        for r in range(2):
+            uv.t.zero_()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.solve(fv, uv)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        fp64_s[k] = e0.elapsed_time(e1) / 1000.0
+        del s, fv, uv
+    for o, (_, kinds, _, _) in zip(out, streams):
+        t = sum(fp64_s[k] for k in kinds)
+        o["fp64_dropin_one_at_a_time_solves_per_s"] = len(kinds) / t
+        o["served_vs_fp64_dropin"] = o["solves_per_s"] / (len(kinds) / t)
+    return {"rates": out, "requests_per_rate": per_rate,
+            "mix": "0.7 x 2D (uniform L2-6 or circle L3-7; 16^2/32^2/64^2), 0.3 x 3D (uniform L2-4; 8^3/16^3); "
+                   "8 random sine modes, u = 0; 150 GB budget",
+            "distinct_meshes": len(fp64_s), "latency_from": "scheduled arrival",
+            "requests_note": "bounded count per rate (the configuration names 10,000) so the default run "
+                             "finishes in minutes"}
 
 
 def run_gpu(args):
@@ -759,19 +900,54 @@ def run_gpu(args):
     d_res = fp64.residual(f1, u1)
     u_fp64 = u1.numpy()
 
-    # ---- e2e: the served step through the C ABI from pinned host memory
+    # ---- e2e: the served step through the C ABI from pinned host memory.  Every step copies its
+    # right-hand sides host->device and its solutions device->host inside the timed region; the
+    # copies run on a copy stream, overlapped with the neighbouring steps' solves (step k+1's
+    # inputs go up and step k-1's results come down while step k solves; device buffers are
+    # double-buffered).  Time: CUDA events from before the first upload to after the last download.
     hf = torch.from_numpy(fB_np).pin_memory()
-    hu = torch.empty(fB_np.shape, dtype=torch.float64).pin_memory()
+    hu = [torch.empty(fB_np.shape, dtype=torch.float64).pin_memory() for _ in range(2)]
+    fBs = [fB, te.Vector.from_numpy(served.finest, fB_np)]
+    uBs = [uB, te.Vector(served.finest)]
+    cstream = torch.cuda.Stream()
 
-    def e2e_step():
-        fB.t.copy_(hf, non_blocking=True)
-        uB.t.zero_()
-        out = served.solve_batched(fB, uB, offsets[0])
-        hu.copy_(uB.t, non_blocking=True)
-        return out
+    def e2e_run(k_steps):
+        ev_up = [torch.cuda.Event() for _ in range(k_steps)]
+        ev_done = [torch.cuda.Event() for _ in range(k_steps)]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        cstream.wait_stream(stream)
+        with torch.cuda.stream(cstream):
+            fBs[0].t.copy_(hf, non_blocking=True)
+            ev_up[0].record(cstream)
+        for k in range(k_steps):
+            with torch.cuda.stream(cstream):
+                if k + 1 < k_steps:
+                    if k >= 1:
+                        cstream.wait_event(ev_done[k - 1])  # step k-1 no longer reads its input buffer
+                    fBs[(k + 1) % 2].t.copy_(hf, non_blocking=True)
+                    ev_up[k + 1].record(cstream)
+                if k >= 1:
+                    cstream.wait_event(ev_done[k - 1])
+                    hu[(k - 1) % 2].copy_(uBs[(k - 1) % 2].t, non_blocking=True)
+            stream.wait_event(ev_up[k])
+            uBs[k % 2].t.zero_()
+            served.solve_batched(fBs[k % 2], uBs[k % 2], offsets[0])
+            ev_done[k].record(stream)
+        with torch.cuda.stream(cstream):
+            cstream.wait_event(ev_done[k_steps - 1])
+            hu[(k_steps - 1) % 2].copy_(uBs[(k_steps - 1) % 2].t, non_blocking=True)
+        stream.wait_stream(cstream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1000.0
 
-    e_times, _ = timed(e2e_step, max(3, args.steps // 2), 1)
-    e2e = world * B * len(e_times) / sum(e_times)
+    e2e_run(2)  # warm-up: graphs of the second buffer set
+    k_e2e = max(4, args.steps // 2)
+    e_time = e2e_run(k_e2e)
+    e2e = world * B * k_e2e / e_time
+    e2e_copy_gbs = 2 * fB_np.nbytes * k_e2e / e_time / 1e9
 
     # ---- dominant kernel: per-phase device times of the served batch's V-cycle, averaged over
     # several eager applications (CUDA events on the cycle's stream around each launch)
@@ -807,6 +983,7 @@ def run_gpu(args):
             return {"error": f"{type(e).__name__}: {e}"}
 
     stream = optional(serving_stream, args, te) if (args.stream > 0 and not args.only_mixed and rank == 0) else None
+    c5 = optional(config5_stream, args, te) if (extra and args.c5_requests > 0) else None
     c1 = optional(config1_measure, te) if extra else None
     c3 = optional(config3_measure, te) if extra else None
     c4 = optional(config4_measure, te) if extra else None
@@ -822,7 +999,7 @@ def run_gpu(args):
             lv0 = levels[0]
             r2 = refs.get("config2")
             out = {"config2_served_batch_solve0": err_vs(uB_np[:P0], r2, lv0),
-                   "config2_e2e_solve0": err_vs(hu.numpy()[:P0], r2, lv0),
+                   "config2_e2e_solve0": err_vs(hu[(k_e2e - 1) % 2].numpy()[:P0], r2, lv0),
                    "config2_single_mixed": err_vs(u_single, r2, lv0),
                    "config2_fp64_dropin": err_vs(u_fp64, r2, lv0)}
             if isinstance(c1, tuple):
@@ -834,6 +1011,7 @@ def run_gpu(args):
 
                 r3 = refs.get("config3")
                 lv3 = PB.config3()[0][0]
+                out["config3_bf16_ir"] = err_vs(c3[1]["bf16_ir"], r3, lv3)
                 out["config3_mixed"] = err_vs(c3[1]["mixed"], r3, lv3)
                 out["config3_fp64_dropin"] = err_vs(c3[1]["fp64"], r3, lv3)
                 del r3
@@ -884,7 +1062,9 @@ def run_gpu(args):
                         "final_rel_residual_fp64": d_res},
         "speedup_served_vs_fp64_dropin": value / world / (len(d_times) / sum(d_times)),
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": int(fB_np.nbytes),
-                "d2h_bytes_per_step": int(fB_np.nbytes)},
+                "d2h_bytes_per_step": int(fB_np.nbytes), "steps": k_e2e,
+                "copies": "pinned host buffers, copy stream overlapped with the neighbouring steps' solves",
+                "copy_gbs_sustained": e2e_copy_gbs},
         "gpu_launches": int(launches),
         "roofline": {"kernel": f"{top_name} (fused V-cycle phase, served batch)", "bound": "hbm",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -893,10 +1073,12 @@ def run_gpu(args):
                      "share_of_vcycle": top_ms / cyc_total if cyc_total else None},
         "vcycle_phases_ms": [[n, round(t, 4)] for n, t in phases[:6]],
         "err_vs_oracle": oracle_err,
+        "autotuner": optional(tuner_report, te),
         "cpu_baseline": cpu,
         "clocks": clocks,
         "wall_s_timed": t_wall,
         "serving_stream": stream,
+        "config5_stream": c5,
         "config1": c1,
         "config3": c3,
         "config4": c4,

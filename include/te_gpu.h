@@ -26,6 +26,8 @@
 #ifndef TE_GPU_H
 #define TE_GPU_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -97,6 +99,17 @@ int te_domain_destroy(te_domain* d);
 /* doubles (or floats) of one patch with ncomp components, ghosts included */
 long long te_domain_patch_stride(const te_domain* d, int ncomp);
 int te_domain_num_patches(const te_domain* d);
+/* A zero-filled device level buffer of the domain (num_patches * patch_stride
+ * elements of TE_F64 or TE_F32), for a Vector<D> made with the unmanaged
+ * constructor (Vector.h:199-215); free it with te_level_free. */
+int te_level_alloc(const te_domain* d, int ncomp, int dtype, void** out);
+int te_level_free(void* buffer);
+/* Plain device memory and a synchronous copy in either direction (host or
+ * device pointers, unified addressing), for callers without the CUDA runtime
+ * headers (the C++ adapters' boundary-data arrays). */
+int te_device_alloc(size_t bytes, void** out);
+int te_device_free(void* p);
+int te_copy(void* dst, const void* src, size_t bytes);
 
 /* ---- Vector<D> algebra (Vector.h:391-611); interior cells only unless
  *      with_ghost.  x, a, b, c are device level buffers of the domain. ---- */
@@ -157,6 +170,35 @@ int te_operator_apply(const te_operator* op, int ncomp, int dtype, void* u, void
  * u's ghosts (which the caller has filled) */
 int te_operator_modify_rhs(const te_operator* op, int ncomp, int dtype, const void* u, void* f);
 
+/* ---- right-hand-side boundary helpers -------------------------------------
+ * The reference's helpers take the boundary data as functions of a point
+ * (std::function); across the ABI the caller evaluates them at the boundary
+ * points and passes the values.  Boundary data arrays are device FP64
+ * [P][2D][FS] with FS = te_domain_face_stride: side s = 2 * axis + is_upper,
+ * face cell e = the tangential cell indices in increasing axis order, the
+ * first fastest; entries of sides with a neighbour are ignored.
+ * te_domain_boundary_points writes the points themselves into a device array
+ * [P][2D][FS][D], as DomainTools::GetRealCoordBound (DomainTools.h:179-210)
+ * computes them: the side's own coordinate on the patch boundary, cell
+ * centres in the other directions.  Sides are processed in the reference's
+ * order and each term in its operation order, so FP64 results match the
+ * reference bit for bit. */
+long long te_domain_face_stride(const te_domain* d);
+int te_domain_boundary_points(const te_domain* d, double* coords);
+/* Poisson::StarPatchOperator::addDrichletBCToRHS (Poisson/StarPatchOperator.h:187-204):
+ * f += -2 g / h^2 on the interior cells next to every side without a neighbour;
+ * VarPoisson::StarPatchOperator::addDrichletBCToRHS (VarPoisson/StarPatchOperator.h:194-219):
+ * f -= 2 g c / h^2 with cvals the coefficient at the boundary points (NULL for
+ * the Poisson operator, required for VarPoisson). */
+int te_operator_add_dirichlet_bc_to_rhs(const te_operator* op, int dtype, void* f, const double* gvals,
+                                        const double* cvals);
+/* Poisson::StarPatchOperator::addNeumannBCToRHS (Poisson/StarPatchOperator.h:212-242):
+ * f += dg / h on lower sides and f -= dg / h on upper sides, dgvals = the
+ * derivative of g along the side's axis at the boundary points.  The
+ * VarPoisson operator has no Neumann helper (TE_ERR_UNSUPPORTED), as in the
+ * reference. */
+int te_operator_add_neumann_bc_to_rhs(const te_operator* op, int dtype, void* f, const double* dgvals);
+
 /* ---- PatchSolver<D> / GMG::Smoother<D> (PatchSolver.h:107-170) ---------- */
 /* Poisson::DFTPatchSolver (Poisson/DFTPatchSolver.h:385-450); neumann_mask
  * bit i = Side index i is Neumann (when it has no neighbour). */
@@ -178,6 +220,18 @@ int te_patch_solver_apply(const te_patch_solver* s, int ncomp, int dtype, const 
  * 3D, one set of transform matrices for the level; TE_NO_TC=1 at creation
  * turns it off).  No counterpart in the reference. */
 int te_patch_solver_uses_tensor_cores(const te_patch_solver* s, int* out);
+/* Poisson::DFTPatchSolver (Poisson/DFTPatchSolver.h:385-450) with the arithmetic
+ * of its FP32 tensor-core transforms chosen (no counterpart in the reference):
+ * TE_TC_TF32X3 = 3xTF32 split products (what te_dft_patch_solver_create uses,
+ * about FP32 accuracy), TE_TC_BF16 = BF16 operands with FP32 accumulation, each
+ * patch's right-hand side scaled by a power of two that brings its largest
+ * magnitude into [1, 2) and the result scaled back (8 significant bits per
+ * operand: a preconditioner for an FP64 outer loop, te_ir_solve or BiCGStab).
+ * FP64 solves of the same solver stay FP64.  TE_TC_BF16 where the tensor-core
+ * path does not apply gives TE_ERR_UNSUPPORTED. */
+enum { TE_TC_TF32X3 = 0, TE_TC_BF16 = 1 };
+int te_dft_patch_solver_create_tc(const te_operator* op, int neumann_mask, int tc_precision,
+                                  te_patch_solver** out);
 
 /* ---- GMG transfers -------------------------------------------------------- */
 /* GMG::LinearRestrictor (GMG/LinearRestrictor.h:166-191, MPIRestrictor.h:55-83)
@@ -263,6 +317,17 @@ int te_bicgstab_solve(const te_operator* A, int ncomp, void* x, const void* b, c
 int te_cg_solve(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M, double tol,
                 int max_iterations, int* iterations, double* final_residual);
 
+/* ---- iterative refinement (no counterpart in the reference) ----------------
+ * FP64 iterative refinement around a cycle, behind the Iterative::Solver
+ * signature (Iterative/Solver.h:64-69): r = b - A x in FP64; while
+ * ||r||/||b|| > tol: x += M r, r = b - A x.  The stopping test is on the true
+ * FP64 residual every iteration; *final_residual is that residual.  M is
+ * required (typically an FP32 cycle, whose tensor-core transforms may run in
+ * BF16, te_patch_solver_set_tc_precision).  A zero b returns at once with x
+ * unchanged; a non-finite b or residual returns TE_ERR_BREAKDOWN. */
+int te_ir_solve(const te_operator* A, int ncomp, void* x, const void* b, const te_cycle* M, double tol,
+                int max_iterations, int* iterations, double* final_residual);
+
 /* Batched form: num_solves independent systems whose finest-level patches
  * are the contiguous ranges [patch_offsets[i], patch_offsets[i+1]) of A's
  * domain (a union of meshes of equal depth; M a V-cycle on the union).  Each
@@ -307,6 +372,19 @@ int te_bicgstab_batch_sync_x(te_bicgstab_batch* batch);
 int te_bicgstab_batch_finish_slots(te_bicgstab_batch* batch, int num_slots, const int* slots, int* finished);
 int te_bicgstab_batch_reset(te_bicgstab_batch* batch, int slot);
 int te_bicgstab_batch_destroy(te_bicgstab_batch* batch);
+
+/* ---- autotuner (no counterpart in the reference) ---------------------------
+ * Launch shapes and kernel variants of the tunable kernels (the tensor-core
+ * patch solve: operand placement and resident CTAs per SM; the BiCGStab patch
+ * smoother: threads per patch) are chosen per (device, kernel, shape key) by
+ * timing every candidate with CUDA events the first time the shape is met
+ * outside a stream capture; cycles tune their levels before capturing their
+ * graphs.  TE_TUNE=0 keeps the defaults; TE_TUNE_CACHE=<file> keeps choices
+ * across processes.  te_tune_report writes the choices and each candidate's
+ * median milliseconds as JSON into buf (len bytes) and the length needed
+ * (with the terminating zero) into *needed; te_tune_reset forgets them. */
+int te_tune_report(char* buf, int len, int* needed);
+int te_tune_reset(void);
 
 /* ---- dot product without allocation ---------------------------------------
  * No counterpart in the reference (ThunderEgg reduces on the host).

@@ -9,11 +9,19 @@
 //   GpuGhostFiller<D>          GhostFiller<D>                 (GhostFiller.h:46-53)
 //   GpuStarPatchOperator<D>    PatchOperator<D>, Poisson or VarPoisson (PatchOperator.h:61-151)
 //   GpuDFTPatchSolver<D>       PatchSolver<D> (= GMG::Smoother<D>) (PatchSolver.h:98-170)
+//   GpuBiCGStabPatchSolver<D>  PatchSolver<D>: Iterative::PatchSolver with an inner BiCGStab
+//                              (Iterative/PatchSolver.h:53-175)
 //   GpuLinearRestrictor<D>     GMG::Restrictor<D>             (GMG/Restrictor.h:48-54)
 //   GpuDirectInterpolator<D>   GMG::Interpolator<D>           (GMG/Interpolator.h:47-54)
-//   GpuVCycle<D>               Operator<D> applying a whole V-cycle (the Mr of BiCGStab)
+//   GpuCycle<D>                GMG::Cycle<D> (GMG/Cycle.h:39-105) over a GMG::Level<D> chain of
+//                              GPU parts, e.g. CycleBuilder::getCycle()->getFinestLevel()
+//   GpuCycleBuilder<D>         GMG::CycleBuilder<D>'s interface (GMG/CycleBuilder.h:97-192),
+//                              getCycle() returning a GpuCycle
+//   GpuVCycle<D>               Operator<D> applying a whole cycle built from raw handles
 //   GpuBiCGStab<D>             Iterative::Solver<D>           (Iterative/Solver.h:47-69)
 //   GpuCG<D>                   Iterative::Solver<D>, Iterative::CG's right-preconditioned form (CG.h:126-194)
+//   GpuIterativeRefinement<D>  Iterative::Solver<D>: FP64 iterative refinement around a cycle (no
+//                              reference counterpart)
 //
 // Vectors: ThunderEgg's Vector<D> is concrete; a device-backed one is made
 // with its unmanaged constructor (Vector.h:199-215) over a GpuDomain's level
@@ -28,7 +36,9 @@
 #pragma once
 
 #include <ThunderEgg/Domain.h>
+#include <ThunderEgg/GMG/Cycle.h>
 #include <ThunderEgg/GMG/CycleOpts.h>
+#include <ThunderEgg/GMG/Level.h>
 #include <ThunderEgg/GMG/Interpolator.h>
 #include <ThunderEgg/GMG/Restrictor.h>
 #include <ThunderEgg/GhostFiller.h>
@@ -40,10 +50,9 @@
 #include <ThunderEgg/RuntimeError.h>
 #include <ThunderEgg/Vector.h>
 
-#include <cuda_runtime.h>
-
 #include <array>
 #include <cstdio>
+#include <functional>
 #include <memory>
 #include <string>
 #include <vector>
@@ -191,11 +200,10 @@ class GpuDomain {
   DeviceVector makeVector(int ncomp = 1) const {
     const long long stride = patchStride(ncomp);
     const int P = dom_.getNumLocalPatches();
-    double* p = nullptr;
-    if (cudaMalloc(&p, sizeof(double) * (size_t)stride * P) != cudaSuccess)
-      throw ThunderEgg::RuntimeError("cudaMalloc of a level buffer failed");
-    cudaMemset(p, 0, sizeof(double) * (size_t)stride * P);
-    std::shared_ptr<double> mem(p, [](double* x) { cudaFree(x); });
+    void* raw = nullptr;
+    check(te_level_alloc(h_.get(), ncomp, TE_F64, &raw));
+    double* p = static_cast<double*>(raw);
+    std::shared_ptr<double> mem(p, [](double* x) { te_level_free(x); });
     std::vector<double*> starts(P);
     for (int i = 0; i < P; i++) starts[i] = p + (size_t)i * stride;
     std::array<int, D + 1> strides, lengths;
@@ -300,7 +308,59 @@ class GpuStarPatchOperator : public ThunderEgg::PatchOperator<D> {
   te_operator* handle() const { return h_.get(); }
   const std::shared_ptr<GpuDomain<D>>& gpuDomain() const { return gd_; }
 
+  using PointFn = std::function<double(const std::array<double, D>&)>;
+  // Poisson/StarPatchOperator.h:187-204 (Poisson) and VarPoisson/StarPatchOperator.h:194-219
+  // (VarPoisson: hfunc is the coefficient): the functions are evaluated on the host at the
+  // boundary points, the terms are added on the device
+  void addDrichletBCToRHS(ThunderEgg::Vector<D>& f, PointFn gfunc, PointFn hfunc = nullptr) const {
+    std::vector<std::vector<double>> vals = boundaryValues({gfunc, hfunc ? hfunc : gfunc});
+    DeviceData g(vals[0]), c(vals[1]);
+    check(te_operator_add_dirichlet_bc_to_rhs(h_.get(), TE_F64, levelPointer(f, *gd_), g.p,
+                                              hfunc ? c.p : nullptr));
+  }
+  // Poisson/StarPatchOperator.h:212-242: gfunc_grad[axis] is the derivative along that axis
+  void addNeumannBCToRHS(ThunderEgg::Vector<D>& f, PointFn /*gfunc*/, std::array<PointFn, D> gfunc_grad) const {
+    std::vector<PointFn> fns(gfunc_grad.begin(), gfunc_grad.end());
+    std::vector<std::vector<double>> vals = boundaryValues(fns);
+    const long long fs = te_domain_face_stride(gd_->handle());
+    std::vector<double> sel(vals[0].size());
+    for (size_t i = 0; i < sel.size(); i++) sel[i] = vals[(i / fs % (2 * D)) >> 1][i];
+    DeviceData g(sel);
+    check(te_operator_add_neumann_bc_to_rhs(h_.get(), TE_F64, levelPointer(f, *gd_), g.p));
+  }
+
  private:
+  // FP64 device copy of a host array
+  struct DeviceData {
+    double* p = nullptr;
+    explicit DeviceData(const std::vector<double>& v) {
+      void* raw = nullptr;
+      check(te_device_alloc(v.size() * sizeof(double), &raw));
+      p = static_cast<double*>(raw);
+      check(te_copy(p, v.data(), v.size() * sizeof(double)));
+    }
+    ~DeviceData() { te_device_free(p); }
+    DeviceData(const DeviceData&) = delete;
+    DeviceData& operator=(const DeviceData&) = delete;
+  };
+  // each function at the boundary points of te_domain_boundary_points, [P][2D][face stride]
+  std::vector<std::vector<double>> boundaryValues(const std::vector<PointFn>& fns) const {
+    const long long fs = te_domain_face_stride(gd_->handle());
+    const size_t npts = (size_t)gd_->domain().getNumLocalPatches() * 2 * D * fs;
+    std::vector<double> pts(npts * D);
+    {
+      DeviceData dev(pts);
+      check(te_domain_boundary_points(gd_->handle(), dev.p));
+      check(te_copy(pts.data(), dev.p, pts.size() * sizeof(double)));
+    }
+    std::vector<std::vector<double>> out(fns.size(), std::vector<double>(npts, 0.0));
+    std::array<double, D> x;
+    for (size_t i = 0; i < npts; i++) {
+      for (int a = 0; a < D; a++) x[a] = pts[i * D + a];
+      for (size_t k = 0; k < fns.size(); k++) out[k][i] = fns[k](x);
+    }
+    return out;
+  }
   std::shared_ptr<GpuDomain<D>> gd_;
   std::shared_ptr<te_operator> h_;
 };
@@ -308,16 +368,10 @@ class GpuStarPatchOperator : public ThunderEgg::PatchOperator<D> {
 // ---------------------------------------------------------------------------
 // PatchSolver<D> (also a GMG::Smoother<D>): the DFT patch solver
 // ---------------------------------------------------------------------------
+// the level-wide apply/smooth of any GPU patch solver
 template <int D>
-class GpuDFTPatchSolver : public ThunderEgg::PatchSolver<D> {
+class GpuPatchSolver : public ThunderEgg::PatchSolver<D> {
  public:
-  explicit GpuDFTPatchSolver(const GpuStarPatchOperator<D>& op, int neumann_mask = 0)
-      : ThunderEgg::PatchSolver<D>(op.gpuDomain()->domain(), op.getGhostFiller()), gd_(op.gpuDomain()) {
-    te_patch_solver* h = nullptr;
-    check(te_dft_patch_solver_create(op.handle(), neumann_mask, &h));
-    h_ = std::shared_ptr<te_patch_solver>(h, [](te_patch_solver* x) { te_patch_solver_destroy(x); });
-  }
-  GpuDFTPatchSolver* clone() const override { return new GpuDFTPatchSolver(*this); }
   void apply(const ThunderEgg::Vector<D>& f, ThunderEgg::Vector<D>& u) const override {
     check(te_patch_solver_apply(h_.get(), u.getNumComponents(), TE_F64, levelPointer(f, *gd_),
                                 levelPointer(u, *gd_)));
@@ -328,13 +382,54 @@ class GpuDFTPatchSolver : public ThunderEgg::PatchSolver<D> {
   }
   void solveSinglePatch(const ThunderEgg::PatchInfo<D>&, const ThunderEgg::PatchView<const double, D>&,
                         const ThunderEgg::PatchView<double, D>&) const override {
-    throw ThunderEgg::RuntimeError("GpuDFTPatchSolver runs whole levels; use apply() or smooth()");
+    throw ThunderEgg::RuntimeError("GPU patch solvers run whole levels; use apply() or smooth()");
   }
   te_patch_solver* handle() const { return h_.get(); }
 
- private:
+ protected:
+  explicit GpuPatchSolver(const GpuStarPatchOperator<D>& op)
+      : ThunderEgg::PatchSolver<D>(op.gpuDomain()->domain(), op.getGhostFiller()), gd_(op.gpuDomain()) {}
+  void own(te_patch_solver* h) {
+    h_ = std::shared_ptr<te_patch_solver>(h, [](te_patch_solver* x) { te_patch_solver_destroy(x); });
+  }
   std::shared_ptr<GpuDomain<D>> gd_;
   std::shared_ptr<te_patch_solver> h_;
+};
+
+template <int D>
+class GpuDFTPatchSolver : public GpuPatchSolver<D> {
+ public:
+  // tc_precision (no reference counterpart): TE_TC_TF32X3 or TE_TC_BF16 for the FP32 tensor-core transforms
+  explicit GpuDFTPatchSolver(const GpuStarPatchOperator<D>& op, int neumann_mask = 0,
+                             int tc_precision = TE_TC_TF32X3)
+      : GpuPatchSolver<D>(op) {
+    te_patch_solver* h = nullptr;
+    check(te_dft_patch_solver_create_tc(op.handle(), neumann_mask, tc_precision, &h));
+    this->own(h);
+  }
+  GpuDFTPatchSolver* clone() const override { return new GpuDFTPatchSolver(*this); }
+};
+
+// Iterative::PatchSolver<D> (Iterative/PatchSolver.h:121-175) with an inner BiCGStab: every patch
+// solved by its own BiCGStab with internal Dirichlet conditions, one CTA per patch
+template <int D>
+class GpuBiCGStabPatchSolver : public GpuPatchSolver<D> {
+ public:
+  GpuBiCGStabPatchSolver(const GpuStarPatchOperator<D>& op, double tolerance = 1e-12, int max_iterations = 1000,
+                         bool continue_on_breakdown = false)
+      : GpuPatchSolver<D>(op) {
+    te_patch_solver* h = nullptr;
+    check(te_bicgstab_patch_solver_create(op.handle(), tolerance, max_iterations, continue_on_breakdown ? 1 : 0,
+                                          &h));
+    this->own(h);
+  }
+  // the reference's form: PatchSolver(const Iterative::Solver<D>& solver, const PatchOperator<D>& op,
+  // bool continue_on_breakdown) with the inner solver's tolerance and iteration limit
+  template <class InnerSolver>
+  GpuBiCGStabPatchSolver(const InnerSolver& solver, const GpuStarPatchOperator<D>& op,
+                         bool continue_on_breakdown = false)
+      : GpuBiCGStabPatchSolver(op, solver.getTolerance(), solver.getMaxIterations(), continue_on_breakdown) {}
+  GpuBiCGStabPatchSolver* clone() const override { return new GpuBiCGStabPatchSolver(*this); }
 };
 
 // Poisson::FFTWPatchSolver<D> (Poisson/FFTWPatchSolver.h:189-308) computes the
@@ -368,6 +463,7 @@ class GpuLinearRestrictor : public ThunderEgg::GMG::Restrictor<D> {
     if (keep_.size() > 4) keep_.erase(keep_.begin());
     return out.vec;
   }
+  te_restrictor* handle() const { return h_.get(); }
 
  private:
   std::shared_ptr<GpuDomain<D>> fine_, coarse_;
@@ -389,6 +485,7 @@ class GpuDirectInterpolator : public ThunderEgg::GMG::Interpolator<D> {
     check(te_interpolate(h_.get(), fine.getNumComponents(), TE_F64, levelPointer(coarse, *coarse_),
                          levelPointer(fine, *fine_)));
   }
+  te_interpolator* handle() const { return h_.get(); }
 
  private:
   std::shared_ptr<GpuDomain<D>> coarse_, fine_;
@@ -401,12 +498,19 @@ class GpuDirectInterpolator : public ThunderEgg::GMG::Interpolator<D> {
 // CycleBuilder::getCycle (GMG/CycleBuilder.h:176-191) makes for cycle_type
 // "W" / "F"
 // ---------------------------------------------------------------------------
+// what the GPU Krylov adapters need from a cycle used as Mr
+class GpuCycleHandle {
+ public:
+  virtual ~GpuCycleHandle() = default;
+  virtual te_cycle* handle() const = 0;
+};
+
 template <int D>
-class GpuVCycle : public ThunderEgg::Operator<D> {
+class GpuVCycle : public ThunderEgg::Operator<D>, public GpuCycleHandle {
  public:
   struct LevelParts {
     const GpuStarPatchOperator<D>* op;
-    const GpuDFTPatchSolver<D>* smoother;
+    const GpuPatchSolver<D>* smoother;
     te_restrictor* restrictor;      // null on the coarsest level
     te_interpolator* interpolator;  // null on the finest level
   };
@@ -440,11 +544,123 @@ class GpuVCycle : public ThunderEgg::Operator<D> {
   void apply(const ThunderEgg::Vector<D>& f, ThunderEgg::Vector<D>& u) const override {
     check(te_cycle_apply(h_.get(), u.getNumComponents(), levelPointer(f, *finest_), levelPointer(u, *finest_)));
   }
-  te_cycle* handle() const { return h_.get(); }
+  te_cycle* handle() const override { return h_.get(); }
 
  private:
   std::shared_ptr<GpuDomain<D>> finest_;
   std::shared_ptr<te_cycle> h_;
+};
+
+// ---------------------------------------------------------------------------
+// GMG::Cycle<D> on the GPU.  Built from a GMG::Level<D> chain whose parts are GPU
+// adapters -- the chain a GMG::CycleBuilder<D> makes when it is handed GPU parts
+// (CycleBuilder::getCycle()->getFinestLevel()), or the one GpuCycleBuilder<D> makes.
+// apply runs the whole cycle on the device (Cycle::apply, GMG/Cycle.h:94-98: u is
+// cleared, then the levels are visited); cycle_type "V", "W" or "F" as CycleOpts.
+// ---------------------------------------------------------------------------
+template <int D>
+class GpuCycle : public ThunderEgg::GMG::Cycle<D>, public GpuCycleHandle {
+ public:
+  // dtype TE_F32: the mixed-precision cycle (FP32 on every level, FP64 in and out)
+  GpuCycle(const ThunderEgg::GMG::Level<D>& finest, const ThunderEgg::GMG::CycleOpts& opts, int dtype = TE_F32)
+      : ThunderEgg::GMG::Cycle<D>(finest) {
+    std::vector<te_cycle_level> lv;
+    const ThunderEgg::GMG::Level<D>* level = &finest;
+    while (true) {
+      te_cycle_level t{};
+      const auto* op = dynamic_cast<const GpuStarPatchOperator<D>*>(&level->getOperator());
+      const auto* sm = dynamic_cast<const GpuPatchSolver<D>*>(&level->getSmoother());
+      if (!op || !sm) throw ThunderEgg::RuntimeError("GpuCycle needs GPU operators and patch solvers on every level");
+      t.op = op->handle();
+      t.smoother = sm->handle();
+      if (!level->finest()) {
+        const auto* in = dynamic_cast<const GpuDirectInterpolator<D>*>(&level->getInterpolator());
+        if (!in) throw ThunderEgg::RuntimeError("GpuCycle needs GpuDirectInterpolators");
+        t.interpolator = in->handle();
+      }
+      if (!level->coarsest()) {
+        const auto* rs = dynamic_cast<const GpuLinearRestrictor<D>*>(&level->getRestrictor());
+        if (!rs) throw ThunderEgg::RuntimeError("GpuCycle needs GpuLinearRestrictors");
+        t.restrictor = rs->handle();
+      }
+      if (lv.empty()) finest_ = op->gpuDomain();
+      lv.push_back(t);
+      if (level->coarsest()) break;
+      level = &level->getCoarser();
+    }
+    te_cycle* h = nullptr;
+    check(te_cycle_create(lv.data(), (int)lv.size(),
+                          te_cycle_opts{opts.pre_sweeps, opts.post_sweeps, opts.mid_sweeps, opts.coarse_sweeps},
+                          GpuVCycle<D>::cycle_type_of(opts.cycle_type), dtype, &h));
+    h_ = std::shared_ptr<te_cycle>(h, [](te_cycle* x) { te_cycle_destroy(x); });
+  }
+  GpuCycle* clone() const override { return new GpuCycle(*this); }
+  void apply(const ThunderEgg::Vector<D>& f, ThunderEgg::Vector<D>& u) const override {
+    check(te_cycle_apply(h_.get(), u.getNumComponents(), levelPointer(f, *finest_), levelPointer(u, *finest_)));
+  }
+  te_cycle* handle() const override { return h_.get(); }
+
+ protected:
+  void visit(const ThunderEgg::GMG::Level<D>&, const ThunderEgg::Vector<D>&, ThunderEgg::Vector<D>&) const override {
+    throw ThunderEgg::RuntimeError("GpuCycle visits its levels on the device; use apply()");
+  }
+
+ private:
+  std::shared_ptr<GpuDomain<D>> finest_;
+  std::shared_ptr<te_cycle> h_;
+};
+
+// GMG::CycleBuilder<D>'s interface and ordering rules (GMG/CycleBuilder.h:97-192) for GPU parts;
+// getCycle() returns a GpuCycle
+template <int D>
+class GpuCycleBuilder {
+ public:
+  explicit GpuCycleBuilder(const ThunderEgg::GMG::CycleOpts& opts, int dtype = TE_F32) : opts_(opts), dtype_(dtype) {}
+  void addFinestLevel(const ThunderEgg::Operator<D>& op, const ThunderEgg::GMG::Smoother<D>& smoother,
+                      const ThunderEgg::GMG::Restrictor<D>& restrictor) {
+    if (finest_) throw ThunderEgg::RuntimeError("addFinestLevel has already been called");
+    finest_ = std::make_shared<ThunderEgg::GMG::Level<D>>();
+    finest_->setOperator(op);
+    finest_->setSmoother(smoother);
+    finest_->setRestrictor(restrictor);
+    chain_.push_back(finest_);
+  }
+  void addIntermediateLevel(const ThunderEgg::Operator<D>& op, const ThunderEgg::GMG::Smoother<D>& smoother,
+                            const ThunderEgg::GMG::Restrictor<D>& restrictor,
+                            const ThunderEgg::GMG::Interpolator<D>& interpolator) {
+    if (!finest_) throw ThunderEgg::RuntimeError("addFinestLevel has not been called yet");
+    if (done_) throw ThunderEgg::RuntimeError("addCoarsestLevel has already been called");
+    auto lv = std::make_shared<ThunderEgg::GMG::Level<D>>();
+    lv->setOperator(op);
+    lv->setSmoother(smoother);
+    lv->setRestrictor(restrictor);
+    lv->setInterpolator(interpolator);
+    chain_.push_back(lv);
+  }
+  void addCoarsestLevel(const ThunderEgg::Operator<D>& op, const ThunderEgg::GMG::Smoother<D>& smoother,
+                        const ThunderEgg::GMG::Interpolator<D>& interpolator) {
+    if (!finest_) throw ThunderEgg::RuntimeError("addFinestLevel has not been called yet");
+    if (done_) throw ThunderEgg::RuntimeError("addCoarsestLevel has already been called");
+    auto lv = std::make_shared<ThunderEgg::GMG::Level<D>>();
+    lv->setOperator(op);
+    lv->setSmoother(smoother);
+    lv->setInterpolator(interpolator);
+    chain_.push_back(lv);
+    done_ = true;
+  }
+  std::shared_ptr<ThunderEgg::GMG::Cycle<D>> getCycle() const {
+    if (!done_) throw ThunderEgg::RuntimeError("Cycle is not finalized: addCoarsestLevel has not been called");
+    // each level points to the next coarser one (Level::setCoarser, as CycleBuilder does)
+    for (size_t k = chain_.size() - 1; k > 0; k--) chain_[k - 1]->setCoarser(chain_[k]);
+    return std::make_shared<GpuCycle<D>>(*finest_, opts_, dtype_);
+  }
+
+ private:
+  ThunderEgg::GMG::CycleOpts opts_;
+  int dtype_;
+  std::shared_ptr<ThunderEgg::GMG::Level<D>> finest_;
+  std::vector<std::shared_ptr<ThunderEgg::GMG::Level<D>>> chain_;
+  bool done_ = false;
 };
 
 // ---------------------------------------------------------------------------
@@ -462,8 +678,8 @@ class GpuBiCGStab : public ThunderEgg::Iterative::Solver<D> {
             std::ostream& os = std::cout) const override {
     const auto* op = dynamic_cast<const GpuStarPatchOperator<D>*>(&A);
     if (!op) throw ThunderEgg::RuntimeError("GpuBiCGStab needs a GpuStarPatchOperator");
-    const auto* cyc = Mr ? dynamic_cast<const GpuVCycle<D>*>(Mr) : nullptr;
-    if (Mr && !cyc) throw ThunderEgg::RuntimeError("GpuBiCGStab needs a GpuVCycle (or no) preconditioner");
+    const auto* cyc = Mr ? dynamic_cast<const GpuCycleHandle*>(Mr) : nullptr;
+    if (Mr && !cyc) throw ThunderEgg::RuntimeError("GpuBiCGStab needs a GPU cycle (or no) preconditioner");
     if (output) return solvePrinting(*op, x, b, cyc, os);
     int its = 0;
     double res = 0;
@@ -478,7 +694,7 @@ class GpuBiCGStab : public ThunderEgg::Iterative::Solver<D> {
   // before the first iteration and after each, from a resumable batch of one solve
   // advanced one iteration at a time
   int solvePrinting(const GpuStarPatchOperator<D>& op, ThunderEgg::Vector<D>& x, const ThunderEgg::Vector<D>& b,
-                    const GpuVCycle<D>* cyc, std::ostream& os) const {
+                    const GpuCycleHandle* cyc, std::ostream& os) const {
     const int offs[2] = {0, op.gpuDomain()->domain().getNumLocalPatches()};
     te_bicgstab_batch* h = nullptr;
     check(te_bicgstab_batch_create(op.handle(), x.getNumComponents(), levelPointer(x, *op.gpuDomain()),
@@ -526,13 +742,41 @@ class GpuCG : public ThunderEgg::Iterative::Solver<D> {
             std::ostream& os = std::cout) const override {
     const auto* op = dynamic_cast<const GpuStarPatchOperator<D>*>(&A);
     if (!op) throw ThunderEgg::RuntimeError("GpuCG needs a GpuStarPatchOperator");
-    const auto* cyc = Mr ? dynamic_cast<const GpuVCycle<D>*>(Mr) : nullptr;
-    if (Mr && !cyc) throw ThunderEgg::RuntimeError("GpuCG needs a GpuVCycle (or no) preconditioner");
+    const auto* cyc = Mr ? dynamic_cast<const GpuCycleHandle*>(Mr) : nullptr;
+    if (Mr && !cyc) throw ThunderEgg::RuntimeError("GpuCG needs a GPU cycle (or no) preconditioner");
     int its = 0;
     double res = 0;
     check(te_cg_solve(op->handle(), x.getNumComponents(), levelPointer(x, *op->gpuDomain()),
                       levelPointer(b, *op->gpuDomain()), cyc ? cyc->handle() : nullptr, tolerance, max_iterations,
                       &its, &res));
+    if (output) {
+      char buf[64];
+      std::snprintf(buf, sizeof buf, "%5d %16.8e\n", its, res);
+      os << buf;
+    }
+    return its;
+  }
+};
+
+// FP64 iterative refinement around a GPU cycle (te_ir_solve; no reference counterpart):
+// x += Mr (b - A x) until the true FP64 residual ||b - A x|| / ||b|| <= tolerance
+template <int D>
+class GpuIterativeRefinement : public ThunderEgg::Iterative::Solver<D> {
+ public:
+  double tolerance = 1e-10;
+  int max_iterations = 200;
+  GpuIterativeRefinement* clone() const override { return new GpuIterativeRefinement(*this); }
+  int solve(const ThunderEgg::Operator<D>& A, ThunderEgg::Vector<D>& x, const ThunderEgg::Vector<D>& b,
+            const ThunderEgg::Operator<D>* Mr = nullptr, bool output = false,
+            std::ostream& os = std::cout) const override {
+    const auto* op = dynamic_cast<const GpuStarPatchOperator<D>*>(&A);
+    if (!op) throw ThunderEgg::RuntimeError("GpuIterativeRefinement needs a GpuStarPatchOperator");
+    const auto* cyc = Mr ? dynamic_cast<const GpuCycleHandle*>(Mr) : nullptr;
+    if (!cyc) throw ThunderEgg::RuntimeError("GpuIterativeRefinement needs a GPU cycle as Mr");
+    int its = 0;
+    double res = 0;
+    check(te_ir_solve(op->handle(), x.getNumComponents(), levelPointer(x, *op->gpuDomain()),
+                      levelPointer(b, *op->gpuDomain()), cyc->handle(), tolerance, max_iterations, &its, &res));
     if (output) {
       char buf[64];
       std::snprintf(buf, sizeof buf, "%5d %16.8e\n", its, res);

@@ -150,6 +150,27 @@ class Oracle:
                                             cont, mode, ncomp, _ptr(f), _ptr(u), ctypes.byref(its)))
         return u, its.value
 
+    # -- right-hand-side boundary helpers ---------------------------------------------
+    _point_fn = ctypes.CFUNCTYPE(ctypes.c_double, ctypes.POINTER(ctypes.c_double))
+
+    def add_bc_to_rhs(self, lvl, f, gfun=None, hfun=None, grad=None, kind=0, neumann=0):
+        """addDrichletBCToRHS (kind 0 Poisson, 1 VarPoisson with coefficient hfun) or, with
+        neumann=1, Poisson's addNeumannBCToRHS (grad: one function per axis).  Each function
+        takes the point's coordinates x, y[, z] as floats."""
+        D = lvl.dim
+        f = np.ascontiguousarray(f, dtype=np.float64).copy()
+
+        def wrap(fn):
+            if fn is None:
+                return self._point_fn(0)
+            return self._point_fn(lambda x: float(fn(*[x[a] for a in range(D)])))
+
+        keep = [wrap(gfun), wrap(hfun)] + [wrap(g) for g in (grad or [None] * D)]
+        garr = (self._point_fn * D)(*keep[2:])
+        d = lvl.to_desc()
+        self._check(self._f("add_bc_to_rhs")(ctypes.byref(d), kind, neumann, keep[0], keep[1], garr, _ptr(f)))
+        return f
+
     # -- transfers -------------------------------------------------------------
     def restrict(self, fine, coarse, vf, extrapolate=0, ncomp=1):
         vf = np.ascontiguousarray(vf, dtype=np.float64)

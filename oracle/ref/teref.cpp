@@ -27,6 +27,7 @@
 
 #include <array>
 #include <cstring>
+#include <functional>
 #include <memory>
 #include <stdexcept>
 #include <type_traits>
@@ -34,88 +35,17 @@
 #include <vector>
 
 #include "thunderegg_gb300/adapters.hpp"
+#include "teref_domain.hpp"
 
 using namespace ThunderEgg;
 
 namespace {
 std::string g_err;
 
-int slots(int D) { return D == 2 ? 8 : 26; }
-
-template <int D, int M>
-void set_face_nbrs(PatchInfo<D>& pi, const te_level_desc* d, int p, int slot0) {
-  for (int f = 0; f < (int)Face<D, M>::number_of; f++) {
-    int slot = slot0 + f;
-    size_t k = (size_t)p * slots(D) + slot;
-    int t = d->nbr_type[k];
-    const int* ids = d->nbr_ids + k * 4;
-    Face<D, M> face((unsigned char)f);
-    if (t == TE_NBR_NORMAL) {
-      pi.setNbrInfo(face, new NormalNbrInfo<M>(ids[0]));
-    } else if (t == TE_NBR_COARSE) {
-      pi.setNbrInfo(face, new CoarseNbrInfo<M>(ids[0], Orthant<M>((unsigned char)d->nbr_orth[k])));
-    } else if (t == TE_NBR_FINE) {
-      std::array<int, Orthant<M>::num_orthants> a;
-      for (size_t i = 0; i < a.size(); i++) a[i] = ids[i];
-      pi.setNbrInfo(face, new FineNbrInfo<M>(a));
-    }
-  }
-}
-
-template <int D>
-Domain<D> make_domain(const te_level_desc* d, int domain_id = 0) {
-  std::vector<PatchInfo<D>> pinfos(d->num_patches);
-  std::array<int, D> ns;
-  for (int a = 0; a < D; a++) ns[a] = d->ns[a];
-  for (int p = 0; p < d->num_patches; p++) {
-    PatchInfo<D>& pi = pinfos[p];
-    pi.id = d->id[p];
-    pi.rank = 0;
-    pi.refine_level = d->refine_level[p];
-    pi.parent_id = d->parent_id[p];
-    pi.parent_rank = d->parent_id[p] >= 0 ? 0 : -1;
-    pi.orth_on_parent = d->orth_on_parent[p] >= 0 ? Orthant<D>((unsigned char)d->orth_on_parent[p])
-                                                  : Orthant<D>::null();
-    for (int c = 0; c < (1 << D); c++) {
-      pi.child_ids[c] = d->child_ids[(size_t)p * (1 << D) + c];
-      pi.child_ranks[c] = pi.child_ids[c] >= 0 ? 0 : -1;
-    }
-    pi.num_ghost_cells = d->num_ghost;
-    pi.ns = ns;
-    for (int a = 0; a < D; a++) {
-      pi.starts[a] = d->starts[(size_t)p * D + a];
-      pi.spacings[a] = d->spacings[(size_t)p * D + a];
-    }
-    if constexpr (D == 2) {
-      set_face_nbrs<2, 0>(pi, d, p, 0);
-      set_face_nbrs<2, 1>(pi, d, p, 4);
-    } else {
-      set_face_nbrs<3, 0>(pi, d, p, 0);
-      set_face_nbrs<3, 1>(pi, d, p, 8);
-      set_face_nbrs<3, 2>(pi, d, p, 20);
-    }
-  }
-  return Domain<D>(Communicator(MPI_COMM_WORLD), domain_id, ns, d->num_ghost, pinfos.begin(),
-                   pinfos.end());
-}
-
-// Vector aliasing a caller buffer (Vector.h:199-215, unmanaged constructor)
-template <int D>
-Vector<D> wrap(const Domain<D>& dom, int nc, double* data) {
-  std::array<int, D + 1> strides, lengths;
-  int st = 1;
-  for (int a = 0; a < D; a++) {
-    strides[a] = st;
-    lengths[a] = dom.getNs()[a];
-    st *= dom.getNs()[a] + 2 * dom.getNumGhostCells();
-  }
-  strides[D] = st;
-  lengths[D] = nc;
-  long ps = (long)st * nc;
-  std::vector<double*> starts(dom.getNumLocalPatches());
-  for (size_t i = 0; i < starts.size(); i++) starts[i] = data + i * ps;
-  return Vector<D>(Communicator(MPI_COMM_WORLD), starts, strides, lengths, dom.getNumGhostCells());
-}
+using teref_tables::make_domain;
+using teref_tables::set_face_nbrs;
+using teref_tables::slots;
+using teref_tables::wrap;
 template <int D>
 void copy_out(const Vector<D>& v, double* out) {
   // copy every cell (ghosts included) of a managed vector into a flat buffer
@@ -465,6 +395,46 @@ int teref_gmg_solve(const te_level_desc* levels, int nlevels, const teo_gmg_conf
 // Domain<D> built by ThunderEgg from the tables, flattened again by the C++
 // adapters' thunderegg_gb300::flatten (include/thunderegg_gb300/adapters.hpp):
 // the round trip the adapters rely on.  Output arrays have the input's sizes.
+// the reference's own right-hand-side boundary helpers (Poisson/StarPatchOperator.h:187-242,
+// VarPoisson/StarPatchOperator.h:194-219) with C callbacks as the boundary data
+int teref_add_bc_to_rhs(const te_level_desc* d, int kind, int neumann, teo_point_fn gfun, teo_point_fn hfun,
+                        const teo_point_fn* grad, double* f) {
+  return guard([&] {
+    auto run = [&](auto dom, auto tag) {
+      constexpr int D = decltype(tag)::value;
+      auto wrapfn = [](teo_point_fn fn) {
+        return std::function<double(const std::array<double, D>&)>(
+            [fn](const std::array<double, D>& x) { return fn(x.data()); });
+      };
+      auto gf = make_filler<D>(dom, TE_GHOST_BILINEAR + (D == 3 ? 2 : 0), TE_FILL_FACES);
+      Vector<D> fv = wrap<D>(dom, 1, f);
+      if (kind == 0) {
+        Poisson::StarPatchOperator<D> op(dom, *gf);
+        if (neumann) {
+          std::array<std::function<double(const std::array<double, D>&)>, D> g;
+          for (int a = 0; a < D; a++) g[a] = wrapfn(grad[a]);
+          op.addNeumannBCToRHS(fv, wrapfn(gfun), g);
+        } else {
+          op.addDrichletBCToRHS(fv, wrapfn(gfun));
+        }
+      } else {
+        std::vector<double> ones((size_t)dom.getNumLocalPatches() * [&] {
+          long s = 1;
+          for (int a = 0; a < D; a++) s *= dom.getNs()[a] + 2 * dom.getNumGhostCells();
+          return s;
+        }(), 1.0);
+        Vector<D> c = wrap<D>(dom, 1, ones.data());
+        VarPoisson::StarPatchOperator<D> op(c, dom, *gf);
+        op.addDrichletBCToRHS(fv, wrapfn(gfun), wrapfn(hfun));
+      }
+    };
+    if (d->dim == 2)
+      run(make_domain<2>(d), std::integral_constant<int, 2>());
+    else
+      run(make_domain<3>(d), std::integral_constant<int, 3>());
+  });
+}
+
 int teref_flatten_roundtrip(const te_level_desc* in, int* id, int* refine_level, int* parent_id,
                             int* orth_on_parent, int* child_ids, double* starts, double* spacings, int* nbr_type,
                             int* nbr_ids, int* nbr_orth) {

@@ -1243,6 +1243,61 @@ int teo_modify_rhs(const te_level_desc* d, int scheme, int fill_type, int kind, 
   });
 }
 
+// Right-hand-side boundary helpers: Poisson::StarPatchOperator::addDrichletBCToRHS
+// (Poisson/StarPatchOperator.h:187-204) and addNeumannBCToRHS (:212-242),
+// VarPoisson::StarPatchOperator::addDrichletBCToRHS (VarPoisson/StarPatchOperator.h:194-219).
+// Every side without a neighbour, in side order, adds to the interior cells next to it a
+// term of the boundary data at the point DomainTools::GetRealCoordBound gives
+// (DomainTools.h:179-210): the side's own coordinate on the boundary, the cell centre in
+// the other directions.  kind 0 Poisson, 1 VarPoisson (hfun = coefficient); neumann = 1
+// adds the Neumann terms (Poisson only) from grad[axis].
+int teo_add_bc_to_rhs(const te_level_desc* d, int kind, int neumann, teo_point_fn gfun, teo_point_fn hfun,
+                      const teo_point_fn* grad, double* f) {
+  return guard([&] {
+    Level L(d);
+    const int D = L.D;
+    for (int p = 0; p < L.P; p++) {
+      double* fp = f + p * L.pstride(1);
+      for (int side = 0; side < 2 * D; side++) {
+        if (L.has(p, D - 1, side)) continue;
+        const int axis = side >> 1, upper = side & 1;
+        const double h = L.h(p, axis);
+        const double h2 = std::pow(h, 2);
+        const int t0 = axis == 0 ? 1 : 0, t1 = axis == 2 ? 1 : 2;
+        const int m0 = L.n[t0], m1 = D == 3 ? L.n[t1] : 1;
+        for (int j = 0; j < m1; j++)
+          for (int i = 0; i < m0; i++) {
+            double x[3] = {0, 0, 0};
+            int c[3] = {0, 0, 0};
+            for (int a = 0; a < D; a++) {
+              if (a == axis) {
+                x[a] = upper ? L.starts[(size_t)p * D + a] + L.spacings[(size_t)p * D + a] * L.n[a]
+                             : L.starts[(size_t)p * D + a];
+                c[a] = upper ? L.n[a] - 1 : 0;
+              } else {
+                const int k = a == t0 ? i : j;
+                x[a] = L.starts[(size_t)p * D + a] + L.spacings[(size_t)p * D + a] / 2.0 +
+                       L.spacings[(size_t)p * D + a] * k;
+                c[a] = k;
+              }
+            }
+            double& cell = fp[L.at(c[0], c[1], c[2], 0)];
+            if (neumann) {
+              if (!upper)
+                cell += grad[axis](x) / h;
+              else
+                cell -= grad[axis](x) / h;
+            } else if (kind == 0) {
+              cell += -2.0 * gfun(x) / h2;
+            } else {
+              cell -= 2 * gfun(x) * hfun(x) / h2;
+            }
+          }
+      }
+    }
+  });
+}
+
 // smoother: 0 DFT, 1 BiCGStab patch solver; mode 0 smooth, 1 apply
 int teo_patch_solver(const te_level_desc* d, int scheme, int fill_type, int kind, const double* coeffs,
                      int smoother, int dft_neumann_mask, double tol, int max_it, int cont, int mode, int nc,

@@ -28,6 +28,10 @@ typedef struct teo_gmg_config {
                              reference's alpha*p (te_gpu.h flag
                              TE_BICGSTAB_PRECONDITIONED_EXIT); 0 = reference */
 } teo_gmg_config;
+
+/* A function of a point of the domain (x[0..D-1]): the boundary data of the
+ * right-hand-side helpers (addDrichletBCToRHS / addNeumannBCToRHS). */
+typedef double (*teo_point_fn)(const double* x);
 #ifdef __cplusplus
 }
 #endif

@@ -21,5 +21,13 @@ template class thunderegg_gb300::GpuBiCGStab<2>;
 template class thunderegg_gb300::GpuBiCGStab<3>;
 template class thunderegg_gb300::GpuCG<2>;
 template class thunderegg_gb300::GpuCG<3>;
+template class thunderegg_gb300::GpuBiCGStabPatchSolver<2>;
+template class thunderegg_gb300::GpuBiCGStabPatchSolver<3>;
+template class thunderegg_gb300::GpuCycle<2>;
+template class thunderegg_gb300::GpuCycle<3>;
+template class thunderegg_gb300::GpuCycleBuilder<2>;
+template class thunderegg_gb300::GpuCycleBuilder<3>;
+template class thunderegg_gb300::GpuIterativeRefinement<2>;
+template class thunderegg_gb300::GpuIterativeRefinement<3>;
 template thunderegg_gb300::LevelTables<2> thunderegg_gb300::flatten<2>(const ThunderEgg::Domain<2>&);
 template thunderegg_gb300::LevelTables<3> thunderegg_gb300::flatten<3>(const ThunderEgg::Domain<3>&);

@@ -215,3 +215,51 @@ def test_fftw_patch_solver_is_the_dft_solve(te, oracle):
             s.smooth(te.Vector.from_numpy(dom, f, dtype=dt), uv)
             inner = (Ellipsis, slice(1, -1), slice(1, -1))
             assert rel_err(uv.numpy()[inner], want[inner]) <= tol, (mask, dt)
+
+
+def _bc_cases():
+    from thunderegg_gb300 import mesh as M
+
+    return [M.circle_mesh(n=8, lo=2, hi=4)[0], M.random_mesh(4, n=5, lo=1, hi=4)[0],
+            M.random_mesh(5, n=4, dim=3, lo=1, hi=3)[0]]
+
+
+@pytest.mark.parametrize("idx", range(3))
+def test_bc_rhs_helpers_match_oracle(te, oracle, idx):
+    """addDrichletBCToRHS / addNeumannBCToRHS (Poisson) and VarPoisson's addDrichletBCToRHS on the
+    device: bit for bit the oracle's FP64 result (pinned bit-exact to the reference) for polynomial
+    boundary data; exp(x y) data within 1e-15 (numpy's vectorised exp may differ by an ulp)."""
+    lv = _bc_cases()[idx]
+    D = lv.dim
+    dom = te.Domain(lv)
+    gf = [te.BiQuadraticGhostFiller, te.TriLinearGhostFiller][D - 2](dom)  # BiLinear needs even n
+    if D == 2:
+        g = lambda x, y: 1.5 + x * x - 0.25 * x * y + y  # noqa: E731
+        grad = [lambda x, y: 2 * x - 0.25 * y, lambda x, y: 1.0 - 0.25 * x]
+        gexp = lambda x, y: np.exp(x * y)  # noqa: E731
+        coef = lambda x, y: 1 + 0.5 * x  # noqa: E731
+    else:
+        g = lambda x, y, z: 1 + x * y - z * z + 0.5 * x  # noqa: E731
+        grad = [lambda x, y, z: y + 0.5, lambda x, y, z: x, lambda x, y, z: -2 * z]
+        gexp = lambda x, y, z: np.exp(x * y * z)  # noqa: E731
+        coef = lambda x, y, z: 1 + 0.5 * x * z  # noqa: E731
+    f = np.random.default_rng(60 + idx).standard_normal(lv.padded_shape(1))
+    op = te.PoissonStarPatchOperator(dom, gf)
+    cvec = te.Vector.from_numpy(dom, np.ones(lv.padded_shape(1)))
+    vop = te.VarPoissonStarPatchOperator(cvec, dom, gf)
+    cases = [("dirichlet", lambda v: op.addDrichletBCToRHS(v, g), dict(gfun=g), True),
+             ("dirichlet exp", lambda v: op.addDrichletBCToRHS(v, gexp), dict(gfun=gexp), False),
+             ("neumann", lambda v: op.addNeumannBCToRHS(v, g, grad), dict(gfun=g, grad=grad, neumann=1), True),
+             ("varpoisson", lambda v: vop.addDrichletBCToRHS(v, g, coef), dict(gfun=g, hfun=coef, kind=1), True)]
+    for name, run, kw, exact in cases:
+        want = oracle.add_bc_to_rhs(lv, f, **kw)
+        v = te.Vector.from_numpy(dom, f)
+        run(v)
+        got = v.numpy()
+        if exact:
+            assert np.array_equal(got, want), name
+        else:
+            assert rel_err(got, want) <= 1e-15, name
+        v32 = te.Vector.from_numpy(dom, f, dtype=te.TE_F32)
+        run(v32)
+        assert rel_err(v32.numpy(), want) <= 2e-6, name

@@ -162,3 +162,26 @@ def test_serving_slot_fill(te):
     assert results[5].restarts == 0
     assert all(results[i].restarts == 0 for i in range(5)) or srv.stats["reforms"] > 1
     _check(te, reqs, results)
+
+
+def test_serving_packs_depths_into_one_class(te):
+    """Solves of one patch size but different depths (uniform L1, L3 and a circle mesh of five
+    levels) form one class: the union pads the shallower hierarchies with copies of their
+    coarsest level, every result still matches its solo solve."""
+    from thunderegg_gb300 import mesh as M
+    from thunderegg_gb300 import problems as PB
+    from thunderegg_gb300.gmg import GmgOptions
+    from thunderegg_gb300.serve import Request, Server
+
+    rng = np.random.default_rng(41)
+    opts = GmgOptions(scheme=1, smoother=0, cycle_dtype=te.TE_F32, bicgstab_flags=1)
+    meshes = [M.uniform_mesh(2, 1, 16), M.uniform_mesh(2, 3, 16), M.circle_mesh(n=16, lo=2, hi=4)]
+    assert len({len(m) for m in meshes}) == 3
+    reqs = [Request(m, PB.sine_modes_rhs(m[0], rng), opts) for m in meshes for _ in range(2)]
+    with Server(budget_bytes=50e9, steps_per_round=2) as srv:
+        for r in reqs:
+            srv.submit(r)
+        res = srv.run()
+        assert len(srv.classes) == 1
+        assert srv.stats["max_batch"] >= len(reqs)
+    _check(te, reqs, res)

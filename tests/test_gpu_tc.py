@@ -227,3 +227,50 @@ def test_tc_w_and_fmg_cycles(te, oracle, name, cycle_type):
     uv3 = te.Vector(s3.finest)
     s3.solve(fv, uv3)
     assert s3.residual(fv, uv3) <= 1e-10
+
+
+def test_tc_kernel_variants_give_the_same_bits(te, monkeypatch):
+    """The autotuner may run the 3xTF32 solve with its operands in shared memory or in tensor
+    memory, at any resident-CTA count: every choice computes the same products in the same order,
+    so results are bit-identical (which keeps a batched solve equal to the same solve alone)."""
+    from thunderegg_gb300 import mesh as M
+
+    outs = []
+    for mode in ("smem", "tmem"):
+        monkeypatch.setenv("TE_TC_OPERANDS", mode)
+        for levels in (M.circle_mesh(n=32, lo=2, hi=4), M.uniform_mesh(3, 1, 16)):
+            lv = levels[0]
+            dom = te.Domain(lv)
+            sc = 1 if lv.dim == 2 else 2
+            op = te.PoissonStarPatchOperator(dom, _filler(te, sc)(dom))
+            ps = te.DFTPatchSolver(op)
+            f = np.random.default_rng(80 + lv.dim).standard_normal(lv.padded_shape(1))
+            u = te.Vector(dom, 1, te.TE_F32)
+            ps.apply(te.Vector.from_numpy(dom, f, dtype=te.TE_F32), u)
+            outs.append(u.numpy())
+    assert np.array_equal(outs[0], outs[2]) and np.array_equal(outs[1], outs[3])
+
+
+def test_autotuner_report(te):
+    """After a tensor-core solve the tuner names its choice per shape, with every candidate's time."""
+    import ctypes
+    import json
+
+    from thunderegg_gb300 import mesh as M
+
+    lv = M.uniform_mesh(2, 4, 32)[0]
+    dom = te.Domain(lv)
+    op = te.PoissonStarPatchOperator(dom, te.BiLinearGhostFiller(dom))
+    ps = te.DFTPatchSolver(op)
+    u = te.Vector(dom, 1, te.TE_F32)
+    ps.apply(te.Vector.from_numpy(dom, np.ones(lv.padded_shape(1)), dtype=te.TE_F32), u)
+    need = ctypes.c_int(0)
+    te.capi.check(te.capi.lib().te_tune_report(None, 0, ctypes.byref(need)))
+    buf = ctypes.create_string_buffer(need.value)
+    te.capi.check(te.capi.lib().te_tune_report(buf, need.value, ctypes.byref(need)))
+    rep = json.loads(buf.value.decode())
+    mine = [r for r in rep if "|dft_tc|D=2 n=32 P~2^8 " in r["key"]]
+    assert mine, rep
+    r = mine[0]
+    assert r["choice"] in r["ms"] and len(r["ms"]) >= 2
+    assert all(v is None or v > 0 for v in r["ms"].values())

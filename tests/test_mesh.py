@@ -218,3 +218,27 @@ def test_reference_reads_written_json(make, tmp_path):
         outs["nbr_orth"][coarse_corner] = lv.nbr_orth[coarse_corner]
         for name, a in outs.items():
             assert np.array_equal(a, np.asarray(getattr(lv, name))), name
+
+
+def test_pad_hierarchy_copies_the_coarsest_level():
+    """pad_hierarchy extends a hierarchy with copied levels: the old coarsest patches point to
+    themselves with a null orthant, each copy has that patch as its only child; a padded
+    hierarchy joins a deeper one in a union."""
+    shallow, deep = M.uniform_mesh(2, 1, 8), M.circle_mesh(n=8, lo=2, hi=4)
+    padded = M.pad_hierarchy(shallow, len(deep))
+    assert len(padded) == len(deep)
+    for k in range(len(shallow) - 1):
+        assert np.array_equal(padded[k].parent_id, shallow[k].parent_id)
+    for k in range(len(shallow) - 1, len(deep)):
+        lv = padded[k]
+        assert np.array_equal(lv.id, shallow[-1].id) and np.array_equal(lv.nbr_type, shallow[-1].nbr_type)
+        if k + 1 < len(deep):
+            assert np.array_equal(lv.parent_id, lv.id) and np.all(lv.orth_on_parent == -1)
+        else:
+            assert np.all(lv.parent_id == -1)
+        if k >= len(shallow):
+            assert np.array_equal(lv.child_ids[:, 0], lv.id) and np.all(lv.child_ids[:, 1:] == -1)
+    levels, offsets = M.union_hierarchy([padded, deep])
+    assert [lv.num_patches for lv in levels] == [a.num_patches + b.num_patches for a, b in zip(padded, deep)]
+    with pytest.raises(ValueError):
+        M.pad_hierarchy(deep, 2)

@@ -183,3 +183,37 @@ def test_oracle_matches_reference_live_operators_and_transfers(oracle, ref):
         cfg = gmg_config(scheme=sc, op_kind=1, smoother=1, tol=1e-9, max_it=100)
         a, b = oracle.solve(levels, f, cfg, coeffs=coeffs), ref.solve(levels, f, cfg, coeffs=coeffs)
         assert a[1] == b[1] and a[3] == b[3] and np.array_equal(a[0][inner], b[0][inner]), sc
+
+
+def _bc_meshes():
+    from thunderegg_gb300 import mesh as M
+
+    return [M.circle_mesh(n=8, lo=2, hi=4)[0], M.random_mesh(4, n=5, lo=1, hi=4)[0],
+            M.random_mesh(5, n=4, dim=3, lo=1, hi=3)[0]]
+
+
+# boundary data: a polynomial (exactly the same in every evaluation order) and a transcendental one
+_BC_FUNCS = {
+    2: (lambda x, y: 1.5 + x * x - 0.25 * x * y + y, lambda x, y: 2 * x - 0.25 * y, lambda x, y: 1.0 - 0.25 * x,
+        lambda x, y: np.exp(x * y)),
+    3: (lambda x, y, z: 1 + x * y - z * z + 0.5 * x, lambda x, y, z: y + 0.5, lambda x, y, z: x,
+        lambda x, y, z: np.exp(x * y * z)),
+}
+
+
+@pytest.mark.parametrize("idx", range(3))
+def test_oracle_bc_rhs_helpers_match_reference_live(oracle, ref, idx):
+    """addDrichletBCToRHS / addNeumannBCToRHS (Poisson) and VarPoisson's addDrichletBCToRHS:
+    the restatement adds the same terms to the same cells in the same order as the reference."""
+    lv = _bc_meshes()[idx]
+    D = lv.dim
+    g, *grad, gexp = _BC_FUNCS[D]
+    if D == 3:
+        grad = [lambda x, y, z: y + 0.5, lambda x, y, z: x, lambda x, y, z: -2 * z]
+    coef = (lambda x, y: 1 + 0.5 * x) if D == 2 else (lambda x, y, z: 1 + 0.5 * x * z)
+    f = np.random.default_rng(50 + idx).standard_normal(lv.padded_shape(1))
+    for kw in (dict(gfun=g), dict(gfun=gexp), dict(gfun=g, grad=grad, neumann=1), dict(gfun=g, hfun=coef, kind=1)):
+        want = ref.add_bc_to_rhs(lv, f, **kw)
+        got = oracle.add_bc_to_rhs(lv, f, **kw)
+        assert np.array_equal(got, want), kw.keys()
+        assert not np.array_equal(got, f)

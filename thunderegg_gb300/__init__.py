@@ -38,7 +38,7 @@ from .capi import (TE_F32, TE_F64, TE_FILL_CORNERS, TE_FILL_EDGES, TE_FILL_FACES
 __all__ = ["Domain", "Vector", "BiLinearGhostFiller", "BiQuadraticGhostFiller", "TriLinearGhostFiller",
            "PoissonStarPatchOperator", "VarPoissonStarPatchOperator", "DFTPatchSolver",
            "BiCGStabPatchSolver", "LinearRestrictor", "DirectInterpolator", "CycleOpts", "CycleBuilder",
-           "BiCGStab", "CG", "Cycle", "FFTWPatchSolver", "BreakdownError", "TeError", "mesh", "capi",
+           "BiCGStab", "CG", "IterativeRefinement", "Cycle", "FFTWPatchSolver", "BreakdownError", "TeError", "mesh", "capi",
            "GhostFillingType", "TE_F32", "TE_F64", "TE_FILL_FACES", "TE_FILL_EDGES", "TE_FILL_CORNERS"]
 
 
@@ -256,6 +256,23 @@ class _Operator(_Handle):
     def getGhostFiller(self):
         return self.ghost_filler
 
+    def _boundary_values(self, *fns):
+        """The functions evaluated at the boundary points (DomainTools::GetRealCoordBound),
+        as device FP64 arrays [P][2D][face stride].  Each function takes the coordinate
+        arrays x, y[, z] (numpy) and returns values of their shape."""
+        torch = _torch()
+        dom = self.domain
+        D = dom.dim
+        fs = int(lib().te_domain_face_stride(dom.h))
+        pts = torch.empty((dom.level.num_patches, 2 * D, fs, D), dtype=torch.float64, device="cuda")
+        check(lib().te_domain_boundary_points(dom.h, ctypes.c_void_p(pts.data_ptr())))
+        X = pts.cpu().numpy()
+        out = []
+        for fn in fns:
+            v = np.broadcast_to(np.asarray(fn(*[X[..., a] for a in range(D)]), dtype=np.float64), X.shape[:-1])
+            out.append(torch.from_numpy(np.array(v, dtype=np.float64)).cuda())
+        return out
+
 
 class PoissonStarPatchOperator(_Operator):
     """Poisson::StarPatchOperator (Poisson/StarPatchOperator.h:52-63)."""
@@ -265,6 +282,26 @@ class PoissonStarPatchOperator(_Operator):
         _bind_stream()
         self.domain, self.ghost_filler = domain, ghost_filler
         check(lib().te_poisson_operator_create(domain.h, ghost_filler.h, int(neumann), ctypes.byref(self.h)))
+
+    def addDrichletBCToRHS(self, f: Vector, gfunc):
+        """Poisson/StarPatchOperator.h:187-204: f += -2 g(x_b) / h^2 next to every domain-boundary
+        side, on the device; gfunc(x, y[, z]) takes numpy coordinate arrays."""
+        (g,) = self._boundary_values(gfunc)
+        check(lib().te_operator_add_dirichlet_bc_to_rhs(self.h, f.dtype, f.ptr, ctypes.c_void_p(g.data_ptr()), None))
+        _torch().cuda.current_stream().synchronize()
+
+    def addNeumannBCToRHS(self, f: Vector, gfunc, gfunc_grad):
+        """Poisson/StarPatchOperator.h:212-242: f += dg/dn / h (lower sides), -= (upper sides);
+        gfunc_grad[axis](x, y[, z]) is the derivative of gfunc along that axis (gfunc itself is
+        not used, as in the reference)."""
+        D = self.domain.dim
+        vals = self._boundary_values(*gfunc_grad)
+        # the derivative along each side's own axis
+        sel = vals[0].clone()
+        for side in range(2 * D):
+            sel[:, side] = vals[side >> 1][:, side]
+        check(lib().te_operator_add_neumann_bc_to_rhs(self.h, f.dtype, f.ptr, ctypes.c_void_p(sel.data_ptr())))
+        _torch().cuda.current_stream().synchronize()
 
 
 class VarPoissonStarPatchOperator(_Operator):
@@ -277,6 +314,14 @@ class VarPoissonStarPatchOperator(_Operator):
         self.domain, self.ghost_filler = domain, ghost_filler
         self._coeffs = coeffs
         check(lib().te_varpoisson_operator_create(domain.h, ghost_filler.h, coeffs.ptr, ctypes.byref(self.h)))
+
+    def addDrichletBCToRHS(self, f: Vector, gfunc, hfunc):
+        """VarPoisson/StarPatchOperator.h:194-219: f -= 2 g(x_b) h(x_b) / h^2 next to every
+        domain-boundary side, on the device; hfunc is the coefficient."""
+        g, c = self._boundary_values(gfunc, hfunc)
+        check(lib().te_operator_add_dirichlet_bc_to_rhs(self.h, f.dtype, f.ptr, ctypes.c_void_p(g.data_ptr()),
+                                                        ctypes.c_void_p(c.data_ptr())))
+        _torch().cuda.current_stream().synchronize()
 
 
 class _PatchSolver(_Handle):
@@ -292,11 +337,18 @@ class _PatchSolver(_Handle):
 class DFTPatchSolver(_PatchSolver):
     """Poisson::DFTPatchSolver (Poisson/DFTPatchSolver.h:385-450)."""
 
-    def __init__(self, op: _Operator, neumann_mask: int = 0):
+    def __init__(self, op: _Operator, neumann_mask: int = 0, tc_precision: int = capi.TE_TC_TF32X3):
+        """tc_precision (no reference counterpart): the arithmetic of the FP32 tensor-core
+        transforms, TE_TC_TF32X3 (3xTF32, about FP32 accuracy) or TE_TC_BF16 (BF16 operands,
+        FP32 accumulation, per-patch power-of-two scaling)."""
         super().__init__()
         _bind_stream()
         self.op = op
-        check(lib().te_dft_patch_solver_create(op.h, int(neumann_mask), ctypes.byref(self.h)))
+        if tc_precision == capi.TE_TC_TF32X3:
+            check(lib().te_dft_patch_solver_create(op.h, int(neumann_mask), ctypes.byref(self.h)))
+        else:
+            check(lib().te_dft_patch_solver_create_tc(op.h, int(neumann_mask), int(tc_precision),
+                                                      ctypes.byref(self.h)))
 
     @property
     def uses_tensor_cores(self) -> bool:
@@ -504,6 +556,39 @@ class BiCGStab:
             return its[0]
         finally:
             lib().te_bicgstab_batch_destroy(h)
+
+
+class IterativeRefinement:
+    """FP64 iterative refinement around a cycle (no reference counterpart; the
+    Iterative::Solver interface, Iterative/Solver.h:64-69): x += Mr (b - A x)
+    until the true FP64 residual ||b - A x|| / ||b|| <= tolerance."""
+
+    def __init__(self, tolerance=1e-10, max_iterations=200):
+        self.tolerance, self.max_iterations = tolerance, max_iterations
+        self.final_residual = None
+
+    def setTolerance(self, tol):
+        self.tolerance = tol
+
+    def setMaxIterations(self, n):
+        self.max_iterations = n
+
+    def getTolerance(self):
+        return self.tolerance
+
+    def getMaxIterations(self):
+        return self.max_iterations
+
+    def solve(self, A, x: Vector, b: Vector, Mr=None):
+        if Mr is None:
+            raise RuntimeError("IterativeRefinement needs a preconditioner (a cycle)")
+        its = ctypes.c_int(0)
+        res = ctypes.c_double(0)
+        rc = lib().te_ir_solve(A.h, x.ncomp, x.ptr, b.ptr, Mr.h, float(self.tolerance), int(self.max_iterations),
+                               ctypes.byref(its), ctypes.byref(res))
+        self.final_residual = res.value
+        check(rc)
+        return its.value
 
 
 class CG:

@@ -20,6 +20,7 @@ TE_FILL_FACES, TE_FILL_EDGES, TE_FILL_CORNERS = 0, 1, 2
 TE_NOALLOC_MAX_PARTIALS = 65536
 TE_CYCLE_V, TE_CYCLE_W, TE_CYCLE_FMG = 0, 1, 2
 TE_BICGSTAB_PRECONDITIONED_EXIT, TE_BICGSTAB_FP64_OUTER, TE_BICGSTAB_SLOTS = 1, 2, 4
+TE_TC_TF32X3, TE_TC_BF16 = 0, 1
 
 _ip = ctypes.POINTER(ctypes.c_int)
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -91,12 +92,24 @@ _SIGS = {
     "te_operator_destroy": (_I, [_V]),
     "te_operator_apply": (_I, [_V, _I, _I, _V, _V]),
     "te_operator_modify_rhs": (_I, [_V, _I, _I, _V, _V]),
+    "te_level_alloc": (_I, [_V, _I, _I, ctypes.POINTER(_V)]),
+    "te_level_free": (_I, [_V]),
+    "te_device_alloc": (_I, [ctypes.c_size_t, ctypes.POINTER(_V)]),
+    "te_device_free": (_I, [_V]),
+    "te_copy": (_I, [_V, _V, ctypes.c_size_t]),
+    "te_tune_report": (_I, [ctypes.c_char_p, _I, ctypes.POINTER(_I)]),
+    "te_tune_reset": (_I, []),
+    "te_domain_face_stride": (ctypes.c_longlong, [_V]),
+    "te_domain_boundary_points": (_I, [_V, _V]),
+    "te_operator_add_dirichlet_bc_to_rhs": (_I, [_V, _I, _V, _V, _V]),
+    "te_operator_add_neumann_bc_to_rhs": (_I, [_V, _I, _V, _V]),
     "te_dft_patch_solver_create": (_I, [_V, _I, ctypes.POINTER(_V)]),
     "te_bicgstab_patch_solver_create": (_I, [_V, _D, _I, _I, ctypes.POINTER(_V)]),
     "te_patch_solver_destroy": (_I, [_V]),
     "te_patch_solver_smooth": (_I, [_V, _I, _I, _V, _V]),
     "te_patch_solver_apply": (_I, [_V, _I, _I, _V, _V]),
     "te_patch_solver_uses_tensor_cores": (_I, [_V, _ip]),
+    "te_dft_patch_solver_create_tc": (_I, [_V, _I, _I, ctypes.POINTER(_V)]),
     "te_bicgstab_batch_create": (_I, [_V, _I, _V, _V, _V, ctypes.c_double, _I, _I, _I, _ip, ctypes.POINTER(_V)]),
     "te_bicgstab_batch_step": (_I, [_V, _I, _ip]),
     "te_bicgstab_batch_state": (_I, [_V, _ip, _dp, _ip, _ip]),
@@ -111,6 +124,7 @@ _SIGS = {
     "te_vcycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, ctypes.POINTER(_V)]),
     "te_cycle_create": (_I, [ctypes.POINTER(TeCycleLevel), _I, TeCycleOpts, _I, _I, ctypes.POINTER(_V)]),
     "te_cg_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
+    "te_ir_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, ctypes.POINTER(_I), ctypes.POINTER(_D)]),
     "te_bicgstab_batch_finish_slots": (_I, [_V, _I, ctypes.POINTER(_I), ctypes.POINTER(_I)]),
     "te_bicgstab_batch_reset": (_I, [_V, _I]),
     "te_cycle_destroy": (_I, [_V]),

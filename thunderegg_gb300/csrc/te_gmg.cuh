@@ -1,6 +1,7 @@
 // te_gmg.cuh -- transfer and cycle handles (internal).
 #pragma once
 #include <map>
+#include <set>
 #include <string>
 #include <utility>
 
@@ -84,6 +85,7 @@ struct te_cycle {
     long long launches = 0;
   };
   std::map<std::pair<const void*, void*>, G> graphs;
+  std::set<std::pair<const void*, void*>> warmed;  // keys whose first application ran eagerly
   // per-level work buffers in the cycle's precision
   std::vector<te::DevBuf<char>> f, u, r;
   std::vector<te::DevBuf<char>> corr;  // tensor-core post-smooth: right-hand-side corrections per level
@@ -362,6 +364,17 @@ struct te_cycle {
     }
     auto key = std::make_pair(f64, u64);
     auto it = graphs.find(key);
+    if (it == graphs.end() && !warmed.count(key)) {
+      cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+      TE_CUDA(cudaStreamIsCapturing(s, &cs));
+      if (cs == cudaStreamCaptureStatusNone) {
+        // the first application runs eagerly: the autotuner times the launch shapes it has not
+        // met (a capture cannot be timed); the graph is captured on the next application
+        warmed.insert(key);
+        body(f64, u64, s);
+        return;
+      }
+    }
     if (it == graphs.end()) {
       G g;
       long long l0 = te::g_launches.load();

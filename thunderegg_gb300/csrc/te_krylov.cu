@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <set>
 #include <string>
 #include <algorithm>
 #include <tuple>
@@ -926,6 +927,8 @@ struct KrylovWork {
   };
   // keyed by x, b, the cycle's serial number and buffer generation, tol, flags
   std::map<std::tuple<void*, const void*, unsigned long long, unsigned long long, double, int>, G> graphs;
+  // keys whose first iteration ran eagerly (the autotuner times launch shapes it has not met then)
+  std::set<std::tuple<void*, const void*, unsigned long long, unsigned long long, double, int>> warmed;
   KrylovWork(const te_domain* d, int nc, const std::vector<int>& offsets) : d(d), nc(nc) {
     B = (int)offsets.size() - 1;
     h_offs = offsets;
@@ -1249,7 +1252,14 @@ struct BatchRun {
   void iterate_once() {
     KrylovWork& W = *Wp;
     folded = false;
-    if (use_graph) {
+    bool eager = !use_graph;
+    if (use_graph && !W.graphs.count(gkey) && !W.warmed.count(gkey)) {
+      // the first iteration of a new graph key runs eagerly: launches of shapes the autotuner
+      // has not met yet are timed there (a capture cannot be), and later captures reuse the choices
+      W.warmed.insert(gkey);
+      eager = true;
+    }
+    if (!eager) {
       auto it = W.graphs.find(gkey);
       if (it == W.graphs.end()) {
         KrylovWork::G g;

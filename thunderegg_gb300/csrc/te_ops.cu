@@ -19,6 +19,7 @@
 
 #include "te_dft.cuh"
 #include "te_ops.cuh"
+#include "te_tune.cuh"
 
 namespace te {
 
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(1024) dft_kernel(Layout L, int ti_max, const i
 // ---------------------------------------------------------------------------
 // BiCGStab patch solver
 // ---------------------------------------------------------------------------
-constexpr int BCG_THREADS = 256;
+// threads per patch of the BiCGStab patch solver: tuned among 64, 128, 256 and 512
 
 __device__ __forceinline__ double bsum(double v, double* red) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -400,14 +401,14 @@ __device__ void patch_apply(const Layout& L, const int8_t* ntype, int F, int p, 
     body;                                                    \
   }
 
-template <class T, int KIND>
-__global__ void __launch_bounds__(BCG_THREADS)
+template <class T, int KIND, int NT>
+__global__ void __launch_bounds__(NT)
     bicgstab_patch_kernel(Layout L, const int8_t* __restrict__ ntype, int F, const T* __restrict__ sp,
                           int neumann, const T* __restrict__ coeff, const T* __restrict__ f, T* u, double tol,
                           int max_it, int cont, bool use_smem, T* gscratch, unsigned long long* its_out,
                           int* status) {
   extern __shared__ unsigned char smraw[];
-  __shared__ double red[BCG_THREADS / 32];
+  __shared__ double red[NT / 32];
   int p = blockIdx.x;
   int cs = L.cs;
   T* base = use_smem ? reinterpret_cast<T*>(smraw) : gscratch + (long long)p * 8 * cs;
@@ -484,6 +485,59 @@ __global__ void __launch_bounds__(BCG_THREADS)
   if (threadIdx.x == 0) atomicAdd(its_out, (unsigned long long)it);
 }
 
+// Right-hand-side boundary helpers (Poisson/StarPatchOperator.h:187-242,
+// VarPoisson/StarPatchOperator.h:194-219): one CTA per patch walks its sides in
+// side order (a barrier between sides), so an edge or corner cell receives its
+// terms in the reference's order; each term is formed in the reference's
+// operation order with FP64 arithmetic that is not contracted into FMAs, so
+// FP64 results match it bit for bit.  mode 0: Poisson Dirichlet, f += -2 g / h^2;
+// mode 1: VarPoisson Dirichlet, f -= 2 g c / h^2; mode 2: Neumann, f += dg / h on
+// lower sides and f -= dg / h on upper sides.  Boundary data: [P][2D][fs].
+__host__ __device__ inline long long face_stride(const Layout& L) {
+  long long a = (long long)L.n1 * L.n2, b = (long long)L.n0 * L.n2, c = (long long)L.n0 * L.n1;
+  long long m = a > b ? a : b;
+  return L.D == 3 ? (m > c ? m : c) : (L.n0 > L.n1 ? L.n0 : L.n1);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256)
+    bc_rhs_kernel(Layout L, const int8_t* __restrict__ ntype, int F, const double* __restrict__ sp, int mode,
+                  long long fs, const double* __restrict__ gv, const double* __restrict__ cv, T* f) {
+  const int p = blockIdx.x, D = L.D;
+  const int side0 = D == 2 ? 4 : 20;
+  T* fp = f + (long long)p * L.cs;
+  for (int side = 0; side < 2 * D; side++) {
+    if (ntype[(size_t)p * F + side0 + side] < 0) {
+      const int axis = side >> 1, upper = side & 1;
+      const int t0 = axis == 0 ? 1 : 0, t1 = axis == 2 ? 1 : 2;
+      const int m0 = L.n(t0), m1 = D == 3 ? L.n(t1) : 1;
+      const double h = sp[(size_t)p * D + axis];
+      const double h2 = __dmul_rn(h, h);
+      const long long base = ((long long)p * 2 * D + side) * fs;
+      for (int e = threadIdx.x; e < m0 * m1; e += blockDim.x) {
+        int c[3] = {0, 0, 0};
+        c[t0] = e % m0;
+        if (D == 3) c[t1] = e / m0;
+        c[axis] = upper ? L.n(axis) - 1 : 0;
+        const int k = L.at(c[0], c[1], c[2]);
+        const double g = gv[base + e];
+        double v;
+        if (mode == 0)
+          v = __ddiv_rn(__dmul_rn(-2.0, g), h2);
+        else if (mode == 1)
+          v = -__ddiv_rn(__dmul_rn(__dmul_rn(2.0, g), cv[base + e]), h2);
+        else
+          v = upper ? -__ddiv_rn(g, h) : __ddiv_rn(g, h);
+        if (sizeof(T) == 8)
+          fp[k] = (T)__dadd_rn((double)fp[k], v);
+        else
+          fp[k] = fp[k] + (T)v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
 static size_t dft_smem(const Layout& L, int tsize) {
   SmemLay S = smem_lay(L);
   return ((size_t)S.mats + smem_mat_elems(L)) * tsize;
@@ -522,40 +576,88 @@ static void dft_set_smem_limits(size_t smem64, size_t smem32) {
   set((const void*)dft_kernel<float, 1, false>, smem32);
 }
 
-template <class T>
-static void launch_bcg(const te_patch_solver* ps, const T* f, T* u, const T* coeff, cudaStream_t s) {
+template <class T, int KIND, int NT>
+static void launch_bcg_nt(const te_patch_solver* ps, const T* f, T* u, const T* coeff, cudaStream_t s) {
   const te_domain* d = ps->op->dom;
   const Layout& L = d->lay;
   size_t need = (size_t)8 * L.cs * sizeof(T);
   bool use_smem = need <= 200 * 1024;
   T* scratch = use_smem ? nullptr : reinterpret_cast<T*>(ps->scratch.p);
   size_t smem = use_smem ? need : 0;
-  auto kern = ps->op->kind == 0 ? bicgstab_patch_kernel<T, 0> : bicgstab_patch_kernel<T, 1>;
-  kern<<<L.P, BCG_THREADS, smem, s>>>(L, d->d_nbr_type.p, d->F, d->template inv<T>(), ps->op->neumann, coeff, f, u,
-                                       ps->tol, ps->max_it, ps->cont, use_smem, scratch, ps->its.p, ps->status.p);
+  bicgstab_patch_kernel<T, KIND, NT><<<L.P, NT, smem, s>>>(L, d->d_nbr_type.p, d->F, d->template inv<T>(),
+                                                          ps->op->neumann, coeff, f, u, ps->tol, ps->max_it, ps->cont,
+                                                          use_smem, scratch, ps->its.p, ps->status.p);
   count_launch();
   TE_LAUNCH_CHECK();
+}
+
+// The thread count is tuned per (dimension, patch shape, precision, operator), not per patch
+// count, so that a solve alone and the same solve in a batch use the same kernel (the count
+// sets the order of the block reductions).  Tuning runs on scratch copies of u, since a
+// candidate overwrites it.
+template <class T>
+static void launch_bcg(const te_patch_solver* ps, const T* f, T* u, const T* coeff, cudaStream_t s) {
+  const Layout& L = ps->op->dom->lay;
+  const int kind = ps->op->kind;
+  auto run = [&](int nt, T* out) {
+    if (kind == 0) {
+      if (nt == 64) launch_bcg_nt<T, 0, 64>(ps, f, out, coeff, s);
+      else if (nt == 128) launch_bcg_nt<T, 0, 128>(ps, f, out, coeff, s);
+      else if (nt == 256) launch_bcg_nt<T, 0, 256>(ps, f, out, coeff, s);
+      else launch_bcg_nt<T, 0, 512>(ps, f, out, coeff, s);
+    } else {
+      if (nt == 64) launch_bcg_nt<T, 1, 64>(ps, f, out, coeff, s);
+      else if (nt == 128) launch_bcg_nt<T, 1, 128>(ps, f, out, coeff, s);
+      else if (nt == 256) launch_bcg_nt<T, 1, 256>(ps, f, out, coeff, s);
+      else launch_bcg_nt<T, 1, 512>(ps, f, out, coeff, s);
+    }
+  };
+  static const int nts[4] = {256, 128, 64, 512};  // 256 (the default) first
+  char key[128];
+  std::snprintf(key, sizeof key, "D=%d n=%dx%dx%d %s kind=%d", L.D, L.n0, L.n1, L.n2, sizeof(T) == 8 ? "f64" : "f32",
+                kind);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  TE_CUDA(cudaStreamIsCapturing(s, &cap));
+  std::vector<TuneCandidate> cands;
+  DevBuf<T> tmp;
+  if (cap == cudaStreamCaptureStatusNone && !tune_settled("bcg_patch", key)) {
+    const size_t n = (size_t)L.P * L.cs;
+    tmp.alloc(n);
+    for (int i = 0; i < 4; i++)
+      cands.push_back({"threads=" + std::to_string(nts[i]), [&, i, n] {
+                         TE_CUDA(cudaMemcpyAsync(tmp.p, u, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+                         run(nts[i], tmp.p);
+                       }});
+  } else {
+    for (int i = 0; i < 4; i++) cands.push_back({"threads=" + std::to_string(nts[i]), [] {}});
+  }
+  const int pick = tune_select("bcg_patch", key, cands, s, 3);
+  run(nts[pick], u);
 }
 
 // shared-memory limits and global scratch are set up when the solver is
 // created, so that launches can be captured into CUDA graphs
 static void bcg_prepare(te_patch_solver* ps) {
   const Layout& L = ps->op->dom->lay;
-  auto setup = [&](auto tag, const void* k0, const void* k1) {
+  auto setup = [&](auto tag, std::initializer_list<const void*> ks) {
     using T = decltype(tag);
     size_t need = (size_t)8 * L.cs * sizeof(T);
     if (need <= 200 * 1024) {
-      if (need > 40 * 1024) {
-        TE_CUDA(cudaFuncSetAttribute(k0, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-        TE_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
-      }
+      if (need > 40 * 1024)
+        for (const void* k : ks) TE_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
     } else {
       size_t bytes = (size_t)L.P * need;
       if (ps->scratch.n < bytes) ps->scratch.alloc(bytes);
     }
   };
-  setup(double(0), (const void*)bicgstab_patch_kernel<double, 0>, (const void*)bicgstab_patch_kernel<double, 1>);
-  setup(float(0), (const void*)bicgstab_patch_kernel<float, 0>, (const void*)bicgstab_patch_kernel<float, 1>);
+  setup(double(0), {(const void*)bicgstab_patch_kernel<double, 0, 64>, (const void*)bicgstab_patch_kernel<double, 1, 64>,
+                    (const void*)bicgstab_patch_kernel<double, 0, 128>, (const void*)bicgstab_patch_kernel<double, 1, 128>,
+                    (const void*)bicgstab_patch_kernel<double, 0, 256>, (const void*)bicgstab_patch_kernel<double, 1, 256>,
+                    (const void*)bicgstab_patch_kernel<double, 0, 512>, (const void*)bicgstab_patch_kernel<double, 1, 512>});
+  setup(float(0), {(const void*)bicgstab_patch_kernel<float, 0, 64>, (const void*)bicgstab_patch_kernel<float, 1, 64>,
+                   (const void*)bicgstab_patch_kernel<float, 0, 128>, (const void*)bicgstab_patch_kernel<float, 1, 128>,
+                   (const void*)bicgstab_patch_kernel<float, 0, 256>, (const void*)bicgstab_patch_kernel<float, 1, 256>,
+                   (const void*)bicgstab_patch_kernel<float, 0, 512>, (const void*)bicgstab_patch_kernel<float, 1, 512>});
 }
 
 void patch_smooth(const te_patch_solver* ps, int nc, int dtype, const void* f, void* u, bool zero_first,
@@ -845,10 +947,97 @@ int te_patch_solver_smooth(const te_patch_solver* s, int nc, int dtype, const vo
 int te_patch_solver_apply(const te_patch_solver* s, int nc, int dtype, const void* f, void* u) {
   return solver_call(s, nc, dtype, f, u, true);
 }
+long long te_domain_face_stride(const te_domain* d) { return d ? face_stride(d->lay) : -1; }
+
+int te_domain_boundary_points(const te_domain* d, double* coords) {
+  return guard([&] {
+    require(d && coords, "null argument");
+    const Layout& L = d->lay;
+    const int D = L.D;
+    const long long fs = face_stride(L);
+    std::vector<double> h((size_t)L.P * 2 * D * fs * D, 0.0);
+    for (int p = 0; p < L.P; p++)
+      for (int side = 0; side < 2 * D; side++) {
+        const int axis = side >> 1, upper = side & 1;
+        const int t0 = axis == 0 ? 1 : 0, t1 = axis == 2 ? 1 : 2;
+        const int m0 = L.n(t0), m1 = D == 3 ? L.n(t1) : 1;
+        for (int e = 0; e < m0 * m1; e++) {
+          double* x = &h[(((size_t)p * 2 * D + side) * fs + e) * D];
+          const int k[3] = {e % m0, e / m0, 0};
+          for (int a = 0; a < D; a++) {
+            const double st = d->starts[(size_t)p * D + a], sp = d->spacings[(size_t)p * D + a];
+            // DomainTools::GetRealCoordBound (DomainTools.h:179-210)
+            if (a == axis)
+              x[a] = upper ? st + sp * L.n(a) : st;
+            else
+              x[a] = st + sp / 2.0 + sp * k[a == t0 ? 0 : 1];
+          }
+        }
+      }
+    TE_CUDA(cudaMemcpyAsync(coords, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, d->stream));
+    TE_CUDA(cudaStreamSynchronize(d->stream));
+  });
+}
+
+static int add_bc_rhs(const te_operator* op, int dtype, void* f, int mode, const double* g, const double* c) {
+  return guard([&] {
+    require(op && f && g, "null argument");
+    require(dtype == TE_F64 || dtype == TE_F32, "bad dtype");
+    const te_domain* d = op->dom;
+    const long long fs = face_stride(d->lay);
+    if (dtype == TE_F64)
+      bc_rhs_kernel<double><<<d->lay.P, 256, 0, d->stream>>>(d->lay, d->d_nbr_type.p, d->F, d->d_spacings.p, mode,
+                                                            fs, g, c, (double*)f);
+    else
+      bc_rhs_kernel<float><<<d->lay.P, 256, 0, d->stream>>>(d->lay, d->d_nbr_type.p, d->F, d->d_spacings.p, mode,
+                                                           fs, g, c, (float*)f);
+    count_launch();
+    TE_LAUNCH_CHECK();
+  });
+}
+
+int te_operator_add_dirichlet_bc_to_rhs(const te_operator* op, int dtype, void* f, const double* gvals,
+                                        const double* cvals) {
+  if (op && op->kind == 1 && !cvals) {
+    return guard([&] { require(false, "VarPoisson's addDrichletBCToRHS needs the coefficient at the boundary points"); });
+  }
+  return add_bc_rhs(op, dtype, f, op && op->kind == 1 ? 1 : 0, gvals, cvals);
+}
+
+int te_operator_add_neumann_bc_to_rhs(const te_operator* op, int dtype, void* f, const double* dgvals) {
+  if (op && op->kind != 0) {
+    return guard([&] {
+      require(false, "addNeumannBCToRHS exists for the Poisson operator only (as in the reference)",
+              TE_ERR_UNSUPPORTED);
+    });
+  }
+  return add_bc_rhs(op, dtype, f, 2, dgvals, nullptr);
+}
+
 int te_patch_solver_uses_tensor_cores(const te_patch_solver* s, int* out) {
   return guard([&] {
     require(s && out, "null argument");
     *out = s->tc_ok ? 1 : 0;
+  });
+}
+
+int te_dft_patch_solver_create_tc(const te_operator* op, int neumann_mask, int tc_precision, te_patch_solver** out) {
+  int rc = te_dft_patch_solver_create(op, neumann_mask, out);
+  if (rc != TE_OK) return rc;
+  return guard([&] {
+    te_patch_solver* ps = *out;
+    if (tc_precision != TE_TC_TF32X3 && tc_precision != TE_TC_BF16) {
+      te_patch_solver_destroy(ps);
+      *out = nullptr;
+      require(false, "tc_precision must be TE_TC_TF32X3 or TE_TC_BF16");
+    }
+    if (tc_precision == TE_TC_BF16 && !(ps->tc_ok && ps->tc_operands != 1)) {
+      te_patch_solver_destroy(ps);
+      *out = nullptr;
+      require(false, "BF16 transforms need the tensor-core path (cubic patches n = 16, 32, 64 in 2D or 16 in 3D, "
+                     "one set of transform matrices per level)", TE_ERR_UNSUPPORTED);
+    }
+    ps->tc_prec = tc_precision;
   });
 }
 

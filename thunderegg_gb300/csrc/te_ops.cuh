@@ -49,6 +49,10 @@ struct te_patch_solver {
   int tc_pass_mat[6] = {0, 0, 0, 0, 0, 0};
   int tc_nmat = 0;
   float tc_scale = 1.f;  // prod 2/n
+  int tc_operands = 0;    // kernel variants the autotuner may pick: 0 both, 1 operands in shared memory
+                          // only, 2 operands in tensor memory only (TE_TC_OPERANDS=smem / tmem)
+  int tc_prec = 0;        // transforms: 0 = 3xTF32, 1 = BF16 operands with per-patch scaling
+  te::DevBuf<uint16_t> tc_bmat16;  // [tc_nmat][n*n] BF16 bits, row-major
   te::DevBuf<float> tc_bmat;  // [tc_nmat][2][n*n] TF32 hi/lo parts, row-major
   te::DevBuf<int> tc_err;     // set when an MMA wait timed out
 };

@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <mutex>
 
+#include "te_df64.cuh"
 #include "te_internal.cuh"
 
 namespace te {
@@ -204,9 +205,19 @@ __global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double*
   // VEC_UNROLL independent partial sums per thread (loads of a round issued
   // together), combined in a fixed order: the result depends only on the
   // level's layout and the launch shape
+  // FP64 data accumulate in FP64.  FP32 data stay on the FP32 pipes (GB300's FP64 rate is
+  // 1/64 of its FP32 rate): dot products accumulate in float-float with Ogita-Rump-Oishi
+  // Dot2 (exact FP32 products, compensated sums; about twice FP32's precision), the
+  // maximum in FP32 (exact); each thread's partials become FP64 once, at the end
+  constexpr bool F32 = sizeof(T) == 4;
   double acc[VEC_UNROLL];
+  dot2 acc2[VEC_UNROLL];
+  float accm[VEC_UNROLL];
 #pragma unroll
-  for (int r = 0; r < VEC_UNROLL; r++) acc[r] = 0.0;
+  for (int r = 0; r < VEC_UNROLL; r++) {
+    acc[r] = 0.0;
+    accm[r] = 0.f;
+  }
   const int N = L.interior();
   for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
     const long long base = (long long)pc * L.cs;
@@ -221,12 +232,23 @@ __global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double*
       }
 #pragma unroll
       for (int r = 0; r < VEC_UNROLL; r++) {
-        if (MODE == 0)
-          acc[r] += (double)xs[r] * (double)ys[r];
-        else
-          acc[r] = fmax((double)xs[r], acc[r]);
+        if (F32) {
+          if (MODE == 0)
+            acc2[r].add(df64((float)xs[r], 0.f), df64((float)ys[r], 0.f));
+          else
+            accm[r] = fmaxf((float)xs[r], accm[r]);
+        } else {
+          if (MODE == 0)
+            acc[r] += (double)xs[r] * (double)ys[r];
+          else
+            acc[r] = fmax((double)xs[r], acc[r]);
+        }
       }
     }
+  }
+  if (F32) {
+#pragma unroll
+    for (int r = 0; r < VEC_UNROLL; r++) acc[r] = MODE == 0 ? df_to_double(acc2[r].value()) : (double)accm[r];
   }
   static_assert(VEC_UNROLL == 4, "the partial sums are combined as four");
   double t = MODE == 0 ? (acc[0] + acc[1]) + (acc[2] + acc[3]) : fmax(fmax(acc[0], acc[1]), fmax(acc[2], acc[3]));
@@ -434,6 +456,57 @@ int te_domain_destroy(te_domain* d) {
 
 long long te_domain_patch_stride(const te_domain* d, int ncomp) { return d ? d->lay.pstride(ncomp) : -1; }
 int te_domain_num_patches(const te_domain* d) { return d ? d->lay.P : -1; }
+
+int te_level_alloc(const te_domain* d, int nc, int dt, void** out) {
+  return guard([&] {
+    require(d && out, "null argument");
+    require(nc >= 1, "ncomp must be >= 1");
+    require(dt == TE_F64 || dt == TE_F32, "bad dtype");
+    const size_t bytes = (size_t)d->lay.P * d->lay.pstride(nc) * (dt == TE_F64 ? 8 : 4);
+    void* p = nullptr;
+    cuda_check(cudaMalloc(&p, bytes), "cudaMalloc (level buffer)");
+    const cudaError_t e = cudaMemsetAsync(p, 0, bytes, d->stream);
+    if (e == cudaSuccess) {
+      const cudaError_t e2 = cudaStreamSynchronize(d->stream);
+      if (e2 != cudaSuccess) {
+        cudaFree(p);
+        cuda_check(e2, "cudaStreamSynchronize (level buffer)");
+      }
+    } else {
+      cudaFree(p);
+      cuda_check(e, "cudaMemsetAsync (level buffer)");
+    }
+    *out = p;
+  });
+}
+
+int te_device_alloc(size_t bytes, void** out) {
+  return guard([&] {
+    require(out, "null argument");
+    void* p = nullptr;
+    if (bytes) cuda_check(cudaMalloc(&p, bytes), "cudaMalloc");
+    *out = p;
+  });
+}
+
+int te_device_free(void* p) {
+  return guard([&] {
+    if (p) cuda_check(cudaFree(p), "cudaFree");
+  });
+}
+
+int te_copy(void* dst, const void* src, size_t bytes) {
+  return guard([&] {
+    require((dst && src) || !bytes, "null argument");
+    if (bytes) cuda_check(cudaMemcpy(dst, src, bytes, cudaMemcpyDefault), "cudaMemcpy");
+  });
+}
+
+int te_level_free(void* p) {
+  return guard([&] {
+    if (p) cuda_check(cudaFree(p), "cudaFree (level buffer)");
+  });
+}
 
 int te_vec_set(const te_domain* d, int nc, int dt, void* x, double alpha, int with_ghost) {
   return guard([&] {

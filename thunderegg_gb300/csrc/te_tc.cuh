@@ -30,6 +30,31 @@ __host__ __device__ __forceinline__ uint32_t tile_offset(int m, int k, int rows,
   return (uint32_t)ka * rows * pitch + o;
 }
 
+// the same layout for 2-byte elements (BF16 operand tiles): pitch = min(2n, 128)
+// bytes, so a K atom holds pitch / 2 elements
+__host__ __device__ __forceinline__ uint32_t tile_offset16(int m, int k, int rows, int n) {
+  const int pitch = 2 * n >= 128 ? 128 : 2 * n;
+  const int per = pitch / 2;
+  const int ka = k / per, kk = k % per;
+  uint32_t o = (uint32_t)m * pitch + (uint32_t)kk * 2;
+  const uint32_t mask = pitch / 16 - 1;
+  o ^= ((o >> 7) & mask) << 4;
+  return (uint32_t)ka * rows * pitch + o;
+}
+
+// shared-memory matrix descriptor of a K-major swizzled tile with rows of
+// `pitch` bytes (128, 64 or 32), starting at the byte address `addr`
+__device__ __forceinline__ uint64_t smem_desc_pitch(uint32_t addr, int pitch) {
+  const uint64_t layout = pitch == 128 ? 2 : (pitch == 64 ? 4 : 6);  // 128B / 64B / 32B swizzle
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)((8 * pitch) >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= layout << 61;
+  return d;
+}
+
 // shared-memory matrix descriptor of a K-major swizzled tile (starting at the
 // byte address `addr`, already offset to the row block and K step)
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, int n) {
@@ -53,11 +78,40 @@ __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
          | ((uint32_t)(M >> 4) << 24); // M / 16
 }
 
+// instruction descriptor: kind::f16 with BF16 operands, FP32 accumulate, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4)                    // D format F32
+         | (1u << 7)                  // A format BF16
+         | (1u << 10)                 // B format BF16
+         | ((uint32_t)(N >> 3) << 17)
+         | ((uint32_t)(M >> 4) << 24);
+}
+
+// kind::f16 MMA (BF16 operands, K = 16 per instruction) with A in tensor memory: the
+// 16 elements of a row's K step packed in pairs into 8 consecutive 32-bit columns
+__device__ __forceinline__ void mma_bf16_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                            int accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
 __device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, int accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
       "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+// the same MMA with operand A in tensor memory: M = 128 rows in the 128 TMEM lanes, the
+// K = 8 TF32 elements of a step in 8 consecutive 32-bit columns starting at `a_tmem`
+__device__ __forceinline__ void mma_tf32_ta(uint32_t d_tmem, uint32_t a_tmem, uint64_t b, uint32_t idesc,
+                                            int accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(accumulate));
 }
 
 // arrive on `bar` when every MMA this thread issued so far has completed
@@ -104,6 +158,32 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
   for (int i = 0; i < 8; i++) v[i] = __uint_as_float(r[i]);
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// store 16 / 8 consecutive 32-bit columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16};" ::"r"(taddr),
+      "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
+      "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
+      "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+      "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+      "r"(__float_as_uint(v[15]))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_st4u(uint32_t taddr, const uint32_t (&v)[4]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr), "r"(v[0]), "r"(v[1]),
+               "r"(v[2]), "r"(v[3])
+               : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // mbarrier with a single expected arrival per phase
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {

@@ -10,7 +10,7 @@ from __future__ import annotations
 from dataclasses import dataclass
 
 from . import (CG, BiCGStab, BiCGStabPatchSolver, BiLinearGhostFiller, BiQuadraticGhostFiller, CycleBuilder,
-               CycleOpts, DFTPatchSolver, DirectInterpolator, Domain, LinearRestrictor,
+               CycleOpts, DFTPatchSolver, DirectInterpolator, Domain, IterativeRefinement, LinearRestrictor,
                PoissonStarPatchOperator, TriLinearGhostFiller, VarPoissonStarPatchOperator, Vector)
 from .capi import TE_F64
 
@@ -35,7 +35,19 @@ class GmgOptions:
     max_it: int = 1000
     cycle_dtype: int = TE_F64       # TE_F32: mixed-precision V-cycle
     bicgstab_flags: int = 0         # 1: preconditioned early-exit update
-    krylov: str = "bicgstab"        # outer solver: "bicgstab" or "cg"
+    krylov: str = "bicgstab"        # outer solver: "bicgstab", "cg" or "ir" (FP64 iterative refinement)
+    tc_precision: int = 0           # FP32 tensor-core transforms: 0 3xTF32, 1 BF16 (per-patch scaled)
+
+
+def _tc_capable(op):
+    """Levels whose FP32 DFT solves can run on the tensor cores: cubic patches of n = 16, 32, 64
+    (2D) or 16 (3D) with one ghost layer; the solver itself checks the transform matrices."""
+    lv = op.domain.level if hasattr(op, "domain") and hasattr(op.domain, "level") else None
+    if lv is None:
+        return True
+    n = lv.ns[0]
+    return (all(x == n for x in lv.ns) and lv.num_ghost == 1
+            and ((lv.dim == 2 and n in (16, 32, 64)) or (lv.dim == 3 and n == 16)))
 
 
 class GmgSolver:
@@ -55,7 +67,7 @@ class GmgSolver:
         else:
             self.ops = [PoissonStarPatchOperator(d, g) for d, g in zip(self.domains, self.fillers)]
         if opts.smoother == SMOOTHER_DFT:
-            self.smoothers = [DFTPatchSolver(op) for op in self.ops]
+            self.smoothers = [DFTPatchSolver(op, 0, opts.tc_precision if _tc_capable(op) else 0) for op in self.ops]
         else:
             self.smoothers = [BiCGStabPatchSolver(op, opts.inner_tol, opts.inner_max_it,
                                                   opts.inner_continue_on_breakdown) for op in self.ops]
@@ -76,6 +88,8 @@ class GmgSolver:
         self.cycle = b.getCycle(opts.cycle_dtype)
         if opts.krylov == "cg":
             self.krylov = CG(opts.tol, opts.max_it)
+        elif opts.krylov == "ir":
+            self.krylov = IterativeRefinement(opts.tol, opts.max_it)
         else:
             self.krylov = BiCGStab(opts.tol, opts.max_it, opts.bicgstab_flags)
 

@@ -28,6 +28,7 @@ from __future__ import annotations
 import ctypes
 import itertools
 import json
+import dataclasses
 import math
 from dataclasses import dataclass, field
 
@@ -722,6 +723,29 @@ def cell_centers(lvl: MeshLevel):
 # ---------------------------------------------------------------------------
 # batches: several independent hierarchies as one
 # ---------------------------------------------------------------------------
+def pad_hierarchy(levels, depth):
+    """The hierarchy extended to `depth` levels by repeating its coarsest level: the patches
+    of the old coarsest level are copied to each new level (parent = the patch itself, no
+    orthant; the new level's patch has that one child), which is the reference's rule for
+    patches that are not coarsened (P4estDomainGenerator.cpp:272-321).  A cycle on the
+    padded hierarchy restricts into the copies and adds their corrections back; on a
+    one-patch coarsest level, whose smooth is an exact solve, they change the result only by
+    rounding.  Lets solves of different depths share one union hierarchy."""
+    out = list(levels)
+    if len(out) > depth:
+        raise ValueError("the hierarchy is deeper than the requested depth")
+    while len(out) < depth:
+        c = out[-1]
+        fine = dataclasses.replace(c, parent_id=c.id.copy(), orth_on_parent=np.full_like(c.orth_on_parent, -1))
+        child = np.full_like(c.child_ids, -1)
+        child[:, 0] = c.id
+        coarse = dataclasses.replace(c, parent_id=np.full_like(c.parent_id, -1),
+                                     orth_on_parent=np.full_like(c.orth_on_parent, -1), child_ids=child)
+        out[-1] = fine
+        out.append(coarse)
+    return out
+
+
 def union_hierarchy(hierarchies):
     """Concatenate the levels of several hierarchies of equal depth.
 

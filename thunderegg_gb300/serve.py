@@ -1,9 +1,10 @@
 """Continuous batching of independent Poisson solves on one GPU.
 
 A request is one GMG-preconditioned BiCGStab solve on its own mesh
-hierarchy.  Requests whose hierarchies share patch shape, depth and solver
-options form a class; the active requests of a class are packed into one
-union hierarchy (mesh.union_hierarchy), so every per-level kernel of the
+hierarchy.  Requests whose hierarchies share patch shape and solver options
+form a class, whatever their depth; the active requests of a class are packed
+into one union hierarchy (mesh.union_hierarchy, shallower members padded with
+copies of their coarsest level by mesh.pad_hierarchy), so every per-level kernel of the
 V-cycle and every Krylov kernel runs over all of them in one launch (one CUDA
 graph replay per iteration).  A batch is a fixed set of slots, one solve each
 (TE_BICGSTAB_SLOTS): the server steps each class's batch a few iterations at a
@@ -99,10 +100,11 @@ def request_bytes(levels, opts: GmgOptions) -> int:
 
 
 def _class_key(r: Request):
-    """Requests batch together when their patch shape, depth, coefficient use and every
-    solver option agree."""
+    """Requests batch together when their patch shape, coefficient use and every solver option
+    agree, whatever their depth: a union pads its shallower members with copies of their
+    coarsest level (mesh.pad_hierarchy), so their patches share every per-level launch."""
     lv = r.levels[0]
-    return (lv.dim, tuple(lv.ns), lv.num_ghost, len(r.levels), r.coeffs is not None) + dataclasses.astuple(r.opts)
+    return (lv.dim, tuple(lv.ns), lv.num_ghost, r.coeffs is not None) + dataclasses.astuple(r.opts)
 
 
 class _Active:
@@ -119,10 +121,13 @@ class _Union:
     def __init__(self, reqs, opts):
         import torch
 
-        levels, offsets = M.union_hierarchy([r.levels for r in reqs])
+        depth = max(len(r.levels) for r in reqs)
+        levels, offsets = M.union_hierarchy([M.pad_hierarchy(r.levels, depth) for r in reqs])
         coeffs = None
         if reqs[0].coeffs is not None:
-            coeffs = [np.concatenate([r.coeffs[k] for r in reqs], axis=0) for k in range(len(levels))]
+            # a padded member's copied levels take the coefficients of its coarsest level
+            coeffs = [np.concatenate([r.coeffs[min(k, len(r.coeffs) - 1)] for r in reqs], axis=0)
+                      for k in range(len(levels))]
         self.solver = GmgSolver(levels, opts, coeffs)
         self.offsets = offsets[0]
         shape = self.solver.finest.padded_shape(1)
@@ -135,7 +140,7 @@ class _Union:
 
 
 def _union_key(reqs):
-    # the class (patch shape, depth, solver options) and the members' meshes and coefficients
+    # the class (patch shape, solver options) and the members' meshes and coefficients
     return (_class_key(reqs[0]),) + tuple((id(r.levels), id(r.coeffs)) for r in reqs)
 
 
