@@ -454,16 +454,26 @@ def tuner_report(te):
     te.capi.check(lib.te_tune_report(None, 0, ctypes.byref(need)))
     buf = ctypes.create_string_buffer(max(1, need.value))
     te.capi.check(lib.te_tune_report(buf, need.value, ctypes.byref(need)))
-    out = []
-    for r in json.loads(buf.value.decode() or "[]"):
+    import re
+
+    rows = {}
+    entries = json.loads(buf.value.decode() or "[]")
+    for r in entries:
         ms = r["ms"]
         default = next(iter(ms)) if ms else None
         gain = None
         if ms and ms.get(default) and ms.get(r["choice"]):
             gain = ms[default] / ms[r["choice"]]
-        out.append({"kernel_shape": r["key"].split("|", 1)[1], "choice": r["choice"], "default": default,
-                    "gain_over_default": gain, "candidates_ms": ms})
-    return out
+        shape = r["key"].split("|", 1)[1]
+        m = re.search(r"P~2\^(\d+)", shape)
+        bucket = int(m.group(1)) if m else 0
+        group = re.sub(r" P~2\^\d+", "", shape)
+        row = {"kernel_shape": shape, "choice": r["choice"], "default": default, "gain_over_default": gain,
+               "candidates_ms": ms}
+        # one line per kernel and shape: its largest patch-count bucket (the timed levels)
+        if group not in rows or bucket > rows[group][0]:
+            rows[group] = (bucket, row)
+    return {"tuned_shapes": len(entries), "largest_level_per_shape": [v[1] for v in rows.values()]}
 
 
 def replica_throughput(local_seconds, local_solves, device="cuda"):

@@ -21,7 +21,8 @@
  * edges 8..19, sides 20..25.  Side index = 2*axis + is_upper (Face.h:558-584).
  *
  * Threading: a handle is bound to the stream that was current (te_set_stream)
- * when it was created; calls on one handle are not thread safe.
+ * in the creating thread when it was created; calls on one handle are not
+ * thread safe, handles of different streams may be used from different threads.
  */
 #ifndef TE_GPU_H
 #define TE_GPU_H
@@ -84,8 +85,9 @@ typedef struct te_cycle te_cycle;
 
 /* ---- library ------------------------------------------------------------ */
 const char* te_last_error_message(void);
-/* Stream used by handles created after this call (a cudaStream_t, or NULL
- * for the legacy default stream). */
+/* Stream used by handles this thread creates after this call (a cudaStream_t,
+ * or NULL for the legacy default stream); each thread has its own.  The text
+ * of te_last_error_message is per thread as well. */
 int te_set_stream(void* cuda_stream);
 int te_synchronize(void);
 /* Number of kernels this library has launched since load (for accounting). */

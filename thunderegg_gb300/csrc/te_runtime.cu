@@ -20,7 +20,9 @@
 namespace te {
 
 static thread_local std::string t_err;
-static cudaStream_t g_stream = nullptr;
+// per thread: a worker thread can create handles bound to its own stream while other threads
+// launch on theirs
+static thread_local cudaStream_t g_stream = nullptr;
 std::atomic<long long> g_launches{0};
 
 void set_error(const std::string& msg) { t_err = msg; }
