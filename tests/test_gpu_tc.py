@@ -275,21 +275,3 @@ def test_autotuner_report(te):
     assert r["choice"] in r["ms"] and len(r["ms"]) >= 2
     assert all(v is None or v > 0 for v in r["ms"].values())
 
-
-def test_restriction_variants_give_the_same_bits(te, monkeypatch):
-    """The fused residual + restriction runs one fine patch per CTA or as persistent pipelined
-    CTAs (the autotuner picks); every variant computes the same cells in the same order."""
-    from thunderegg_gb300 import mesh as M
-    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
-
-    outs = []
-    for v in ("0", "1", "2"):
-        monkeypatch.setenv("TE_RESTRICT_VARIANT", v)
-        for levels, sc in ((M.circle_mesh(n=32, lo=2, hi=4), 1), (M.uniform_mesh(3, 2, 16), 2)):
-            s = GmgSolver(levels, GmgOptions(scheme=sc, smoother=0, cycle_dtype=te.TE_F32))
-            f = np.random.default_rng(90 + levels[0].dim).standard_normal(levels[0].padded_shape(1))
-            u = te.Vector(s.finest)
-            s.cycle.apply(te.Vector.from_numpy(s.finest, f), u)
-            outs.append(u.numpy())
-    assert np.array_equal(outs[0], outs[2]) and np.array_equal(outs[0], outs[4])
-    assert np.array_equal(outs[1], outs[3]) and np.array_equal(outs[1], outs[5])

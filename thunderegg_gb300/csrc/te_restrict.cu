@@ -18,14 +18,8 @@
 // patches are cubic with n = 16, 32 or 64 (2D) or 8 or 16 (3D) and one ghost
 // layer; other hierarchies use the coarse-patch-centric kernel in te_fused.cu.
 
-#include <algorithm>
-#include <cstdio>
-#include <cstdlib>
-#include <vector>
-
 #include "te_ghost_dev.cuh"
 #include "te_gmg.cuh"
-#include "te_tune.cuh"
 
 namespace te {
 
@@ -39,86 +33,82 @@ struct RShape {
   static constexpr int NF = DIM == 3 ? NN * NN : NN;       // cells of one side face
 };
 
-// The pieces of one fine patch's residual + restriction, shared by the one-patch-per-CTA
-// kernel and the persistent pipelined kernel (the same arithmetic, so the same bits).
-template <class T, class TF, int DIM, int NN>
-struct RPatch {
+template <class T, class TF, int KIND, int SCHEME, int DIM, int NN>
+__global__ void __launch_bounds__(RShape<DIM, NN>::NT, 2048 / RShape<DIM, NN>::NT)
+    vc_restrict_fine_kernel(const int* __restrict__ fparent, const int* __restrict__ forth,
+                            const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
+                            const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
+                            const GCall* __restrict__ calls, const int* __restrict__ side_code,
+                            const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse) {
   using S = RShape<DIM, NN>;
-  static constexpr int NB = DIM == 3 ? 8 : 4;                     // fine cells per thread
-  static constexpr int NG = 2 * DIM * S::NF;                       // side ghost cells
-  static constexpr int GPT = (NG + S::NT - 1) / S::NT;             // per thread
-  static constexpr bool VEC = (S::CS * sizeof(T)) % 16 == 0;
-  static constexpr int V = 16 / sizeof(T);
-  static constexpr int TPT = VEC ? (S::CS / V + S::NT - 1) / S::NT : 1;
-  // loads in flight for one patch: its side codes, 16-byte pieces of the padded patch, the
-  // right-hand-side values of this thread's cells and the neighbour-side ghosts
-  int code[GPT];
-  float4 tv[TPT];
+  constexpr int NB = DIM == 3 ? 8 : 4;  // fine cells per thread
+  __shared__ __align__(16) T tile[S::CS];
+  __shared__ T gbuf[2 * DIM * S::NF];
+  const int p = blockIdx.x, t = threadIdx.x;
+  const int side0 = DIM == 2 ? 4 : 20;
+  const T* up = u + (long long)p * S::CS;
+  const int bx = t % S::H, by = (t / S::H) % S::H, bz = DIM == 3 ? t / (S::H * S::H) : 0;
+  // this thread's right-hand-side values, in flight while the patch is staged
+  const TF* ff = f + (long long)p * S::CS;
   TF fv[NB];
+#pragma unroll
+  for (int q = 0; q < NB; q++) {
+    const int x = 2 * bx + (q & 1), y = 2 * by + ((q >> 1) & 1), z = 2 * bz + (q >> 2);
+    fv[q] = __ldg(ff + (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0));
+  }
+  const int8_t* nt = fntype + (size_t)p * FS + side0;
+  // every load is issued before the first shared-memory store: this thread's
+  // side codes, its 16-byte pieces of the padded patch, then the neighbour-side
+  // ghosts (gathered from the neighbours' values, not this tile)
+  constexpr int NG = 2 * DIM * S::NF;
+  constexpr int GPT = (NG + S::NT - 1) / S::NT;
+  int code[GPT];
+#pragma unroll
+  for (int i = 0; i < GPT; i++) {
+    const int e = t + i * S::NT;
+    code[i] = (NG % S::NT == 0 || e < NG) ? side_code[p * 2 * DIM + e / S::NF] : -1;
+  }
+  constexpr bool VEC = (S::CS * sizeof(T)) % 16 == 0;
+  constexpr int V = 16 / sizeof(T);
+  constexpr int TPT = VEC ? (S::CS / V + S::NT - 1) / S::NT : 1;
+  float4 tv[TPT];
+  if (VEC) {
+    const float4* src = reinterpret_cast<const float4*>(up);
+#pragma unroll
+    for (int i = 0; i < TPT; i++) {
+      const int e = t + i * S::NT;
+      if ((S::CS / V) % S::NT == 0 || e < S::CS / V) tv[i] = __ldg(src + e);
+    }
+  }
+  const PlainAcc<T> acc{u, (long long)S::CS, 0};
   T gv[GPT];
-
-  __device__ __forceinline__ void load_codes(int p, const int* __restrict__ side_code) {
-    const int t = threadIdx.x;
 #pragma unroll
-    for (int i = 0; i < GPT; i++) {
+  for (int i = 0; i < GPT; i++) {
+    const int e = t + i * S::NT;
+    if (code[i] != -1) {
+      const int s = e / S::NF, r = e % S::NF;
+      gv[i] = side_ghost<T, SCHEME>(acc, p, s, code[i], slabs, calls, ft, DIM, r % NN, r / NN);
+    }
+  }
+  // 1. the padded patch (its ghosts are replaced below) and the gathered ghosts
+  if (VEC) {
+    float4* dst = reinterpret_cast<float4*>(tile);
+#pragma unroll
+    for (int i = 0; i < TPT; i++) {
       const int e = t + i * S::NT;
-      code[i] = (NG % S::NT == 0 || e < NG) ? side_code[p * 2 * DIM + e / S::NF] : -1;
+      if ((S::CS / V) % S::NT == 0 || e < S::CS / V) dst[e] = tv[i];
     }
+  } else {
+    for (int e = t; e < S::CS; e += S::NT) tile[e] = up[e];
   }
-  template <int SCHEME>
-  __device__ __forceinline__ void load(int p, const T* __restrict__ u, const TF* __restrict__ f, FaceTable ft,
-                                       const GSlab* __restrict__ slabs, const GCall* __restrict__ calls) {
-    const int t = threadIdx.x;
-    const int bx = t % S::H, by = (t / S::H) % S::H, bz = DIM == 3 ? t / (S::H * S::H) : 0;
-    const TF* ff = f + (long long)p * S::CS;
 #pragma unroll
-    for (int q = 0; q < NB; q++) {
-      const int x = 2 * bx + (q & 1), y = 2 * by + ((q >> 1) & 1), z = 2 * bz + (q >> 2);
-      fv[q] = __ldg(ff + (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0));
-    }
-    if (VEC) {
-      const float4* src = reinterpret_cast<const float4*>(u + (long long)p * S::CS);
-#pragma unroll
-      for (int i = 0; i < TPT; i++) {
-        const int e = t + i * S::NT;
-        if ((S::CS / V) % S::NT == 0 || e < S::CS / V) tv[i] = __ldg(src + e);
-      }
-    }
-    const PlainAcc<T> acc{const_cast<T*>(u), (long long)S::CS, 0};
-#pragma unroll
-    for (int i = 0; i < GPT; i++) {
-      const int e = t + i * S::NT;
-      if (code[i] != -1) {
-        const int s = e / S::NF, r = e % S::NF;
-        gv[i] = side_ghost<T, SCHEME>(acc, p, s, code[i], slabs, calls, ft, DIM, r % NN, r / NN);
-      }
-    }
-  }
-  // the padded patch and the gathered ghosts into shared memory
-  __device__ __forceinline__ void stage(int p, const T* __restrict__ u, T* tile, T* gbuf) const {
-    const int t = threadIdx.x;
-    if (VEC) {
-      float4* dst = reinterpret_cast<float4*>(tile);
-#pragma unroll
-      for (int i = 0; i < TPT; i++) {
-        const int e = t + i * S::NT;
-        if ((S::CS / V) % S::NT == 0 || e < S::CS / V) dst[e] = tv[i];
-      }
-    } else {
-      const T* up = u + (long long)p * S::CS;
-      for (int e = t; e < S::CS; e += S::NT) tile[e] = up[e];
-    }
-#pragma unroll
-    for (int i = 0; i < GPT; i++)
-      if (code[i] != -1) gbuf[t + i * S::NT] = gv[i];
-  }
-};
-
-// the side ghost ring of a staged patch: the gathered values, or the boundary condition
-template <class T, int DIM, int NN>
-__device__ __forceinline__ void restrict_ghost_ring(const int8_t* nt, int neumann, T* tile, const T* gbuf) {
-  using S = RShape<DIM, NN>;
-  for (int e = threadIdx.x; e < 2 * DIM * S::NF; e += S::NT) {
+  for (int i = 0; i < GPT; i++)
+    if (code[i] != -1) gbuf[t + i * S::NT] = gv[i];
+  const T i0 = finv[(size_t)p * 6 + (KIND ? 3 : 0)], i1 = finv[(size_t)p * 6 + (KIND ? 3 : 0) + 1];
+  const T i2 = DIM == 3 ? finv[(size_t)p * 6 + (KIND ? 3 : 0) + 2] : T(0);
+  __syncthreads();
+  // 2. the side ghost ring: gathered values, or the boundary condition
+  for (int e = t; e < 2 * DIM * S::NF; e += S::NT) {
     const int s = e / S::NF, r = e % S::NF;
     const int a = s >> 1, upr = s & 1;
     const int i = r % NN, j = r / NN;
@@ -135,21 +125,8 @@ __device__ __forceinline__ void restrict_ghost_ring(const int8_t* nt, int neuman
     const int st = a == 0 ? 1 : (a == 1 ? S::SY : S::SZ);
     tile[in + (upr ? st : -st)] = nt[s] >= 0 ? gbuf[e] : (neumann ? tile[in] : -tile[in]);
   }
-}
-
-// residuals of this thread's fine cells from the staged tile, restricted into the parent
-// (or written cell by cell for a copied patch); the orthant-0 child or the copy zeroes the
-// parent's ghost cells
-template <class T, class TF, int KIND, int DIM, int NN>
-__device__ __forceinline__ void restrict_cells(int p, const T* tile, const TF (&fv)[DIM == 3 ? 8 : 4],
-                                               const T* __restrict__ finv, const T* __restrict__ coeff,
-                                               const int* __restrict__ fparent, const int* __restrict__ forth,
-                                               T* __restrict__ coarse) {
-  using S = RShape<DIM, NN>;
-  const int t = threadIdx.x;
-  const int bx = t % S::H, by = (t / S::H) % S::H, bz = DIM == 3 ? t / (S::H * S::H) : 0;
-  const T i0 = finv[(size_t)p * 6 + (KIND ? 3 : 0)], i1 = finv[(size_t)p * 6 + (KIND ? 3 : 0) + 1];
-  const T i2 = DIM == 3 ? finv[(size_t)p * 6 + (KIND ? 3 : 0) + 2] : T(0);
+  __syncthreads();
+  // 3. residuals of this thread's fine cells, restricted
   const T* cf = KIND ? coeff + (long long)p * S::CS : nullptr;
   auto resid = [&](int x, int y, int z, TF fval) -> T {
     const int k = (x + 1) + (y + 1) * S::SY + (DIM == 3 ? (z + 1) * S::SZ : 0);
@@ -205,86 +182,6 @@ __device__ __forceinline__ void restrict_cells(int p, const T* tile, const TF (&
   }
 }
 
-// one CTA per fine patch
-template <class T, class TF, int KIND, int SCHEME, int DIM, int NN>
-__global__ void __launch_bounds__(RShape<DIM, NN>::NT, 2048 / RShape<DIM, NN>::NT)
-    vc_restrict_fine_kernel(const int* __restrict__ fparent, const int* __restrict__ forth,
-                            const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
-                            const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                            const GCall* __restrict__ calls, const int* __restrict__ side_code,
-                            const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse) {
-  using S = RShape<DIM, NN>;
-  __shared__ __align__(16) T tile[S::CS];
-  __shared__ T gbuf[2 * DIM * S::NF];
-  const int p = blockIdx.x;
-  const int side0 = DIM == 2 ? 4 : 20;
-  RPatch<T, TF, DIM, NN> L;
-  L.load_codes(p, side_code);
-  L.template load<SCHEME>(p, u, f, ft, slabs, calls);
-  L.stage(p, u, tile, gbuf);
-  __syncthreads();
-  restrict_ghost_ring<T, DIM, NN>(fntype + (size_t)p * FS + side0, neumann, tile, gbuf);
-  __syncthreads();
-  restrict_cells<T, TF, KIND, DIM, NN>(p, tile, L.fv, finv, coeff, fparent, forth, coarse);
-}
-
-// Persistent CTAs, software-pipelined: while the CTA restricts patch p from one shared-memory
-// buffer, the loads of its next patch (tile, right-hand side, neighbour ghosts; the side codes
-// one patch further ahead) are in flight, and land in the other buffer.  MINB resident CTAs
-// per SM (the register budget).
-template <class T, class TF, int KIND, int SCHEME, int DIM, int NN, int MINB>
-__global__ void __launch_bounds__(RShape<DIM, NN>::NT, MINB)
-    vc_restrict_pipe_kernel(const int* __restrict__ fparent, const int* __restrict__ forth,
-                            const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
-                            const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                            const GCall* __restrict__ calls, const int* __restrict__ side_code,
-                            const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse, int P) {
-  using S = RShape<DIM, NN>;
-  using RP = RPatch<T, TF, DIM, NN>;
-  extern __shared__ __align__(16) unsigned char rsm[];
-  constexpr int TILE = (S::CS * (int)sizeof(T) + 15) / 16 * 16;
-  constexpr int GB = (2 * DIM * S::NF * (int)sizeof(T) + 15) / 16 * 16;
-  T* tile[2] = {reinterpret_cast<T*>(rsm), reinterpret_cast<T*>(rsm + TILE + GB)};
-  T* gbuf[2] = {reinterpret_cast<T*>(rsm + TILE), reinterpret_cast<T*>(rsm + 2 * TILE + GB)};
-  const int side0 = DIM == 2 ? 4 : 20;
-  const int G = gridDim.x;
-  int p = blockIdx.x;
-  if (p >= P) return;
-  RP cur, nxt;
-  cur.load_codes(p, side_code);
-  cur.template load<SCHEME>(p, u, f, ft, slabs, calls);
-  if (p + G < P) nxt.load_codes(p + G, side_code);
-  cur.stage(p, u, tile[0], gbuf[0]);
-  __syncthreads();
-  restrict_ghost_ring<T, DIM, NN>(fntype + (size_t)p * FS + side0, neumann, tile[0], gbuf[0]);
-  __syncthreads();
-  int b = 0;
-  for (; p < P; p += G) {
-    const int pn = p + G;
-    const bool more = pn < P;  // the same for every thread of the CTA
-    if (more) nxt.template load<SCHEME>(pn, u, f, ft, slabs, calls);
-    int ahead[RP::GPT];
-#pragma unroll
-    for (int i = 0; i < RP::GPT; i++) ahead[i] = -1;
-    if (more && pn + G < P) {
-      RP a;
-      a.load_codes(pn + G, side_code);
-#pragma unroll
-      for (int i = 0; i < RP::GPT; i++) ahead[i] = a.code[i];
-    }
-    restrict_cells<T, TF, KIND, DIM, NN>(p, tile[b], cur.fv, finv, coeff, fparent, forth, coarse);
-    if (more) nxt.stage(pn, u, tile[b ^ 1], gbuf[b ^ 1]);
-    __syncthreads();
-    if (more) restrict_ghost_ring<T, DIM, NN>(fntype + (size_t)pn * FS + side0, neumann, tile[b ^ 1], gbuf[b ^ 1]);
-    __syncthreads();
-#pragma unroll
-    for (int q = 0; q < RP::NB; q++) cur.fv[q] = nxt.fv[q];
-#pragma unroll
-    for (int i = 0; i < RP::GPT; i++) nxt.code[i] = ahead[i];
-    b ^= 1;
-  }
-}
-
 template <class T, class TF, int KIND, int SCHEME, int DIM, int NN>
 static void launch_fine(const te_restrictor* r, const te_operator* op, const T* u, const TF* f, T* coarse,
                         cudaStream_t s) {
@@ -292,43 +189,10 @@ static void launch_fine(const te_restrictor* r, const te_operator* op, const T* 
   const te_domain* fd = r->fine;
   const te_ghost_filler* g = op->gf;
   const T* coeff = KIND ? (const T*)op->coeff_ptr(sizeof(T) == 8 ? TE_F64 : TE_F32) : nullptr;
-  static int sm_count = 0;
-  if (!sm_count) TE_CUDA(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, 0));
-  const int P = fd->lay.P;
-  constexpr size_t pipe_smem =
-      2 * ((S::CS * sizeof(T) + 15) / 16 * 16 + (2 * DIM * S::NF * sizeof(T) + 15) / 16 * 16);
-  auto one = [&] {
-    vc_restrict_fine_kernel<T, TF, KIND, SCHEME, DIM, NN><<<P, S::NT, 0, s>>>(
-        r->fine_parent.p, r->fine_orth.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(), op->neumann, coeff,
-        g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_code.p, u, f, coarse);
-    count_launch();
-  };
-  auto pipe = [&](auto minb) {
-    constexpr int MINB = decltype(minb)::value;
-    auto kern = vc_restrict_pipe_kernel<T, TF, KIND, SCHEME, DIM, NN, MINB>;
-    if (pipe_smem > 48 * 1024)
-      TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pipe_smem));
-    int occ = 0;
-    TE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)kern, S::NT, pipe_smem));
-    require(occ >= 1, "pipelined restriction does not fit on an SM", TE_ERR_UNSUPPORTED);
-    const int grid = std::min(P, std::min(occ, MINB) * sm_count);
-    kern<<<grid, S::NT, pipe_smem, s>>>(r->fine_parent.p, r->fine_orth.p, fd->d_nbr_type.p, fd->F,
-                                        fd->template inv<T>(), op->neumann, coeff, g->faces, g->d_slabs.p,
-                                        g->d_calls.p, g->d_side_code.p, u, f, coarse, P);
-    count_launch();
-  };
-  // every variant writes disjoint parts of the coarse level and reads only u and f, so a
-  // candidate can run again for timing; all compute the same bits
-  std::vector<TuneCandidate> cands = {{"one patch per CTA", one},
-                                      {"pipelined ctas=4", [&] { pipe(IntC<4>()); }},
-                                      {"pipelined ctas=8", [&] { pipe(IntC<8>()); }}};
-  char key[128];
-  std::snprintf(key, sizeof key, "D=%d n=%d P~2^%d %s/%s kind=%d scheme=%d", DIM, NN, tune_bucket(P),
-                sizeof(T) == 8 ? "f64" : "f32", sizeof(TF) == 8 ? "f64" : "f32", KIND, SCHEME);
-  // TE_RESTRICT_VARIANT=0/1/2 forces a candidate (comparisons and tests)
-  const char* force = std::getenv("TE_RESTRICT_VARIANT");
-  const int pick = force && force[0] >= '0' && force[0] <= '2' ? force[0] - '0' : tune_select("restrict_fine", key, cands, s);
-  cands[pick].run();
+  vc_restrict_fine_kernel<T, TF, KIND, SCHEME, DIM, NN><<<fd->lay.P, S::NT, 0, s>>>(
+      r->fine_parent.p, r->fine_orth.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(), op->neumann, coeff, g->faces,
+      g->d_slabs.p, g->d_calls.p, g->d_side_code.p, u, f, coarse);
+  count_launch();
   TE_LAUNCH_CHECK();
 }
 

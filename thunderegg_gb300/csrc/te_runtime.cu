@@ -63,6 +63,19 @@ __device__ __forceinline__ int interior_offset(const Layout& L, int e) {
   return L.at(x, y, z);
 }
 
+// offset of interior cell e of a cubic patch with one ghost layer (NN cells a side), or of any
+// patch through the layout (NN = 0)
+template <int DIM, int NN>
+__device__ __forceinline__ int cell_offset(const Layout& L, int e) {
+  if constexpr (NN > 0) {
+    constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0;
+    const int x = e % NN, r = e / NN;
+    return (x + 1) + (r % NN + 1) * SY + (DIM == 3 ? (r / NN + 1) * SZ : 0);
+  } else {
+    return interior_offset(L, e);
+  }
+}
+
 template <class T, int OP>
 __device__ __forceinline__ T vec_op(T xv, T av, T bv, double alpha, double beta, double gamma) {
   if (OP == OP_SET) xv = (T)alpha;
@@ -85,22 +98,23 @@ __device__ __forceinline__ T vec_op(T xv, T av, T bv, double alpha, double beta,
 // loads all of their operands before it computes, so several loads per thread
 // are in flight; x is read only by the operations that use it.
 constexpr int VEC_UNROLL = 4;
-template <class T, int OP>
+template <class T, int OP, int DIM = 0, int NN = 0>
 __global__ void vec_kernel(Layout L, int npc, T* x, const T* a, const T* b, double alpha, double beta,
                            double gamma) {
   constexpr bool RX = OP != OP_SET && OP != OP_COPY;
   constexpr bool RA = OP != OP_SET && OP != OP_SCALE && OP != OP_SHIFT;
   constexpr bool RB = OP == OP_ADD_SCALED2 || OP == OP_SCALE_THEN_ADD_SCALED2;
-  const int N = L.interior();
+  const int N = NN > 0 ? (DIM == 3 ? NN * NN * NN : NN * NN) : L.interior();
+  const int CS = NN > 0 ? (DIM == 3 ? (NN + 2) * (NN + 2) * (NN + 2) : (NN + 2) * (NN + 2)) : L.cs;
   for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    const long long base = (long long)pc * L.cs;
+    const long long base = (long long)pc * CS;
     for (int e0 = threadIdx.x; e0 < N; e0 += VEC_UNROLL * blockDim.x) {
       long long kk[VEC_UNROLL];
       T xs[VEC_UNROLL], as[VEC_UNROLL], bs[VEC_UNROLL];
 #pragma unroll
       for (int r = 0; r < VEC_UNROLL; r++) {
         const int e = e0 + r * blockDim.x;
-        kk[r] = e < N ? base + interior_offset(L, e) : -1;
+        kk[r] = e < N ? base + cell_offset<DIM, NN>(L, e) : -1;
         xs[r] = RX && kk[r] >= 0 ? x[kk[r]] : T(0);
         as[r] = RA && kk[r] >= 0 ? a[kk[r]] : T(0);
         bs[r] = RB && kk[r] >= 0 ? b[kk[r]] : T(0);
@@ -138,9 +152,18 @@ static void launch_vec(const te_domain* d, int nc, int op, T* x, const T* a, con
   int npc = d->lay.P * nc;
   if (npc == 0) return;
   int grid = npc < 152 * 8 ? npc : 152 * 8;
-#define TE_VEC_CASE(OPV)                                                                   \
-  case OPV:                                                                                \
-    vec_kernel<T, OPV><<<grid, 256, 0, s>>>(d->lay, npc, x, a, b, al, be, ga);            \
+  // cubic patches with one ghost layer: constant index arithmetic (nc == 1)
+  auto run = [&](auto opc) {
+    constexpr int OPV = decltype(opc)::value;
+    const bool cubic = nc == 1 && with_cubic_size(d->lay, [&](auto dim, auto nn) {
+                         vec_kernel<T, OPV, decltype(dim)::value, decltype(nn)::value>
+                             <<<grid, 256, 0, s>>>(d->lay, npc, x, a, b, al, be, ga);
+                       });
+    if (!cubic) vec_kernel<T, OPV><<<grid, 256, 0, s>>>(d->lay, npc, x, a, b, al, be, ga);
+  };
+#define TE_VEC_CASE(OPV)  \
+  case OPV:               \
+    run(IntC<OPV>());     \
     break;
   switch (op) {
     TE_VEC_CASE(OP_SET)
@@ -200,8 +223,9 @@ __device__ double block_reduce(double v) {
   return v;
 }
 
-// MODE 0: dot(x, y); MODE 1: max(x) with 0 floor (Vector::infNorm, Vector.h:568-578)
-template <class T, int MODE>
+// MODE 0: dot(x, y); MODE 1: max(x) with 0 floor (Vector::infNorm, Vector.h:568-578).
+// DIM, NN > 0: cubic patches of NN cells with one ghost layer, constant index arithmetic
+template <class T, int MODE, int DIM = 0, int NN = 0>
 __global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double* partials,
                               unsigned int* counter, double* out) {
   // VEC_UNROLL independent partial sums per thread (loads of a round issued
@@ -220,15 +244,16 @@ __global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double*
     acc[r] = 0.0;
     accm[r] = 0.f;
   }
-  const int N = L.interior();
+  const int N = NN > 0 ? (DIM == 3 ? NN * NN * NN : NN * NN) : L.interior();
+  const int CS = NN > 0 ? (DIM == 3 ? (NN + 2) * (NN + 2) * (NN + 2) : (NN + 2) * (NN + 2)) : L.cs;
   for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    const long long base = (long long)pc * L.cs;
+    const long long base = (long long)pc * CS;
     for (int e0 = threadIdx.x; e0 < N; e0 += VEC_UNROLL * blockDim.x) {
       T xs[VEC_UNROLL], ys[VEC_UNROLL];
 #pragma unroll
       for (int r = 0; r < VEC_UNROLL; r++) {
         const int e = e0 + r * blockDim.x;
-        const long long k = e < N ? base + interior_offset(L, e) : -1;
+        const long long k = e < N ? base + cell_offset<DIM, NN>(L, e) : -1;
         xs[r] = k >= 0 ? x[k] : T(0);
         ys[r] = MODE == 0 && k >= 0 ? y[k] : T(0);
       }
@@ -282,6 +307,30 @@ static void reduce_launch(const te_domain* d, int nc, int dtype, const void* x, 
                           double* d_out, cudaStream_t s) {
   int npc = d->lay.P * nc;
   int grid = std::min(d->red_blocks, npc);
+  // cubic patches with one ghost layer: constant index arithmetic (the same sums in the same order)
+  const bool cubic = with_cubic_size(d->lay, [&](auto dim, auto nn) {
+    constexpr int DIM = decltype(dim)::value, NN = decltype(nn)::value;
+    if (dtype == TE_F64) {
+      if (mode == 0)
+        reduce_kernel<double, 0, DIM, NN><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, (const double*)y,
+                                                                      d->d_partials.p, d->d_counter.p, d_out);
+      else
+        reduce_kernel<double, 1, DIM, NN><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, nullptr,
+                                                                      d->d_partials.p, d->d_counter.p, d_out);
+    } else {
+      if (mode == 0)
+        reduce_kernel<float, 0, DIM, NN><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const float*)x, (const float*)y,
+                                                                     d->d_partials.p, d->d_counter.p, d_out);
+      else
+        reduce_kernel<float, 1, DIM, NN><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const float*)x, nullptr,
+                                                                     d->d_partials.p, d->d_counter.p, d_out);
+    }
+  });
+  if (cubic) {
+    count_launch();
+    TE_LAUNCH_CHECK();
+    return;
+  }
   if (dtype == TE_F64) {
     if (mode == 0)
       reduce_kernel<double, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, (const double*)y,
