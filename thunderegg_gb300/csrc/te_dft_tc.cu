@@ -488,6 +488,19 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
   const int my_i = line / S::RPP, my_line = line % S::RPP;
   uint32_t phase = 0;
   bool abort = false;
+  int late = 0;  // this warp's last MMA wait ran out
+  // A transpose between 2D passes moves values only among the lines of one patch, which the
+  // warps {w, w + 4} (n <= 32) or {w, w + 1, w + 4, w + 5} (n = 64) hold: a named barrier of
+  // those warps suffices.  In 3D a patch spans the whole CTA.
+  auto xchg_sync = [&] {
+    if constexpr (DIM == 2 && NN <= 32) {
+      asm volatile("bar.sync %0, 64;" ::"r"(1 + (warp & 3)) : "memory");
+    } else if constexpr (DIM == 2) {
+      asm volatile("bar.sync %0, 128;" ::"r"(1 + ((warp & 3) >> 1)) : "memory");
+    } else {
+      __syncthreads();
+    }
+  };
 
   // this thread's line from the exchange buffer
   auto read_row = [&](float (&v)[JN]) {
@@ -602,7 +615,11 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
     for (int q = 0; q < 2 * DIM; q++) {
       tc::tmem_st_wait();
       tc::fence_before_sync();
-      __syncthreads();
+      // the A operands of every line are in place; a warp whose last wait timed out ends the group
+      if (__syncthreads_or(late)) {
+        abort = true;
+        break;
+      }
       if (t == 0) {
         tc::fence_after_sync();
         if (OPK == 0) {
@@ -637,12 +654,11 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
         }
         tc::commit(&bar);
       }
-      int late = 0;
-      if (t == 0) late = !tc::mbar_wait(&bar, phase, kWaitLimit);
-      if (__syncthreads_or(late)) {
-        abort = true;
-        break;
-      }
+      // each warp waits for the MMAs itself (lane 0 polls, bounded) and starts its epilogue at
+      // once; a timeout is carried to the next CTA barrier, where every warp leaves together
+      int ok = 1;
+      if ((t & 31) == 0) ok = tc::mbar_wait(&bar, phase, kWaitLimit) ? 1 : 0;
+      if (!__shfl_sync(0xffffffffu, ok, 0)) late = 1;
       phase ^= 1;
       tc::fence_after_sync();
       float v[JN];
@@ -706,7 +722,7 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
           const int k = nx == 0 ? cx : (nx == 1 ? cy : cz);
           xb[xbuf_index<NN>(my_i * S::RPP + nline, k)] = v[j];
         }
-        __syncthreads();
+        xchg_sync();
         read_row(v);
         store_a(v);
       }
@@ -716,10 +732,12 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
       for (int k = 0; k < CPER; k++) cbuf[t + k * NT] = cpf[k];
     }
     // the output rows in the exchange buffer are read before the next group writes it
-    __syncthreads();
+    if (__syncthreads_or(late)) abort = true;
   }
   if (abort) {
-    if (t == 0) tc::mbar_wait(&bar, phase, kWaitLimit);
+    // the MMAs last issued (every warp toggled its phase after its wait): wait for them once more
+    // before TMEM is freed
+    if (t == 0) tc::mbar_wait(&bar, phase ^ 1, kWaitLimit);
     if (t == 0) atomicExch(a.err, 1);
   }
   tc::fence_before_sync();
@@ -921,8 +939,7 @@ static void dft_tc_t(const te_patch_solver* ps, const TI* in, TO* out, cudaStrea
       const size_t idx = shapes.size() - 1;
       cands.push_back({std::string(v.name) + " ctas=" + std::to_string(l.ctas), [&, idx] {
                          const TcLaunch& sh = shapes[idx];
-                         TE_CUDA(cudaFuncSetAttribute(sh.kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                      (int)sh.smem));
+                         allow_max_dynamic_smem(sh.kern);
                          TE_CUDA(cudaFuncSetAttribute(sh.kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
                          void* args[] = {(void*)&a, (void*)&in, (void*)&out};
                          TE_CUDA(cudaLaunchKernel(sh.kern, dim3(sh.grid), dim3(S::THREADS), args, sh.smem, s));

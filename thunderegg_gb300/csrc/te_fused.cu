@@ -414,7 +414,7 @@ static int gstride_of(const Layout& L) {
 template <class K>
 static void raise_smem(K kern, size_t bytes) {
   if (bytes > 40 * 1024)  // leave room for the static shared memory
-    TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    allow_max_dynamic_smem((const void*)kern);
 }
 
 static double dft_scale(const Layout& L) {

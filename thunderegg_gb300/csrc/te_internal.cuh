@@ -39,6 +39,11 @@ inline void require(bool ok, const std::string& msg, int code = TE_ERR_INVALID) 
 
 // current stream for newly created handles; launch accounting
 cudaStream_t current_stream();
+// Raise a kernel's dynamic shared-memory limit, once, to the device's opt-in maximum.  The
+// limit belongs to the function, not to a launch: setting it per launch to that launch's size
+// would let a later, smaller setting invalidate a launch recorded earlier in a CUDA graph.
+// The shared memory each launch requests still sets its occupancy.
+void allow_max_dynamic_smem(const void* kern);
 extern std::atomic<long long> g_launches;
 inline void count_launch(int n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 #define TE_LAUNCH_CHECK() ::te::cuda_check(cudaGetLastError(), "kernel launch")

@@ -873,7 +873,7 @@ static void apply_df_launch(const te_operator* A, const float* u, DV f, cudaStre
   CV coeff{KIND ? A->coeffs_df.p : nullptr, KIND ? A->coeffs_df.p + n : nullptr};
   auto kern = apply_df_kernel<KIND, SCHEME, DIM, NN>;
   if (smem > 40 * 1024)
-    TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    allow_max_dynamic_smem((const void*)kern);
   kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff,
                                g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_code.p, gs, u, f);
   count_launch();
@@ -1037,7 +1037,7 @@ static void apply_dots_launch(const te_operator* A, KrylovWork& W, const float* 
   CV coeff{KIND ? A->coeffs_df.p : nullptr, KIND ? A->coeffs_df.p + n : nullptr};
   auto kern = apply_dots_kernel<KIND, SCHEME, DIM, NN, NV>;
   if (smem > 40 * 1024)
-    TE_CUDA(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    allow_max_dynamic_smem((const void*)kern);
   kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff, g->faces,
                                g->d_slabs.p, g->d_calls.p, g->d_side_code.p, gs, u, f, w, W.batch(),
                                W.patch_solve.p, W.part_p.p, W.counter.p, W.S.p, slot0, fin);

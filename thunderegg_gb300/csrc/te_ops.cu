@@ -564,7 +564,7 @@ static void launch_dft(const te_patch_solver* ps, const T* f, T* u, const T* coe
 // raise the dynamic shared-memory limit of every DFT kernel instance once
 static void dft_set_smem_limits(size_t smem64, size_t smem32) {
   auto set = [](const void* k, size_t sm) {
-    if (sm > 40 * 1024) TE_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (sm > 40 * 1024) allow_max_dynamic_smem(k);
   };
   set((const void*)dft_kernel<double, 0, true>, smem64);
   set((const void*)dft_kernel<double, 0, false>, smem64);
@@ -644,7 +644,7 @@ static void bcg_prepare(te_patch_solver* ps) {
     size_t need = (size_t)8 * L.cs * sizeof(T);
     if (need <= 200 * 1024) {
       if (need > 40 * 1024)
-        for (const void* k : ks) TE_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need));
+        for (const void* k : ks) allow_max_dynamic_smem(k);
     } else {
       size_t bytes = (size_t)L.P * need;
       if (ps->scratch.n < bytes) ps->scratch.alloc(bytes);

@@ -18,8 +18,13 @@
 // patches are cubic with n = 16, 32 or 64 (2D) or 8 or 16 (3D) and one ghost
 // layer; other hierarchies use the coarse-patch-centric kernel in te_fused.cu.
 
+#include <cstdio>
+#include <string>
+#include <vector>
+
 #include "te_ghost_dev.cuh"
 #include "te_gmg.cuh"
+#include "te_tune.cuh"
 
 namespace te {
 
@@ -33,8 +38,10 @@ struct RShape {
   static constexpr int NF = DIM == 3 ? NN * NN : NN;       // cells of one side face
 };
 
-template <class T, class TF, int KIND, int SCHEME, int DIM, int NN>
-__global__ void __launch_bounds__(RShape<DIM, NN>::NT, 2048 / RShape<DIM, NN>::NT)
+// CPS: resident CTAs per SM the registers are budgeted for (0: as many as the threads allow);
+// the autotuner picks it, every choice computes the same bits
+template <class T, class TF, int KIND, int SCHEME, int DIM, int NN, int CPS = 0>
+__global__ void __launch_bounds__(RShape<DIM, NN>::NT, CPS ? CPS : 2048 / RShape<DIM, NN>::NT)
     vc_restrict_fine_kernel(const int* __restrict__ fparent, const int* __restrict__ forth,
                             const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
                             const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
@@ -189,10 +196,24 @@ static void launch_fine(const te_restrictor* r, const te_operator* op, const T* 
   const te_domain* fd = r->fine;
   const te_ghost_filler* g = op->gf;
   const T* coeff = KIND ? (const T*)op->coeff_ptr(sizeof(T) == 8 ? TE_F64 : TE_F32) : nullptr;
-  vc_restrict_fine_kernel<T, TF, KIND, SCHEME, DIM, NN><<<fd->lay.P, S::NT, 0, s>>>(
-      r->fine_parent.p, r->fine_orth.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(), op->neumann, coeff, g->faces,
-      g->d_slabs.p, g->d_calls.p, g->d_side_code.p, u, f, coarse);
-  count_launch();
+  // candidates: the register budget of as many resident CTAs as the threads allow (the
+  // default), of three quarters of them and of half of them (more registers, no spills)
+  constexpr int C0 = 2048 / S::NT, C1 = C0 * 3 / 4 > 0 ? C0 * 3 / 4 : 1, C2 = C0 / 2 > 0 ? C0 / 2 : 1;
+  auto run = [&](auto cps) {
+    vc_restrict_fine_kernel<T, TF, KIND, SCHEME, DIM, NN, decltype(cps)::value><<<fd->lay.P, S::NT, 0, s>>>(
+        r->fine_parent.p, r->fine_orth.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(), op->neumann, coeff,
+        g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_code.p, u, f, coarse);
+    count_launch();
+  };
+  // the kernel writes disjoint parts of the coarse level and reads only u and f, so a
+  // candidate can run again for timing
+  std::vector<TuneCandidate> cands = {{"ctas=" + std::to_string(C0), [&] { run(IntC<C0>()); }},
+                                      {"ctas=" + std::to_string(C1), [&] { run(IntC<C1>()); }},
+                                      {"ctas=" + std::to_string(C2), [&] { run(IntC<C2>()); }}};
+  char key[128];
+  std::snprintf(key, sizeof key, "D=%d n=%d P~2^%d %s/%s kind=%d scheme=%d", DIM, NN, tune_bucket(fd->lay.P),
+                sizeof(T) == 8 ? "f64" : "f32", sizeof(TF) == 8 ? "f64" : "f32", KIND, SCHEME);
+  cands[tune_select("restrict_fine", key, cands, s)].run();
   TE_LAUNCH_CHECK();
 }
 

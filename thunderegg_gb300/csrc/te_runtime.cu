@@ -13,6 +13,7 @@
 #include <cstring>
 #include <algorithm>
 #include <mutex>
+#include <set>
 
 #include "te_df64.cuh"
 #include "te_internal.cuh"
@@ -45,6 +46,21 @@ void cuda_check(cudaError_t e, const char* what) {
 }
 
 cudaStream_t current_stream() { return g_stream; }
+
+void allow_max_dynamic_smem(const void* kern) {
+  static std::mutex mu;
+  static std::set<std::pair<int, const void*>> done;
+  int dev = 0;
+  TE_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count({dev, kern})) return;
+  int optin = 0;
+  TE_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  TE_CUDA(cudaFuncGetAttributes(&fa, kern));
+  TE_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  done.insert({dev, kern});
+}
 
 // ---------------------------------------------------------------------------
 // element access in either precision
