@@ -397,6 +397,24 @@ __device__ __forceinline__ int xbuf_index(int row, int k) {
   return pr * NN + (((k >> 2) ^ sw) << 2) + (k & 3);
 }
 
+// 2D exchange buffer: rows of NN + 4 floats (a patch's rows contiguous; 16 floats between
+// the patches of n = 16).  Row (i, r), element k sits at i * XPS + r * XP + k, so a warp's
+// transposed scalar writes (32 lines of one patch, or 16 of two), its 16-byte row reads
+// (a quarter warp: eight consecutive rows) and its cell-order accesses (consecutive x) hit
+// distinct banks, and every index a thread touches is its own base plus a compile-time
+// offset.
+template <int NN>
+struct Xb2 {
+  static constexpr int XP = NN + 4;
+  static constexpr int XPS = NN * XP + (NN == 16 ? 16 : 0);
+};
+
+// floats of the exchange buffer
+template <int DIM, int NN>
+constexpr int xbuf_floats() {
+  return DIM == 2 ? TcShape<DIM, NN>::G * Xb2<NN>::XPS : TcShape<DIM, NN>::ROWS * NN;
+}
+
 // OPK = 0: 3xTF32 products (A hi and lo in TMEM, FP32 accumulation); OPK = 1: BF16 operands
 // (one product per K step, FP32 accumulation), each patch's right-hand side scaled by a power
 // of two that brings its largest magnitude into [1, 2) and the result scaled back
@@ -427,21 +445,36 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
   const uint32_t raw = tc::smem_addr(dsm);
   uint8_t* sm = dsm + ((1024 - (raw & 1023)) & 1023);
   uint8_t* Bm = sm;                                                   // matrices: 1024-byte aligned tiles
-  float* xb = reinterpret_cast<float*>(Bm + a.nmat * BT);             // exchange buffer [ROWS][NN]
-  float* cbuf = xb + S::ROWS * NN;                                    // [G][2D][NF] corrections
+  float* xb = reinterpret_cast<float*>(Bm + a.nmat * BT);             // exchange buffer
+  float* cbuf = xb + xbuf_floats<DIM, NN>();                          // [G][2D][NF] corrections
   __shared__ uint32_t pmax[2][S::G];                                  // BF16: |f| maximum per patch (bits)
   const bool has_corr = a.corr != nullptr;
+  // a thread's k-th cell of a group (e = t + k * NT) lies in patch k / KPP; in 2D its x is
+  // tx and its y is ty + YS * (k % KPP)
+  constexpr int KPP = S::NCELL / NT;
+  constexpr int YS = NT / NN;
+  constexpr int XP = Xb2<NN>::XP, XPS = Xb2<NN>::XPS;
+  const int tx = t % NN, ty = t / NN;
+  const int gbase = (tx + 1) + (ty + 1) * SY;  // 2D: offset of the thread's first cell in a padded patch
+  const int xbase = ty * XP + tx;              // 2D: its exchange-buffer index
 
   TI pf[PER];
   float cpf[CPER];
   auto prefetch = [&](int grp) {
     const int p0 = grp * S::G;
+    if constexpr (DIM == 2) {
+      const TI* src = in + (long long)p0 * CS + gbase;
 #pragma unroll
-    for (int k = 0; k < PER; k++) {
-      int e = t + k * NT;
-      int i = e / S::NCELL, c = e % S::NCELL;
-      int p = p0 + i;
-      pf[k] = p < P ? __ldg(in + (long long)p * CS + interior_offset<DIM, NN>(c)) : TI(0);
+      for (int k = 0; k < PER; k++)
+        pf[k] = p0 + k / KPP < P ? __ldg(src + (k / KPP) * CS + YS * (k % KPP) * SY) : TI(0);
+    } else {
+#pragma unroll
+      for (int k = 0; k < PER; k++) {
+        int e = t + k * NT;
+        int i = e / S::NCELL, c = e % S::NCELL;
+        int p = p0 + i;
+        pf[k] = p < P ? __ldg(in + (long long)p * CS + interior_offset<DIM, NN>(c)) : TI(0);
+      }
     }
     if (has_corr) {
 #pragma unroll
@@ -502,11 +535,13 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
     }
   };
 
+  // 2D: this thread's row of the exchange buffer (its line, from column j0)
+  const int rbase = my_i * XPS + my_line * XP + j0;
   // this thread's line from the exchange buffer
   auto read_row = [&](float (&v)[JN]) {
 #pragma unroll
     for (int c = 0; c < JN; c += 4) {
-      const float4 q = *reinterpret_cast<const float4*>(xb + xbuf_index<NN>(line, j0 + c));
+      const float4 q = *reinterpret_cast<const float4*>(xb + (DIM == 2 ? rbase + c : xbuf_index<NN>(line, j0 + c)));
       v[c] = q.x;
       v[c + 1] = q.y;
       v[c + 2] = q.z;
@@ -541,7 +576,19 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
 
   for (int grp = blockIdx.x; grp < a.ngroups && !abort; grp += gridDim.x) {
     const int p0 = grp * S::G;
-    if (has_corr) {
+    if (DIM == 2 && has_corr) {
+      // f - corrections, x side first, then y side (the order of the general form below)
+      if (tx == 0 || tx == NN - 1) {
+        const float* cs = cbuf + (tx == 0 ? 0 : NF) + ty;
+#pragma unroll
+        for (int k = 0; k < PER; k++) pf[k] -= (TI)cs[(k / KPP) * 4 * NF + YS * (k % KPP)];
+      }
+#pragma unroll
+      for (int k = 0; k < PER; k++) {
+        const int y = ty + YS * (k % KPP);
+        if (y == 0 || y == NN - 1) pf[k] -= (TI)cbuf[(k / KPP) * 4 * NF + (y == 0 ? 2 : 3) * NF + tx];
+      }
+    } else if (has_corr) {
       const int xt = t % NN;
       if (xt == 0 || xt == NN - 1) {
         const int side = xt == 0 ? 0 : 1;
@@ -572,11 +619,15 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
     for (int i = 0; i < S::G; i++) pm[i] = 0.f;
 #pragma unroll
     for (int k = 0; k < PER; k++) {
-      const int e = t + k * NT;
-      const int i = e / S::NCELL, c = e % S::NCELL;
       const float v = (float)pf[k];
-      xb[xbuf_index<NN>(i * S::RPP + c / NN, c % NN)] = v;
-      if (OPK) pm[k / (S::NCELL / NT)] = fmaxf(pm[k / (S::NCELL / NT)], fabsf(v));
+      if constexpr (DIM == 2) {
+        xb[(k / KPP) * XPS + xbase + YS * (k % KPP) * XP] = v;
+      } else {
+        const int e = t + k * NT;
+        const int i = e / S::NCELL, c = e % S::NCELL;
+        xb[xbuf_index<NN>(i * S::RPP + c / NN, c % NN)] = v;
+      }
+      if (OPK) pm[k / KPP] = fmaxf(pm[k / KPP], fabsf(v));
     }
     const int pbuf = ((grp - (int)blockIdx.x) / (int)gridDim.x) & 1;
     if (OPK) {
@@ -687,15 +738,23 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
           w.y = v[c + 1] * sc;
           w.z = v[c + 2] * sc;
           w.w = v[c + 3] * sc;
-          *reinterpret_cast<float4*>(xb + xbuf_index<NN>(line, j0 + c)) = w;
+          *reinterpret_cast<float4*>(xb + (DIM == 2 ? rbase + c : xbuf_index<NN>(line, j0 + c))) = w;
         }
         __syncthreads();
+        if constexpr (DIM == 2) {
+          TO* dst = out + (long long)p0 * CS + gbase;
 #pragma unroll
-        for (int k = 0; k < PER; k++) {
-          const int e = t + k * NT;
-          const int i = e / S::NCELL, c = e % S::NCELL;
-          const int p = p0 + i;
-          if (p < P) out[(long long)p * CS + interior_offset<DIM, NN>(c)] = (TO)xb[xbuf_index<NN>(i * S::RPP + c / NN, c % NN)];
+          for (int k = 0; k < PER; k++)
+            if (p0 + k / KPP < P)
+              dst[(k / KPP) * CS + YS * (k % KPP) * SY] = (TO)xb[(k / KPP) * XPS + xbase + YS * (k % KPP) * XP];
+        } else {
+#pragma unroll
+          for (int k = 0; k < PER; k++) {
+            const int e = t + k * NT;
+            const int i = e / S::NCELL, c = e % S::NCELL;
+            const int p = p0 + i;
+            if (p < P) out[(long long)p * CS + interior_offset<DIM, NN>(c)] = (TO)xb[xbuf_index<NN>(i * S::RPP + c / NN, c % NN)];
+          }
         }
         if (a.zero_ghosts) {
           for (int e = t; e < S::G * CS; e += NT) {
@@ -714,13 +773,20 @@ __global__ void __launch_bounds__(TcShape<DIM, NN>::THREADS, TcShape<DIM, NN>::M
       if (nx == ax) {
         store_a(v);
       } else {
+        if constexpr (DIM == 2) {
+          // line (i, a), column b becomes line (i, b), column a
+          float* tb = xb + my_i * XPS + j0 * XP + my_line;
 #pragma unroll
-        for (int j = 0; j < JN; j++) {
-          int cx, cy, cz;
-          line_coords(ax, my_line, j0 + j, NN, cx, cy, cz);
-          const int nline = nx == 0 ? cy + NN * cz : (nx == 1 ? cx + NN * cz : cx + NN * cy);
-          const int k = nx == 0 ? cx : (nx == 1 ? cy : cz);
-          xb[xbuf_index<NN>(my_i * S::RPP + nline, k)] = v[j];
+          for (int j = 0; j < JN; j++) tb[j * XP] = v[j];
+        } else {
+#pragma unroll
+          for (int j = 0; j < JN; j++) {
+            int cx, cy, cz;
+            line_coords(ax, my_line, j0 + j, NN, cx, cy, cz);
+            const int nline = nx == 0 ? cy + NN * cz : (nx == 1 ? cx + NN * cz : cx + NN * cy);
+            const int k = nx == 0 ? cx : (nx == 1 ? cy : cz);
+            xb[xbuf_index<NN>(my_i * S::RPP + nline, k)] = v[j];
+          }
         }
         xchg_sync();
         read_row(v);
@@ -776,7 +842,7 @@ template <int DIM, int NN>
 size_t tct_smem_bytes(int nmat, int opk) {
   using S = TcShape<DIM, NN>;
   const size_t bt = opk ? (size_t)S::BTILE16 : 2 * (size_t)S::BTILE;
-  return 1024 + (size_t)nmat * bt + (size_t)S::ROWS * NN * 4 + (size_t)S::G * 2 * DIM * S::RPP * 4;
+  return 1024 + (size_t)nmat * bt + (size_t)xbuf_floats<DIM, NN>() * 4 + (size_t)S::G * 2 * DIM * S::RPP * 4;
 }
 
 uint16_t bf16_round_host(float x) {

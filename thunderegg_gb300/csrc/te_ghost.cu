@@ -328,8 +328,30 @@ int te_ghost_filler_create(const te_domain* d, int scheme, int fill_type, te_gho
       }
       side_code[(size_t)s.patch * 2 * D + s.face] = code;
     }
+    std::vector<SideRec> side_rec((size_t)P * 2 * D);
+    for (size_t k = 0; k < side_rec.size(); k++) {
+      SideRec r;
+      std::memset(&r, 0, sizeof r);
+      r.code = side_code[k];
+      r.own_type = -1;
+      r.own_orth = -1;
+      if (r.code <= -2) {
+        const GSlab& s = g->h_slabs[(size_t)(-2 - r.code)];
+        r.own_type = s.own_type;
+        r.own_orth = s.own_orth;
+        r.zero = s.zero;
+        if (s.ncalls <= kSideRecCalls) {
+          r.ncalls = s.ncalls;
+          for (int c = 0; c < s.ncalls; c++) r.calls[c] = hc[(size_t)s.call0 + c];
+        } else {
+          r.ncalls = -1;
+        }
+      }
+      side_rec[k] = r;
+    }
     cudaStream_t st = d->stream;
     g->d_side_code.upload(side_code, st);
+    g->d_side_rec.upload(side_rec, st);
     g->d_slabs.upload(g->h_slabs, st);
     g->d_calls.upload(hc, st);
     g->d_slab_start.upload(g->h_slab_start, st);

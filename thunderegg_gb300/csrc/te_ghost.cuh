@@ -40,6 +40,20 @@ struct GCall {
   int src;
   int8_t type, orth, src_face, pad;
 };
+// Everything the gather of one side of one patch needs, in one record
+// (te_ghost_filler::d_side_rec, [P * 2D]): the side's code as in d_side_code and,
+// for a side with a slab, the slab's own term and its incoming calls inline, so
+// a gather costs one record load before the neighbours' values instead of a
+// chain code -> slab -> call -> values.  A slab with more than kSideRecCalls
+// calls (none arise from a 2:1 balanced mesh) keeps ncalls = -1: its gather
+// reads the slab table.
+constexpr int kSideRecCalls = 4;
+struct __align__(16) SideRec {
+  int code;
+  int8_t own_type, own_orth, zero, ncalls;
+  GCall calls[kSideRecCalls];
+  int pad[2];
+};
 
 FaceTable make_face_table(const Layout& L);
 int slot_of(int D, int M, int face);
@@ -60,6 +74,7 @@ struct te_ghost_filler {
   // face (a Normal neighbour and no own term), -1 no neighbour, <= -2 the
   // side's slab is -2 - code
   te::DevBuf<int> d_side_code;
+  te::DevBuf<te::SideRec> d_side_rec;  // [P * 2D] the same sides with their slabs inline
   bool other_slabs = false;  // slabs beyond d_side_code (edges, corners, sides without a neighbour)
   te::FaceTable faces;
 };

@@ -191,6 +191,29 @@ __device__ __forceinline__ T side_ghost(const Acc& acc, int p, int s, int code, 
   return gather_ghost<T, SCHEME>(acc, p, sl, ft.f[side0 + s], ft, calls, D, i, j, T(0));
 }
 
+// side_ghost from the side's record (te_ghost_filler::d_side_rec, code not -1):
+// the same terms in the same order, with the slab's own term and calls read
+// from the record.  A side has one incoming call per neighbour: at most 2 in
+// 2D and 4 in 3D; a record with more (ncalls -1 or above that) reads its slab.
+template <class T, int SCHEME, int D, class Acc>
+__device__ __forceinline__ T side_ghost_rec(const Acc& acc, int p, int s, const SideRec& r,
+                                            const GSlab* __restrict__ slabs, const GCall* __restrict__ calls,
+                                            const FaceTable& ft, int i, int j) {
+  constexpr int side0 = D == 2 ? 4 : 20;
+  constexpr int MAXC = D == 2 ? 2 : kSideRecCalls;
+  if (r.code >= 0) return sv<T>(acc, r.code, ft.f[side0 + (s ^ 1)], 0, i, j);
+  if (r.ncalls < 0 || r.ncalls > MAXC) return side_ghost<T, SCHEME>(acc, p, s, r.code, slabs, calls, ft, D, i, j);
+  T v = T(0);
+  v = own_term<T, SCHEME>(v, acc, p, ft.f[side0 + s], D - 1, D, r.own_type, r.own_orth, i, j);
+#pragma unroll
+  for (int k = 0; k < MAXC; k++) {
+    if (k >= r.ncalls) break;
+    const GCall cl = r.calls[k];
+    v = call_term<T, SCHEME>(v, acc, cl.src, ft.f[side0 + cl.src_face], D - 1, D, cl.type, cl.orth, i, j);
+  }
+  return v;
+}
+
 // Face (side) ghosts of up to NP patches into shared memory,
 // G[(q * 2D + side) * gstride + j*nt0 + i] for patch slot q, for every side
 // with a neighbour; side_code[p * 2D + side] is that side's code (-1: none,

@@ -684,7 +684,8 @@ template <int KIND, int SCHEME, int DIM, int NN, int NV>
 __global__ void __launch_bounds__(256, 6)
     apply_dots_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const float2* __restrict__ inv_df,
                       int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
-                      const GCall* __restrict__ calls, const int* __restrict__ side_code, int gs,
+                      const GCall* __restrict__ calls, const int* __restrict__ side_code,
+                      const SideRec* __restrict__ recs, int gs,
                       const float* __restrict__ u, DV f, CV w, Batch bt, const int* __restrict__ patch_solve,
                       double* part, unsigned int* counter, double* S, int slot0, int finalize_kind) {
   extern __shared__ df64 G[];  // [2D][gs]
@@ -716,8 +717,14 @@ __global__ void __launch_bounds__(256, 6)
     gv[i] = df64(0.f, 0.f);
     if (NG % 256 == 0 || e < NG) {
       const int s = e / NF, r = e % NF;
-      const int code = side_code[p * 2 * DIM + s];
-      if (code != -1) gv[i] = side_ghost<df64, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, r % NN, r / NN);
+      if constexpr (GPT == 1) {
+        // the side's record: a coarse-fine side's values are one dependent load away
+        const SideRec rec = recs[p * 2 * DIM + s];
+        if (rec.code != -1) gv[i] = side_ghost_rec<df64, SCHEME, DIM>(acc, p, s, rec, slabs, calls, ft, r % NN, r / NN);
+      } else {
+        const int code = side_code[p * 2 * DIM + s];
+        if (code != -1) gv[i] = side_ghost<df64, SCHEME>(acc, p, s, code, slabs, calls, ft, DIM, r % NN, r / NN);
+      }
     }
   }
   if (threadIdx.x < 2 * DIM) has[threadIdx.x] = ntype[(size_t)p * FS + side0 + threadIdx.x] >= 0;
@@ -904,6 +911,36 @@ static void apply_df(const te_operator* A, const float* u, DV f, cudaStream_t st
 #undef TE_AD
 }
 
+// scalar exchange between a Krylov run's device state and mapped host memory (KrylovWork)
+__global__ void scalars_to_host(double* __restrict__ dst, const double* __restrict__ src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+__global__ void scalars_from_host(double* __restrict__ dst, const double* __restrict__ src, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+struct FlagChunk {
+  static constexpr int N = 256;
+  int v[N];
+};
+__global__ void set_flags(int* __restrict__ dst, FlagChunk c, int n) {
+  if ((int)threadIdx.x < n) dst[threadIdx.x] = c.v[threadIdx.x];
+}
+struct ErrFlags {
+  static constexpr int N = 32;
+  int* p[N];
+  int n;
+};
+// or of the flags (each cleared) into *out
+__global__ void take_flags(ErrFlags f, int* out) {
+  int v = 0;
+  if ((int)threadIdx.x < f.n) {
+    v = f.p[threadIdx.x][0];
+    f.p[threadIdx.x][0] = 0;
+  }
+  v = __any_sync(0xffffffffu, v != 0);
+  if (threadIdx.x == 0) *(volatile int*)out = v;
+}
+
 struct KrylovWork {
   const te_domain* d;
   int nc;
@@ -916,8 +953,11 @@ struct KrylovWork {
   DevBuf<int> patch_solve;  // [P] solve of each finest patch
   DevBuf<double> part_p;    // [2][P] per-patch dot partials of the fused apply
   DevBuf<double> dx;        // float-float loop: correction to x since the last fold (allocated on first use)
-  double* h = nullptr;
+  double* h = nullptr;       // per-solve scalars on the host (pinned, mapped)
+  double* h_dev = nullptr;   // the same memory as the device sees it
   int* h_active = nullptr;
+  int* h_tcerr = nullptr;    // tensor-core smoother error flags gathered for the host (pinned, mapped)
+  int* h_tcerr_dev = nullptr;
   cudaStream_t cap = nullptr;
   cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   struct G {
@@ -952,8 +992,11 @@ struct KrylovWork {
     }
     nch.upload(h_nch, d->stream);
     active.alloc(B);
-    TE_CUDA(cudaMallocHost(&h, (size_t)B * S_NSLOTS * sizeof(double)));
+    TE_CUDA(cudaHostAlloc(&h, (size_t)B * S_NSLOTS * sizeof(double), cudaHostAllocMapped));
+    TE_CUDA(cudaHostGetDevicePointer((void**)&h_dev, h, 0));
     TE_CUDA(cudaMallocHost(&h_active, (size_t)B * sizeof(int)));
+    TE_CUDA(cudaHostAlloc(&h_tcerr, sizeof(int), cudaHostAllocMapped));
+    TE_CUDA(cudaHostGetDevicePointer((void**)&h_tcerr_dev, h_tcerr, 0));
     TE_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
     TE_CUDA(cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming));
     TE_CUDA(cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming));
@@ -965,6 +1008,7 @@ struct KrylovWork {
     }
     if (h) cudaFreeHost(h);
     if (h_active) cudaFreeHost(h_active);
+    if (h_tcerr) cudaFreeHost(h_tcerr);
     if (ev_in) cudaEventDestroy(ev_in);
     if (ev_out) cudaEventDestroy(ev_out);
     if (cap) cudaStreamDestroy(cap);
@@ -975,12 +1019,33 @@ struct KrylovWork {
   CV cv(const DevBuf<double>& v) const { return CV{(const float*)v.p, (const float*)v.p + n}; }
   float* f32(DevBuf<double>& v) const { return (float*)v.p; }
   int grid() const { return B * MAX_CHUNKS; }
+  // The per-iteration scalar exchange uses no copy engine: a kernel writes the scalars into
+  // mapped host memory (and reads them from there), and the active flags travel as kernel
+  // arguments.  Copies of other streams (a serving loop's uploads and downloads of whole
+  // right-hand sides and solutions) then cannot hold up an iteration's convergence test.
   void read_scalars(cudaStream_t st) {
-    TE_CUDA(cudaMemcpyAsync(h, S.p, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyDeviceToHost, st));
+    scalars_to_host<<<1, 256, 0, st>>>(h_dev, S.p, B * S_NSLOTS);
+    count_launch();
+    TE_LAUNCH_CHECK();
     TE_CUDA(cudaStreamSynchronize(st));
   }
+  // the host's scalars of solves [i0, i1) into the device copy
+  void push_scalars(cudaStream_t st, int i0 = 0, int i1 = -1) {
+    if (i1 < 0) i1 = B;
+    scalars_from_host<<<1, 256, 0, st>>>(S.p + (size_t)i0 * S_NSLOTS, h_dev + (size_t)i0 * S_NSLOTS,
+                                         (i1 - i0) * S_NSLOTS);
+    count_launch();
+    TE_LAUNCH_CHECK();
+  }
   void push_active(cudaStream_t st) {
-    TE_CUDA(cudaMemcpyAsync(active.p, h_active, (size_t)B * sizeof(int), cudaMemcpyHostToDevice, st));
+    for (int i0 = 0; i0 < B; i0 += FlagChunk::N) {
+      FlagChunk c;
+      const int m = std::min(FlagChunk::N, B - i0);
+      for (int k = 0; k < m; k++) c.v[k] = h_active[i0 + k];
+      set_flags<<<1, FlagChunk::N, 0, st>>>(active.p + i0, c, m);
+      count_launch();
+      TE_LAUNCH_CHECK();
+    }
   }
 };
 
@@ -1039,7 +1104,7 @@ static void apply_dots_launch(const te_operator* A, KrylovWork& W, const float* 
   if (smem > 40 * 1024)
     allow_max_dynamic_smem((const void*)kern);
   kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff, g->faces,
-                               g->d_slabs.p, g->d_calls.p, g->d_side_code.p, gs, u, f, w, W.batch(),
+                               g->d_slabs.p, g->d_calls.p, g->d_side_code.p, g->d_side_rec.p, gs, u, f, w, W.batch(),
                                W.patch_solve.p, W.part_p.p, W.counter.p, W.S.p, slot0, fin);
   count_launch();
   TE_LAUNCH_CHECK();
@@ -1245,7 +1310,7 @@ struct BatchRun {
       }
       nactive += W.h_active[i];
     }
-    TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
+    W.push_scalars(st);
     W.push_active(st);
   }
 
@@ -1371,7 +1436,7 @@ struct BatchRun {
     kd_split3<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), W.dv(W.rhat), W.dv(W.p), nvals);
     count_launch();
     TE_LAUNCH_CHECK();
-    TE_CUDA(cudaMemcpyAsync(W.S.p, W.h, (size_t)B * S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
+    W.push_scalars(st);
     return true;
   }
 
@@ -1384,12 +1449,19 @@ struct BatchRun {
 
   // a tensor-core DFT smoother whose MMA completion wait timed out flags it; the results are invalid
   void check_tc() {
-    if (M)
-      for (const te_cycle_level& lv : M->levels)
-        if (lv.smoother && dft_tc_error(lv.smoother, st)) {
-          TE_CUDA(cudaMemsetAsync(lv.smoother->tc_err.p, 0, sizeof(int), st));
-          throw Error(TE_ERR_TIMEOUT, "tensor-core DFT: an MMA completion wait timed out; results are invalid");
-        }
+    if (!M) return;
+    ErrFlags ef;
+    ef.n = 0;
+    for (const te_cycle_level& lv : M->levels)
+      if (lv.smoother && lv.smoother->tc_ok && ef.n < ErrFlags::N) ef.p[ef.n++] = lv.smoother->tc_err.p;
+    if (ef.n == 0) return;
+    // every level's flag, read and cleared on the device, or-ed into mapped host memory
+    take_flags<<<1, 32, 0, st>>>(ef, Wp->h_tcerr_dev);
+    count_launch();
+    TE_LAUNCH_CHECK();
+    TE_CUDA(cudaStreamSynchronize(st));
+    if (*(volatile int*)Wp->h_tcerr)
+      throw Error(TE_ERR_TIMEOUT, "tensor-core DFT: an MMA completion wait timed out; results are invalid");
   }
 
   // ---- slot mode: one solve reset or finished while the others keep their state
@@ -1438,7 +1510,7 @@ struct BatchRun {
     h[S_RHO] = rr;
     h[S_R0] = r0[i];
     rho[i] = rr;
-    TE_CUDA(cudaMemcpyAsync(W.S.p + (size_t)i * S_NSLOTS, h, S_NSLOTS * sizeof(double), cudaMemcpyHostToDevice, st));
+    W.push_scalars(st, i, i + 1);
   }
   // a new system in solve i: its b and x have been written into its patch range
   void reset_slot(int i) {
