@@ -388,6 +388,71 @@ int te_bicgstab_batch_destroy(te_bicgstab_batch* batch);
 int te_tune_report(char* buf, int len, int* needed);
 int te_tune_reset(void);
 
+/* ---- serving: continuous batching of independent solves --------------------
+ * No counterpart in the reference (one solve per Iterative::BiCGStab::solve
+ * call, BiCGStab.h:111-203); the native form of thunderegg_gb300.serve.Server.
+ * A request is one GMG-preconditioned BiCGStab solve of -Lap u = f (Poisson
+ * star operator, Dirichlet sides, V-cycle) on its own hierarchy, finest level
+ * first, with its right-hand side on the host (finest level, padded layout,
+ * FP64).  te_serve_submit copies the tables and f and queues the request
+ * (TE_ERR_BUDGET when it alone needs more device memory than the budget).
+ * Each te_serve_step is one scheduling round: it admits queued requests while
+ * the estimated device memory of the admitted ones and of cached idle unions
+ * fits the budget; packs the admitted requests of one class (equal patch shape
+ * and te_solve_opts, any depth) into one union hierarchy so that every
+ * per-level kernel covers all of them; starts waiting requests in free slots
+ * built on their mesh while the others iterate; re-forms a class's batch when
+ * requests wait without such a slot (running solves continue from their
+ * current iterates); runs steps_per_round BiCGStab iterations of every batch;
+ * and finishes the solves that stopped (FP64 true residual; restart when it
+ * is above tol).  *unfinished = requests queued or still solving.
+ * te_serve_poll returns TE_PENDING until the request has finished, then
+ * TE_OK once, with u (finest level, padded layout, FP64, host) and the
+ * result.  A request's result matches the same solve run alone within the
+ * solver tolerance.  One thread drives a server; its handles bind to the
+ * stream that was current (te_set_stream) at te_serve_create. */
+enum { TE_PENDING = 8 };
+typedef struct te_server te_server;
+typedef struct te_serve_opts {
+  double budget_bytes; /* device memory the admitted requests may hold (estimated) */
+  int steps_per_round; /* BiCGStab iterations per batch per round (>= 1)             */
+  int max_batch;       /* most solves in one batch (>= 1)                            */
+} te_serve_opts;
+typedef struct te_solve_opts {
+  int scheme;                      /* TE_GHOST_*                                   */
+  int fill_type;                   /* TE_FILL_*                                    */
+  int smoother;                    /* 0 DFT patch solver, 1 BiCGStab patch solver  */
+  double inner_tol;                /* BiCGStab patch solver: tolerance,            */
+  int inner_max_iterations;        /*   iteration limit,                           */
+  int inner_continue_on_breakdown; /*   continue on breakdown                      */
+  int pre_sweeps, post_sweeps, coarse_sweeps;
+  double tol;                      /* outer BiCGStab: relative residual            */
+  int max_iterations;
+  int cycle_dtype;                 /* TE_F32 mixed precision, TE_F64 plain         */
+  int flags;                       /* TE_BICGSTAB_PRECONDITIONED_EXIT, ..._FP64_OUTER */
+  int tc_precision;                /* TE_TC_TF32X3 or TE_TC_BF16                    */
+} te_solve_opts;
+typedef struct te_serve_result {
+  int status;        /* TE_OK or TE_ERR_BREAKDOWN                             */
+  int iterations;    /* outer iterations, over every batch it was in          */
+  double residual;   /* final relative residual (FP64 true residual with an FP32 cycle) */
+  double latency_s;  /* submit to result                                      */
+  int restarts;      /* batch re-formations the request went through          */
+} te_serve_result;
+typedef struct te_serve_counters {
+  long long submitted, admitted, completed, rejected;
+  long long union_builds, union_cache_hits, slot_fills, reforms, rounds;
+  int queued, active, classes;
+  double bytes_in_use; /* estimate: admitted requests and cached idle unions */
+} te_serve_counters;
+int te_serve_create(const te_serve_opts* opts, te_server** out);
+int te_serve_destroy(te_server* s);
+int te_serve_submit(te_server* s, const te_level_desc* levels, int num_levels, const te_solve_opts* opts,
+                    const double* f, long long* request_id);
+int te_serve_step(te_server* s, int* unfinished);
+int te_serve_poll(te_server* s, long long request_id, double* u, te_serve_result* result);
+int te_serve_stats(const te_server* s, te_serve_counters* out);
+
 /* ---- dot product without allocation ---------------------------------------
  * No counterpart in the reference (ThunderEgg reduces on the host).
  * For callers that cannot call cudaMalloc when they need a reduction: hosts

@@ -21,6 +21,7 @@ TE_NOALLOC_MAX_PARTIALS = 65536
 TE_CYCLE_V, TE_CYCLE_W, TE_CYCLE_FMG = 0, 1, 2
 TE_BICGSTAB_PRECONDITIONED_EXIT, TE_BICGSTAB_FP64_OUTER, TE_BICGSTAB_SLOTS = 1, 2, 4
 TE_TC_TF32X3, TE_TC_BF16 = 0, 1
+TE_PENDING = 8
 
 _ip = ctypes.POINTER(ctypes.c_int)
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -44,6 +45,32 @@ class TeCycleLevel(ctypes.Structure):
 class TeCycleOpts(ctypes.Structure):
     _fields_ = [("pre_sweeps", ctypes.c_int), ("post_sweeps", ctypes.c_int),
                 ("mid_sweeps", ctypes.c_int), ("coarse_sweeps", ctypes.c_int)]
+
+
+class TeServeOpts(ctypes.Structure):
+    _fields_ = [("budget_bytes", ctypes.c_double), ("steps_per_round", ctypes.c_int), ("max_batch", ctypes.c_int)]
+
+
+class TeSolveOpts(ctypes.Structure):
+    _fields_ = [("scheme", ctypes.c_int), ("fill_type", ctypes.c_int), ("smoother", ctypes.c_int),
+                ("inner_tol", ctypes.c_double), ("inner_max_iterations", ctypes.c_int),
+                ("inner_continue_on_breakdown", ctypes.c_int), ("pre_sweeps", ctypes.c_int),
+                ("post_sweeps", ctypes.c_int), ("coarse_sweeps", ctypes.c_int), ("tol", ctypes.c_double),
+                ("max_iterations", ctypes.c_int), ("cycle_dtype", ctypes.c_int), ("flags", ctypes.c_int),
+                ("tc_precision", ctypes.c_int)]
+
+
+class TeServeResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("iterations", ctypes.c_int), ("residual", ctypes.c_double),
+                ("latency_s", ctypes.c_double), ("restarts", ctypes.c_int)]
+
+
+class TeServeCounters(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_longlong), ("admitted", ctypes.c_longlong), ("completed", ctypes.c_longlong),
+                ("rejected", ctypes.c_longlong), ("union_builds", ctypes.c_longlong),
+                ("union_cache_hits", ctypes.c_longlong), ("slot_fills", ctypes.c_longlong),
+                ("reforms", ctypes.c_longlong), ("rounds", ctypes.c_longlong), ("queued", ctypes.c_int),
+                ("active", ctypes.c_int), ("classes", ctypes.c_int), ("bytes_in_use", ctypes.c_double)]
 
 
 class TeError(RuntimeError):
@@ -133,6 +160,13 @@ _SIGS = {
     "te_bicgstab_solve": (_I, [_V, _I, _V, _V, _V, _D, _I, _I, _ip, _dp]),
     "te_bicgstab_solve_batched": (_I, [_V, _I, _V, _V, _V, _D, _I, _I, _I, _ip, _ip, _dp, _ip]),
     "te_level_dot_noalloc": (_I, [_I, _ip, _I, _I, _I, _I, _V, _V, _dp, _V]),
+    "te_serve_create": (_I, [ctypes.POINTER(TeServeOpts), ctypes.POINTER(_V)]),
+    "te_serve_destroy": (_I, [_V]),
+    "te_serve_submit": (_I, [_V, ctypes.POINTER(TeLevelDesc), _I, ctypes.POINTER(TeSolveOpts), _dp,
+                             ctypes.POINTER(ctypes.c_longlong)]),
+    "te_serve_step": (_I, [_V, _ip]),
+    "te_serve_poll": (_I, [_V, ctypes.c_longlong, _dp, ctypes.POINTER(TeServeResult)]),
+    "te_serve_stats": (_I, [_V, ctypes.POINTER(TeServeCounters)]),
 }
 
 _lib = None

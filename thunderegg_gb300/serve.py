@@ -514,3 +514,92 @@ class Server:
     def __exit__(self, *exc):
         self.close()
         return False
+
+
+class NativeServer:
+    """The C ABI's serving loop (te_serve_*, include/te_gpu.h): continuous batching of the
+    same kind as Server, run by the library itself for callers outside Python.  Supports
+    Poisson requests with V-cycle-preconditioned BiCGStab (GmgOptions with cycle_type "V",
+    krylov "bicgstab", no coefficients, no boundary-ghost extrapolation)."""
+
+    def __init__(self, budget_bytes=150e9, steps_per_round=2, max_batch=64):
+        from .capi import TeServeOpts
+
+        o = TeServeOpts(float(budget_bytes), int(steps_per_round), int(max_batch))
+        h = ctypes.c_void_p()
+        check(lib().te_serve_create(ctypes.byref(o), ctypes.byref(h)))
+        self.h = h
+        self._f = {}
+
+    @staticmethod
+    def solve_opts(o: GmgOptions):
+        from .capi import TeSolveOpts
+
+        if o.cycle_type != "V" or o.krylov != "bicgstab" or o.extrapolate_boundary_ghosts:
+            raise ValueError("the native server runs V-cycle-preconditioned BiCGStab without extrapolation")
+        return TeSolveOpts(o.scheme, o.fill_type, o.smoother, o.inner_tol, o.inner_max_it,
+                           int(o.inner_continue_on_breakdown), o.pre_sweeps, o.post_sweeps, o.coarse_sweeps,
+                           o.tol, o.max_it, o.cycle_dtype, o.bicgstab_flags, o.tc_precision)
+
+    def submit(self, levels, f, opts: GmgOptions = GmgOptions()) -> int:
+        from .capi import TeLevelDesc
+
+        descs = (TeLevelDesc * len(levels))(*[lv.to_desc() for lv in levels])
+        so = self.solve_opts(opts)
+        fa = np.ascontiguousarray(f, dtype=np.float64)
+        rid = ctypes.c_longlong()
+        check(lib().te_serve_submit(self.h, descs, len(levels), ctypes.byref(so),
+                                    fa.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(rid)))
+        self._f[rid.value] = fa.shape
+        return rid.value
+
+    def step(self) -> int:
+        n = ctypes.c_int()
+        check(lib().te_serve_step(self.h, ctypes.byref(n)))
+        return n.value
+
+    def poll(self, rid):
+        """The request's Result once it has finished (returned once), else None."""
+        from .capi import TE_PENDING, TeServeResult
+
+        shape = self._f[rid]
+        u = np.empty(shape, dtype=np.float64)
+        r = TeServeResult()
+        rc = lib().te_serve_poll(self.h, rid, u.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(r))
+        if rc == TE_PENDING:
+            return None
+        check(rc)
+        del self._f[rid]
+        return Result(u, r.iterations, r.residual, r.status, r.latency_s, r.restarts)
+
+    def stats(self) -> dict:
+        from .capi import TeServeCounters
+
+        c = TeServeCounters()
+        check(lib().te_serve_stats(self.h, ctypes.byref(c)))
+        return {name: getattr(c, name) for name, _ in TeServeCounters._fields_}
+
+    def run(self, ids, max_rounds=10**9):
+        """Step until every listed request has finished; {id: Result}."""
+        out, r = {}, 0
+        while len(out) < len(ids) and r < max_rounds:
+            self.step()
+            r += 1
+            for i in ids:
+                if i not in out:
+                    res = self.poll(i)
+                    if res is not None:
+                        out[i] = res
+        return out
+
+    def close(self):
+        if self.h:
+            check(lib().te_serve_destroy(self.h))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+        return False
