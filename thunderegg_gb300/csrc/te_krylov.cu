@@ -47,6 +47,7 @@ enum Slot {
   S_BETA,
   S_DONE,
   S_BB,
+  S_XNZ = 14,   // the solve's x has a nonzero value on entry
   S_TRUE = 15,  // float-float loop: ||b - A x||^2 in FP64 after convergence
   S_NSLOTS = 16
 };
@@ -911,6 +912,21 @@ static void apply_df(const te_operator* A, const float* u, DV f, cudaStream_t st
 #undef TE_AD
 }
 
+// S[solve][S_XNZ] = 1 for every solve whose x (its patch range, ghosts included) has a nonzero
+// value; every writer stores the same value
+__global__ void x_nonzero(const double* __restrict__ x, long long n, long long pstride,
+                          const int* __restrict__ patch_solve, double* __restrict__ S) {
+  const long long step = (long long)gridDim.x * blockDim.x;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += 4 * step) {
+    double v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = i + k * step < n ? __ldg(x + i + k * step) : 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+      if (v[k] != 0.0) S[(size_t)patch_solve[(i + k * step) / pstride] * S_NSLOTS + S_XNZ] = 1.0;
+  }
+}
+
 // scalar exchange between a Krylov run's device state and mapped host memory (KrylovWork)
 __global__ void scalars_to_host(double* __restrict__ dst, const double* __restrict__ src, int n) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
@@ -1227,6 +1243,7 @@ struct BatchRun {
   std::vector<int> its, statuses;
   int nactive = 0, restart = 0;
   bool done = false, use_graph = true;
+  bool zero_x = false;  // float-float start: every solve's x was zero
   // slot mode (TE_BICGSTAB_SLOTS): solves are reset and finished one at a time while the
   // others iterate; step() only iterates
   bool slot_mode = false;
@@ -1272,24 +1289,38 @@ struct BatchRun {
       if (!W.dx.p) W.dx.alloc(W.n);
       TE_CUDA(cudaMemsetAsync(W.dx.p, 0, (size_t)W.n * sizeof(double), st));
       folded = true;
-      operator_residual(A, nc, x, b, W.ap.p, st);
-      // rhat = resid here, so rhat . resid and resid . resid are one sum (the same bits)
-      launch_dots(W, 2, b, b, W.ap.p, W.ap.p, nullptr, nullptr, S_BB, 0, st);
-      kd_split3<<<1216, 256, 0, st>>>(W.ap.p, W.dv(W.resid), W.dv(W.rhat), W.dv(W.p), nvals);
+      // when every solve starts from x = 0 (a served request's first batch), b - A x is b itself,
+      // bit for bit (A 0 = 0), and the FP64 operator pass is skipped
+      x_nonzero<<<1216, 256, 0, st>>>(x, nvals, d->lay.pstride(nc), W.patch_solve.p, W.S.p);
       count_launch();
       TE_LAUNCH_CHECK();
+      launch_dots(W, 1, b, b, nullptr, nullptr, nullptr, nullptr, S_BB, 0, st);
+      W.read_scalars(st);
+      zero_x = true;
+      for (int i = 0; i < B; i++) zero_x = zero_x && W.h[(size_t)i * S_NSLOTS + S_XNZ] == 0.0;
+      const double* r_in = b;
+      if (!zero_x) {
+        operator_residual(A, nc, x, b, W.ap.p, st);
+        r_in = W.ap.p;
+        // rhat = resid here, so rhat . resid and resid . resid are one sum (the same bits)
+        launch_dots(W, 2, b, b, W.ap.p, W.ap.p, nullptr, nullptr, S_BB, 0, st);
+      }
+      kd_split3<<<1216, 256, 0, st>>>(r_in, W.dv(W.resid), W.dv(W.rhat), W.dv(W.p), nvals);
+      count_launch();
+      TE_LAUNCH_CHECK();
+      if (!zero_x) W.read_scalars(st);
     } else {
       // resid = b - A x; rhat = p = resid (BiCGStab.h:113-131)
       operator_residual(A, nc, x, b, W.resid.p, st);
       TE_CUDA(cudaMemcpyAsync(W.rhat.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
       TE_CUDA(cudaMemcpyAsync(W.p.p, W.resid.p, bytes, cudaMemcpyDeviceToDevice, st));
       launch_dots(W, 2, b, b, W.resid.p, W.resid.p, nullptr, nullptr, S_BB, 0, st);
+      W.read_scalars(st);
     }
-    W.read_scalars(st);
     nactive = 0;
     for (int i = 0; i < B; i++) {
       double* h = W.h + (size_t)i * S_NSLOTS;
-      double bb = h[S_BB], rr = h[S_BB + 1], rh = rr;
+      double bb = h[S_BB], rr = df && zero_x ? bb : h[S_BB + 1], rh = rr;
       r0[i] = std::sqrt(bb);
       rho[i] = rh;
       residual[i] = r0[i] != 0 ? std::sqrt(rr) / r0[i] : 0.0;
