@@ -229,19 +229,37 @@ __device__ void k_reduce(double (&v)[NV], const Batch& bt, int b, int ch, double
   const int ch = blockIdx.x % MAX_CHUNKS;   \
   if (ch >= (bt).nch[b] || !(bt).active[b]) return;
 
-// dots of up to three pairs into S[b][slot0 ...]
-template <int NV>
-__global__ void __launch_bounds__(KT) k_dots(Layout L, int nc, Batch bt, const double* a0, const double* b0,
-                                             const double* a1, const double* b1, const double* a2, const double* b2,
-                                             double* part, unsigned int* counter, double* S, int slot0, int fin) {
+// dots of up to three pairs into S[b][slot0 ...], walking the cells with a Cells
+// walker (ChunkCells, or CubeCells for cubic patches) four at a time, their loads
+// issued before their products are summed in visit order
+template <int NV, class Cells>
+__global__ void __launch_bounds__(KT) k_dots_c(Layout L, int nc, Batch bt, const double* a0, const double* b0,
+                                               const double* a1, const double* b1, const double* a2,
+                                               const double* b2, double* part, unsigned int* counter, double* S,
+                                               int slot0, int fin) {
   TE_BLOCK_SOLVE(bt);
   double v[NV];
   for (int i = 0; i < NV; i++) v[i] = 0;
-  TE_CHUNK_LOOP(bt, L, nc, b, ch, k, {
-    v[0] += a0[k] * b0[k];
-    if (NV > 1) v[1] += a1[k] * b1[k];
-    if (NV > 2) v[2] += a2[k] * b2[k];
-  });
+  const double* as[3] = {a0, a1, a2};
+  const double* bs[3] = {b0, b1, b2};
+  Cells cells(bt, L, nc, b, ch);
+  long long k[4];
+  while (cells.next(k)) {
+    double x[NV][4], y[NV][4];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (k[u] >= 0)
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+          x[i][u] = __ldg(as[i] + k[u]);
+          y[i][u] = __ldg(bs[i] + k[u]);
+        }
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      if (k[u] >= 0)
+#pragma unroll
+        for (int i = 0; i < NV; i++) v[i] += x[i][u] * y[i][u];
+  }
   k_reduce<NV>(v, bt, b, ch, part, counter, S, slot0, fin, 0);
 }
 
@@ -384,6 +402,64 @@ struct ChunkCells {
   }
 };
 
+// ChunkCells for cubic patches of NN cells with one ghost layer whose interior is a
+// multiple of KT cells (2D n = 16, 32, 64; 3D n = 8, 16), launched with KT threads:
+// the same cells in the same order per thread, each at its thread's offset in the
+// patch plus a compile-time step (thread t's j-th cell of a patch is e = t + KT j).
+template <int DIM, int NN, int U>
+struct CubeCells {
+  static constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0;
+  static constexpr int N = DIM == 3 ? NN * NN * NN : NN * NN;
+  static constexpr int CPT = N / KT;
+  static constexpr int STEP = DIM == 2 ? (KT / NN) * SY : (KT / (NN * NN)) * SZ;
+  static_assert(N % KT == 0 && KT % NN == 0 && (DIM == 2 || KT % (NN * NN) == 0), "cells must tile the threads");
+  const int nc, pend, pstep, cs;
+  const long long ps;
+  const int toff;
+  int p, c, j;
+  long long base;
+  __device__ __forceinline__ CubeCells(const Batch& bt, const Layout& L, int nc_, int b, int ch)
+      : nc(nc_), pend(bt.offs[b + 1]), pstep(bt.nch[b]), cs(L.cs), ps(L.pstride(nc_)),
+        toff((int)(threadIdx.x % NN + 1) + (int)((threadIdx.x / NN) % NN + 1) * SY +
+             (DIM == 3 ? (int)(threadIdx.x / (NN * NN) + 1) * SZ : 0)) {
+    p = bt.offs[b] + ch;
+    c = 0;
+    j = 0;
+    base = (long long)p * ps + toff;
+  }
+  __device__ __forceinline__ bool next(long long (&k)[U]) {
+#pragma unroll
+    for (int r = 0; r < U; r++) {
+      if (j == CPT) {
+        j = 0;
+        if (++c == nc) {
+          c = 0;
+          p += pstep;
+        }
+        base = (long long)p * ps + (long long)c * cs + toff;
+      }
+      k[r] = p < pend ? base + (long long)j * STEP : -1;
+      j++;
+    }
+    return k[0] >= 0;
+  }
+};
+
+// calls fn(CubeCells<...>) for the layouts CubeCells covers, else fn(ChunkCells)
+template <int U, class Fn>
+void with_cells(const Layout& L, Fn&& fn) {
+  bool done = false;
+  with_cubic_size(L, [&](auto dim, auto nn) {
+    constexpr int DIM = decltype(dim)::value, NN = decltype(nn)::value;
+    constexpr int N = DIM == 3 ? NN * NN * NN : NN * NN;
+    if constexpr (N % KT == 0 && KT % NN == 0 && (DIM == 2 || KT % (NN * NN) == 0)) {
+      fn((CubeCells<DIM, NN, U>*)nullptr);
+      done = true;
+    }
+  });
+  if (!done) fn((ChunkCells<U>*)nullptr);
+}
+
 // block sums of float-float accumulators (the FP64 pipe stays idle until the last block)
 template <int NV>
 __device__ void kd_reduce(df64 (&v)[NV], const Batch& bt, int b, int ch, double* part, unsigned int* counter,
@@ -427,6 +503,7 @@ __global__ void __launch_bounds__(KT) kd_dots(Layout L, int nc, Batch bt, CV a0,
   kd_reduce<NV>(v, bt, b, ch, part, counter, S, slot0, fin, 0);
 }
 
+template <class Cells>
 __global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double tol, CV r, CV ap, DV s, double* part,
                                            unsigned int* counter, double* S) {
   TE_BLOCK_SOLVE(bt);
@@ -434,7 +511,7 @@ __global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double to
   kd_scalars(S + (size_t)b * S_NSLOTS, sc, 1, S_ALPHA, S_ALPHA);
   const df64 nalpha = -sc[0];
   dot2 d;
-  ChunkCells<2> cells(bt, L, nc, b, ch);
+  Cells cells(bt, L, nc, b, ch);
   long long k[2];
   while (cells.next(k)) {
     df64 rv[2], av[2];
@@ -456,6 +533,7 @@ __global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double to
   kd_reduce<1>(v, bt, b, ch, part, counter, S, S_SS, 5, tol);
 }
 
+template <class Cells>
 __global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV dx, DV r, const float* mp,
                                             const float* ms,
                                             CV ap, CV as, CV rhat, CV dir, double* part, unsigned int* counter,
@@ -472,7 +550,7 @@ __global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV dx
   if (done) {
     TE_CHUNK_LOOP(bt, L, nc, b, ch, k, { stv(dx, k, ldv(xc, k) + ldv(dir, k) * alpha); });
   } else {
-    ChunkCells<2> cells(bt, L, nc, b, ch);
+    Cells cells(bt, L, nc, b, ch);
     long long k[2];
     while (cells.next(k)) {
       df64 xv[2], rv[2], av[2], sv[2], hv[2];
@@ -503,6 +581,7 @@ __global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV dx
   kd_reduce<2>(v, bt, b, ch, part, counter, S, S_RR, 3, 0);
 }
 
+template <class Cells>
 __global__ void __launch_bounds__(KT) kd_p(Layout L, int nc, Batch bt, DV p, CV ap, CV r, const double* S) {
   TE_BLOCK_SOLVE(bt);
   const double* Sb = S + (size_t)b * S_NSLOTS;
@@ -511,7 +590,7 @@ __global__ void __launch_bounds__(KT) kd_p(Layout L, int nc, Batch bt, DV p, CV 
   kd_scalars(Sb, sc, 2, S_OMEGA, S_BETA);
   const df64 nomega = -sc[0], beta = sc[1];
   const CV pc = as_cv(p);
-  ChunkCells<2> cells(bt, L, nc, b, ch);
+  Cells cells(bt, L, nc, b, ch);
   long long k[2];
   while (cells.next(k)) {
     df64 pv[2], av[2], rv[2];
@@ -1069,12 +1148,18 @@ static void launch_dots(KrylovWork& W, int nv, const double* a0, const double* b
                         const double* a2, const double* b2, int slot0, int fin, cudaStream_t st) {
   const Layout& L = W.d->lay;
   Batch bt = W.batch();
-  if (nv == 1)
-    k_dots<1><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
-  else if (nv == 2)
-    k_dots<2><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
-  else
-    k_dots<3><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p, slot0, fin);
+  with_cells<4>(L, [&](auto* cells) {
+    using C = std::remove_pointer_t<decltype(cells)>;
+    if (nv == 1)
+      k_dots_c<1, C><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p,
+                                              slot0, fin);
+    else if (nv == 2)
+      k_dots_c<2, C><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p,
+                                              slot0, fin);
+    else
+      k_dots_c<3, C><<<W.grid(), KT, 0, st>>>(L, W.nc, bt, a0, b0, a1, b1, a2, b2, W.part.p, W.counter.p, W.S.p,
+                                              slot0, fin);
+  });
   count_launch();
   TE_LAUNCH_CHECK();
 }
@@ -1188,8 +1273,10 @@ static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, doubl
     count_launch();
     TE_LAUNCH_CHECK();
   }
-  kd_s<<<W.grid(), KT, 0, st>>>(L, nc, bt, tol, W.cv(W.resid), W.cv(W.ap), W.dv(W.s), W.part.p, W.counter.p,
-                                W.S.p);
+  with_cells<2>(L, [&](auto* cells) {
+    kd_s<std::remove_pointer_t<decltype(cells)>><<<W.grid(), KT, 0, st>>>(
+        L, nc, bt, tol, W.cv(W.resid), W.cv(W.ap), W.dv(W.s), W.part.p, W.counter.p, W.S.p);
+  });
   count_launch();
   TE_LAUNCH_CHECK();
   M->body_f32(W.f32(W.s), W.f32(W.ms), st);
@@ -1201,11 +1288,17 @@ static void iteration_df(KrylovWork& W, const te_operator* A, te_cycle* M, doubl
     TE_LAUNCH_CHECK();
   }
   const CV dir = (flags & TE_BICGSTAB_PRECONDITIONED_EXIT) ? CV{W.f32(W.mp), nullptr} : W.cv(W.p);
-  kd_xr<<<W.grid(), KT, 0, st>>>(L, nc, bt, W.dv(W.dx), W.dv(W.resid), W.f32(W.mp), W.f32(W.ms), W.cv(W.ap),
-                                 W.cv(W.as), W.cv(W.rhat), dir, W.part.p, W.counter.p, W.S.p);
+  with_cells<2>(L, [&](auto* cells) {
+    kd_xr<std::remove_pointer_t<decltype(cells)>><<<W.grid(), KT, 0, st>>>(
+        L, nc, bt, W.dv(W.dx), W.dv(W.resid), W.f32(W.mp), W.f32(W.ms), W.cv(W.ap), W.cv(W.as), W.cv(W.rhat), dir,
+        W.part.p, W.counter.p, W.S.p);
+  });
   count_launch();
   TE_LAUNCH_CHECK();
-  kd_p<<<W.grid(), KT, 0, st>>>(L, nc, bt, W.dv(W.p), W.cv(W.ap), W.cv(W.resid), W.S.p);
+  with_cells<2>(L, [&](auto* cells) {
+    kd_p<std::remove_pointer_t<decltype(cells)>><<<W.grid(), KT, 0, st>>>(L, nc, bt, W.dv(W.p), W.cv(W.ap),
+                                                                          W.cv(W.resid), W.S.p);
+  });
   count_launch();
   TE_LAUNCH_CHECK();
 }
