@@ -760,6 +760,43 @@ def config5_stream(args, te):
                     "union_builds": srv.stats["union_builds"] - builds0,
                     "union_cache_hits": srv.stats["union_hits"] - hits0})
     srv.close()
+    # the same request lists through the C ABI's native serving loop (te_serve_*)
+    from thunderegg_gb300.serve import NativeServer
+
+    nsrv = NativeServer(budget_bytes=150e9, steps_per_round=2)
+    warm = [nsrv.submit(mesh(k), PB.sine_modes_rhs(mesh(k)[0], rng), opts(k, te.TE_F32))
+            for k in sorted({k for _, kinds, _, _ in streams for k in kinds})]
+    nsrv.run(warm)
+    for o, (rate, kinds, reqs, arrivals) in zip(out, streams):
+        st0 = nsrv.stats()
+        t0 = time.perf_counter()
+        pending, nxt, lat, res_max = {}, 0, [], 0.0
+        while nxt < len(reqs) or pending:
+            now = time.perf_counter() - t0
+            while nxt < len(reqs) and arrivals[nxt] <= now:
+                pending[nsrv.submit(reqs[nxt].levels, reqs[nxt].f, reqs[nxt].opts)] = arrivals[nxt]
+                nxt += 1
+            if not pending:
+                time.sleep(max(0.0, min(arrivals[nxt] - now, 0.01)))
+                continue
+            nsrv.step()
+            for rid in list(pending):
+                r = nsrv.poll(rid)
+                if r is not None:
+                    lat.append(time.perf_counter() - t0 - pending.pop(rid))
+                    res_max = max(res_max, r.residual)
+        wall = time.perf_counter() - t0
+        lat.sort()
+        pick = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]  # noqa: E731
+        st1 = nsrv.stats()
+        o["native_server"] = {"solves_per_s": len(reqs) / wall, "latency_ms_p50": 1000 * pick(0.5),
+                              "latency_ms_p99": 1000 * pick(0.99), "max_rel_residual": res_max,
+                              "union_builds": st1["union_builds"] - st0["union_builds"],
+                              "union_cache_hits": st1["union_cache_hits"] - st0["union_cache_hits"],
+                              "slot_fills": st1["slot_fills"] - st0["slot_fills"],
+                              "host_s": {k: round(st1[k] - st0[k], 4) for k in ("build_s", "form_s", "step_s",
+                                                                                 "finish_s")}}
+    nsrv.close()
     # the plain FP64 drop-in, one solve at a time, over the same request lists
     stream = torch.cuda.current_stream()
     fp64_s = {}

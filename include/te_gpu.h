@@ -444,6 +444,10 @@ typedef struct te_serve_counters {
   long long union_builds, union_cache_hits, slot_fills, reforms, rounds;
   int queued, active, classes;
   double bytes_in_use; /* estimate: admitted requests and cached idle unions */
+  double build_s;      /* host seconds spent building unions (device objects)   */
+  double step_s;       /* host seconds in te_bicgstab_batch_step                 */
+  double finish_s;     /* host seconds finishing solves and copying results out  */
+  double form_s;       /* host seconds forming batches (iterates, uploads), without builds */
 } te_serve_counters;
 int te_serve_create(const te_serve_opts* opts, te_server** out);
 int te_serve_destroy(te_server* s);

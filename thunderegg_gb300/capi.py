@@ -70,7 +70,9 @@ class TeServeCounters(ctypes.Structure):
                 ("rejected", ctypes.c_longlong), ("union_builds", ctypes.c_longlong),
                 ("union_cache_hits", ctypes.c_longlong), ("slot_fills", ctypes.c_longlong),
                 ("reforms", ctypes.c_longlong), ("rounds", ctypes.c_longlong), ("queued", ctypes.c_int),
-                ("active", ctypes.c_int), ("classes", ctypes.c_int), ("bytes_in_use", ctypes.c_double)]
+                ("active", ctypes.c_int), ("classes", ctypes.c_int), ("bytes_in_use", ctypes.c_double),
+                ("build_s", ctypes.c_double), ("step_s", ctypes.c_double), ("finish_s", ctypes.c_double),
+                ("form_s", ctypes.c_double)]
 
 
 class TeError(RuntimeError):

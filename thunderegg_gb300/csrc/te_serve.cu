@@ -410,7 +410,9 @@ struct te_server {
     // had room for: idle unions give way, least recently used first
     while (!idle.empty() && live_bytes + idle_bytes() > o.budget_bytes) idle.pop_back();
     c.union_builds++;
+    const double t0 = now_s();
     auto u = build_union(ms, so);
+    c.build_s += now_s() - t0;
     u->key = key;
     u->members = members;
     return u;
@@ -448,6 +450,11 @@ struct te_server {
 
   // a new batch for the class: its running requests (iterates carried over) and waiting ones
   void reform(const std::string& ck, Class& cl) {
+    const double t0 = now_s(), b0 = c.build_s;
+    reform_(ck, cl);
+    c.form_s += (now_s() - t0) - (c.build_s - b0);
+  }
+  void reform_(const std::string& ck, Class& cl) {
     std::vector<Req*> members;
     if (cl.batch) {
       chk(te_bicgstab_batch_sync_x(cl.batch), "te_serve: sync");
@@ -468,6 +475,9 @@ struct te_server {
       members.push_back(cl.waiting.front());
       cl.waiting.pop_front();
     }
+    // slots in mesh order: a class that meets the same set of meshes again gets the same union
+    // key, so its cached union (and the union's captured graphs) are reused
+    std::stable_sort(members.begin(), members.end(), [](const Req* a, const Req* b) { return a->key < b->key; });
     cl.slot.clear();
     cl.slot_mesh.clear();
     cl.slot_key.clear();
@@ -559,7 +569,10 @@ struct te_server {
       // 4. iterate, then finish the solves that stopped
       if (!cl.batch) continue;
       int nrun = 0;
+      const double t0 = now_s();
       chk(te_bicgstab_batch_step(cl.batch, std::max(1, o.steps_per_round), &nrun), "te_serve: step");
+      const double t1 = now_s();
+      c.step_s += t1 - t0;
       const size_t B = cl.slot.size();
       std::vector<int> its(B), sts(B), running(B);
       std::vector<double> res(B);
@@ -574,6 +587,7 @@ struct te_server {
         for (size_t k = 0; k < stop.size(); k++)
           if (fin[k]) finish(cl, stop[k], its[stop[k]], res[stop[k]], sts[stop[k]]);
       }
+      c.finish_s += now_s() - t1;
       // an empty batch goes back to the cache
       bool any = false;
       for (Req* r : cl.slot) any = any || r;
