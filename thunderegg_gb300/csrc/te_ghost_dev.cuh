@@ -195,7 +195,10 @@ __device__ __forceinline__ T side_ghost(const Acc& acc, int p, int s, int code, 
 // the same terms in the same order, with the slab's own term and calls read
 // from the record.  A side has one incoming call per neighbour: at most 2 in
 // 2D and 4 in 3D; a record with more (ncalls -1 or above that) reads its slab.
-template <class T, int SCHEME, int D, class Acc>
+// IN_SMEM: the record is in shared memory, so the calls are read one at a time in a
+// loop (one copy of the call's code); otherwise the loop is unrolled, so that a record
+// held in registers is indexed with constants.
+template <class T, int SCHEME, int D, bool IN_SMEM = false, class Acc>
 __device__ __forceinline__ T side_ghost_rec(const Acc& acc, int p, int s, const SideRec& r,
                                             const GSlab* __restrict__ slabs, const GCall* __restrict__ calls,
                                             const FaceTable& ft, int i, int j) {
@@ -205,11 +208,19 @@ __device__ __forceinline__ T side_ghost_rec(const Acc& acc, int p, int s, const 
   if (r.ncalls < 0 || r.ncalls > MAXC) return side_ghost<T, SCHEME>(acc, p, s, r.code, slabs, calls, ft, D, i, j);
   T v = T(0);
   v = own_term<T, SCHEME>(v, acc, p, ft.f[side0 + s], D - 1, D, r.own_type, r.own_orth, i, j);
+  if constexpr (IN_SMEM) {
+#pragma unroll 1
+    for (int k = 0; k < r.ncalls; k++) {
+      const GCall cl = r.calls[k];
+      v = call_term<T, SCHEME>(v, acc, cl.src, ft.f[side0 + cl.src_face], D - 1, D, cl.type, cl.orth, i, j);
+    }
+  } else {
 #pragma unroll
-  for (int k = 0; k < MAXC; k++) {
-    if (k >= r.ncalls) break;
-    const GCall cl = r.calls[k];
-    v = call_term<T, SCHEME>(v, acc, cl.src, ft.f[side0 + cl.src_face], D - 1, D, cl.type, cl.orth, i, j);
+    for (int k = 0; k < MAXC; k++) {
+      if (k >= r.ncalls) break;
+      const GCall cl = r.calls[k];
+      v = call_term<T, SCHEME>(v, acc, cl.src, ft.f[side0 + cl.src_face], D - 1, D, cl.type, cl.orth, i, j);
+    }
   }
   return v;
 }

@@ -46,7 +46,8 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT, CPS ? CPS : 2048 / RShape
                             const int8_t* __restrict__ fntype, int FS, const T* __restrict__ finv, int neumann,
                             const T* __restrict__ coeff, FaceTable ft, const GSlab* __restrict__ slabs,
                             const GCall* __restrict__ calls, const int* __restrict__ side_code,
-                            const T* __restrict__ u, const TF* __restrict__ f, T* __restrict__ coarse) {
+                            const SideRec* __restrict__ recs, const T* __restrict__ u,
+                            const TF* __restrict__ f, T* __restrict__ coarse) {
   using S = RShape<DIM, NN>;
   constexpr int NB = DIM == 3 ? 8 : 4;  // fine cells per thread
   __shared__ __align__(16) T tile[S::CS];
@@ -69,11 +70,31 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT, CPS ? CPS : 2048 / RShape
   // ghosts (gathered from the neighbours' values, not this tile)
   constexpr int NG = 2 * DIM * S::NF;
   constexpr int GPT = (NG + S::NT - 1) / S::NT;
+  // 2D (one ghost per thread, a warp's threads on one or two sides): each warp copies the
+  // records of its sides (te_ghost_filler::d_side_rec) into shared memory, so a coarse-fine
+  // side's values are one dependent load away and no record is held in registers
+  constexpr bool REC = DIM == 2 && GPT == 1 && NG % 32 == 0;
+  constexpr int SPW = S::NF >= 32 ? 1 : 32 / S::NF;  // sides per gathering warp
+  __shared__ SideRec srec[REC ? (NG / 32) * SPW : 1];
   int code[GPT];
+  int my_rec = 0;
+  if constexpr (REC) {
+    code[0] = -1;
+    if (t < NG) {
+      const int w = t >> 5, l = t & 31, s0 = (w * 32) / S::NF;
+      constexpr int WORDS = sizeof(SideRec) / sizeof(int);
+      if (l < WORDS * SPW)
+        reinterpret_cast<int*>(srec + w * SPW)[l] = reinterpret_cast<const int*>(recs + p * 2 * DIM + s0)[l];
+      __syncwarp();
+      my_rec = w * SPW + t / S::NF - s0;
+      code[0] = srec[my_rec].code;
+    }
+  } else {
 #pragma unroll
-  for (int i = 0; i < GPT; i++) {
-    const int e = t + i * S::NT;
-    code[i] = (NG % S::NT == 0 || e < NG) ? side_code[p * 2 * DIM + e / S::NF] : -1;
+    for (int i = 0; i < GPT; i++) {
+      const int e = t + i * S::NT;
+      code[i] = (NG % S::NT == 0 || e < NG) ? side_code[p * 2 * DIM + e / S::NF] : -1;
+    }
   }
   constexpr bool VEC = (S::CS * sizeof(T)) % 16 == 0;
   constexpr int V = 16 / sizeof(T);
@@ -94,7 +115,10 @@ __global__ void __launch_bounds__(RShape<DIM, NN>::NT, CPS ? CPS : 2048 / RShape
     const int e = t + i * S::NT;
     if (code[i] != -1) {
       const int s = e / S::NF, r = e % S::NF;
-      gv[i] = side_ghost<T, SCHEME>(acc, p, s, code[i], slabs, calls, ft, DIM, r % NN, r / NN);
+      if constexpr (REC)
+        gv[i] = side_ghost_rec<T, SCHEME, DIM, true>(acc, p, s, srec[my_rec], slabs, calls, ft, r % NN, r / NN);
+      else
+        gv[i] = side_ghost<T, SCHEME>(acc, p, s, code[i], slabs, calls, ft, DIM, r % NN, r / NN);
     }
   }
   // 1. the padded patch (its ghosts are replaced below) and the gathered ghosts
@@ -202,7 +226,7 @@ static void launch_fine(const te_restrictor* r, const te_operator* op, const T* 
   auto run = [&](auto cps) {
     vc_restrict_fine_kernel<T, TF, KIND, SCHEME, DIM, NN, decltype(cps)::value><<<fd->lay.P, S::NT, 0, s>>>(
         r->fine_parent.p, r->fine_orth.p, fd->d_nbr_type.p, fd->F, fd->template inv<T>(), op->neumann, coeff,
-        g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_code.p, u, f, coarse);
+        g->faces, g->d_slabs.p, g->d_calls.p, g->d_side_code.p, g->d_side_rec.p, u, f, coarse);
     count_launch();
   };
   // the kernel writes disjoint parts of the coarse level and reads only u and f, so a
