@@ -262,17 +262,33 @@ __global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double*
   }
   const int N = NN > 0 ? (DIM == 3 ? NN * NN * NN : NN * NN) : L.interior();
   const int CS = NN > 0 ? (DIM == 3 ? (NN + 2) * (NN + 2) * (NN + 2) : (NN + 2) * (NN + 2)) : L.cs;
-  for (int pc = blockIdx.x; pc < npc; pc += gridDim.x) {
-    const long long base = (long long)pc * CS;
-    for (int e0 = threadIdx.x; e0 < N; e0 += VEC_UNROLL * blockDim.x) {
-      T xs[VEC_UNROLL], ys[VEC_UNROLL];
+  // the rounds (patch-component pc, first cell e0) of this thread, in order; the next round's
+  // loads are issued before the current round is summed
+  auto load = [&](int pc_, int e0_, T (&xs)[VEC_UNROLL], T (&ys)[VEC_UNROLL]) {
+    const long long base = (long long)pc_ * CS;
 #pragma unroll
-      for (int r = 0; r < VEC_UNROLL; r++) {
-        const int e = e0 + r * blockDim.x;
-        const long long k = e < N ? base + cell_offset<DIM, NN>(L, e) : -1;
-        xs[r] = k >= 0 ? x[k] : T(0);
-        ys[r] = MODE == 0 && k >= 0 ? y[k] : T(0);
-      }
+    for (int r = 0; r < VEC_UNROLL; r++) {
+      const int e = e0_ + r * blockDim.x;
+      const long long k = pc_ < npc && e < N ? base + cell_offset<DIM, NN>(L, e) : -1;
+      xs[r] = k >= 0 ? x[k] : T(0);
+      ys[r] = MODE == 0 && k >= 0 ? y[k] : T(0);
+    }
+  };
+  int pc = blockIdx.x, e0 = threadIdx.x;
+  if (e0 >= N) {  // more threads than cells: this thread's first round is the next patch's
+    e0 = N;
+  }
+  T xs[VEC_UNROLL], ys[VEC_UNROLL];
+  load(pc, e0, xs, ys);
+  while (pc < npc) {
+    int pc1 = pc, e1 = e0 + VEC_UNROLL * blockDim.x;
+    if (e1 >= N) {
+      pc1 += gridDim.x;
+      e1 = threadIdx.x;
+    }
+    T xn[VEC_UNROLL], yn[VEC_UNROLL];
+    load(pc1, e1, xn, yn);
+    {
 #pragma unroll
       for (int r = 0; r < VEC_UNROLL; r++) {
         if (F32) {
@@ -288,6 +304,13 @@ __global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double*
         }
       }
     }
+#pragma unroll
+    for (int r = 0; r < VEC_UNROLL; r++) {
+      xs[r] = xn[r];
+      ys[r] = yn[r];
+    }
+    pc = pc1;
+    e0 = e1;
   }
   if (F32) {
 #pragma unroll
@@ -319,48 +342,51 @@ __global__ void reduce_kernel(Layout L, int npc, const T* x, const T* y, double*
   }
 }
 
+// blocks of a reduction launch: as many as are resident at once (one wave, no tail), at most
+// the partials the domain holds and one per patch-component
+static int red_grid(const void* kern, const te_domain* d, int npc) {
+  static std::mutex mu;
+  static std::map<const void*, int> occ;
+  static int sms = 0;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!sms) TE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+  auto it = occ.find(kern);
+  if (it == occ.end()) {
+    int o = 0;
+    TE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, RED_THREADS, 0));
+    it = occ.emplace(kern, std::max(1, o)).first;
+  }
+  return std::max(1, std::min({sms * it->second, d->red_blocks, npc}));
+}
+
 static void reduce_launch(const te_domain* d, int nc, int dtype, const void* x, const void* y, int mode,
                           double* d_out, cudaStream_t s) {
-  int npc = d->lay.P * nc;
-  int grid = std::min(d->red_blocks, npc);
+  const int npc = d->lay.P * nc;
+  auto run = [&](auto kern, auto* xp, auto* yp) {
+    kern<<<red_grid((const void*)kern, d, npc), RED_THREADS, 0, s>>>(d->lay, npc, xp, yp, d->d_partials.p,
+                                                                     d->d_counter.p, d_out);
+  };
+  const double *xd = (const double*)x, *yd = (const double*)y;
+  const float *xf = (const float*)x, *yf = (const float*)y;
   // cubic patches with one ghost layer: constant index arithmetic (the same sums in the same order)
   const bool cubic = with_cubic_size(d->lay, [&](auto dim, auto nn) {
     constexpr int DIM = decltype(dim)::value, NN = decltype(nn)::value;
     if (dtype == TE_F64) {
-      if (mode == 0)
-        reduce_kernel<double, 0, DIM, NN><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, (const double*)y,
-                                                                      d->d_partials.p, d->d_counter.p, d_out);
-      else
-        reduce_kernel<double, 1, DIM, NN><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, nullptr,
-                                                                      d->d_partials.p, d->d_counter.p, d_out);
+      if (mode == 0) run(reduce_kernel<double, 0, DIM, NN>, xd, yd);
+      else run(reduce_kernel<double, 1, DIM, NN>, xd, (const double*)nullptr);
     } else {
-      if (mode == 0)
-        reduce_kernel<float, 0, DIM, NN><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const float*)x, (const float*)y,
-                                                                     d->d_partials.p, d->d_counter.p, d_out);
-      else
-        reduce_kernel<float, 1, DIM, NN><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const float*)x, nullptr,
-                                                                     d->d_partials.p, d->d_counter.p, d_out);
+      if (mode == 0) run(reduce_kernel<float, 0, DIM, NN>, xf, yf);
+      else run(reduce_kernel<float, 1, DIM, NN>, xf, (const float*)nullptr);
     }
   });
-  if (cubic) {
-    count_launch();
-    TE_LAUNCH_CHECK();
-    return;
-  }
-  if (dtype == TE_F64) {
-    if (mode == 0)
-      reduce_kernel<double, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, (const double*)y,
-                                                            d->d_partials.p, d->d_counter.p, d_out);
-    else
-      reduce_kernel<double, 1><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const double*)x, nullptr,
-                                                            d->d_partials.p, d->d_counter.p, d_out);
-  } else {
-    if (mode == 0)
-      reduce_kernel<float, 0><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const float*)x, (const float*)y,
-                                                           d->d_partials.p, d->d_counter.p, d_out);
-    else
-      reduce_kernel<float, 1><<<grid, RED_THREADS, 0, s>>>(d->lay, npc, (const float*)x, nullptr,
-                                                           d->d_partials.p, d->d_counter.p, d_out);
+  if (!cubic) {
+    if (dtype == TE_F64) {
+      if (mode == 0) run(reduce_kernel<double, 0>, xd, yd);
+      else run(reduce_kernel<double, 1>, xd, (const double*)nullptr);
+    } else {
+      if (mode == 0) run(reduce_kernel<float, 0>, xf, yf);
+      else run(reduce_kernel<float, 1>, xf, (const float*)nullptr);
+    }
   }
   count_launch();
   TE_LAUNCH_CHECK();
