@@ -534,7 +534,7 @@ __global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double to
 }
 
 template <class Cells>
-__global__ void __launch_bounds__(KT, 3) kd_xr(Layout L, int nc, Batch bt, DV dx, DV r, const float* mp,
+__global__ void __launch_bounds__(KT, 4) kd_xr(Layout L, int nc, Batch bt, DV dx, DV r, const float* mp,
                                             const float* ms,
                                             CV ap, CV as, CV rhat, CV dir, double* part, unsigned int* counter,
                                             double* S) {
@@ -761,7 +761,7 @@ __global__ void __launch_bounds__(256)
 // ghosts, the boundary shell after it.  f's ghost cells are not written (the
 // outer loop never reads them).
 template <int KIND, int SCHEME, int DIM, int NN, int NV>
-__global__ void __launch_bounds__(256, 6)
+__global__ void __launch_bounds__(256, 8)
     apply_dots_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const float2* __restrict__ inv_df,
                       int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
                       const GCall* __restrict__ calls, const int* __restrict__ side_code,
