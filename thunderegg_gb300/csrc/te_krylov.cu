@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(KT) kd_dots(Layout L, int nc, Batch bt, CV a0,
 }
 
 template <class Cells>
-__global__ void __launch_bounds__(KT) kd_s(Layout L, int nc, Batch bt, double tol, CV r, CV ap, DV s, double* part,
+__global__ void __launch_bounds__(KT, 8) kd_s(Layout L, int nc, Batch bt, double tol, CV r, CV ap, DV s, double* part,
                                            unsigned int* counter, double* S) {
   TE_BLOCK_SOLVE(bt);
   __shared__ df64 sc[1];
