@@ -69,7 +69,7 @@ def dist_info():
 # ---------------------------------------------------------------------------
 # CPU legs (the oracle is test infrastructure: used here only as the baseline)
 # ---------------------------------------------------------------------------
-def _cpu_solve_worker(q):
+def _cpu_solve_worker(q, ready=None, go=None):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as orc
     from thunderegg_gb300 import problems as PB
@@ -77,6 +77,9 @@ def _cpu_solve_worker(q):
     levels, f, _ = PB.config2()
     cfg = orc.gmg_config(scheme=1, smoother=0, tol=1e-10)
     O = orc.Oracle("teo")
+    if ready is not None:  # the mesh is built: wait until every worker is, then solve together
+        ready.put(1)
+        go.wait()
     t = time.perf_counter()
     u, its, res, rc = O.solve(levels, f, cfg)
     q.put((time.perf_counter() - t, its, rc))
@@ -163,7 +166,9 @@ def err_vs(u, ref, lv):
 
 
 def cpu_solves(nproc):
-    """Run nproc independent solves in parallel processes; returns (wall, [times])."""
+    """Run nproc independent solves in parallel processes; returns (wall, [times]).  The wall
+    runs from the moment every process has built its mesh to the last solution: process start-up
+    and the Python mesh build are outside it."""
     import multiprocessing as mp
 
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -171,15 +176,19 @@ def cpu_solves(nproc):
 
     orc.build()
     ctx = mp.get_context("spawn")
-    q = ctx.Queue()
-    procs = [ctx.Process(target=_cpu_solve_worker, args=(q,)) for _ in range(nproc)]
-    t = time.perf_counter()
+    q, ready, go = ctx.Queue(), ctx.Queue(), ctx.Event()
+    procs = [ctx.Process(target=_cpu_solve_worker, args=(q, ready, go)) for _ in range(nproc)]
     for p in procs:
         p.start()
+    for _ in procs:
+        ready.get()
+    t = time.perf_counter()
+    go.set()
     out = [q.get() for _ in procs]
+    wall = time.perf_counter() - t
     for p in procs:
         p.join()
-    return time.perf_counter() - t, out
+    return wall, out
 
 
 def run_reference(args):
@@ -188,8 +197,9 @@ def run_reference(args):
         return
     cores = os.cpu_count() or 1
     steps, warm = max(1, args.steps), max(0, args.warmup)
-    # bounded: each step is one round of `cores` parallel solves; cap total rounds
-    rounds, warm = min(steps, 3), min(warm, 3)
+    # bounded: each step is one round of `cores` parallel solves (about 5 s on 16 Grace cores);
+    # at most 20 timed rounds and 3 warm-up rounds, so a run ends within two minutes
+    rounds, warm = min(steps, 20), min(warm, 3)
     for _ in range(warm):
         cpu_solves(cores)
     walls, its = [], None
@@ -352,6 +362,38 @@ def level_kernel_rooflines(te, solver, hbm, reps=15, warm=3):
                         "frac": round(gbs / hbm, 3)})
     return {"level": f"{f0.num_patches} patches of {f0.ns[0]}^{f0.dim} (+ {f1.num_patches} coarse)",
             "peak_gbs": hbm, "l2": "flushed before every call", "kernels": out}
+
+
+def fp64_krylov_measure(te, blevels, offsets, fB, reps=3):
+    """The served config-2 batch with the outer BiCGStab in FP64 (TE_BICGSTAB_FP64_OUTER: FP64
+    vectors, inner products and updates) around the same FP32 V-cycle, beside the default
+    float-float loop: what keeping the Krylov arithmetic in FP64 costs on GB300."""
+    import torch
+
+    from thunderegg_gb300.gmg import GmgOptions, GmgSolver
+
+    s = GmgSolver(blevels, GmgOptions(scheme=1, smoother=0, tol=1e-10, cycle_dtype=te.TE_F32,
+                                      bicgstab_flags=1 | te.capi.TE_BICGSTAB_FP64_OUTER))
+    u = te.Vector(s.finest)
+    stream = torch.cuda.current_stream()
+    times, its = [], None
+    for r in range(reps + 1):
+        u.t.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its, res, st = s.solve_batched(fB, u, offsets[0])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if r > 0:
+            times.append(e0.elapsed_time(e1) / 1000.0)
+    B = len(offsets[0]) - 1
+    t = statistics.median(times)
+    out = {"ms_per_batch": 1000 * t, "solves_per_s": B / t, "outer_iterations": max(its),
+           "max_final_rel_residual": max(res),
+           "form": "FP32 V-cycle (3xTF32 transforms) inside an FP64 BiCGStab (TE_BICGSTAB_FP64_OUTER)"}
+    del s, u
+    return out
 
 
 def batch_scaling_measure(te, sizes=(1, 4, 16, 32, 64), reps=3):
@@ -1037,6 +1079,7 @@ def run_gpu(args):
     lk = optional(level_kernel_rooflines, te, served, hbm) if extra else None
     sv = optional(solver_variants_measure, te) if extra else None
     bs = optional(batch_scaling_measure, te) if extra else None
+    fk = optional(fp64_krylov_measure, te, blevels, offsets, fB) if extra else None
 
     # error of every result against the oracle's FP64 solve of the same problem
     oracle_err = None
@@ -1132,6 +1175,7 @@ def run_gpu(args):
         "level_kernels": lk,
         "solver_variants": sv,
         "batch_scaling": bs,
+        "served_fp64_krylov": fk,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
