@@ -190,16 +190,19 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+// test the phase; while it is incomplete the thread is suspended in hardware (issuing
+// nothing) until it completes or about `suspend_ns` nanoseconds have passed
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity, uint32_t suspend_ns = 1000000u) {
   uint32_t ok;
   asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
       : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(suspend_ns)
       : "memory");
   return ok != 0;
 }
 // wait for the phase with the given parity to complete; false after ~`limit` clock cycles
+// (each try suspends for at most about a millisecond, so the limit is checked regularly)
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long limit) {
   long long t0 = clock64();
   while (!mbar_try_wait(bar, parity))
