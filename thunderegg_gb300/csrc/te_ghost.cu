@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(GHOST_THREADS)
 // corners) follow slab by slab when `other` is set.  Slabs write disjoint
 // ghost cells and read only interior cells, so they need no order.
 template <class T, int SCHEME>
-__global__ void __launch_bounds__(GHOST_THREADS)
+__global__ void __launch_bounds__(GHOST_THREADS, 12)
     ghost_fill_sides_kernel(Layout L, int nc, FaceTable ft, const GSlab* __restrict__ slabs,
                             const GCall* __restrict__ calls, const int* __restrict__ slab_start,
                             const int* __restrict__ side_code, int NP, int gmax, int other, T* u) {
