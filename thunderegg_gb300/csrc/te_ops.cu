@@ -149,24 +149,9 @@ __global__ void modify_rhs_kernel(Layout L, int nc, const int8_t* __restrict__ n
 }
 
 // apply_kernel for cubic patches of NN cells with one ghost layer: the same
-// per-cell arithmetic with constant strides; a thread loads all of its cells'
-// stencils before it stores, so each thread keeps several loads in flight.
-template <class T, int KIND, int DIM, int SY, int SZ>
-__device__ __forceinline__ T stencil_n(const T* u, const T* c, int k, const T* inv) {
-  T r = T(0);
-#pragma unroll
-  for (int a = 0; a < DIM; a++) {
-    const int st = a == 0 ? 1 : (a == 1 ? SY : SZ);
-    T lo = u[k - st], mid = u[k], hi = u[k + st];
-    if (KIND == 0) {
-      r += ((hi - T(2) * mid) + lo) * inv[a];
-    } else {
-      T cl = c[k - st], cm = c[k], cu = c[k + st];
-      r += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
-    }
-  }
-  return r;
-}
+// per-cell arithmetic with constant strides (stencil_n, te_ops.cuh); a thread
+// loads all of its cells' stencils before it stores, so each thread keeps
+// several loads in flight.
 template <class T, int KIND, int DIM, int NN>
 __global__ void __launch_bounds__(256)
     apply_n_kernel(Layout L, int nc, const int8_t* __restrict__ ntype, int F, const T* __restrict__ sp,
@@ -228,6 +213,7 @@ static bool launch_apply(const te_operator* op, int nc, const T* inv, const T* c
 
 void operator_residual(const te_operator* op, int nc, void* u, const void* b, void* r, cudaStream_t s) {
   const te_domain* d = op->dom;
+  if (operator_apply_fused<double>(op, nc, (double*)u, (double*)r, (const double*)b, s)) return;
   ghost_fill(op->gf, nc, TE_F64, u, s);
   const bool fused =
       op->kind == 0
@@ -246,6 +232,9 @@ void operator_residual(const te_operator* op, int nc, void* u, const void* b, vo
 
 void operator_apply(const te_operator* op, int nc, int dtype, void* u, void* f, cudaStream_t s) {
   const te_domain* d = op->dom;
+  if (dtype == TE_F64 ? operator_apply_fused<double>(op, nc, (double*)u, (double*)f, nullptr, s)
+                      : operator_apply_fused<float>(op, nc, (float*)u, (float*)f, nullptr, s))
+    return;
   ghost_fill(op->gf, nc, dtype, u, s);
   if (dtype == TE_F64) {
     if (op->kind == 0)

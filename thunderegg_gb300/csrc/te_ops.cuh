@@ -58,6 +58,29 @@ struct te_patch_solver {
 };
 
 namespace te {
+// one interior cell k of the star stencil of a cubic patch (constant strides SY, SZ), axis 0
+// first, in the reference's operation order (Poisson/StarPatchOperator.h:96-110,
+// VarPoisson/StarPatchOperator.h:93-113); u and c may point to global or shared memory
+template <class T, int KIND, int DIM, int SY, int SZ>
+__device__ __forceinline__ T stencil_n(const T* u, const T* c, int k, const T* inv) {
+  T r = T(0);
+#pragma unroll
+  for (int a = 0; a < DIM; a++) {
+    const int st = a == 0 ? 1 : (a == 1 ? SY : SZ);
+    T lo = u[k - st], mid = u[k], hi = u[k + st];
+    if (KIND == 0) {
+      r += ((hi - T(2) * mid) + lo) * inv[a];
+    } else {
+      T cl = c[k - st], cm = c[k], cu = c[k + st];
+      r += ((cu + cm) * (hi - mid) - (cl + cm) * (mid - lo)) * inv[a];
+    }
+  }
+  return r;
+}
+// f = A u (rhs null) or rhs - A u with u's side ghosts filled, in one kernel where the level
+// qualifies (te_apply.cu); false when nothing ran
+template <class T>
+bool operator_apply_fused(const te_operator* op, int nc, T* u, T* f, const T* rhs, cudaStream_t s);
 void operator_apply(const te_operator* op, int nc, int dtype, void* u, void* f, cudaStream_t s);
 // r = b - A u (FP64; u's ghosts are filled as by operator_apply); one pass on cubic levels
 void operator_residual(const te_operator* op, int nc, void* u, const void* b, void* r, cudaStream_t s);
