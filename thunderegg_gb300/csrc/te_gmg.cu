@@ -9,10 +9,12 @@
 //   Iterative::BiCGStab::solve (Iterative/BiCGStab.h:111-203).
 
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 
 #include "te_gmg.cuh"
+#include "te_tune.cuh"
 
 namespace te {
 
@@ -209,8 +211,10 @@ __global__ void __launch_bounds__(256)
 // for a patch that is its own parent, copies its interior (copyToParent,
 // :129-147).  The coarse ghost ring is zero: the orthant-0 child (or the
 // copied patch) writes it.
-template <class T, int DIM, int NN>
-__global__ void __launch_bounds__(256)
+// NTR threads per CTA: 256, or 128 (two coarse cells per thread at twice the resident CTAs;
+// the autotuner picks, both give the same bits)
+template <class T, int DIM, int NN, int NTR = 256>
+__global__ void __launch_bounds__(NTR, 2048 / NTR)
     restrict_n_kernel(int nc, const int* __restrict__ fparent, const int* __restrict__ forth,
                       const T* __restrict__ fine, T* __restrict__ coarse) {
   constexpr int SY = NN + 2, SZ = DIM == 3 ? SY * SY : 0, CS = DIM == 3 ? SY * SY * SY : SY * SY;
@@ -227,32 +231,32 @@ __global__ void __launch_bounds__(256)
     const T* fc = fv + (long long)c * CS;
     T* cc = cv + (long long)c * CS;
     if (o < 0) {
-      constexpr int PER = (NI + 255) / 256;
+      constexpr int PER = (NI + NTR - 1) / NTR;
       T v[PER];
 #pragma unroll
       for (int r = 0; r < PER; r++) {
-        const int e = threadIdx.x + r * 256;
-        if (NI % 256 == 0 || e < NI) {
+        const int e = threadIdx.x + r * NTR;
+        if (NI % NTR == 0 || e < NI) {
           const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
           v[r] = fc[(x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0)];
         }
       }
 #pragma unroll
       for (int r = 0; r < PER; r++) {
-        const int e = threadIdx.x + r * 256;
-        if (NI % 256 == 0 || e < NI) {
+        const int e = threadIdx.x + r * NTR;
+        if (NI % NTR == 0 || e < NI) {
           const int x = e % NN, y = (e / NN) % NN, z = DIM == 3 ? e / (NN * NN) : 0;
           cc[(x + 1) + (y + 1) * SY + (DIM == 3 ? (z + 1) * SZ : 0)] = v[r];
         }
       }
     } else {
       const int ox = (o & 1) ? H : 0, oy = (o & 2) ? H : 0, oz = (o & 4) ? H : 0;
-      constexpr int PER = (NQ + 255) / 256;
+      constexpr int PER = (NQ + NTR - 1) / NTR;
       T v[PER];
 #pragma unroll
       for (int r = 0; r < PER; r++) {
-        const int e = threadIdx.x + r * 256;
-        if (NQ % 256 == 0 || e < NQ) {
+        const int e = threadIdx.x + r * NTR;
+        if (NQ % NTR == 0 || e < NQ) {
           const int x = e % H, y = (e / H) % H, z = DIM == 3 ? e / (H * H) : 0;
           const int k = (2 * x + 1) + (2 * y + 1) * SY + (DIM == 3 ? (2 * z + 1) * SZ : 0);
           T s = T(0);
@@ -267,8 +271,8 @@ __global__ void __launch_bounds__(256)
       }
 #pragma unroll
       for (int r = 0; r < PER; r++) {
-        const int e = threadIdx.x + r * 256;
-        if (NQ % 256 == 0 || e < NQ) {
+        const int e = threadIdx.x + r * NTR;
+        if (NQ % NTR == 0 || e < NQ) {
           const int x = e % H, y = (e / H) % H, z = DIM == 3 ? e / (H * H) : 0;
           cc[(x + ox + 1) + (y + oy + 1) * SY + (DIM == 3 ? (z + oz + 1) * SZ : 0)] = v[r];
         }
@@ -277,7 +281,7 @@ __global__ void __launch_bounds__(256)
     if (o <= 0) {
       // ghost ring: 2D rows 0 and SY-1, then the end cells of rows 1..NN; 3D planes
       // 0 and SY-1, then the 2D ring of planes 1..NN
-      for (int e = threadIdx.x; e < RING; e += 256) {
+      for (int e = threadIdx.x; e < RING; e += NTR) {
         int k;
         if (DIM == 2) {
           if (e < 2 * SY) {
@@ -537,15 +541,25 @@ void restrict_level(const te_restrictor* r, int nc, int dtype, const void* fine,
   if (r->complete && !r->extrapolate && F.n0 == C.n0 && F.n1 == C.n1 && F.n2 == C.n2 && F.P > 0) {
     const bool fixed = with_cubic_size(F, [&](auto dim, auto nn) {
       constexpr int DIM = decltype(dim)::value, NN = decltype(nn)::value;
-      if (dtype == TE_F64)
-        restrict_n_kernel<double, DIM, NN><<<F.P, 256, 0, s>>>(nc, r->fine_parent.p, r->fine_orth.p,
-                                                              (const double*)fine, (double*)coarse);
-      else
-        restrict_n_kernel<float, DIM, NN><<<F.P, 256, 0, s>>>(nc, r->fine_parent.p, r->fine_orth.p,
-                                                             (const float*)fine, (float*)coarse);
+      auto run = [&](auto ntr) {
+        constexpr int NTR = decltype(ntr)::value;
+        if (dtype == TE_F64)
+          restrict_n_kernel<double, DIM, NN, NTR><<<F.P, NTR, 0, s>>>(nc, r->fine_parent.p, r->fine_orth.p,
+                                                                     (const double*)fine, (double*)coarse);
+        else
+          restrict_n_kernel<float, DIM, NN, NTR><<<F.P, NTR, 0, s>>>(nc, r->fine_parent.p, r->fine_orth.p,
+                                                                    (const float*)fine, (float*)coarse);
+        count_launch();
+      };
+      // a candidate rewrites the same coarse values, so it can run again for timing
+      std::vector<TuneCandidate> cands = {{"threads=256", [&] { run(IntC<256>()); }},
+                                          {"threads=128", [&] { run(IntC<128>()); }}};
+      char key[96];
+      std::snprintf(key, sizeof key, "D=%d n=%d P~2^%d %s nc=%d", DIM, NN, tune_bucket(F.P),
+                    dtype == TE_F64 ? "f64" : "f32", nc);
+      cands[tune_select("restrict_n", key, cands, s)].run();
     });
     if (fixed) {
-      count_launch();
       TE_LAUNCH_CHECK();
       return;
     }
