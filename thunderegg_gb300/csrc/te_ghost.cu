@@ -272,13 +272,26 @@ int te_ghost_filler_create(const te_domain* d, int scheme, int fill_type, te_gho
       for (auto& c : g->calls)
         require(c[4] == TE_NBR_NORMAL, "BiLinear with odd patch size across a coarse-fine face",
                 TE_ERR_UNSUPPORTED);
-    // transpose: incoming calls per (patch, slot), kept in call order
-    std::vector<std::vector<int>> incoming((size_t)P * F);
+    // transpose: incoming calls per (patch, slot), kept in call order (CSR: in_start, in_call)
+    std::vector<int> in_start((size_t)P * F + 1, 0), in_slot(g->calls.size());
     for (size_t k = 0; k < g->calls.size(); k++) {
       auto& c = g->calls[k];
       int tgt = c[1], M = c[2], opp = face_opposite(D, M, c[3]);
-      incoming[(size_t)tgt * F + slot_of(D, M, opp)].push_back((int)k);
+      in_slot[k] = (int)((size_t)tgt * F + slot_of(D, M, opp));
+      in_start[(size_t)in_slot[k] + 1]++;
     }
+    for (size_t q = 0; q < (size_t)P * F; q++) in_start[q + 1] += in_start[q];
+    std::vector<int> in_call(g->calls.size()), fill_pos(in_start.begin(), in_start.end() - 1);
+    for (size_t k = 0; k < g->calls.size(); k++) in_call[(size_t)fill_pos[(size_t)in_slot[k]]++] = (int)k;
+    struct Incoming {
+      const int* b;
+      const int* e;
+      bool empty() const { return b == e; }
+      size_t size() const { return (size_t)(e - b); }
+      const int* begin() const { return b; }
+      const int* end() const { return e; }
+    };
+    auto incoming_of = [&](size_t q) { return Incoming{in_call.data() + in_start[q], in_call.data() + in_start[q + 1]}; };
     std::vector<GCall> hc;
     g->h_slab_start.assign(P + 1, 0);
     for (int p = 0; p < P; p++) {
@@ -287,7 +300,7 @@ int te_ghost_filler_create(const te_domain* d, int scheme, int fill_type, te_gho
         for (int f = 0; f < num_faces(D, M); f++) {
           int slot = slot_of(D, M, f);
           int t = d->nbr_type[(size_t)p * F + slot];
-          auto& inc = incoming[(size_t)p * F + slot];
+          const Incoming inc = incoming_of((size_t)p * F + slot);
           if (t < 0 && inc.empty()) continue;
           GSlab s;
           std::memset(&s, 0, sizeof s);

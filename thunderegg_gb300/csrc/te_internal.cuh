@@ -11,6 +11,7 @@
 #include <stdexcept>
 #include <string>
 #include <type_traits>
+#include <unordered_map>
 #include <vector>
 
 #include "te_gpu.h"
@@ -162,7 +163,7 @@ struct te_domain {
   std::vector<int> id, refine_level, parent_id, orth_on_parent, child_ids, nbr_type, nbr_ids, nbr_orth,
       nbr_local;
   std::vector<double> starts, spacings;
-  std::map<int, int> id2l;
+  std::unordered_map<int, int> id2l;
   // device copies
   te::DevBuf<int8_t> d_nbr_type;   // [P*F]
   te::DevBuf<int8_t> d_nbr_orth;   // [P*F]

@@ -486,6 +486,7 @@ int te_domain_create(const te_level_desc* desc, te_domain** out) {
     d->nbr_ids.assign(desc->nbr_ids, desc->nbr_ids + (size_t)P * F * 4);
     d->nbr_orth.assign(desc->nbr_orth, desc->nbr_orth + (size_t)P * F);
     // Domain::indexPatchesLocal (Domain.h:94-110): local index = position
+    d->id2l.reserve((size_t)P * 2);
     for (int p = 0; p < P; p++) {
       require(d->id2l.count(d->id[p]) == 0, "duplicate patch id");
       d->id2l[d->id[p]] = p;
