@@ -929,22 +929,37 @@ __global__ void __launch_bounds__(256, 8)
     }
     emit(k, res);
   }
-  // block sums in float-float, then this solve's patch partials in patch order
-  __shared__ df64 red[NV][256 / 32];
+  // block sums of the threads' compensated pairs (s, c), then this solve's patch partials in
+  // patch order: every pair into shared memory; the 32 threads of warp 0 merge eight pairs each
+  // (thread l: l, l + 32, ...), then across the warp -- a merge adds the s parts exactly
+  // (TwoSum) and carries its error with the c parts, as Dot2 accumulates one pair
+  __shared__ float2 red[NV][256];
 #pragma unroll
-  for (int i = 0; i < NV; i++) {
-    df64 x = v[i].value();
-    for (int o = 16; o > 0; o >>= 1) x += df_shfl_down(x, o);
-    if ((threadIdx.x & 31) == 0) red[i][threadIdx.x >> 5] = x;
-  }
+  for (int i = 0; i < NV; i++) red[i][threadIdx.x] = make_float2(v[i].s, v[i].c);
   __syncthreads();
   double blk[NV];
-  if (threadIdx.x == 0)
+  if (threadIdx.x < 32) {
+    const int l = threadIdx.x;
+#pragma unroll
     for (int i = 0; i < NV; i++) {
-      df64 t = red[i][0];
-      for (int q = 1; q < (int)(blockDim.x >> 5); q++) t += red[i][q];
-      blk[i] = df_to_double(t);
+      float sm = red[i][l].x, cm = red[i][l].y;
+#pragma unroll
+      for (int q = 1; q < 8; q++) {
+        const float2 o = red[i][l + 32 * q];
+        const df64 t2 = two_sum(sm, o.x);
+        sm = t2.hi;
+        cm = __fadd_rn(cm, __fadd_rn(o.y, t2.lo));
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const float so = __shfl_down_sync(0xffffffffu, sm, off), co = __shfl_down_sync(0xffffffffu, cm, off);
+        const df64 t2 = two_sum(sm, so);
+        sm = t2.hi;
+        cm = __fadd_rn(cm, __fadd_rn(co, t2.lo));
+      }
+      blk[i] = df_to_double(two_sum(sm, cm));
     }
+  }
   const int first = bt.offs[b];
   kp_reduce<NV>(blk, bt.B, b, first, bt.offs[b + 1] - first, p, part, L.P, counter, S, slot0, finalize_kind);
 }
