@@ -1033,7 +1033,7 @@ def run_gpu(args):
         return e0.elapsed_time(e1) / 1000.0
 
     e2e_run(2)  # warm-up: graphs of the second buffer set
-    k_e2e = max(4, args.steps // 2)
+    k_e2e = max(4, args.steps)
     e_time = e2e_run(k_e2e)
     e2e = world * B * k_e2e / e_time
     e2e_copy_gbs = 2 * fB_np.nbytes * k_e2e / e_time / 1e9

@@ -52,5 +52,27 @@ int main() {
                             -1e-300, 2.0e-23, 1.5, 0.1, 1.0 / 3.0};
   for (double d : special) check(d);
   std::printf("%lld of %lld splits differ\n", bad, n);
-  return bad == 0 ? 0 : 1;
+  // f2d_bits: the exact widening of every float class (normal, zero of both signs, subnormal,
+  // infinite, NaN) equals the cast bit for bit
+  long long badw = 0, nw = 0;
+  auto checkw = [&](uint32_t fb) {
+    float f;
+    std::memcpy(&f, &fb, 4);
+    const double a = te::f2d_bits(f), want = (double)f;
+    uint64_t ab, wb;
+    std::memcpy(&ab, &a, 8);
+    std::memcpy(&wb, &want, 8);
+    nw++;
+    if (ab != wb && !(a != a && want != want)) {
+      if (badw < 10) std::printf("widening mismatch f=%a: got %a want %a\n", f, a, want);
+      badw++;
+    }
+  };
+  for (uint32_t e = 0; e < 256; e++)
+    for (int i = 0; i < 4000; i++) checkw((uint32_t)(g() & 0x807fffffu) | (e << 23));
+  const uint32_t fspecial[] = {0u, 0x80000000u, 1u, 0x807fffffu, 0x00800000u, 0x7f7fffffu, 0x7f800000u,
+                               0xff800000u, 0x7fc00000u, 0x3f800000u};
+  for (uint32_t fb : fspecial) checkw(fb);
+  std::printf("%lld of %lld widenings differ\n", badw, nw);
+  return bad == 0 && badw == 0 ? 0 : 1;
 }

@@ -1,7 +1,8 @@
 """The integer float-float split used for FP64 vectors (df_split_bits in
 thunderegg_gb300/csrc/te_df64.cuh) equals the FP64 formula hi = RN(d),
 lo = RN(d - hi) bit for bit on random bit patterns, the solver's value
-range, rounding ties and carries, and special values (host code, no GPU)."""
+range, rounding ties and carries, and special values; and the integer widening
+f2d_bits equals the float-to-double cast for every float class (host code, no GPU)."""
 import os
 import shutil
 import subprocess

@@ -81,6 +81,38 @@ __host__ __device__ __forceinline__ df64 df_split_bits(double d) {
 }
 __host__ __device__ __forceinline__ double df_to_double(df64 a) { return (double)a.hi + (double)a.lo; }
 
+// (double)f built from f's bits with integer operations (the exponent rebiased from 127 to
+// 1023, the significand shifted into place), exact like the conversion; zeros keep their sign.
+// Subnormal, infinite and NaN values take the conversion instruction.  On GB300 the conversion
+// runs on the FP64 pipe (1/64 of the FP32 rate); this form does not.
+__host__ __device__ __forceinline__ double f2d_bits(float f) {
+  unsigned int u;
+#ifdef __CUDA_ARCH__
+  u = __float_as_uint(f);
+#else
+  __builtin_memcpy(&u, &f, 4);
+#endif
+  const unsigned int e = (u >> 23) & 0xff, m = u & 0x7fffff;
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  unsigned long long b;
+  if (e == 0 && m == 0) {
+    b = sign;
+  } else if (e == 0 || e == 255) {
+    return (double)f;
+  } else {
+    b = sign | ((unsigned long long)(e + 896) << 52) | ((unsigned long long)m << 29);
+  }
+  double d;
+#ifdef __CUDA_ARCH__
+  d = __longlong_as_double((long long)b);
+#else
+  __builtin_memcpy(&d, &b, 8);
+#endif
+  return d;
+}
+// df_to_double with the conversions done by f2d_bits: the same value, one FP64 addition
+__host__ __device__ __forceinline__ double df_to_double_bits(df64 a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+
 // s + e == a + b exactly
 __device__ __forceinline__ df64 two_sum(float a, float b) {
   float s = __fadd_rn(a, b);

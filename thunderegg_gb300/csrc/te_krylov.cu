@@ -633,6 +633,7 @@ __global__ void kd_split3(const double* __restrict__ src, DV d0, DV d1, DV d2, l
 }
 
 // x += dx in FP64, then dx = 0: the loop's float-float correction folded into the FP64 iterate
+// (dx's parts widened by integer operations: two FP64 additions per element, no conversions)
 __global__ void kd_fold(DV dx, double* __restrict__ x, long long n) {
   const long long stride = (long long)gridDim.x * blockDim.x;
   for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += CONV_U * stride) {
@@ -648,7 +649,7 @@ __global__ void kd_fold(DV dx, double* __restrict__ x, long long n) {
     for (int u = 0; u < CONV_U; u++) {
       const long long i = i0 + u * stride;
       if (i >= n) continue;
-      x[i] = v[u] + df_to_double(d[u]);
+      x[i] = v[u] + df_to_double_bits(d[u]);
       stv(dx, i, df64(0.f, 0.f));
     }
   }
