@@ -40,7 +40,8 @@ __host__ __device__ __forceinline__ df64 df_from_double(double d) { return df64(
 // r = (M mod 2^29) - [rounded up] 2^29 times 2^(E-52), and RN(r) as an FP32
 // integer conversion scaled by the exact power 2^(E-52) is RN(d - hi).  Used
 // when E is in [-74, 126], so hi and a nonzero lo are normal FP32 numbers;
-// other values (zeros, subnormals, huge, Inf, NaN) take the FP64 formula.
+// zeros are (+-0, +0) as in the formula; other values (subnormals, huge, Inf,
+// NaN) take the FP64 formula.
 __host__ __device__ __forceinline__ df64 df_split_bits(double d) {
   unsigned long long b;
 #ifdef __CUDA_ARCH__
@@ -48,6 +49,8 @@ __host__ __device__ __forceinline__ df64 df_split_bits(double d) {
 #else
   __builtin_memcpy(&b, &d, 8);
 #endif
+  // zeros (the ghost cells of a padded level are): (+-0, +0), as the formula gives, without it
+  if ((b << 1) == 0) return df64((b >> 63) ? -0.f : 0.f, 0.f);
   const int E = (int)((b >> 52) & 0x7ff) - 1023;
   if (E < -74 || E > 126) return df64(d);
   const unsigned long long M = (b & ((1ull << 52) - 1)) | (1ull << 52);

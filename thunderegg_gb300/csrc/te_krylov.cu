@@ -1014,14 +1014,17 @@ static void apply_df(const te_operator* A, const float* u, DV f, cudaStream_t st
 // value; every writer stores the same value
 __global__ void x_nonzero(const double* __restrict__ x, long long n, long long pstride,
                           const int* __restrict__ patch_solve, double* __restrict__ S) {
+  // x != 0.0 tested on the bits (every value but +0 and -0 has a nonzero bit below the sign),
+  // so the FP64 pipe stays idle
+  const long long* xb = reinterpret_cast<const long long*>(x);
   const long long step = (long long)gridDim.x * blockDim.x;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += 4 * step) {
-    double v[4];
+    unsigned long long v[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) v[k] = i + k * step < n ? __ldg(x + i + k * step) : 0.0;
+    for (int k = 0; k < 4; k++) v[k] = i + k * step < n ? (unsigned long long)__ldg(xb + i + k * step) : 0ull;
 #pragma unroll
     for (int k = 0; k < 4; k++)
-      if (v[k] != 0.0) S[(size_t)patch_solve[(i + k * step) / pstride] * S_NSLOTS + S_XNZ] = 1.0;
+      if ((v[k] << 1) != 0ull) S[(size_t)patch_solve[(i + k * step) / pstride] * S_NSLOTS + S_XNZ] = 1.0;
   }
 }
 
