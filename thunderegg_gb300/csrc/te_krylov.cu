@@ -764,8 +764,8 @@ __global__ void __launch_bounds__(256)
 // away from the patch boundary before the barrier that publishes the gathered
 // ghosts, the boundary shell after it.  f's ghost cells are not written (the
 // outer loop never reads them).
-template <int KIND, int SCHEME, int DIM, int NN, int NV>
-__global__ void __launch_bounds__(256, 8)
+template <int KIND, int SCHEME, int DIM, int NN, int NV, int NT>
+__global__ void __launch_bounds__(NT, 2048 / NT)
     apply_dots_kernel(Layout L, const int8_t* __restrict__ ntype, int FS, const float2* __restrict__ inv_df,
                       int neumann, CV coeff, FaceTable ft, const GSlab* __restrict__ slabs,
                       const GCall* __restrict__ calls, const int* __restrict__ side_code,
@@ -793,13 +793,13 @@ __global__ void __launch_bounds__(256, 8)
   // memory after the interior cells, so the gather's dependent loads overlap
   // the interior work instead of delaying the barrier
   constexpr int NG = 2 * DIM * NF;
-  constexpr int GPT = (NG + 255) / 256;
+  constexpr int GPT = (NG + NT - 1) / NT;
   df64 gv[GPT];
 #pragma unroll
   for (int i = 0; i < GPT; i++) {
-    const int e = threadIdx.x + i * 256;
+    const int e = threadIdx.x + i * NT;
     gv[i] = df64(0.f, 0.f);
-    if (NG % 256 == 0 || e < NG) {
+    if (NG % NT == 0 || e < NG) {
       const int s = e / NF, r = e % NF;
       if constexpr (GPT == 1) {
         // the side's record: a coarse-fine side's values are one dependent load away
@@ -833,15 +833,15 @@ __global__ void __launch_bounds__(256, 8)
   // cells away from the boundary: every neighbour is an interior FP32 value
   if (KIND == 0) {
     // two cells per round, all their loads issued before either is computed
-    for (int e0 = threadIdx.x; e0 < NIN; e0 += 512) {
+    for (int e0 = threadIdx.x; e0 < NIN; e0 += 2 * NT) {
       int kk[2];
       bool ok[2];
       float m[2], xp[2], xm[2], yp[2], ym[2], zp[2], zm[2];
       df64 wv[2];
 #pragma unroll
       for (int q = 0; q < 2; q++) {
-        ok[q] = e0 + q * 256 < NIN;
-        const int k = interior_k(ok[q] ? e0 + q * 256 : e0);
+        ok[q] = e0 + q * NT < NIN;
+        const int k = interior_k(ok[q] ? e0 + q * NT : e0);
         kk[q] = k;
         m[q] = up[k];
         xp[q] = up[k + 1];
@@ -878,8 +878,8 @@ __global__ void __launch_bounds__(256, 8)
   }
 #pragma unroll
   for (int i = 0; i < GPT; i++) {
-    const int e = threadIdx.x + i * 256;
-    if (NG % 256 == 0 || e < NG) G[(e / NF) * gs + e % NF] = gv[i];
+    const int e = threadIdx.x + i * NT;
+    if (NG % NT == 0 || e < NG) G[(e / NF) * gs + e % NF] = gv[i];
   }
   __syncthreads();
   // the boundary shell: 2D: the ring; 3D: the z = 0 and z = NN-1 planes, then the ring of every inner slice
@@ -934,10 +934,10 @@ __global__ void __launch_bounds__(256, 8)
     emit(k, res);
   }
   // block sums of the threads' compensated pairs (s, c), then this solve's patch partials in
-  // patch order: every pair into shared memory; the 32 threads of warp 0 merge eight pairs each
-  // (thread l: l, l + 32, ...), then across the warp -- a merge adds the s parts exactly
+  // patch order: every pair into shared memory; the 32 threads of warp 0 merge NT / 32 pairs
+  // each (thread l: l, l + 32, ...), then across the warp -- a merge adds the s parts exactly
   // (TwoSum) and carries its error with the c parts, as Dot2 accumulates one pair
-  __shared__ float2 red[NV][256];
+  __shared__ float2 red[NV][NT];
 #pragma unroll
   for (int i = 0; i < NV; i++) red[i][threadIdx.x] = make_float2(v[i].s, v[i].c);
   __syncthreads();
@@ -948,7 +948,7 @@ __global__ void __launch_bounds__(256, 8)
     for (int i = 0; i < NV; i++) {
       float sm = red[i][l].x, cm = red[i][l].y;
 #pragma unroll
-      for (int q = 1; q < 8; q++) {
+      for (int q = 1; q < NT / 32; q++) {
         const float2 o = red[i][l + 32 * q];
         const df64 t2 = two_sum(sm, o.x);
         sm = t2.hi;
@@ -1223,10 +1223,13 @@ static void apply_dots_launch(const te_operator* A, KrylovWork& W, const float* 
   const size_t smem = (size_t)2 * L.D * gs * sizeof(df64);
   const long long n = (long long)L.P * L.cs;
   CV coeff{KIND ? A->coeffs_df.p : nullptr, KIND ? A->coeffs_df.p + n : nullptr};
-  auto kern = apply_dots_kernel<KIND, SCHEME, DIM, NN, NV>;
+  // 2D patches up to 32^2: 128 threads per patch, twice the patches resident of 256 (the gather of
+  // a 32^2 patch's 128 side ghosts is one per thread); larger patches keep 256
+  constexpr int NT = DIM == 2 && NN <= 32 ? 128 : 256;
+  auto kern = apply_dots_kernel<KIND, SCHEME, DIM, NN, NV, NT>;
   if (smem > 40 * 1024)
     allow_max_dynamic_smem((const void*)kern);
-  kern<<<L.P, 256, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff, g->faces,
+  kern<<<L.P, NT, smem, st>>>(L, d->d_nbr_type.p, d->F, (const float2*)d->d_inv_df.p, A->neumann, coeff, g->faces,
                                g->d_slabs.p, g->d_calls.p, g->d_side_code.p, g->d_side_rec.p, gs, u, f, w, W.batch(),
                                W.patch_solve.p, W.part_p.p, W.counter.p, W.S.p, slot0, fin);
   count_launch();
